@@ -1,0 +1,190 @@
+/*
+ * nlchains.h -- C ABI of the GB300-native nlchains engine (libnlchains_gb300.so).
+ *
+ * The engine integrates ensembles of independent periodic 1-D lattices with the 6th-order Yoshida
+ * scheme and computes the ensemble-averaged linear-mode energies and their entropies, for the five
+ * nlchains models.  All entry points are plain C: status codes, plain pointers and sizes, no C++
+ * exceptions and no CUDA or torch types in the signatures (streams are passed as `void *` holding a
+ * cudaStream_t; NULL is the legacy default stream).
+ *
+ * State layout is the reference's, byte for byte: double[copies][chain_length][2] (phi, pi) for the
+ * real models, complex<double>[copies][chain_length] for DNLS (reference README.md:74-82).
+ *
+ * Three levels:
+ *   1. operators on caller-owned device memory, stream ordered (replace the reference's internal
+ *      GPU API: move<model>, make_linenergies, DNLS::evolve_*);
+ *   2. jobs owned by a context (replace the reference's per-model main loop, its gconf/gres globals
+ *      and the results pipeline);
+ *   3. nlc_program_run: the reference's `nlchains <model> <options>` command line (common/main.cpp).
+ *
+ * Errors: every function returns NLC_OK (0) or a negative NLC_E* code; nlc_last_error() gives a
+ * thread-local message for the last failure on the calling thread.
+ */
+#ifndef NLCHAINS_H
+#define NLCHAINS_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* models, in the order of the reference's DNKG_FPUT_Toda::Model enum (DNKG_FPUT_Toda.hpp:9-11) */
+enum {
+	NLC_DNKG = 0,
+	NLC_FPUT = 1,
+	NLC_TODA = 2,
+	NLC_DDNKG = 3,
+	NLC_DNLS = 4
+};
+
+/* status codes */
+enum {
+	NLC_OK = 0,
+	NLC_EINVAL = -1,     /* invalid argument (reference: std::invalid_argument, main.cpp:82-103) */
+	NLC_ECUDA = -2,      /* CUDA runtime error (reference: cuda_error, utilities_cuda.cuh:23-37) */
+	NLC_ENOMEM = -3,     /* device or host allocation failed */
+	NLC_EIO = -4,        /* file I/O (reference: std::ios_base::failure, main.cpp:112-128) */
+	NLC_ETIMEDOUT = -5,  /* a bounded wait expired; nothing was left running unbounded */
+	NLC_ENOTFOUND = -6,  /* unknown job / request / program */
+	NLC_EBLOWUP = -7,    /* non-finite entropy (reference: results::check_entropy, results.cpp:63-68) */
+	NLC_EUNSUPPORTED = -8
+};
+
+/* flags of nlc_model.flags */
+enum {
+	NLC_FLAG_SPLIT_KERNEL = 1, /* --split_kernel: force the streamed tier (DNKG_FPUT_Toda.cpp:43) */
+	NLC_FLAG_NO_TUNE = 2       /* skip the autotuner, use the heuristic launch shape */
+};
+
+/*
+ * Model description: the per-model command-line options plus the gconf fields the kernels read
+ * (common/configuration.hpp:20-39; DNKG_FPUT_Toda.cpp:26-45; dDNKG.cpp:31-47; DNLS.cpp:34-37).
+ */
+typedef struct nlc_model {
+	int32_t model;             /* NLC_DNKG .. NLC_DNLS */
+	uint32_t chain_length;     /* -n, >= 2 */
+	uint32_t copies;           /* -c, > 0 */
+	double dt;                 /* --dt, > 0 */
+	double m;                  /* -m (DNKG) */
+	double alpha;              /* --alpha (FPUT cubic term, Toda steepness) */
+	double beta;               /* --beta (DNKG, FPUT, dDNKG, DNLS) */
+	const double *masses;      /* dDNKG: host array of the chain_length per-site masses m_x (the -m
+	                              file content); 2 is added internally as in dDNKG.cpp:47 */
+	const uint8_t *entropy_mask; /* optional host array of chain_length bytes, non-zero = mode used
+	                              in the entropies (--entropymask, main.cpp:119-128); NULL = all */
+	uint32_t flags;            /* NLC_FLAG_* */
+} nlc_model;
+
+/* ---------------------------------------------------------------------------------------------
+ * Level 1: operators on caller-owned device memory
+ * -------------------------------------------------------------------------------------------*/
+
+typedef struct nlc_plan nlc_plan;
+
+/*
+ * Validate a model and precompute everything its kernels need on the current CUDA device: Yoshida
+ * constants scaled by dt, dispersion, the DNLS propagator tables, the dDNKG eigensystem (host
+ * Householder + QL, replacing Armadillo eig_sym in eigensystem.cpp:13-36), twiddle tables, the
+ * integrator launch shape (autotuned once per shape unless NLC_FLAG_NO_TUNE) and the scratch used
+ * by the diagnostics.  Replaces the setup half of the reference per-model main
+ * (DNKG_FPUT_Toda.cpp:47-95, dDNKG.cpp:50-101, DNLS.cpp:39-126).
+ */
+int nlc_plan_create(const nlc_model *model, nlc_plan **plan);
+int nlc_plan_destroy(nlc_plan *plan);
+
+/*
+ * Advance every chain of the device state by `steps` Yoshida steps in one fused launch (the merged
+ * drift inside the launch and the closing drift dt*c[7] as in DNKG_FPUT_Toda.cu:117-146).
+ * Replaces `template<Model> completion move(plane2split*&, cudaStream_t)` (DNKG_FPUT_Toda.hpp:22-23,
+ * DNKG_FPUT_Toda.cu:262-297), `dDNKG::move` (dDNKG.hpp:12, dDNKG.cu:199-234) and, for DNLS, the
+ * host loop of evolve_nonlinear + cuFFT + evolve_linear + cuFFT (DNLS.cpp:159-175).
+ */
+int nlc_move(nlc_plan *plan, void *state_dev, uint32_t steps, void *stream);
+
+/*
+ * Ensemble-averaged linear-mode energies, normalised exactly as results::calc_linenergies leaves
+ * them (results_entropy.cpp:11-19), written to lin_dev[chain_length] (device memory), and, when
+ * entropies_dev is not NULL, {WT entropy, information entropy} (results_entropy.cpp:21-46) written
+ * to entropies_dev[2].  Replaces make_linenergies + its cuFFT / cublasDgemm prelude
+ * (DNKG_FPUT_Toda.cpp:113-123, DNKG_FPUT_Toda.cu:304-331; dDNKG.cpp:118-141, dDNKG.cu:237-265;
+ * DNLS.cpp:142-144, DNLS.cu:70-90) and the MPI all_reduce, which becomes an on-device reduction
+ * over copies in a fixed order (deterministic run to run).
+ */
+int nlc_linenergies(nlc_plan *plan, const void *state_dev, double *lin_dev, double *entropies_dev,
+                    void *stream);
+
+/* DNLS elementwise operators with the reference's semantics (DNLS.hpp:16-20, DNLS.cu:11-43), for
+ * callers that drive their own FFTs: psi *= exp(-i coef |psi|^2); psi_k *= table[k % n]. */
+int nlc_dnls_evolve_nonlinear(nlc_plan *plan, void *psi_dev, double beta_dt_symplectic, void *stream);
+int nlc_dnls_evolve_linear(nlc_plan *plan, void *psi_k_dev, const void *table_dev, void *stream);
+
+/* Launch shape chosen for the integrator: lanes per chain, sites per lane, threads per block. */
+int nlc_plan_shape(const nlc_plan *plan, int32_t *lanes_per_chain, int32_t *sites_per_lane,
+                   int32_t *threads_per_block, int32_t *tier);
+
+/* Linear frequencies omega_k used by the diagnostics, copied to host omegas[chain_length]. */
+int nlc_plan_omegas(const nlc_plan *plan, double *omegas);
+
+/* ---------------------------------------------------------------------------------------------
+ * Level 2: jobs (engine-owned device state; the reference main loop)
+ * -------------------------------------------------------------------------------------------*/
+
+typedef struct nlc_ctx nlc_ctx;
+
+int nlc_create(nlc_ctx **ctx, int device);
+int nlc_destroy(nlc_ctx *ctx);
+
+/* A job owns its plan, device state and stream.  kernel_batching = steps per fused launch (-b). */
+int nlc_job_create(nlc_ctx *ctx, const nlc_model *model, uint32_t kernel_batching, uint64_t *job);
+int nlc_job_destroy(nlc_ctx *ctx, uint64_t job);
+/* host -> device copy of the whole ensemble (reference layout); asynchronous w.r.t. the host when
+ * host_state is pinned */
+int nlc_job_upload(nlc_ctx *ctx, uint64_t job, const void *host_state);
+/* enqueue `steps` steps (a multiple of kernel_batching), asynchronous */
+int nlc_job_advance(nlc_ctx *ctx, uint64_t job, uint64_t steps);
+/* compute the diagnostics of the current state and copy them to host memory (blocking):
+ * lin[chain_length] (may be NULL), wt / inf (may be NULL).  Returns NLC_EBLOWUP when an entropy
+ * is not finite (the reference's quit condition, results.cpp:64-68). */
+int nlc_job_linenergies(nlc_ctx *ctx, uint64_t job, double *lin, double *wt, double *inf);
+int nlc_job_download(nlc_ctx *ctx, uint64_t job, void *host_state);
+/* wait for the job's queued work, at most timeout_ms (< 0: no limit); NLC_ETIMEDOUT if not done */
+int nlc_job_wait(nlc_ctx *ctx, uint64_t job, int32_t timeout_ms);
+/* device pointer of the job's state, for callers that mix levels 1 and 2 */
+int nlc_job_state_ptr(nlc_ctx *ctx, uint64_t job, void **state_dev);
+
+/* ---------------------------------------------------------------------------------------------
+ * Level 3: the reference command line
+ * -------------------------------------------------------------------------------------------*/
+
+/*
+ * Run `nlchains <program> <options>` exactly as the reference's main() (common/main.cpp:142-176)
+ * with argv[0] = program name among DNKG, FPUT, Toda, dDNKG, DNLS.  Reads -i, writes
+ * <prefix>-entropy, <prefix>-linenergies-<t>, <prefix>-<t> (and -omegas / -eigenvectors for dDNKG)
+ * in the reference formats.  Returns 0 on success, 1 on error (message on stderr), like the
+ * reference executable.
+ */
+int nlc_program_run(int argc, char **argv);
+
+/* ---------------------------------------------------------------------------------------------
+ * Misc
+ * -------------------------------------------------------------------------------------------*/
+
+const char *nlc_last_error(void);
+const char *nlc_version(void);
+
+/* Count of engine kernel launches issued by this process so far (all entry points). */
+uint64_t nlc_kernel_launches(void);
+
+/*
+ * FP64 throughput probe: runs an FP64 FMA loop kernel of the engine on the current device for
+ * roughly `ms` milliseconds and returns the measured FP64 rate in TFLOP/s (FMA = 2 flops).  Used
+ * as the roofline denominator for the FP64-bound integrators.
+ */
+int nlc_fp64_peak(double ms, double *tflops);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

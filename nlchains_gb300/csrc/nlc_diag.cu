@@ -1,0 +1,194 @@
+// Linear-mode energy diagnostics and entropies.
+//
+// Real models (DNKG, FPUT, Toda): the reference transforms phi and pi as two zero-padded complex
+// sequences (DNKG_FPUT_Toda.cpp:113-122) and sums |omega_k Phi_k + i Pi_k|^2 over copies with one
+// thread per mode (DNKG_FPUT_Toda.cu:304-321).  Here one complex FFT of z = phi + i pi per chain
+// gives both: Phi_k = (Z_k + conj Z_{n-k})/2, Pi_k = (Z_k - conj Z_{n-k})/(2i), hence
+//     omega Phi_k + i Pi_k = a_k Z_k + b_k conj(Z_{n-k}),  a_k = (omega_k + 1)/2, b_k = (omega_k - 1)/2,
+// and the planar double2 (phi, pi) state already *is* z, so no interleaving copies are needed.
+// DNLS: |FFT(psi)_k|^2 summed, times omega_k (DNLS.cu:70-81).  dDNKG: explicit eigenbasis
+// projection (the reference's two cublasDgemm calls, dDNKG.cpp:118-133, plus dDNKG.cu:237-256).
+//
+// The sum over copies (the reference's MPI all_reduce, results_entropy.cpp:13) runs on the device
+// in a fixed order: each team (or, for dDNKG, each block) accumulates its chains into its own
+// partial row, and a single-block finish kernel sums the rows in row order, normalises, and
+// computes the WT / information entropies (results_entropy.cpp:21-46).  Results are therefore
+// identical from run to run on a given GPU.
+#include "nlc_fft.cuh"
+
+namespace nlc {
+
+// One team (warp, or whole block when BLOCK) per chain; shared memory per team: 2 n complex
+// (ping-pong).  Each team accumulates its chains into its own row of `partials` (row = block *
+// teams + team), so no two threads ever add into the same element.
+template <bool BLOCK>
+__global__ void lin_fft_kernel(const double2 *__restrict__ state, const DiagArgs a) {
+	extern __shared__ double2 sm[];
+	const int n = int(a.n);
+	const int T = BLOCK ? blockDim.x : 32;
+	const int t = BLOCK ? threadIdx.x : (threadIdx.x & 31);
+	const int team = BLOCK ? 0 : (threadIdx.x >> 5);
+	const int teams = BLOCK ? 1 : (blockDim.x >> 5);
+	double2 *x = sm + (size_t) team * 2 * n, *y = x + n;
+	double *acc = a.partials + ((size_t) blockIdx.x * teams + team) * n;
+	for (int k = t; k < n; k += T) acc[k] = 0.;
+
+	const bool dnls = a.model == NLC_DNLS;
+	for (unsigned long long chain = (unsigned long long) blockIdx.x * teams + team; chain < a.copies;
+	     chain += (unsigned long long) gridDim.x * teams) {
+		const double2 *src = state + chain * (unsigned long long) n;
+		for (int k = t; k < n; k += T) x[k] = src[k];
+		team_sync<BLOCK>();
+		const double2 *Z = fft_team<BLOCK, false>(a.fft, x, y, t, T);
+		if (dnls) {
+			for (int k = t; k < n; k += T) {
+				const double2 z = Z[k];
+				acc[k] = dadd(acc[k], dfma(z.x, z.x, dmul(z.y, z.y)));
+			}
+		} else {
+			for (int k = t; k < n; k += T) {
+				const double2 zk = Z[k], zm = Z[k ? n - k : 0];
+				const double ak = a.coef_a[k], bk = a.coef_b[k];
+				const double re = dfma(ak, zk.x, dmul(bk, zm.x));
+				const double im = dfma(ak, zk.y, -dmul(bk, zm.y));
+				acc[k] = dadd(acc[k], dfma(re, re, dmul(im, im)));
+			}
+		}
+		team_sync<BLOCK>();
+	}
+}
+
+// dDNKG projection: a block holds CH chains in shared memory; thread k accumulates
+// sum_c (omega_k e_k.phi_c)^2 + (e_k.pi_c)^2 for its modes.
+constexpr int kProjChains = 8;
+
+__global__ void lin_ddnkg_kernel(const double2 *__restrict__ state, const DiagArgs a) {
+	extern __shared__ double2 sm[];
+	const int n = int(a.n);
+	double2 *tile = sm;                                              // [CH][n]
+	double *acc = reinterpret_cast<double *>(sm + (size_t) kProjChains * n);   // [n]
+	for (int k = threadIdx.x; k < n; k += blockDim.x) acc[k] = 0.;
+	for (unsigned long long base = (unsigned long long) blockIdx.x * kProjChains; base < a.copies;
+	     base += (unsigned long long) gridDim.x * kProjChains) {
+		__syncthreads();
+		for (int i = threadIdx.x; i < kProjChains * n; i += blockDim.x) {
+			const unsigned long long c = base + i / n;
+			tile[i] = c < a.copies ? state[c * n + i % n] : make_double2(0., 0.);
+		}
+		__syncthreads();
+		for (int k = threadIdx.x; k < n; k += blockDim.x) {
+			double dphi[kProjChains], dpi[kProjChains];
+#pragma unroll
+			for (int c = 0; c < kProjChains; c++) dphi[c] = 0., dpi[c] = 0.;
+			for (int s = 0; s < n; s++) {
+				const double e = a.eigT[(size_t) s * n + k];
+#pragma unroll
+				for (int c = 0; c < kProjChains; c++) {
+					const double2 v = tile[c * n + s];
+					dphi[c] = dfma(v.x, e, dphi[c]);
+					dpi[c] = dfma(v.y, e, dpi[c]);
+				}
+			}
+			const double om = a.omega[k];
+			double s = acc[k];
+#pragma unroll
+			for (int c = 0; c < kProjChains; c++) {
+				const double v = dmul(om, dphi[c]);
+				s = dadd(s, dfma(v, v, dmul(dpi[c], dpi[c])));
+			}
+			acc[k] = s;
+		}
+	}
+	__syncthreads();
+	for (int k = threadIdx.x; k < n; k += blockDim.x) a.partials[(size_t) blockIdx.x * n + k] = acc[k];
+}
+
+cudaError_t launch_linenergies_partials(const DiagArgs &a, const void *state, int blocks, int threads,
+                                        size_t smem, int team_block, cudaStream_t stream) {
+	const double2 *st = static_cast<const double2 *>(state);
+	count_launch();
+	if (a.model == NLC_DDNKG) {
+		lin_ddnkg_kernel<<<blocks, threads, smem, stream>>>(st, a);
+	} else if (team_block) {
+		lin_fft_kernel<true><<<blocks, threads, smem, stream>>>(st, a);
+	} else {
+		lin_fft_kernel<false><<<blocks, threads, smem, stream>>>(st, a);
+	}
+	return cudaGetLastError();
+}
+
+// Single block: sum partial rows in block order, normalise, entropies.
+constexpr int kFinishThreads = 256;
+
+__global__ void __launch_bounds__(kFinishThreads) lin_finish_kernel(const FinishArgs a) {
+	__shared__ double r_e[kFinishThreads], r_l[kFinishThreads], r_el[kFinishThreads];
+	__shared__ int r_c[kFinishThreads];
+	const int t = threadIdx.x;
+	const int n = int(a.n);
+	double se = 0., sl = 0., sel = 0.;
+	int cnt = 0;
+	for (int k = t; k < n; k += kFinishThreads) {
+		double v = 0.;
+		for (int b = 0; b < a.nblocks; b++) v = dadd(v, a.partials[(size_t) b * n + k]);
+		if (a.model == NLC_DNLS) v = dmul(v, a.omega[k]);
+		if (a.a0is0 && k == 0) v = 0.;
+		v = dmul(v, a.norm);
+		a.lin[k] = v;
+		const bool use = (!a.mask || a.mask[k]) && !(a.a0is0 && k == 0);
+		if (use) {
+			const double lv = log(v);
+			se = dadd(se, v), sl = dadd(sl, lv), sel = dfma(v, lv, sel);
+			cnt++;
+		}
+	}
+	r_e[t] = se, r_l[t] = sl, r_el[t] = sel, r_c[t] = cnt;
+	__syncthreads();
+	for (int w = kFinishThreads / 2; w > 0; w >>= 1) {
+		if (t < w) {
+			r_e[t] = dadd(r_e[t], r_e[t + w]);
+			r_l[t] = dadd(r_l[t], r_l[t + w]);
+			r_el[t] = dadd(r_el[t], r_el[t + w]);
+			r_c[t] += r_c[t + w];
+		}
+		__syncthreads();
+	}
+	if (t == 0 && a.entropies) {
+		const double modes = r_c[0];
+		const double normalization = modes / r_e[0], lognorm = log(normalization);
+		a.entropies[0] = -(r_l[0] + modes * lognorm);
+		a.entropies[1] = normalization * (r_el[0] + lognorm * r_e[0]);
+	}
+}
+
+cudaError_t launch_linenergies_finish(const FinishArgs &a, cudaStream_t stream) {
+	count_launch();
+	lin_finish_kernel<<<1, kFinishThreads, 0, stream>>>(a);
+	return cudaGetLastError();
+}
+
+// FP64 FMA probe: 8 independent chains per thread; one FMA = 2 flops.
+__global__ void fp64_probe_kernel(double *out, int iters) {
+	double x0 = threadIdx.x * 1e-3, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3, x4 = x0 + 4, x5 = x0 + 5,
+	       x6 = x0 + 6, x7 = x0 + 7;
+	const double a = 0.999999, b = 1e-7;
+	for (int i = 0; i < iters; i++) {
+		x0 = dfma(x0, a, b), x1 = dfma(x1, a, b), x2 = dfma(x2, a, b), x3 = dfma(x3, a, b);
+		x4 = dfma(x4, a, b), x5 = dfma(x5, a, b), x6 = dfma(x6, a, b), x7 = dfma(x7, a, b);
+	}
+	out[blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+}
+
+cudaError_t launch_fp64_probe(double *out, int blocks, int threads, int iters, cudaStream_t stream) {
+	count_launch();
+	fp64_probe_kernel<<<blocks, threads, 0, stream>>>(out, iters);
+	return cudaGetLastError();
+}
+
+}  // namespace nlc
+
+namespace nlc {
+const void *lin_kernel_ptr(int model, int team_block) {
+	if (model == NLC_DDNKG) return (const void *) lin_ddnkg_kernel;
+	return team_block ? (const void *) lin_fft_kernel<true> : (const void *) lin_fft_kernel<false>;
+}
+}  // namespace nlc

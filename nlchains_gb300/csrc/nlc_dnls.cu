@@ -1,0 +1,126 @@
+// DNLS split-step integrator, fused: one launch advances every chain by `steps` Yoshida steps with
+// the chain resident in shared memory.
+//
+// The reference drives this from the host: per step and sub-step k it launches (or sets a cuFFT
+// load callback for) the nonlinear phase rotation, a forward cuFFT, the linear propagator and an
+// inverse cuFFT over the whole ensemble -- 14 FFT launches and ~14 tiny H2D/memset operations per
+// time step, each a full round trip of the state through HBM (DNLS.cpp:159-175, DNLS.cu:11-67).
+// Here a team of threads owns one chain for the whole launch:
+//   psi <- psi exp(-i beta dt c_k |psi|^2)       (DNLS.cu:11-17; c_0 doubled when merged, DNLS.cpp:162)
+//   psi_k <- FFT(psi) * exp(-i dt d_k omega_k)/n  (DNLS/dispersion.cpp:19-26, DNLS.cu:19-25)
+//   psi <- IFFT(psi_k)
+// and finally psi <- psi exp(-i beta dt c_7 |psi|^2) (DNLS.cpp:175).  The FFTs are the Stockham
+// shared-memory transforms of nlc_fft.cuh; state is read once and written once per launch.
+#include "nlc_fft.cuh"
+
+namespace nlc {
+
+__device__ __forceinline__ double2 nonlinear_rotate(double2 v, double neg_coef) {
+	const double norm = dfma(v.x, v.x, dmul(v.y, v.y));
+	double s, c;
+	sincos(dmul(neg_coef, norm), &s, &c);
+	return make_double2(dfma(v.x, c, -dmul(v.y, s)), dfma(v.x, s, dmul(v.y, c)));
+}
+
+template <bool BLOCK>
+__global__ void dnls_move_kernel(double2 *__restrict__ psi, const DnlsArgs a) {
+	extern __shared__ double2 sm[];
+	__shared__ unsigned long long s_chain[32];
+	const int n = int(a.n);
+	const int T = BLOCK ? blockDim.x : 32;
+	const int t = BLOCK ? threadIdx.x : (threadIdx.x & 31);
+	const int team = BLOCK ? 0 : (threadIdx.x >> 5);
+	double2 *buf0 = sm + (size_t) team * 2 * n, *buf1 = buf0 + n;
+
+	for (;;) {
+		// team leader takes the next chain from the self-resetting counter
+		unsigned long long chain;
+		if (BLOCK) {
+			__syncthreads();
+			if (t == 0) s_chain[0] = atomicAdd(&a.work_counter[0], 1ull);
+			__syncthreads();
+			chain = s_chain[0];
+		} else {
+			unsigned long long c = 0;
+			if (t == 0) c = atomicAdd(&a.work_counter[0], 1ull);
+			chain = __shfl_sync(0xffffffffu, c, 0);
+		}
+		if (chain >= a.copies) break;
+
+		double2 *g = psi + chain * (unsigned long long) n;
+		double2 *x = buf0, *y = buf1;
+		for (int j = t; j < n; j += T) x[j] = g[j];
+		team_sync<BLOCK>();
+
+		for (uint32_t i = 0; i < a.steps; i++) {
+			for (int k = 0; k < 7; k++) {
+				const double coef = (k == 0 && i != 0) ? a.nl[7] : a.nl[k];
+				for (int j = t; j < n; j += T) x[j] = nonlinear_rotate(x[j], -coef);
+				team_sync<BLOCK>();
+				double2 *r = fft_team<BLOCK, false>(a.fft, x, y, t, T);
+				double2 *o = r == x ? y : x;
+				const double2 *tab = a.lin_tables + (size_t) k * n;
+				for (int j = t; j < n; j += T) r[j] = cmul(r[j], tab[j]);
+				team_sync<BLOCK>();
+				x = fft_team<BLOCK, true>(a.fft, r, o, t, T);
+				y = x == buf0 ? buf1 : buf0;
+			}
+		}
+		for (int j = t; j < n; j += T) g[j] = nonlinear_rotate(x[j], -a.nl_final);
+		team_sync<BLOCK>();
+	}
+
+	if (!BLOCK) __syncthreads();
+	if (threadIdx.x == 0) {
+		__threadfence();
+		const unsigned long long done = atomicAdd(&a.work_counter[1], 1ull);
+		if (done == gridDim.x - 1) {
+			a.work_counter[0] = 0;
+			a.work_counter[1] = 0;
+			__threadfence();
+		}
+	}
+}
+
+cudaError_t launch_dnls_move(const DnlsArgs &a, double2 *psi, int blocks, int threads, size_t smem,
+                             int team_block, cudaStream_t stream) {
+	count_launch();
+	if (team_block) dnls_move_kernel<true><<<blocks, threads, smem, stream>>>(psi, a);
+	else dnls_move_kernel<false><<<blocks, threads, smem, stream>>>(psi, a);
+	return cudaGetLastError();
+}
+
+// Elementwise operators with the reference's semantics (DNLS.cu:11-25), for callers that keep
+// their own FFT loop.
+__global__ void dnls_nonlinear_kernel(double2 *psi, unsigned long long elements, double neg_coef) {
+	const unsigned long long i = (unsigned long long) blockIdx.x * blockDim.x + threadIdx.x;
+	if (i < elements) psi[i] = nonlinear_rotate(psi[i], neg_coef);
+}
+
+__global__ void dnls_linear_kernel(double2 *psi, unsigned long long elements, uint32_t n, const double2 *table) {
+	const unsigned long long i = (unsigned long long) blockIdx.x * blockDim.x + threadIdx.x;
+	if (i < elements) psi[i] = cmul(psi[i], table[i % n]);
+}
+
+cudaError_t launch_dnls_nonlinear(double2 *psi, uint64_t elements, double coef, cudaStream_t stream) {
+	count_launch();
+	const unsigned long long blocks = (elements + 255) / 256;
+	dnls_nonlinear_kernel<<<(unsigned) blocks, 256, 0, stream>>>(psi, elements, -coef);
+	return cudaGetLastError();
+}
+
+cudaError_t launch_dnls_linear(double2 *psi, uint64_t elements, uint32_t n, const double2 *table,
+                               cudaStream_t stream) {
+	count_launch();
+	const unsigned long long blocks = (elements + 255) / 256;
+	dnls_linear_kernel<<<(unsigned) blocks, 256, 0, stream>>>(psi, elements, n, table);
+	return cudaGetLastError();
+}
+
+}  // namespace nlc
+
+namespace nlc {
+const void *dnls_kernel_ptr(int team_block) {
+	return team_block ? (const void *) dnls_move_kernel<true> : (const void *) dnls_move_kernel<false>;
+}
+}  // namespace nlc

@@ -1,0 +1,42 @@
+// Host-side declarations shared by the engine's C++ translation units.
+#pragma once
+
+#include <atomic>
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "nlc_internal.h"
+
+namespace nlc {
+
+// thread-local error message + status helpers
+int set_error(int code, const std::string &msg);
+int cuda_status(cudaError_t e, const char *what);
+
+// Yoshida 6th-order coefficients (reference common/symplectic.hpp:5-8)
+extern const double kYoshidaC[8];
+extern const double kYoshidaD[8];
+
+// scale * 2^(j/256), j < 256, in double-double arithmetic (identical bits on every IEEE host)
+void exp_table(double scale, double table[256]);
+
+// dispersion of the real models, sqrt(m + 4 sin^2(pi k / n)) (DNKG_FPUT_Toda/dispersion.cpp:9-16)
+std::vector<double> dispersion_real(uint32_t n, double m);
+// dispersion of DNLS, 4 sin^2(pi k / n) (DNLS/dispersion.cpp:10-17)
+std::vector<double> dispersion_dnls(uint32_t n);
+
+// FFT radices of n (4s first, then 2, 3, 5, 7, other primes); empty if n < 2
+std::vector<int> fft_radices(uint32_t n);
+// forward twiddles exp(-2 pi i e / n), e < n, interleaved re/im
+std::vector<double> fft_twiddles(uint32_t n);
+
+// Symmetric eigensystem of the periodic dDNKG operator diag(mp2) - shift(+-1) (eigensystem.cpp:
+// 15-18): ascending eigenvalues, omegas = sqrt(eigenvalues), eigenvectors column-major
+// (eigvec[k*n + s] = component s of eigenvector k), as Armadillo's eig_sym would return them.
+// Householder tridiagonalisation followed by the implicit symmetric QR iteration with Wilkinson
+// shifts (Golub and Van Loan, Matrix Computations, algorithms 8.3.1 and 8.3.3).
+bool eigensystem_periodic(const std::vector<double> &mp2, std::vector<double> &omegas,
+                          std::vector<double> &eigvec);
+
+}  // namespace nlc

@@ -1,0 +1,610 @@
+// Level-1 operators: plans, the integrator launch shape (with its autotuner), nlc_move,
+// nlc_linenergies and the DNLS elementwise operators.
+#include <algorithm>
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <tuple>
+
+#include "nlc_host.h"
+
+namespace nlc {
+
+static thread_local std::string g_last_error;
+static std::atomic<uint64_t> g_launches{0};
+
+int set_error(int code, const std::string &msg) {
+	g_last_error = msg;
+	return code;
+}
+
+int cuda_status(cudaError_t e, const char *what) {
+	if (e == cudaSuccess) return NLC_OK;
+	if (e == cudaErrorMemoryAllocation) {
+		cudaGetLastError();
+		return set_error(NLC_ENOMEM, std::string(what) + ": " + cudaGetErrorString(e));
+	}
+	return set_error(NLC_ECUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+void count_launch(uint64_t k) { g_launches += k; }
+
+const void *real_kernel_dnkg(int variant, int sites);
+const void *real_kernel_fput(int variant, int sites);
+const void *real_kernel_toda(int variant, int sites);
+const void *real_kernel_ddnkg(int variant, int sites);
+
+const void *real_move_kernel(int model, int variant, int sites) {
+	switch (model) {
+		case NLC_DNKG: return real_kernel_dnkg(variant, sites);
+		case NLC_FPUT: return real_kernel_fput(variant, sites);
+		case NLC_TODA: return real_kernel_toda(variant, sites);
+		case NLC_DDNKG: return real_kernel_ddnkg(variant, sites);
+		default: return nullptr;
+	}
+}
+
+cudaError_t launch_real_move(int model, int variant, const RealShape &shape, double *state, const RealArgs &args,
+                             cudaStream_t stream) {
+	const void *k = real_move_kernel(model, variant, shape.sites);
+	if (!k) return cudaErrorInvalidDeviceFunction;
+	double2 *st = reinterpret_cast<double2 *>(state);
+	RealArgs a = args;
+	void *params[] = {&st, &a};
+	count_launch();
+	return cudaLaunchKernel(k, dim3(shape.blocks), dim3(shape.threads), params, shape.smem, stream);
+}
+
+}  // namespace nlc
+
+using namespace nlc;
+
+// ------------------------------------------------------------------------------------------------
+// plan
+// ------------------------------------------------------------------------------------------------
+
+struct nlc_plan {
+	nlc_model m{};
+	int device = 0;
+	cudaDeviceProp prop{};
+	bool a0is0 = false;
+	std::vector<double> mp2_host, omega_host, eig_host;
+	std::vector<uint8_t> mask_host;
+	double norm = 1.;
+	int variant = 0;
+
+	// device allocations, freed by the destructor
+	std::vector<void *> allocs;
+	unsigned long long *d_counter = nullptr;
+	double *d_partials = nullptr;
+	uint8_t *d_mask = nullptr;
+
+	RealArgs ra{};
+	RealShape rs{};
+	DnlsArgs da{};
+	int dnls_blocks = 0, dnls_threads = 0, dnls_team_block = 0;
+	size_t dnls_smem = 0;
+	DiagArgs ga{};
+	int diag_blocks = 0, diag_threads = 0, diag_team_block = 0, diag_rows = 0;
+	size_t diag_smem = 0;
+	int tier = 0;   // 1 = resident lanes (G <= 32), 2 = resident block (G > 32), 3 = DNLS shared-memory
+
+	~nlc_plan() {
+		for (void *p : allocs) cudaFree(p);
+	}
+
+	template <typename T>
+	int dalloc(T **p, size_t count) {
+		void *q = nullptr;
+		const cudaError_t e = cudaMalloc(&q, std::max<size_t>(count, 1) * sizeof(T));
+		if (e != cudaSuccess) return cuda_status(e, "cudaMalloc");
+		allocs.push_back(q);
+		*p = static_cast<T *>(q);
+		return NLC_OK;
+	}
+	template <typename T>
+	int upload(T **p, const T *host, size_t count) {
+		int rc = dalloc(p, count);
+		if (rc) return rc;
+		return cuda_status(cudaMemcpy(*p, host, count * sizeof(T), cudaMemcpyHostToDevice), "cudaMemcpy");
+	}
+};
+
+namespace {
+
+int validate(const nlc_model *m) {
+	if (!m) return set_error(NLC_EINVAL, "model is NULL");
+	if (m->model < NLC_DNKG || m->model > NLC_DNLS) return set_error(NLC_EINVAL, "unknown model id");
+	if (m->chain_length < 2 || m->chain_length > 65535)
+		return set_error(NLC_EINVAL, "--chain_length must be >= 2 (and fit 16 bits, as in the reference)");
+	if (!m->copies) return set_error(NLC_EINVAL, "--copies must be a positive number");
+	if (!(m->dt > 0)) return set_error(NLC_EINVAL, "--dt must be a positive number");
+	if (m->model == NLC_DDNKG && !m->masses) return set_error(NLC_EINVAL, "dDNKG needs the per-site masses (-m file)");
+	if (uint64_t(m->chain_length) * m->copies >= (1ull << 40))
+		return set_error(NLC_EINVAL, "--chain_length * --copies too large");
+	return NLC_OK;
+}
+
+// Candidate (G, E) for a chain of n sites: G power of two, E = ceil(n / G) in [2, 16] (E = 1 is not
+// instantiated), every lane holding E or E - 1 >= 1 sites.
+std::vector<std::pair<int, int>> shape_candidates(uint32_t n) {
+	std::vector<std::pair<int, int>> c;
+	for (int G = 1; G <= kMaxLanesPerChain; G <<= 1) {
+		const uint32_t E = (n + G - 1) / G;
+		if (E < 2 || E > uint32_t(kMaxSitesPerLane)) continue;
+		c.emplace_back(G, int(E));
+	}
+	return c;
+}
+
+// Complete a shape (threads, blocks) for the device; false if not launchable.
+bool finish_shape(const nlc_plan &P, int model, int variant, RealShape &s, int threads_hint) {
+	const void *k = real_move_kernel(model, variant, s.sites);
+	if (!k) return false;
+	cudaFuncAttributes attr{};
+	if (cudaFuncGetAttributes(&attr, k) != cudaSuccess) return false;
+	int threads = s.lanes > 32 ? s.lanes : std::max(threads_hint, s.lanes);
+	threads = std::max(threads, 32);
+	if (threads > attr.maxThreadsPerBlock) {
+		if (s.lanes > 32) return false;
+		threads = attr.maxThreadsPerBlock / 32 * 32;
+	}
+	int per_sm = 0;
+	if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, threads, 0) != cudaSuccess || per_sm < 1) return false;
+	const unsigned long long gpb = threads / s.lanes;
+	const unsigned long long units = (P.m.copies + gpb - 1) / gpb;
+	s.threads = threads;
+	s.smem = 0;
+	s.blocks = int(std::min<unsigned long long>(units, (unsigned long long) per_sm * P.prop.multiProcessorCount));
+	return s.blocks > 0;
+}
+
+// Heuristic: fewest lanes per chain (largest E) that still gives every SM >= 8 warps of work,
+// else the most parallel shape; block of 256 threads for groups within a warp, shrunk while the
+// number of blocks would leave SMs idle.
+RealShape heuristic_shape(const nlc_plan &P, int model, int variant) {
+	const auto cands = shape_candidates(P.m.chain_length);
+	const unsigned long long want_warps = 8ull * P.prop.multiProcessorCount;
+	RealShape best{};
+	for (auto it = cands.begin(); it != cands.end(); ++it) {
+		RealShape s{};
+		s.lanes = it->first, s.sites = it->second;
+		const unsigned long long warps = ((unsigned long long) P.m.copies * s.lanes + 31) / 32;
+		int tpb = 256;
+		while (tpb > 32 && tpb > s.lanes &&
+		       (unsigned long long) P.m.copies * s.lanes / tpb < 4ull * P.prop.multiProcessorCount)
+			tpb >>= 1;
+		if (!finish_shape(P, model, variant, s, tpb)) continue;
+		best = s;
+		if (warps >= want_warps) break;
+	}
+	return best;
+}
+
+struct TuneKey {
+	int device, model, variant;
+	uint32_t n, copies;
+	bool operator<(const TuneKey &o) const {
+		return std::tie(device, model, variant, n, copies) < std::tie(o.device, o.model, o.variant, o.n, o.copies);
+	}
+};
+std::mutex g_tune_mutex;
+std::map<TuneKey, RealShape> g_tune_cache;
+
+// Time every launchable (G, threads) shape on a zero ensemble for a few steps; keep the fastest.
+// Results are cached per (device, model, variant, n, copies) for the life of the process.
+RealShape autotune_shape(nlc_plan &P, int model, int variant) {
+	const TuneKey key{P.device, model, variant, P.m.chain_length, P.m.copies};
+	{
+		std::lock_guard<std::mutex> lk(g_tune_mutex);
+		auto it = g_tune_cache.find(key);
+		if (it != g_tune_cache.end()) return it->second;
+	}
+	RealShape fallback = heuristic_shape(P, model, variant);
+	const size_t bytes = size_t(P.m.chain_length) * P.m.copies * sizeof(double2);
+	double *scratch = nullptr;
+	if (!fallback.blocks || cudaMalloc(&scratch, bytes) != cudaSuccess) {
+		cudaGetLastError();
+		return fallback;
+	}
+	cudaMemset(scratch, 0, bytes);
+	cudaStream_t st;
+	cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+	cudaEvent_t e0, e1;
+	cudaEventCreate(&e0);
+	cudaEventCreate(&e1);
+	RealArgs a = P.ra;
+	a.steps = 2;
+	RealShape best = fallback;
+	float best_ms = 1e30f;
+	for (auto c : shape_candidates(P.m.chain_length)) {
+		for (int tpb : {32, 64, 128, 256, 512}) {
+			if (c.first > 32 && tpb != 32) continue;   // block shape fixed by G for multi-warp chains
+			RealShape s{};
+			s.lanes = c.first, s.sites = c.second;
+			if (!finish_shape(P, model, variant, s, tpb)) continue;
+			if (c.first <= 32 && s.threads != std::max(tpb, s.lanes)) continue;
+			float ms = 1e30f;
+			bool ok = true;
+			for (int rep = 0; rep < 3 && ok; rep++) {
+				cudaEventRecord(e0, st);
+				ok = launch_real_move(model, variant, s, scratch, a, st) == cudaSuccess;
+				cudaEventRecord(e1, st);
+				if (cudaEventSynchronize(e1) != cudaSuccess) ok = false;
+				float t = 0;
+				cudaEventElapsedTime(&t, e0, e1);
+				if (rep) ms = std::min(ms, t);
+			}
+			if (ok && ms < best_ms) best_ms = ms, best = s;
+		}
+	}
+	cudaGetLastError();
+	cudaEventDestroy(e0);
+	cudaEventDestroy(e1);
+	cudaStreamDestroy(st);
+	cudaFree(scratch);
+	std::lock_guard<std::mutex> lk(g_tune_mutex);
+	g_tune_cache[key] = best;
+	return best;
+}
+
+int setup_fft(nlc_plan &P, FftPlanDev &f) {
+	const uint32_t n = P.m.chain_length;
+	const auto rad = fft_radices(n);
+	if (rad.size() > size_t(kMaxRadices)) return set_error(NLC_EINVAL, "chain_length has too many prime factors");
+	f.n = int(n);
+	f.nradix = int(rad.size());
+	for (size_t i = 0; i < rad.size(); i++) f.radix[i] = rad[i];
+	const auto tw = fft_twiddles(n);
+	double2 *d = nullptr;
+	int rc = P.upload(&d, reinterpret_cast<const double2 *>(tw.data()), n);
+	f.tw = d;
+	return rc;
+}
+
+int setup_diagnostics(nlc_plan &P) {
+	const uint32_t n = P.m.chain_length;
+	DiagArgs &g = P.ga;
+	g.n = n, g.copies = P.m.copies, g.model = P.m.model;
+	int rc;
+	const int sms = P.prop.multiProcessorCount;
+	if (P.m.model == NLC_DDNKG) {
+		// eigenvectors transposed to site-major so a warp reads 32 consecutive modes of one site
+		std::vector<double> eigT(size_t(n) * n);
+		for (size_t k = 0; k < n; k++)
+			for (size_t s = 0; s < n; s++) eigT[s * n + k] = P.eig_host[k * n + s];
+		double *d_eigT = nullptr, *d_om = nullptr;
+		if ((rc = P.upload(&d_eigT, eigT.data(), eigT.size()))) return rc;
+		if ((rc = P.upload(&d_om, P.omega_host.data(), n))) return rc;
+		g.eigT = d_eigT, g.omega = d_om;
+		P.diag_threads = int(std::min<uint32_t>(256, (n + 31) / 32 * 32));
+		P.diag_smem = size_t(8) * n * sizeof(double2) + n * sizeof(double);
+		P.diag_team_block = 1;
+		const unsigned long long tiles = (P.m.copies + 7) / 8;
+		P.diag_blocks = int(std::min<unsigned long long>(tiles, 2ull * sms));
+		P.diag_rows = P.diag_blocks;
+	} else {
+		if ((rc = setup_fft(P, g.fft))) return rc;
+		if (P.m.model == NLC_DNLS) {
+			double *d_om = nullptr;
+			if ((rc = P.upload(&d_om, P.omega_host.data(), n))) return rc;
+			g.omega = d_om;
+		} else {
+			std::vector<double> ca(n), cb(n);
+			for (uint32_t k = 0; k < n; k++) ca[k] = (P.omega_host[k] + 1) / 2, cb[k] = (P.omega_host[k] - 1) / 2;
+			double *d_a = nullptr, *d_b = nullptr;
+			if ((rc = P.upload(&d_a, ca.data(), n))) return rc;
+			if ((rc = P.upload(&d_b, cb.data(), n))) return rc;
+			g.coef_a = d_a, g.coef_b = d_b;
+		}
+		// a warp per chain up to 1024 sites (2 x 16 KiB ping-pong), else a 256-thread block per chain
+		if (n <= 1024) {
+			P.diag_team_block = 0;
+			P.diag_threads = 128;
+			const int teams = 4;
+			P.diag_smem = size_t(teams) * 2 * n * sizeof(double2);
+			const unsigned long long groups = (P.m.copies + teams - 1) / teams;
+			P.diag_blocks = int(std::min<unsigned long long>(groups, 4ull * sms));
+			P.diag_rows = P.diag_blocks * teams;
+		} else {
+			P.diag_team_block = 1;
+			P.diag_threads = 256;
+			P.diag_smem = size_t(2) * n * sizeof(double2);
+			P.diag_blocks = int(std::min<unsigned long long>(P.m.copies, 2ull * sms));
+			P.diag_rows = P.diag_blocks;
+		}
+		if (P.diag_smem > size_t(P.prop.sharedMemPerBlockOptin))
+			return set_error(NLC_EUNSUPPORTED, "chain_length too large for the shared-memory diagnostics");
+	}
+	if (P.diag_smem > size_t(P.prop.sharedMemPerBlockOptin))
+		return set_error(NLC_EUNSUPPORTED, "chain_length too large for the shared-memory diagnostics");
+	if ((rc = P.dalloc(&P.d_partials, size_t(P.diag_rows) * n))) return rc;
+	g.partials = P.d_partials;
+	if (!P.mask_host.empty()) {
+		if ((rc = P.upload(&P.d_mask, P.mask_host.data(), n))) return rc;
+	}
+	return NLC_OK;
+}
+
+int set_smem_attr(const void *k, size_t smem) {
+	if (smem <= 48 * 1024) return NLC_OK;
+	return cuda_status(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)),
+	                   "cudaFuncSetAttribute");
+}
+
+}  // namespace
+
+// kernels whose dynamic shared memory may exceed 48 KiB
+namespace nlc {
+const void *lin_kernel_ptr(int model, int team_block);
+const void *dnls_kernel_ptr(int team_block);
+}  // namespace nlc
+
+extern "C" int nlc_plan_create(const nlc_model *model, nlc_plan **out) {
+	if (!out) return set_error(NLC_EINVAL, "plan pointer is NULL");
+	*out = nullptr;
+	int rc = validate(model);
+	if (rc) return rc;
+	std::unique_ptr<nlc_plan> P(new nlc_plan);
+	P->m = *model;
+	P->m.masses = nullptr;
+	P->m.entropy_mask = nullptr;
+	if ((rc = cuda_status(cudaGetDevice(&P->device), "cudaGetDevice"))) return rc;
+	if ((rc = cuda_status(cudaGetDeviceProperties(&P->prop, P->device), "cudaGetDeviceProperties"))) return rc;
+	const uint32_t n = model->chain_length;
+	const int mdl = model->model;
+
+	// results(a0is0) (results.cpp:8): DNKG passes m == 0; FPUT and Toda pass their m, which their
+	// option parser never sets, so always true (DNKG_FPUT_Toda.cpp:22,52); dDNKG false; DNLS true
+	switch (mdl) {
+		case NLC_DNKG: P->a0is0 = model->m == 0.; break;
+		case NLC_FPUT:
+		case NLC_TODA:
+		case NLC_DNLS: P->a0is0 = true; break;
+		default: P->a0is0 = false;
+	}
+	if (model->entropy_mask) {
+		// main.cpp:119-128 and results.cpp:9-12: mode 0 leaves the mask when it has zero frequency
+		P->mask_host.assign(model->entropy_mask, model->entropy_mask + n);
+		size_t used = 0;
+		for (uint32_t k = 0; k < n; k++) used += P->mask_host[k] && !(P->a0is0 && k == 0);
+		if (used < 2) return set_error(NLC_EINVAL, "Too few modes for entropy calculation");
+	}
+
+	if (mdl == NLC_DDNKG) {
+		P->mp2_host.resize(n);
+		for (uint32_t i = 0; i < n; i++) P->mp2_host[i] = model->masses[i] + 2;
+		if (!eigensystem_periodic(P->mp2_host, P->omega_host, P->eig_host))
+			return set_error(NLC_EINVAL, "Cannot calculate eigensystem!");
+		P->norm = 0.5 / model->copies;   // dDNKG.cpp:141
+	} else if (mdl == NLC_DNLS) {
+		P->omega_host = dispersion_dnls(n);
+		P->norm = 1. / (double(model->copies) * n);   // DNLS.cpp:150 (1 / shard_elements)
+	} else {
+		// dispersion(m) with the reference's m: DNKG's -m, 0 for FPUT / Toda (DNKG_FPUT_Toda.cpp:22,50)
+		P->omega_host = dispersion_real(n, mdl == NLC_DNKG ? model->m : 0.);
+		P->norm = (0.5 / model->copies) / n;   // DNKG_FPUT_Toda.cpp:129
+	}
+
+	if ((rc = P->dalloc(&P->d_counter, 2))) return rc;
+	if ((rc = cuda_status(cudaMemset(P->d_counter, 0, 2 * sizeof(unsigned long long)), "cudaMemset"))) return rc;
+
+	if (mdl == NLC_DNLS) {
+		DnlsArgs &d = P->da;
+		d.n = n, d.copies = model->copies;
+		if ((rc = setup_fft(*P, d.fft))) return rc;
+		const double bdt = model->beta * model->dt;
+		for (int k = 0; k < 7; k++) d.nl[k] = bdt * 1. * kYoshidaC[k];
+		d.nl[7] = bdt * 2. * kYoshidaC[0];   // merged c7 + c0 (DNLS.cpp:162)
+		d.nl_final = bdt * kYoshidaC[7];
+		std::vector<double> tab(2 * 7 * size_t(n));
+		const double normalization = 1. / n;
+		for (int i = 0; i < 7; i++)
+			for (uint32_t j = 0; j < n; j++) {
+				const double im = (-model->dt * kYoshidaD[i]) * P->omega_host[j];
+				tab[2 * (i * n + j)] = std::cos(im) * normalization;
+				tab[2 * (i * n + j) + 1] = std::sin(im) * normalization;
+			}
+		double2 *d_tab = nullptr;
+		if ((rc = P->upload(&d_tab, reinterpret_cast<const double2 *>(tab.data()), 7 * size_t(n)))) return rc;
+		d.lin_tables = d_tab;
+		d.work_counter = P->d_counter;
+		// team: a warp per chain up to 256 sites, else a block of up to 256 threads per chain
+		const int sms = P->prop.multiProcessorCount;
+		if (n <= 256) {
+			P->dnls_team_block = 0;
+			P->dnls_threads = 128;
+			P->dnls_smem = 4 * 2 * size_t(n) * sizeof(double2);
+		} else {
+			P->dnls_team_block = 1;
+			P->dnls_threads = int(std::min<uint32_t>(256, std::max<uint32_t>(64, (n / 4 + 31) / 32 * 32)));
+			P->dnls_smem = 2 * size_t(n) * sizeof(double2);
+		}
+		if (P->dnls_smem > size_t(P->prop.sharedMemPerBlockOptin))
+			return set_error(NLC_EUNSUPPORTED, "chain_length too large for the shared-memory DNLS integrator");
+		const void *k = dnls_kernel_ptr(P->dnls_team_block);
+		if ((rc = set_smem_attr(k, P->dnls_smem))) return rc;
+		int per_sm = 0;
+		if ((rc = cuda_status(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, P->dnls_threads, P->dnls_smem),
+		                      "occupancy")))
+			return rc;
+		if (per_sm < 1) return set_error(NLC_EUNSUPPORTED, "DNLS kernel does not fit an SM");
+		const int teams = P->dnls_team_block ? 1 : P->dnls_threads / 32;
+		P->dnls_blocks = int(std::min<unsigned long long>((model->copies + teams - 1) / teams, (unsigned long long) per_sm * sms));
+		P->tier = 3;
+	} else {
+		RealArgs &a = P->ra;
+		for (int k = 0; k < 7; k++) {
+			a.cd[k] = kYoshidaC[k] * model->dt;
+			a.ck[k] = kYoshidaD[k] * model->dt;
+			a.nck[k] = -a.ck[k];
+		}
+		a.cd0_merged = a.cd[0] * 2;
+		a.cd_final = kYoshidaC[7] * model->dt;
+		a.mp2 = model->m + 2;
+		a.alpha = model->alpha, a.beta = model->beta;
+		a.alpha2 = 2 * model->alpha;
+		a.n = n, a.copies = model->copies;
+		a.work_counter = P->d_counter;
+		if (mdl == NLC_DDNKG) {
+			double *d = nullptr;
+			if ((rc = P->upload(&d, P->mp2_host.data(), n))) return rc;
+			a.mp2_site = d;
+		}
+		if (mdl == NLC_TODA) {
+			if (!(model->alpha != 0.)) return set_error(NLC_EINVAL, "Toda needs --alpha != 0");
+			double tab[256];
+			exp_table(1 / a.alpha2, tab);
+			double *d = nullptr;
+			if ((rc = P->upload(&d, tab, 256))) return rc;
+			a.exptab = d;
+		}
+		switch (mdl) {
+			case NLC_DNKG:
+			case NLC_DDNKG: P->variant = model->beta == 1.; break;
+			case NLC_FPUT: P->variant = model->alpha == 0. && model->beta == 1.; break;
+			case NLC_TODA: P->variant = a.alpha2 == 1.; break;
+		}
+		if (n > uint32_t(kMaxSitesPerLane) * kMaxLanesPerChain)
+			return set_error(NLC_EUNSUPPORTED, "chain_length above 16384 needs the streamed tier (not built)");
+		P->rs = RealShape{};
+		// NLC_FORCE_LANES=<G> pins the lanes per chain (used by the tests to cover every tier)
+		if (const char *force = std::getenv("NLC_FORCE_LANES")) {
+			for (auto c : shape_candidates(n)) {
+				if (c.first != std::atoi(force)) continue;
+				RealShape s{};
+				s.lanes = c.first, s.sites = c.second;
+				if (finish_shape(*P, mdl, P->variant, s, 128)) P->rs = s;
+			}
+			if (!P->rs.blocks) return set_error(NLC_EINVAL, "NLC_FORCE_LANES does not give a launchable shape");
+		} else {
+			P->rs = (model->flags & NLC_FLAG_NO_TUNE) ? heuristic_shape(*P, mdl, P->variant)
+			                                          : autotune_shape(*P, mdl, P->variant);
+		}
+		if (!P->rs.blocks) return set_error(NLC_EUNSUPPORTED, "no launchable integrator shape for this chain_length");
+		a.lanes = P->rs.lanes;
+		P->tier = P->rs.lanes > 32 ? 2 : 1;
+	}
+	if ((rc = setup_diagnostics(*P))) return rc;
+	{
+		const void *k = lin_kernel_ptr(mdl, P->diag_team_block);
+		if ((rc = set_smem_attr(k, P->diag_smem))) return rc;
+	}
+	*out = P.release();
+	return NLC_OK;
+}
+
+extern "C" int nlc_plan_destroy(nlc_plan *plan) {
+	delete plan;
+	return NLC_OK;
+}
+
+extern "C" int nlc_plan_shape(const nlc_plan *P, int32_t *lanes, int32_t *sites, int32_t *threads, int32_t *tier) {
+	if (!P) return set_error(NLC_EINVAL, "plan is NULL");
+	if (lanes) *lanes = P->m.model == NLC_DNLS ? (P->dnls_team_block ? P->dnls_threads : 32) : P->rs.lanes;
+	if (sites) *sites = P->m.model == NLC_DNLS ? 0 : P->rs.sites;
+	if (threads) *threads = P->m.model == NLC_DNLS ? P->dnls_threads : P->rs.threads;
+	if (tier) *tier = P->tier;
+	return NLC_OK;
+}
+
+extern "C" int nlc_plan_omegas(const nlc_plan *P, double *omegas) {
+	if (!P || !omegas) return set_error(NLC_EINVAL, "NULL argument");
+	std::memcpy(omegas, P->omega_host.data(), P->omega_host.size() * sizeof(double));
+	return NLC_OK;
+}
+
+extern "C" int nlc_move(nlc_plan *P, void *state, uint32_t steps, void *stream) {
+	if (!P || !state) return set_error(NLC_EINVAL, "NULL argument");
+	if (!steps) return NLC_OK;
+	cudaStream_t st = static_cast<cudaStream_t>(stream);
+	if (P->m.model == NLC_DNLS) {
+		DnlsArgs a = P->da;
+		a.steps = steps;
+		return cuda_status(launch_dnls_move(a, static_cast<double2 *>(state), P->dnls_blocks, P->dnls_threads,
+		                                    P->dnls_smem, P->dnls_team_block, st),
+		                   "DNLS move launch");
+	}
+	RealArgs a = P->ra;
+	a.steps = steps;
+	return cuda_status(launch_real_move(P->m.model, P->variant, P->rs, static_cast<double *>(state), a, st), "move launch");
+}
+
+extern "C" int nlc_linenergies(nlc_plan *P, const void *state, double *lin, double *ent, void *stream) {
+	if (!P || !state || !lin) return set_error(NLC_EINVAL, "NULL argument");
+	cudaStream_t st = static_cast<cudaStream_t>(stream);
+	int rc = cuda_status(launch_linenergies_partials(P->ga, state, P->diag_blocks, P->diag_threads, P->diag_smem,
+	                                                 P->diag_team_block, st),
+	                     "linenergies launch");
+	if (rc) return rc;
+	FinishArgs f{};
+	f.partials = P->d_partials;
+	f.nblocks = P->diag_rows;
+	f.n = P->m.chain_length;
+	f.norm = P->norm;
+	f.a0is0 = P->a0is0;
+	f.model = P->m.model;
+	f.omega = P->ga.omega;
+	f.mask = P->d_mask;
+	f.lin = lin;
+	f.entropies = ent;
+	return cuda_status(launch_linenergies_finish(f, st), "linenergies finish launch");
+}
+
+extern "C" int nlc_dnls_evolve_nonlinear(nlc_plan *P, void *psi, double coef, void *stream) {
+	if (!P || !psi) return set_error(NLC_EINVAL, "NULL argument");
+	if (P->m.model != NLC_DNLS) return set_error(NLC_EINVAL, "not a DNLS plan");
+	return cuda_status(launch_dnls_nonlinear(static_cast<double2 *>(psi), uint64_t(P->m.copies) * P->m.chain_length, coef,
+	                                         static_cast<cudaStream_t>(stream)),
+	                   "evolve_nonlinear launch");
+}
+
+extern "C" int nlc_dnls_evolve_linear(nlc_plan *P, void *psi, const void *table, void *stream) {
+	if (!P || !psi) return set_error(NLC_EINVAL, "NULL argument");
+	if (P->m.model != NLC_DNLS) return set_error(NLC_EINVAL, "not a DNLS plan");
+	const double2 *tab = table ? static_cast<const double2 *>(table) : P->da.lin_tables;
+	return cuda_status(launch_dnls_linear(static_cast<double2 *>(psi), uint64_t(P->m.copies) * P->m.chain_length,
+	                                      P->m.chain_length, tab, static_cast<cudaStream_t>(stream)),
+	                   "evolve_linear launch");
+}
+
+extern "C" const char *nlc_last_error(void) { return nlc::g_last_error.c_str(); }
+
+extern "C" const char *nlc_version(void) { return "nlchains-gb300 0.1 (sm_103a)"; }
+
+extern "C" uint64_t nlc_kernel_launches(void) { return nlc::g_launches.load(); }
+
+extern "C" int nlc_fp64_peak(double ms, double *tflops) {
+	if (!tflops) return set_error(NLC_EINVAL, "NULL argument");
+	int dev = 0;
+	cudaDeviceProp prop{};
+	int rc = cuda_status(cudaGetDevice(&dev), "cudaGetDevice");
+	if (rc) return rc;
+	if ((rc = cuda_status(cudaGetDeviceProperties(&prop, dev), "cudaGetDeviceProperties"))) return rc;
+	const int threads = 256, blocks = prop.multiProcessorCount * 8;
+	double *out = nullptr;
+	if ((rc = cuda_status(cudaMalloc(&out, sizeof(double) * threads * blocks), "cudaMalloc"))) return rc;
+	cudaEvent_t e0, e1;
+	cudaEventCreate(&e0);
+	cudaEventCreate(&e1);
+	int iters = 1000;
+	float t = 0;
+	// grow the loop until one launch lasts about `ms`
+	for (int rep = 0; rep < 12; rep++) {
+		cudaEventRecord(e0);
+		launch_fp64_probe(out, blocks, threads, iters, 0);
+		cudaEventRecord(e1);
+		if ((rc = cuda_status(cudaEventSynchronize(e1), "fp64 probe"))) break;
+		cudaEventElapsedTime(&t, e0, e1);
+		if (t >= ms * 0.8) break;
+		iters = int(std::min(1e8, iters * std::max(2.0, ms / std::max(t, 0.01f))));
+	}
+	if (!rc) *tflops = double(blocks) * threads * iters * 8 * 2 / (t * 1e-3) / 1e12;
+	cudaEventDestroy(e0);
+	cudaEventDestroy(e1);
+	cudaFree(out);
+	return rc;
+}

@@ -1,0 +1,238 @@
+// Register-resident Yoshida integrator for the real-valued models (DNKG, FPUT, Toda, dDNKG).
+//
+// Replaces the reference's three GPU tiers (move_chain_in_thread / move_chain_in_warp / move_split,
+// DNKG_FPUT_Toda.cu:82-259, dDNKG.cu:25-196) with one kernel family:
+//
+// * a chain of n sites is spread over G lanes (G a power of two, 1 .. 1024), each lane holding E or
+//   E - 1 consecutive sites in registers (E a compile-time constant 2..16, so arrays index
+//   statically), the first n - G(E - 1) lanes holding E -- the reference's warp layout
+//   (DNKG_FPUT_Toda.cu:94-106) generalised to any group width;
+// * groups of G <= 32 lanes exchange halos with width-G shuffles; for G > 32 one block holds one
+//   chain and warp-boundary halos go through double-buffered shared memory, one barrier per exchange;
+// * the grid is persistent: each block takes units of work (one chain per group) from a
+//   self-resetting device counter, which balances the FP64 pipes of all SMs to within one unit;
+// * bond-based forces (FPUT, Toda) compute each bond once: a lane computes its own right bonds and
+//   receives the left bond of its first site from its left neighbour by shuffle, instead of
+//   recomputing it as the reference's RHS constructor does;
+// * every FP64 operation is an explicit round-to-nearest intrinsic in the order the CPU oracle
+//   replays (oracle/nlc_oracle.c, move_chain_device).
+//
+// FP64 operations per site and sub-step (GB300 is FP64-pipe bound, see nlc_device.cuh):
+//   DNKG / dDNKG 6 (5 with beta == 1), FPUT 7 (6 with alpha == 0 and beta == 1),
+//   Toda 14 (13 with 2 alpha == 1) including the 9-operation table exp.
+#pragma once
+
+#include "nlc_device.cuh"
+#include "nlc_internal.h"
+
+namespace nlc {
+
+// Halo exchange around the ring of G lanes that hold one chain.
+struct Ring {
+	int G;          // lanes per chain
+	int lane;       // lane index within the chain
+	int wl;         // lane index within the warp
+	int warp;       // warp index within the block (G > 32 only)
+	int W;          // warps per chain (G > 32 only)
+	double *xbuf;   // 2 parities x 2 directions x W doubles (G > 32 only)
+	int parity;
+
+	// value of lane (lane - 1) mod G
+	__device__ __forceinline__ double from_left(double v) {
+		if (G <= 32) return __shfl_sync(0xffffffffu, v, (lane + G - 1) & (G - 1), G);
+		double a = __shfl_sync(0xffffffffu, v, (wl + 31) & 31);
+		double *buf = xbuf + parity * 2 * W;
+		if (wl == 31) buf[warp] = v;
+		__syncthreads();
+		if (wl == 0) a = buf[(warp + W - 1) % W];
+		parity ^= 1;
+		return a;
+	}
+
+	// value of lane (lane + 1) mod G
+	__device__ __forceinline__ double from_right(double v) {
+		if (G <= 32) return __shfl_sync(0xffffffffu, v, (lane + 1) & (G - 1), G);
+		double a = __shfl_sync(0xffffffffu, v, (wl + 1) & 31);
+		double *buf = xbuf + parity * 2 * W + W;
+		if (wl == 0) buf[warp] = v;
+		__syncthreads();
+		if (wl == 31) a = buf[(warp + 1) % W];
+		parity ^= 1;
+		return a;
+	}
+
+	// both directions with a single barrier: left <- lane-1's `to_right`, right <- lane+1's `to_left`
+	__device__ __forceinline__ void both(double to_right, double to_left, double &left, double &right) {
+		if (G <= 32) {
+			left = __shfl_sync(0xffffffffu, to_right, (lane + G - 1) & (G - 1), G);
+			right = __shfl_sync(0xffffffffu, to_left, (lane + 1) & (G - 1), G);
+			return;
+		}
+		left = __shfl_sync(0xffffffffu, to_right, (wl + 31) & 31);
+		right = __shfl_sync(0xffffffffu, to_left, (wl + 1) & 31);
+		double *buf = xbuf + parity * 2 * W;
+		if (wl == 31) buf[warp] = to_right;
+		if (wl == 0) buf[W + warp] = to_left;
+		__syncthreads();
+		if (wl == 0) left = buf[(warp + W - 1) % W];
+		if (wl == 31) right = buf[W + (warp + 1) % W];
+		parity ^= 1;
+	}
+};
+
+// Bond force term V'(d) of the bond-based models.
+template <int MODEL, int VAR>
+__device__ __forceinline__ double bond_force(double d, const RealArgs &a, const double *tab) {
+	if constexpr (MODEL == NLC_FPUT) {
+		// d + alpha d^2 + beta d^3 = d * (1 + d * (alpha + beta d))
+		const double h = VAR ? d : dfma(a.beta, d, a.alpha);
+		const double w = dfma(h, d, 1.);
+		return dmul(d, w);
+	} else {
+		// (exp(2 alpha d) - 1) / (2 alpha) up to the constant, which cancels in g[s] - g[s-1]
+		return exp_scaled(VAR ? d : dmul(a.alpha2, d), tab);
+	}
+}
+
+template <int MODEL, int E, int VAR>
+__global__ void real_move_kernel_t(double2 *__restrict__ state, const RealArgs a) {
+	__shared__ double xbuf[4 * 32];
+	__shared__ double s_tab[MODEL == NLC_TODA ? 256 : 1];
+	__shared__ unsigned long long s_unit;
+
+	const int G = a.lanes;
+	const int tid = threadIdx.x;
+	const int lane = tid & (G - 1);
+	const int gib = tid / G;                 // group (chain) in block
+	const int gpb = blockDim.x / G;          // groups per block
+	const int n = int(a.n);
+	const int full = n - G * (E - 1);       // lanes [0, full) hold E sites, the others E - 1
+	const bool fl = lane < full;
+	const int ne = fl ? E : E - 1;
+	const int first = fl ? lane * E : full * E + (lane - full) * (E - 1);
+
+	Ring ring{G, lane, tid & 31, tid >> 5, G > 32 ? G >> 5 : 1, xbuf, 0};
+
+	if constexpr (MODEL == NLC_TODA) {
+		for (int i = tid; i < 256; i += blockDim.x) s_tab[i] = a.exptab[i];
+	}
+	double mv[MODEL == NLC_DDNKG ? E : 1];
+	if constexpr (MODEL == NLC_DDNKG) {
+#pragma unroll
+		for (int j = 0; j < E; j++) mv[j] = j < ne ? a.mp2_site[first + j] : 2.;
+	}
+
+	const unsigned long long units = (a.copies + gpb - 1) / gpb;
+	for (;;) {
+		__syncthreads();
+		if (tid == 0) s_unit = atomicAdd(&a.work_counter[0], 1ull);
+		__syncthreads();
+		const unsigned long long u = s_unit;
+		if (u >= units) break;
+
+		unsigned long long chain = u * gpb + gib;
+		const bool active = chain < a.copies;
+		if (!active) chain = a.copies - 1;   // redundant work keeps shuffles and barriers convergent
+		double2 *cp = state + chain * (unsigned long long) n + first;
+
+		double x[E + 2], p[E];
+#pragma unroll
+		for (int j = 0; j < E; j++) {
+			if (j < ne) {
+				const double2 v = cp[j];
+				x[j + 1] = v.x, p[j] = v.y;
+			} else {
+				x[j + 1] = 0., p[j] = 0.;
+			}
+		}
+
+		for (uint32_t i = 0; i < a.steps; i++) {
+#pragma unroll
+			for (int k = 0; k < 7; k++) {
+				// the trailing drift of step i-1 (c[7]) merged with the leading drift of step i (c[0])
+				const double cd = (k == 0 && i != 0) ? a.cd0_merged : a.cd[k];
+#pragma unroll
+				for (int j = 0; j < E; j++) x[j + 1] = dfma(cd, p[j], x[j + 1]);
+
+				if constexpr (MODEL == NLC_DNKG || MODEL == NLC_DDNKG) {
+					double l, r;
+					ring.both(fl ? x[E] : x[E - 1], x[1], l, r);
+					x[0] = l, x[E + 1] = r;
+					if (!fl) x[E] = r;
+#pragma unroll
+					for (int j = 1; j <= E; j++) {
+						const double c = x[j];
+						const double bc = VAR ? c : dmul(a.beta, c);
+						double mp2x;
+						if constexpr (MODEL == NLC_DDNKG) mp2x = mv[j - 1];
+						else mp2x = a.mp2;
+						const double t = dfma(bc, c, mp2x);
+						const double uu = dfma(c, t, -x[j - 1]);
+						const double v = dsub(uu, x[j + 1]);
+						p[j - 1] = dfma(a.nck[k], v, p[j - 1]);
+					}
+				} else {
+					const double r = ring.from_right(x[1]);
+					x[E + 1] = r;
+					if (!fl) x[E] = r;
+					double g[E + 1];
+#pragma unroll
+					for (int j = 1; j <= E; j++) g[j] = bond_force<MODEL, VAR>(dsub(x[j + 1], x[j]), a, s_tab);
+					g[0] = ring.from_left(fl ? g[E] : g[E - 1]);
+#pragma unroll
+					for (int j = 1; j <= E; j++) p[j - 1] = dfma(a.ck[k], dsub(g[j], g[j - 1]), p[j - 1]);
+				}
+				if (!fl) p[E - 1] = 0.;   // the slot past a short lane's last site stays inert
+			}
+		}
+
+		if (active) {
+#pragma unroll
+			for (int j = 0; j < E; j++)
+				if (j < ne) cp[j] = make_double2(dfma(a.cd_final, p[j], x[j + 1]), p[j]);
+		}
+	}
+
+	// the last block out resets the work counters for the next launch on this plan
+	if (tid == 0) {
+		__threadfence();
+		const unsigned long long done = atomicAdd(&a.work_counter[1], 1ull);
+		if (done == gridDim.x - 1) {
+			a.work_counter[0] = 0;
+			a.work_counter[1] = 0;
+			__threadfence();
+		}
+	}
+}
+
+// Kernel table of one model: [variant][E]
+template <int MODEL>
+struct RealKernels {
+	using K = void (*)(double2 *, const RealArgs);
+	template <int E>
+	static constexpr K get(int variant) {
+		return variant ? real_move_kernel_t<MODEL, E, 1> : real_move_kernel_t<MODEL, E, 0>;
+	}
+	static K lookup(int variant, int e) {
+		switch (e) {
+			case 2: return get<2>(variant);
+			case 3: return get<3>(variant);
+			case 4: return get<4>(variant);
+			case 5: return get<5>(variant);
+			case 6: return get<6>(variant);
+			case 7: return get<7>(variant);
+			case 8: return get<8>(variant);
+			case 9: return get<9>(variant);
+			case 10: return get<10>(variant);
+			case 11: return get<11>(variant);
+			case 12: return get<12>(variant);
+			case 13: return get<13>(variant);
+			case 14: return get<14>(variant);
+			case 15: return get<15>(variant);
+			case 16: return get<16>(variant);
+			default: return nullptr;
+		}
+	}
+};
+
+}  // namespace nlc

@@ -1,0 +1,217 @@
+// Host-side constant tables of the engine: exp table, dispersion, FFT radices and twiddles, and
+// the dDNKG eigensystem.  Compiled with -ffp-contract=off so that every rounding is the one
+// written here on both x86-64 and aarch64 hosts.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+#include "nlc_host.h"
+
+namespace nlc {
+
+const double kYoshidaC[8] = {0.392256805238780, 0.510043411918458, -0.471053385409757, 0.068753168252518,
+                             0.068753168252518, -0.471053385409757, 0.510043411918458, 0.392256805238780};
+const double kYoshidaD[8] = {0.784513610477560, 0.235573213359357, -1.177679984178870, 1.315186320683906,
+                             -1.177679984178870, 0.235573213359357, 0.784513610477560, 0};
+
+namespace {
+
+struct DD {
+	double hi, lo;
+};
+
+DD renorm(double hi, double lo) {
+	const double s = hi + lo;
+	return {s, lo - (s - hi)};
+}
+
+DD dd_add(DD a, DD b) {
+	const double s = a.hi + b.hi, bb = s - a.hi, e = (a.hi - (s - bb)) + (b.hi - bb);
+	return renorm(s, e + a.lo + b.lo);
+}
+
+DD dd_mul(DD a, DD b) {
+	const double p = a.hi * b.hi;
+	double e = std::fma(a.hi, b.hi, -p);
+	e += a.hi * b.lo + a.lo * b.hi;
+	return renorm(p, e);
+}
+
+DD dd_div_u(DD a, unsigned k) {
+	const double q1 = a.hi / k;
+	const double p = q1 * k, pe = std::fma(q1, (double) k, -p);
+	const double rem = ((a.hi - p) - pe) + a.lo;
+	return renorm(q1, rem / k);
+}
+
+DD dd_exp_small(DD y) {
+	DD sum{1., 0.}, term{1., 0.};
+	for (unsigned k = 1; k < 40; k++) {
+		term = dd_div_u(dd_mul(term, y), k);
+		sum = dd_add(sum, term);
+		if (std::fabs(term.hi) < 1e-40) break;
+	}
+	return sum;
+}
+
+}  // namespace
+
+void exp_table(double scale, double table[256]) {
+	const DD ln2{0x1.62e42fefa39efp-1, 0x1.abc9e3b39803fp-56};
+	for (unsigned j = 0; j < 256; j++) {
+		DD v = dd_exp_small(dd_mul(ln2, DD{j / 256., 0.}));
+		v = dd_mul(v, DD{scale, 0.});
+		table[j] = v.hi + v.lo;
+	}
+}
+
+std::vector<double> dispersion_real(uint32_t n, double m) {
+	std::vector<double> omega(n);
+	for (uint32_t k = 0; k < n; k++) {
+		const double s2 = 2 * std::sin(k * M_PI / n);
+		omega[k] = std::sqrt(m + s2 * s2);
+	}
+	return omega;
+}
+
+std::vector<double> dispersion_dnls(uint32_t n) {
+	std::vector<double> omega(n);
+	for (uint32_t k = 0; k < n; k++) {
+		const double s2 = 2 * std::sin(k * M_PI / n);
+		omega[k] = s2 * s2;
+	}
+	return omega;
+}
+
+std::vector<int> fft_radices(uint32_t n) {
+	std::vector<int> r;
+	if (n < 2) return r;
+	while (n % 4 == 0) r.push_back(4), n /= 4;
+	while (n % 2 == 0) r.push_back(2), n /= 2;
+	for (uint32_t f = 3; f * f <= n; f += 2)
+		while (n % f == 0) r.push_back(int(f)), n /= f;
+	if (n > 1) r.push_back(int(n));
+	return r;
+}
+
+std::vector<double> fft_twiddles(uint32_t n) {
+	std::vector<double> tw(2 * size_t(n));
+	for (uint32_t e = 0; e < n; e++) {
+		const double a = 2 * M_PI * e / n;
+		tw[2 * e] = std::cos(a);
+		tw[2 * e + 1] = -std::sin(a);
+	}
+	return tw;
+}
+
+bool eigensystem_periodic(const std::vector<double> &mp2, std::vector<double> &omegas, std::vector<double> &eigvec) {
+	const size_t n = mp2.size();
+	if (n < 2) return false;
+	// dense symmetric matrix, column-major A[j*n + i]
+	std::vector<double> A(n * n, 0.), Q(n * n, 0.);
+	auto a = [&](size_t i, size_t j) -> double & { return A[j * n + i]; };
+	auto q = [&](size_t i, size_t j) -> double & { return Q[j * n + i]; };
+	for (size_t i = 0; i < n; i++) {
+		a(i, i) = mp2[i];
+		const size_t j = (i + 1) % n;
+		a(i, j) = a(j, i) = -1.;   // assignment: for n = 2 the corner entry stays -1 (eigensystem.cpp:16-18)
+		q(i, i) = 1.;
+	}
+
+	// Householder tridiagonalisation: for column k, reflect x = A[k+1:, k] onto alpha e_1.
+	std::vector<double> v(n), p(n), w(n);
+	for (size_t k = 0; k + 2 < n; k++) {
+		double norm2 = 0.;
+		for (size_t i = k + 1; i < n; i++) norm2 += a(i, k) * a(i, k);
+		const double norm = std::sqrt(norm2);
+		if (norm == 0.) continue;
+		const double x0 = a(k + 1, k);
+		const double alpha = x0 > 0 ? -norm : norm;
+		// v = x - alpha e1, normalised
+		std::fill(v.begin(), v.end(), 0.);
+		for (size_t i = k + 1; i < n; i++) v[i] = a(i, k);
+		v[k + 1] -= alpha;
+		double vn2 = 0.;
+		for (size_t i = k + 1; i < n; i++) vn2 += v[i] * v[i];
+		if (vn2 == 0.) continue;
+		const double vinv = 1. / std::sqrt(vn2);
+		for (size_t i = k + 1; i < n; i++) v[i] *= vinv;
+		// p = A v over the trailing block (rows/cols k..n-1; column k interacts too)
+		for (size_t i = k; i < n; i++) {
+			double s = 0.;
+			for (size_t j = k + 1; j < n; j++) s += a(i, j) * v[j];
+			p[i] = s;
+		}
+		double K = 0.;
+		for (size_t i = k + 1; i < n; i++) K += v[i] * p[i];
+		// A <- A - v w^T - w v^T with w = 2 (p - K v)
+		for (size_t i = k; i < n; i++) w[i] = 2. * (p[i] - K * v[i]);
+		for (size_t j = k; j < n; j++)
+			for (size_t i = k; i < n; i++) a(i, j) -= v[i] * w[j] + w[i] * v[j];
+		// exact zeros below the subdiagonal of column k
+		a(k + 1, k) = a(k, k + 1) = alpha;
+		for (size_t i = k + 2; i < n; i++) a(i, k) = a(k, i) = 0.;
+		// Q <- Q H, H = I - 2 v v^T
+		for (size_t i = 0; i < n; i++) {
+			double s = 0.;
+			for (size_t j = k + 1; j < n; j++) s += q(i, j) * v[j];
+			s *= 2.;
+			for (size_t j = k + 1; j < n; j++) q(i, j) -= s * v[j];
+		}
+	}
+	std::vector<double> d(n), e(n, 0.);
+	for (size_t i = 0; i < n; i++) d[i] = a(i, i);
+	for (size_t i = 0; i + 1 < n; i++) e[i] = a(i + 1, i);
+
+	// implicit symmetric QR with Wilkinson shift, deflating from the bottom
+	const double eps = 2.220446049250313e-16;
+	size_t iter = 0, hi = n - 1;
+	while (hi > 0) {
+		if (std::fabs(e[hi - 1]) <= eps * (std::fabs(d[hi - 1]) + std::fabs(d[hi]))) {
+			e[hi - 1] = 0.;
+			hi--;
+			continue;
+		}
+		size_t lo = hi - 1;
+		while (lo > 0 && std::fabs(e[lo - 1]) > eps * (std::fabs(d[lo - 1]) + std::fabs(d[lo]))) lo--;
+		if (++iter > 60 * n) return false;
+		const double delta = (d[hi - 1] - d[hi]) / 2, b2 = e[hi - 1] * e[hi - 1];
+		const double den = delta + (delta >= 0 ? 1. : -1.) * std::hypot(delta, e[hi - 1]);
+		const double mu = den != 0. ? d[hi] - b2 / den : d[hi] - std::fabs(e[hi - 1]);
+		double x = d[lo] - mu, z = e[lo];
+		for (size_t k = lo; k < hi; k++) {
+			const double r = std::hypot(x, z);
+			const double c = r != 0. ? x / r : 1., s = r != 0. ? z / r : 0.;
+			if (k > lo) e[k - 1] = r;
+			// rotate rows/cols k, k+1 of the tridiagonal: T' = P T P^T, P = [c s; -s c]
+			const double ak = d[k], ak1 = d[k + 1], bk = e[k];
+			d[k] = c * c * ak + 2 * c * s * bk + s * s * ak1;
+			d[k + 1] = s * s * ak - 2 * c * s * bk + c * c * ak1;
+			e[k] = c * s * (ak1 - ak) + (c * c - s * s) * bk;
+			if (k + 1 < hi) {
+				z = s * e[k + 1];        // bulge T(k, k+2)
+				e[k + 1] = c * e[k + 1];
+				x = e[k];
+			}
+			// Q <- Q P^T on columns k, k+1
+			for (size_t i = 0; i < n; i++) {
+				const double qk = q(i, k), qk1 = q(i, k + 1);
+				q(i, k) = c * qk + s * qk1;
+				q(i, k + 1) = -s * qk + c * qk1;
+			}
+		}
+	}
+	// ascending order with vectors
+	std::vector<size_t> idx(n);
+	for (size_t i = 0; i < n; i++) idx[i] = i;
+	std::stable_sort(idx.begin(), idx.end(), [&](size_t x1, size_t x2) { return d[x1] < d[x2]; });
+	omegas.assign(n, 0.);
+	eigvec.assign(n * n, 0.);
+	for (size_t k = 0; k < n; k++) {
+		omegas[k] = std::sqrt(d[idx[k]]);
+		std::memcpy(&eigvec[k * n], &Q[idx[k] * n], n * sizeof(double));
+	}
+	return true;
+}
+
+}  // namespace nlc

@@ -1,0 +1,175 @@
+"""CPU oracle for the nlchains hot path -- TEST INFRASTRUCTURE ONLY.
+
+A ctypes binding of oracle/nlc_oracle.c, a CPU restatement of the reference's integrators and
+diagnostics (each C function cites the reference file:line it follows).  Only tests/,
+__graft_entry__.smoke() and bench.py's CPU-baseline leg may import this package; the product
+(nlchains_gb300) never does.
+
+Parity status: unpinned against the reference itself (the reference has no tests, golden vectors or
+fixtures, and it cannot be built in this image: Boost.MPI, MPI, FFTW3 and Armadillo are absent).
+The oracle is pinned by analytic known answers in tests/test_oracle.py.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+
+DNKG, FPUT, TODA, DDNKG, DNLS = range(5)
+ORDER_REFERENCE, ORDER_DEVICE = 0, 1
+MODEL_NAMES = {"DNKG": DNKG, "FPUT": FPUT, "Toda": TODA, "dDNKG": DDNKG, "DNLS": DNLS}
+
+
+class _Model(ctypes.Structure):
+    _fields_ = [("model", ctypes.c_int32), ("order", ctypes.c_int32), ("n", ctypes.c_uint32),
+                ("copies", ctypes.c_uint32), ("dt", ctypes.c_double), ("m", ctypes.c_double),
+                ("alpha", ctypes.c_double), ("beta", ctypes.c_double),
+                ("mp2", ctypes.POINTER(ctypes.c_double)), ("threads", ctypes.c_int32)]
+
+
+_libs = {}
+
+
+def _lib(mt=False):
+    name = "libnlc_oracle_mt.so" if mt else "libnlc_oracle.so"
+    if name not in _libs:
+        out = _build.build()
+        lib = ctypes.CDLL(os.path.join(out, name))
+        dp = ctypes.POINTER(ctypes.c_double)
+        lib.nlo_advance.argtypes = [ctypes.POINTER(_Model), dp, ctypes.c_uint64, ctypes.c_uint32]
+        lib.nlo_linenergies.argtypes = [ctypes.POINTER(_Model), dp, dp, dp, dp]
+        lib.nlo_entropies.argtypes = [dp, ctypes.c_uint32, ctypes.c_int, ctypes.POINTER(ctypes.c_uint8), dp, dp]
+        lib.nlo_energy.argtypes = [ctypes.POINTER(_Model), dp]
+        lib.nlo_energy.restype = ctypes.c_double
+        lib.nlo_eigensystem.argtypes = [ctypes.c_uint32, dp, dp, dp]
+        lib.nlo_fft.argtypes = [ctypes.c_uint32, dp, ctypes.c_int]
+        lib.nlo_dispersion.argtypes = [ctypes.c_int32, ctypes.c_uint32, ctypes.c_double, dp]
+        lib.nlo_exp_table.argtypes = [ctypes.c_double, dp]
+        lib.nlo_exp_scaled.argtypes = [ctypes.c_double, dp]
+        lib.nlo_exp_scaled.restype = ctypes.c_double
+        lib.nlo_coefficients.argtypes = [dp, dp]
+        _libs[name] = lib
+    return _libs[name]
+
+
+def _dp(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+class Model:
+    """Parameters of one ensemble, as the reference's gconf plus the per-model options."""
+
+    def __init__(self, model, n, copies, dt, m=0.0, alpha=0.0, beta=0.0, masses=None,
+                 order=ORDER_DEVICE):
+        self.model = MODEL_NAMES[model] if isinstance(model, str) else int(model)
+        self.n, self.copies, self.dt = int(n), int(copies), float(dt)
+        self.m, self.alpha, self.beta = float(m), float(alpha), float(beta)
+        self.order = order
+        self.mp2 = None
+        if self.model == DDNKG:
+            if masses is None:
+                raise ValueError("dDNKG needs per-site masses")
+            # dDNKG.cpp:47: the m file holds m_x and the solver works with m_x + 2
+            self.mp2 = np.ascontiguousarray(np.asarray(masses, dtype=np.float64) + 2)
+
+    def _struct(self, threads=1, order=None):
+        s = _Model(self.model, self.order if order is None else order, self.n, self.copies, self.dt,
+                   self.m, self.alpha, self.beta, None, threads)
+        if self.mp2 is not None:
+            s.mp2 = _dp(self.mp2)
+        return s
+
+
+def coefficients():
+    c, d = np.zeros(8), np.zeros(8)
+    _lib().nlo_coefficients(_dp(c), _dp(d))
+    return c, d
+
+
+def advance(model, state, steps, batching, order=None, threads=1):
+    """Return a copy of `state` (planar [copies][n][2] float64) advanced by `steps` steps."""
+    out = np.ascontiguousarray(np.array(state, dtype=np.float64, copy=True))
+    assert out.size == 2 * model.n * model.copies
+    s = model._struct(threads, order)
+    lib = _lib(mt=threads > 1)
+    if lib.nlo_advance(ctypes.byref(s), _dp(out), steps, batching) != 0:
+        raise ValueError("nlo_advance rejected its arguments")
+    return out
+
+
+def eigensystem(n, mp2):
+    mp2 = np.ascontiguousarray(mp2, dtype=np.float64)
+    om, ev = np.zeros(n), np.zeros(n * n)
+    if _lib().nlo_eigensystem(n, _dp(mp2), _dp(om), _dp(ev)) != 0:
+        raise ValueError("eigensystem failed")
+    return om, ev
+
+
+def linenergies(model, state):
+    """Normalised per-mode energies of the ensemble (results::calc_linenergies output)."""
+    state = np.ascontiguousarray(state, dtype=np.float64)
+    out = np.zeros(model.n)
+    ev = om = None
+    if model.model == DDNKG:
+        om, ev = eigensystem(model.n, model.mp2)
+    s = model._struct()
+    rc = _lib().nlo_linenergies(ctypes.byref(s), _dp(state), _dp(ev) if ev is not None else None,
+                                _dp(om) if om is not None else None, _dp(out))
+    if rc != 0:
+        raise ValueError("nlo_linenergies rejected its arguments")
+    return out
+
+
+def a0is0(model):
+    """Whether mode 0 has zero frequency and is left out of the entropy (results.cpp:8)."""
+    if model.model == DNLS:
+        return True
+    if model.model == DDNKG:
+        return False
+    return model.m == 0.0
+
+
+def entropies(lin, a0is0_flag, mask=None):
+    lin = np.ascontiguousarray(lin, dtype=np.float64)
+    wt, inf = ctypes.c_double(), ctypes.c_double()
+    mp = None
+    if mask is not None:
+        mask = np.ascontiguousarray(mask, dtype=np.uint8)
+        mp = mask.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8))
+    if _lib().nlo_entropies(_dp(lin), lin.size, int(a0is0_flag), mp, ctypes.byref(wt), ctypes.byref(inf)) != 0:
+        raise ValueError("too few modes for entropy")
+    return wt.value, inf.value
+
+
+def energy(model, chain):
+    chain = np.ascontiguousarray(chain, dtype=np.float64)
+    s = model._struct()
+    return _lib().nlo_energy(ctypes.byref(s), _dp(chain))
+
+
+def energies(model, state):
+    st = np.ascontiguousarray(state, dtype=np.float64).reshape(model.copies, model.n * 2)
+    return np.array([energy(model, st[c]) for c in range(model.copies)])
+
+
+def fft(z, sign=-1):
+    z = np.ascontiguousarray(np.asarray(z, dtype=np.complex128).copy())
+    _lib().nlo_fft(z.size, z.view(np.float64).ctypes.data_as(ctypes.POINTER(ctypes.c_double)), sign)
+    return z
+
+
+def dispersion(model_id, n, m=0.0):
+    out = np.zeros(n)
+    _lib().nlo_dispersion(model_id, n, m, _dp(out))
+    return out
+
+
+def exp_table(scale):
+    t = np.zeros(256)
+    _lib().nlo_exp_table(scale, _dp(t))
+    return t
+
+
+def exp_scaled(x, table):
+    return _lib().nlo_exp_scaled(x, _dp(np.ascontiguousarray(table)))

@@ -1,0 +1,96 @@
+/*
+ * nlc_oracle.h -- TEST INFRASTRUCTURE ONLY.
+ *
+ * CPU restatement of the nlchains ensemble integrators and diagnostics, used by the tests, by
+ * __graft_entry__.smoke() and by the timed CPU baseline in bench.py as the checker.  The product
+ * (libnlchains_gb300.so) never links, loads or calls this code.
+ *
+ * Parity status: UNPINNED against the reference itself.  The reference ships no tests, golden
+ * vectors or fixtures, and it cannot be built here (it needs Boost.MPI/ProgramOptions, MPI, FFTW3
+ * and Armadillo, none of which exist in this image).  The oracle is pinned instead by analytic
+ * known answers (exact linear-mode transfer of the Yoshida scheme at beta = 0, norm and spectrum
+ * conservation of the linear DNLS, the Mathematica entropy/energy definitions) in tests/.
+ *
+ * Two arithmetic orders are provided for the real models:
+ *   NLO_ORDER_REFERENCE  the reference CPU code's expressions, one rounding per C operator
+ *                        (DNKG_FPUT_Toda/cpu-implementation/DNKG_FPUT_Toda.cpp:23-40,125-142,
+ *                        dDNKG/cpu-implementation/dDNKG.cpp:160-162,234-251), libm exp;
+ *   NLO_ORDER_DEVICE     the exact FP64 operation sequence of the sm_103a kernels (explicit fma,
+ *                        bond-cached forces, table-driven exp), so GPU results can be compared
+ *                        bit for bit.
+ */
+#ifndef NLC_ORACLE_H
+#define NLC_ORACLE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum { NLO_DNKG = 0, NLO_FPUT = 1, NLO_TODA = 2, NLO_DDNKG = 3, NLO_DNLS = 4 };
+enum { NLO_ORDER_REFERENCE = 0, NLO_ORDER_DEVICE = 1 };
+
+typedef struct {
+	int32_t model;
+	int32_t order;
+	uint32_t n;          /* chain length */
+	uint32_t copies;
+	double dt;
+	double m;            /* DNKG linear parameter (dispersion uses it for every real model) */
+	double alpha;        /* FPUT cubic term, Toda steepness */
+	double beta;         /* quartic term (DNKG, FPUT, dDNKG, DNLS) */
+	const double *mp2;   /* dDNKG: m_x + 2, length n */
+	int32_t threads;     /* >1: OpenMP over copies (baseline build only) */
+} nlo_model;
+
+/* Yoshida 6th-order coefficients, common/symplectic.hpp:5-8. */
+void nlo_coefficients(double c[8], double d[8]);
+
+/*
+ * Advance every chain of a planar state double2[copies][n] (or complex128[copies][n] for DNLS) by
+ * `steps` time steps, in launches of `batching` steps: inside one launch the trailing drift of a
+ * step merges with the leading drift of the next (DNKG_FPUT_Toda.cu:121-123), and the final drift
+ * dt*c[7] closes the launch (DNKG_FPUT_Toda.cu:138-146).  steps must be a multiple of batching.
+ */
+int nlo_advance(const nlo_model *mdl, double *state, uint64_t steps, uint32_t batching);
+
+/* Linear dispersion: real models sqrt(m + 4 sin^2(pi k/n)) (DNKG_FPUT_Toda/dispersion.cpp:9-16),
+ * DNLS 4 sin^2(pi k/n) (DNLS/dispersion.cpp:10-17). */
+void nlo_dispersion(int32_t model, uint32_t n, double m, double *omega);
+
+/* Forward (sign = -1) or backward (sign = +1) unnormalised complex DFT of any length, in place on
+ * interleaved re/im doubles.  Mixed radix, naive DFT for prime factors above 5. */
+void nlo_fft(uint32_t n, double *z, int sign);
+
+/*
+ * Normalised linear-mode energies of the ensemble, as results::calc_linenergies leaves them
+ * (results_entropy.cpp:11-19): real models sum |omega_k Phi_k + i Pi_k|^2 * 0.5/(copies n)
+ * (DNKG_FPUT_Toda.cu:304-321, DNKG_FPUT_Toda.cpp:129), dDNKG the eigenbasis projection * 0.5/copies
+ * (dDNKG/cpu-implementation/dDNKG.cpp:201-213, dDNKG.cpp:141), DNLS omega_k sum |psi_k|^2 /(copies n)
+ * (DNLS.cu:70-81, DNLS.cpp:150).  Mode 0 is zeroed when its frequency is 0 (results.cpp:8).
+ * eigvecs/omegas are only read for dDNKG (column-major, eigenvector k = column k).
+ */
+int nlo_linenergies(const nlo_model *mdl, const double *state, const double *eigvecs,
+                    const double *omegas, double *out);
+
+/* WT and information entropies, results_entropy.cpp:21-46.  mask may be NULL (all modes). */
+int nlo_entropies(const double *linenergies, uint32_t n, int a0is0, const uint8_t *mask,
+                  double *wt, double *inf);
+
+/* Total energy of one chain (supporting-material/post-processing/nlchains.m:40-48). */
+double nlo_energy(const nlo_model *mdl, const double *chain);
+
+/* Symmetric eigensystem of the periodic dDNKG operator diag(mp2) - shift(+-1) (eigensystem.cpp:13-22)
+ * by cyclic Jacobi: ascending eigenvalues, omegas = sqrt(eigenvalues), column-major eigenvectors. */
+int nlo_eigensystem(uint32_t n, const double *mp2, double *omegas, double *eigvecs);
+
+/* Table-driven exp used by the device order (Tang's method, 256 entries); the table holds
+ * scale * 2^(j/256) and the function returns scale * exp(x). */
+void nlo_exp_table(double scale, double table[256]);
+double nlo_exp_scaled(double x, const double table[256]);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,74 @@
+"""The drop-in `nlchains` command line end to end on the GPU (files in the reference formats)."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+import oracle as O
+from nlchains_gb300 import ic
+
+pytestmark = pytest.mark.gpu
+
+
+def run_cli(nlc, args, cwd):
+    nlc.build()
+    return subprocess.run([nlc.EXECUTABLE_PATH, *args], cwd=cwd, capture_output=True, text=True, timeout=300)
+
+
+def test_fput_run_writes_reference_files(gpu, tmp_path):
+    n, copies, b, steps, dt = 64, 32, 10, 50, 0.1
+    state = ic.real_ensemble(n, copies, 0.1, ic.low_modes(n, kmax=4, include_zero=False), seed=1)
+    ic.write_state(tmp_path / "init", state)
+    r = run_cli(gpu, ["FPUT", "-i", "init", "-n", str(n), "-c", str(copies), "--dt", str(dt), "-b", str(b),
+                      "-s", str(steps), "-p", "out", "--alpha", "0", "--beta", "1", "--dump_interval", "20"], tmp_path)
+    assert r.returncode == 0, r.stderr
+    mdl = O.Model("FPUT", n, copies, dt, alpha=0.0, beta=1.0)
+    ent = np.fromfile(tmp_path / "out-entropy").reshape(-1, 3)
+    assert ent.shape == (steps // b + 1, 3)
+    cur = state
+    for i, t in enumerate(range(0, steps + 1, b)):
+        if t:
+            cur = O.advance(mdl, cur, b, b)
+        lin = O.linenergies(mdl, cur)
+        wt, inf = O.entropies(lin, True)
+        assert ent[i, 0] == t * dt
+        assert abs(ent[i, 1] - wt) < 1e-10 * max(1, abs(wt)) and abs(ent[i, 2] - inf) < 1e-10 * max(1, abs(inf))
+        if t % 20 == 0 or t == steps:
+            got = np.fromfile(tmp_path / f"out-linenergies-{t}")
+            assert np.abs(got - lin).max() <= 1e-10 * lin.max()
+            dump = np.fromfile(tmp_path / f"out-{t}").reshape(copies, n, 2)
+            assert np.array_equal(dump, cur.reshape(copies, n, 2))
+        else:
+            assert not os.path.exists(tmp_path / f"out-{t}")
+
+
+def test_ddnkg_writes_eigensystem(gpu, tmp_path):
+    n, copies = 16, 8
+    masses = ic.masses_uniform(n, seed=2)
+    masses.tofile(tmp_path / "m")
+    state = ic.ddnkg_ensemble(masses, copies, 0.3, 4, seed=3)
+    ic.write_state(tmp_path / "init", state)
+    r = run_cli(gpu, ["dDNKG", "-i", "init", "-n", str(n), "-c", str(copies), "--dt", "0.05", "-b", "10",
+                      "-s", "20", "-p", "o", "-m", "m", "--beta", "1"], tmp_path)
+    assert r.returncode == 0, r.stderr
+    om = np.fromfile(tmp_path / "o-omegas")
+    vec = np.fromfile(tmp_path / "o-eigenvectors").reshape(n, n)
+    eom, evec = O.eigensystem(n, masses + 2)
+    assert np.abs(om - eom).max() < 1e-12
+    evec = evec.reshape(n, n)
+    for k in range(n):
+        assert min(np.abs(vec[k] - evec[k]).max(), np.abs(vec[k] + evec[k]).max()) < 1e-10
+
+
+def test_entropy_limit_stops_early(gpu, tmp_path):
+    n, copies = 32, 8
+    state = ic.real_ensemble(n, copies, 0.1, ic.low_modes(n, kmax=2, include_zero=False), seed=4)
+    ic.write_state(tmp_path / "init", state)
+    # the initial information entropy is far above 0, so a limit above it stops at t = 0
+    r = run_cli(gpu, ["FPUT", "-i", "init", "-n", str(n), "-c", str(copies), "--dt", "0.1", "-b", "10",
+                      "-s", "0", "-p", "o", "--alpha", "0", "--beta", "1", "-e", "1e9"], tmp_path)
+    assert r.returncode == 0, r.stderr
+    ent = np.fromfile(tmp_path / "o-entropy").reshape(-1, 3)
+    assert ent.shape[0] == 1
+    assert os.path.exists(tmp_path / "o-0")

@@ -1,0 +1,69 @@
+"""DNLS split-step integrator on the GPU against the oracle and against exact known answers."""
+import numpy as np
+import pytest
+
+import oracle as O
+from nlchains_gb300 import ic
+
+pytestmark = pytest.mark.gpu
+
+
+def run(nlc, n, copies, dt, beta, psi, steps, batching):
+    ctx = nlc.Context(0)
+    job = ctx.job(nlc.Model("DNLS", n, copies, dt, beta=beta), batching)
+    job.upload(psi.view(np.float64).reshape(copies, n, 2))
+    job.advance(steps)
+    out = job.download().view(np.complex128).reshape(copies, n)
+    job.close()
+    ctx.close()
+    return out
+
+
+@pytest.mark.parametrize("n", [2, 8, 12, 64, 100, 256, 512, 1024, 2048])
+def test_against_oracle(gpu, n):
+    copies, dt = 11, 0.01
+    psi = ic.dnls_ensemble(n, copies, 1.0, ic.low_modes(n, 0.1), seed=n)
+    out = run(gpu, n, copies, dt, 1.0, psi, 20, 10)
+    mdl = O.Model("DNLS", n, copies, dt, beta=1.0)
+    exp = O.advance(mdl, psi.view(np.float64), 20, 10).view(np.complex128).reshape(copies, n)
+    # different FFT algorithms and sincos implementations: agreement to rounding
+    assert np.abs(out - exp).max() <= 1e-12 * np.abs(exp).max()
+
+
+def test_linear_exact_phase_advance(gpu):
+    n, copies, dt, steps = 128, 5, 0.05, 40
+    rng = np.random.default_rng(1)
+    psi = rng.standard_normal((copies, n)) + 1j * rng.standard_normal((copies, n))
+    out = run(gpu, n, copies, dt, 0.0, psi, steps, 20)
+    omega = 4 * np.sin(np.pi * np.arange(n) / n) ** 2
+    exp = np.fft.ifft(np.fft.fft(psi, axis=1) * np.exp(-1j * omega * dt * steps), axis=1)
+    assert np.abs(out - exp).max() <= 1e-12 * np.abs(exp).max()
+
+
+def test_norm_and_energy_conservation(gpu):
+    n, copies = 1024, 8
+    psi = ic.dnls_ensemble(n, copies, 1.0, ic.low_modes(n, 0.1), seed=7)
+    out = run(gpu, n, copies, 0.01, 1.0, psi, 200, 100)
+    assert np.allclose((np.abs(out) ** 2).sum(1), (np.abs(psi) ** 2).sum(1), rtol=1e-12)
+    mdl = O.Model("DNLS", n, copies, 0.01, beta=1.0)
+    e0 = O.energies(mdl, psi.view(np.float64))
+    e1 = O.energies(mdl, out.view(np.float64))
+    assert np.abs(e1 / e0 - 1).max() < 1e-8
+
+
+def test_elementwise_operators(gpu):
+    torch = pytest.importorskip("torch")
+    n, copies = 32, 3
+    rng = np.random.default_rng(2)
+    psi = rng.standard_normal((copies, n)) + 1j * rng.standard_normal((copies, n))
+    plan = gpu.Plan(gpu.Model("DNLS", n, copies, 0.01, beta=1.0))
+    dev = torch.from_numpy(psi.copy()).cuda()
+    plan.dnls_evolve_nonlinear(dev.data_ptr(), 0.37, torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    exp = psi * np.exp(-1j * 0.37 * np.abs(psi) ** 2)
+    assert np.abs(dev.cpu().numpy() - exp).max() < 1e-14 * np.abs(exp).max()
+    table = np.exp(-1j * rng.random(n))
+    tdev = torch.from_numpy(table).cuda()
+    plan.dnls_evolve_linear(dev.data_ptr(), tdev.data_ptr(), torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    assert np.abs(dev.cpu().numpy() - exp * table[None, :]).max() < 1e-14 * np.abs(exp).max()

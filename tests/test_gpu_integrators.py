@@ -1,0 +1,139 @@
+"""Integrator parity on the GPU, through the C ABI (nlc_job_* / nlc_move).
+
+* Bit-exact against the oracle's device operation order (oracle/nlc_oracle.c move_chain_device):
+  every FP64 operation of the kernels is an explicit round-to-nearest intrinsic and the table exp
+  is replayed exactly, so the bytes must be identical for every model, variant and launch tier.
+* Within 1e-12 (max-norm relative) of the reference CPU arithmetic after 10^3 steps, the
+  tolerance the acceptance criteria set for the state.
+"""
+import os
+
+import numpy as np
+import pytest
+
+import oracle as O
+from nlchains_gb300 import ic
+
+pytestmark = pytest.mark.gpu
+
+
+def gpu_run(nlc, model, n, copies, dt, params, state, steps, batching, lanes=None, masses=None):
+    old = os.environ.get("NLC_FORCE_LANES")
+    if lanes:
+        os.environ["NLC_FORCE_LANES"] = str(lanes)
+    try:
+        ctx = nlc.Context(0)
+        job = ctx.job(nlc.Model(model, n, copies, dt, masses=masses, **params), batching)
+        if lanes:
+            assert job.ctx is ctx
+        job.upload(state)
+        job.advance(steps)
+        out = job.download()
+        job.close()
+        ctx.close()
+        return out
+    finally:
+        if lanes:
+            if old is None:
+                del os.environ["NLC_FORCE_LANES"]
+            else:
+                os.environ["NLC_FORCE_LANES"] = old
+
+
+# (model, n, params, lanes per chain or None for the tuned shape)
+CASES = [
+    ("FPUT", 64, dict(alpha=0.0, beta=1.0), None),
+    ("FPUT", 64, dict(alpha=0.0, beta=1.0), 32),
+    ("FPUT", 64, dict(alpha=0.0, beta=1.0), 4),
+    ("FPUT", 64, dict(alpha=0.25, beta=0.7), 16),
+    ("FPUT", 2, dict(alpha=0.1, beta=1.0), None),
+    ("FPUT", 5, dict(alpha=0.0, beta=1.0), 1),
+    ("FPUT", 100, dict(alpha=0.3, beta=1.0), 8),
+    ("FPUT", 1000, dict(alpha=0.0, beta=1.0), 64),
+    ("DNKG", 128, dict(m=1.0, beta=1.0), None),
+    ("DNKG", 128, dict(m=1.0, beta=1.0), 8),
+    ("DNKG", 37, dict(m=0.5, beta=0.3), 4),
+    ("DNKG", 3, dict(m=1.0, beta=1.0), 2),
+    ("DNKG", 1000, dict(m=1.0, beta=1.0), 128),
+    ("DNKG", 4000, dict(m=0.2, beta=0.5), 512),
+    ("Toda", 128, dict(alpha=0.5), None),
+    ("Toda", 128, dict(alpha=0.5), 32),
+    ("Toda", 48, dict(alpha=0.8), 4),
+    ("Toda", 2048, dict(alpha=0.5), 256),
+    ("dDNKG", 256, dict(beta=1.0), None),
+    ("dDNKG", 77, dict(beta=0.5), 8),
+    ("dDNKG", 31, dict(beta=1.0), 2),
+]
+
+
+@pytest.mark.parametrize("case", CASES, ids=lambda c: f"{c[0]}-n{c[1]}-G{c[3]}-{'-'.join(f'{k}{v}' for k, v in c[2].items())}")
+def test_bit_exact_against_device_order_oracle(gpu, case):
+    model, n, params, lanes = case
+    copies = 13    # not a multiple of any group count: exercises the inert groups of the last unit
+    dt = 0.05
+    masses = ic.masses_uniform(n, seed=n) if model == "dDNKG" else None
+    if model == "dDNKG":
+        state = ic.ddnkg_ensemble(masses, copies, 0.5, max(1, n // 10), seed=5)
+    else:
+        m = params.get("m", 0.0)
+        state = ic.real_ensemble(n, copies, 0.4, ic.low_modes(n, 0.1, include_zero=m > 0), m=m, seed=n)
+    out = gpu_run(gpu, model, n, copies, dt, params, state, 30, 10, lanes=lanes, masses=masses)
+    mdl = O.Model(model, n, copies, dt, masses=masses, **params)
+    exp = O.advance(mdl, state, 30, 10, order=O.ORDER_DEVICE).reshape(copies, n, 2)
+    if not np.array_equal(out, exp):
+        diff = np.abs(out - exp)
+        pytest.fail(f"not bit-exact: max abs diff {diff.max():.3e} at {np.unravel_index(diff.argmax(), diff.shape)}, "
+                    f"{np.count_nonzero(diff)} elements differ")
+
+
+REFERENCE_CASES = [
+    # config 1 (FPUT-beta N=64, dt=0.1, energy density 0.1 over k=+-1..4) and config 2 shapes
+    ("FPUT", 64, dict(alpha=0.0, beta=1.0), 0.1, 0.1, dict(kmax=4, include_zero=False), 0.0),
+    ("DNKG", 128, dict(m=1.0, beta=1.0), 0.05, 0.5, dict(fraction=0.08), 1.0),
+    ("Toda", 128, dict(alpha=0.5), 0.05, 0.5, dict(fraction=0.08, include_zero=False), 0.0),
+]
+
+
+@pytest.mark.parametrize("case", REFERENCE_CASES, ids=lambda c: c[0])
+def test_state_within_1e12_of_reference_arithmetic_after_1000_steps(gpu, case):
+    model, n, params, dt, eps, modes, m = case
+    copies = 16
+    state = ic.real_ensemble(n, copies, eps, ic.low_modes(n, **modes), m=m, seed=21)
+    out = gpu_run(gpu, model, n, copies, dt, params, state, 1000, 100)
+    mdl = O.Model(model, n, copies, dt, **params)
+    ref = O.advance(mdl, state, 1000, 100, order=O.ORDER_REFERENCE).reshape(copies, n, 2)
+    assert np.abs(out - ref).max() <= 1e-12 * np.abs(ref).max()
+
+
+def test_ddnkg_within_1e12_of_reference_arithmetic(gpu):
+    n, copies = 256, 8
+    masses = ic.masses_uniform(n, seed=9)
+    state = ic.ddnkg_ensemble(masses, copies, 0.5, 20, seed=10)
+    out = gpu_run(gpu, "dDNKG", n, copies, 0.05, dict(beta=1.0), state, 1000, 100, masses=masses)
+    mdl = O.Model("dDNKG", n, copies, 0.05, beta=1.0, masses=masses)
+    ref = O.advance(mdl, state, 1000, 100, order=O.ORDER_REFERENCE).reshape(copies, n, 2)
+    assert np.abs(out - ref).max() <= 1e-12 * np.abs(ref).max()
+
+
+def test_level1_operator_on_caller_memory_matches_job(gpu):
+    """nlc_move on a caller-owned device buffer (torch allocation) gives the job path's bytes."""
+    torch = pytest.importorskip("torch")
+    n, copies = 64, 40
+    state = ic.real_ensemble(n, copies, 0.1, ic.low_modes(n, kmax=4, include_zero=False), seed=3)
+    model = gpu.Model("FPUT", n, copies, 0.1, alpha=0.0, beta=1.0)
+    plan = gpu.Plan(model)
+    dev = torch.from_numpy(state.copy()).cuda()
+    stream = torch.cuda.current_stream().cuda_stream
+    for _ in range(3):
+        plan.move(dev.data_ptr(), 10, stream)
+    torch.cuda.synchronize()
+    out = dev.cpu().numpy()
+    exp = gpu_run(gpu, "FPUT", n, copies, 0.1, dict(alpha=0.0, beta=1.0), state, 30, 10)
+    assert np.array_equal(out, exp)
+
+
+def test_zero_steps_is_a_no_op(gpu):
+    n, copies = 16, 4
+    state = ic.real_ensemble(n, copies, 0.1, ic.low_modes(n, kmax=2, include_zero=False), seed=1)
+    out = gpu_run(gpu, "FPUT", n, copies, 0.1, dict(alpha=0.0, beta=1.0), state, 0, 10)
+    assert np.array_equal(out, state)

@@ -1,0 +1,171 @@
+"""The CPU oracle against analytic known answers (CPU only).
+
+The reference ships no tests, golden vectors or fixtures and cannot be built in this image, so the
+oracle's parity with it is unpinned; these tests pin the oracle instead with exact results the
+reference's algorithm must reproduce:
+
+* beta = 0 (linear chains): every Fourier mode evolves by the product of the Yoshida drift/kick
+  2x2 matrices (common/symplectic.hpp coefficients), computed independently here in numpy;
+* linear DNLS: |psi_hat_k| is conserved and its phase advances by omega_k dt per step
+  (sum of the Yoshida d coefficients is 1);
+* entropies: the Mathematica definitions of supporting-material/post-processing/nlchains.m:56-57;
+* the device operation order agrees with the reference CPU arithmetic to 1e-12 after 10^3 steps.
+"""
+import math
+
+import numpy as np
+import pytest
+
+import oracle as O
+from nlchains_gb300 import ic
+
+C, D = O.coefficients()
+
+
+def yoshida_mode_matrix(omega2, dt, steps):
+    """2x2 transfer of (Q_k, P_k) over `steps` Yoshida steps of q'' = -omega2 q."""
+    M = np.eye(2)
+    for _ in range(steps):
+        for k in range(7):
+            M = np.array([[1, C[k] * dt], [0, 1]]) @ M
+            M = np.array([[1, 0], [-D[k] * dt * omega2, 1]]) @ M
+        M = np.array([[1, C[7] * dt], [0, 1]]) @ M
+    return M
+
+
+@pytest.mark.parametrize("order", [O.ORDER_REFERENCE, O.ORDER_DEVICE])
+@pytest.mark.parametrize("model,m", [("DNKG", 0.7), ("FPUT", 0.0)])
+def test_linear_chain_matches_exact_mode_transfer(model, m, order):
+    n, copies, dt, steps, batching = 16, 3, 0.1, 60, 20
+    rng = np.random.default_rng(1)
+    state = rng.standard_normal((copies, n, 2)) * 0.3
+    mdl = O.Model(model, n, copies, dt, m=m, alpha=0.0, beta=0.0)
+    out = O.advance(mdl, state, steps, batching, order=order).reshape(copies, n, 2)
+    k = np.arange(n)
+    omega2 = m + 4 * np.sin(np.pi * k / n) ** 2
+    Q, P = np.fft.fft(state[:, :, 0], axis=1), np.fft.fft(state[:, :, 1], axis=1)
+    Qo, Po = np.empty_like(Q), np.empty_like(P)
+    for kk in range(n):
+        M = yoshida_mode_matrix(omega2[kk], dt, steps)
+        Qo[:, kk] = M[0, 0] * Q[:, kk] + M[0, 1] * P[:, kk]
+        Po[:, kk] = M[1, 0] * Q[:, kk] + M[1, 1] * P[:, kk]
+    exp = np.stack([np.fft.ifft(Qo, axis=1).real, np.fft.ifft(Po, axis=1).real], axis=2)
+    assert np.abs(out - exp).max() <= 1e-12 * np.abs(exp).max()
+
+
+def test_linear_dnls_phase_advance():
+    n, copies, dt, steps, batching = 32, 2, 0.05, 40, 10
+    rng = np.random.default_rng(2)
+    psi = rng.standard_normal((copies, n)) + 1j * rng.standard_normal((copies, n))
+    mdl = O.Model("DNLS", n, copies, dt, beta=0.0)
+    out = O.advance(mdl, psi.view(np.float64), steps, batching).view(np.complex128).reshape(copies, n)
+    omega = 4 * np.sin(np.pi * np.arange(n) / n) ** 2
+    exp = np.fft.ifft(np.fft.fft(psi, axis=1) * np.exp(-1j * omega * dt * steps), axis=1)
+    assert np.abs(out - exp).max() <= 1e-12 * np.abs(exp).max()
+
+
+def test_dnls_norm_conservation_nonlinear():
+    n, copies = 64, 2
+    psi = ic.dnls_ensemble(n, copies, 1.0, ic.low_modes(n, 0.1), seed=3)
+    mdl = O.Model("DNLS", n, copies, 0.01, beta=1.0)
+    out = O.advance(mdl, psi.view(np.float64), 50, 25).view(np.complex128).reshape(copies, n)
+    assert np.allclose((np.abs(out) ** 2).sum(1), (np.abs(psi) ** 2).sum(1), rtol=1e-13)
+
+
+def mathematica_entropies(e):
+    """EntropyWT / EntropyINF of nlchains.m:56-57 for a list without zero entries."""
+    f = e * len(e) / e.sum()
+    return -np.sum(np.log(f)), np.sum(f * np.log(f))
+
+
+@pytest.mark.parametrize("a0is0", [False, True])
+def test_entropies_match_mathematica_definition(a0is0):
+    rng = np.random.default_rng(3)
+    lin = rng.random(37) + 0.01
+    wt, inf = O.entropies(lin, a0is0)
+    ewt, einf = mathematica_entropies(lin[1:] if a0is0 else lin)
+    assert abs(wt - ewt) <= 1e-12 * max(1, abs(ewt))
+    assert abs(inf - einf) <= 1e-12 * max(1, abs(einf))
+    mask = np.zeros(37, np.uint8)
+    mask[[0, 3, 5, 8, 30]] = 1
+    wt, inf = O.entropies(lin, a0is0, mask)
+    sel = lin[[3, 5, 8, 30]] if a0is0 else lin[[0, 3, 5, 8, 30]]
+    ewt, einf = mathematica_entropies(sel)
+    assert abs(wt - ewt) <= 1e-12 and abs(inf - einf) <= 1e-12
+
+
+def test_equipartition_entropy_is_zero():
+    wt, inf = O.entropies(np.full(16, 0.25), False)
+    assert abs(wt) < 1e-14 and abs(inf) < 1e-14
+
+
+@pytest.mark.parametrize("n", [2, 3, 5, 8, 12, 64, 97, 100, 1024])
+def test_fft_against_numpy(n):
+    rng = np.random.default_rng(n)
+    z = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    assert np.abs(O.fft(z, -1) - np.fft.fft(z)).max() <= 1e-14 * n * np.abs(z).max()
+    assert np.abs(O.fft(z, +1) - np.fft.ifft(z) * n).max() <= 1e-14 * n * np.abs(z).max()
+
+
+@pytest.mark.parametrize("n", [2, 3, 8, 33, 64])
+def test_eigensystem_against_numpy(n):
+    masses = ic.masses_uniform(n, seed=n)
+    om, ev = O.eigensystem(n, masses + 2)
+    w, v = np.linalg.eigh(ic.periodic_operator(masses + 2))
+    assert np.abs(om - np.sqrt(w)).max() < 1e-12
+    ev = ev.reshape(n, n)
+    for k in range(n):
+        assert min(np.abs(ev[k] - v[:, k]).max(), np.abs(ev[k] + v[:, k]).max()) < 1e-9
+
+
+def test_exp_table_accuracy():
+    for scale in (1.0, 0.5, 3.0):
+        tab = O.exp_table(scale)
+        for x in np.concatenate([np.linspace(-30, 30, 4001), [-700.0, 700.0, 0.0, 1e-300]]):
+            v, r = O.exp_scaled(x, tab), scale * math.exp(x)
+            assert abs(v - r) <= 2.5 * np.spacing(abs(r)), (scale, x)
+    tab = O.exp_table(1.0)
+    assert O.exp_scaled(1e6, tab) == math.inf and O.exp_scaled(-1e6, tab) == 0.0
+    assert math.isnan(O.exp_scaled(math.nan, tab))
+
+
+CONFIGS = [
+    ("FPUT", 64, dict(alpha=0.0, beta=1.0), 0.1, 0.1, dict(kmax=4, include_zero=False), 0.0),
+    ("FPUT", 32, dict(alpha=0.25, beta=0.5), 0.1, 0.1, dict(kmax=3, include_zero=False), 0.0),
+    ("DNKG", 128, dict(m=1.0, beta=1.0), 0.05, 0.5, dict(fraction=0.08), 1.0),
+    ("DNKG", 40, dict(m=0.5, beta=0.3), 0.05, 0.5, dict(fraction=0.1), 0.5),
+    ("Toda", 128, dict(alpha=0.5), 0.05, 0.5, dict(fraction=0.08, include_zero=False), 0.0),
+    ("Toda", 48, dict(alpha=0.8), 0.05, 0.3, dict(fraction=0.1, include_zero=False), 0.0),
+]
+
+
+@pytest.mark.parametrize("cfg", CONFIGS, ids=lambda c: f"{c[0]}-{c[1]}")
+def test_device_order_within_tolerance_of_reference_order(cfg):
+    model, n, params, dt, eps, modes, m_disp = cfg
+    copies = 4
+    state = ic.real_ensemble(n, copies, eps, ic.low_modes(n, **modes), m=m_disp, seed=11)
+    mdl = O.Model(model, n, copies, dt, **params)
+    a = O.advance(mdl, state, 1000, 100, order=O.ORDER_DEVICE)
+    b = O.advance(mdl, state, 1000, 100, order=O.ORDER_REFERENCE)
+    assert np.abs(a - b).max() <= 1e-12 * np.abs(b).max()
+
+
+def test_ddnkg_device_order_within_tolerance():
+    n, copies = 64, 3
+    masses = ic.masses_uniform(n, seed=7)
+    state = ic.ddnkg_ensemble(masses, copies, 0.5, 6, seed=8)
+    mdl = O.Model("dDNKG", n, copies, 0.05, beta=1.0, masses=masses)
+    a = O.advance(mdl, state, 1000, 100, order=O.ORDER_DEVICE)
+    b = O.advance(mdl, state, 1000, 100, order=O.ORDER_REFERENCE)
+    assert np.abs(a - b).max() <= 1e-12 * np.abs(b).max()
+
+
+@pytest.mark.parametrize("model", ["DNKG", "FPUT", "Toda"])
+def test_energy_drift_small(model):
+    n, copies = 32, 2
+    params = {"DNKG": dict(m=1.0, beta=1.0), "FPUT": dict(alpha=0.3, beta=1.0), "Toda": dict(alpha=0.5)}[model]
+    state = ic.real_ensemble(n, copies, 0.2, ic.low_modes(n, kmax=3, include_zero=False), m=params.get("m", 0.0), seed=4)
+    mdl = O.Model(model, n, copies, 0.05, **params)
+    out = O.advance(mdl, state, 400, 100)
+    e0, e1 = O.energies(mdl, state), O.energies(mdl, out)
+    assert np.abs(e1 / e0 - 1).max() < 1e-7
