@@ -117,8 +117,23 @@ cudaError_t launch_linenergies_partials(const DiagArgs &a, const void *state, in
 	return cudaGetLastError();
 }
 
-// Single block: sum partial rows in block order, normalise, entropies.
-constexpr int kFinishThreads = 256;
+// Single block: sum the partial rows in a fixed order, normalise, entropies.  For n <= 1024 the
+// rows are split into 1024/n interleaved slices (thread t: mode t % n, slice t / n, coalesced
+// reads), the slices are then added in slice order; the result is identical on every run.
+constexpr int kFinishThreads = 1024;
+
+__device__ __forceinline__ void finish_mode(const FinishArgs &a, int k, double v, double &se, double &sl,
+                                            double &sel, int &cnt) {
+	if (a.model == NLC_DNLS) v = dmul(v, a.omega[k]);
+	if (a.a0is0 && k == 0) v = 0.;
+	v = dmul(v, a.norm);
+	a.lin[k] = v;
+	if ((!a.mask || a.mask[k]) && !(a.a0is0 && k == 0)) {
+		const double lv = log(v);
+		se = dadd(se, v), sl = dadd(sl, lv), sel = dfma(v, lv, sel);
+		cnt++;
+	}
+}
 
 __global__ void __launch_bounds__(kFinishThreads) lin_finish_kernel(const FinishArgs a) {
 	__shared__ double r_e[kFinishThreads], r_l[kFinishThreads], r_el[kFinishThreads];
@@ -127,18 +142,25 @@ __global__ void __launch_bounds__(kFinishThreads) lin_finish_kernel(const Finish
 	const int n = int(a.n);
 	double se = 0., sl = 0., sel = 0.;
 	int cnt = 0;
-	for (int k = t; k < n; k += kFinishThreads) {
+	if (n <= kFinishThreads) {
+		const int slices = kFinishThreads / n;
+		const int k = t % n, sidx = t / n;
 		double v = 0.;
-		for (int b = 0; b < a.nblocks; b++) v = dadd(v, a.partials[(size_t) b * n + k]);
-		if (a.model == NLC_DNLS) v = dmul(v, a.omega[k]);
-		if (a.a0is0 && k == 0) v = 0.;
-		v = dmul(v, a.norm);
-		a.lin[k] = v;
-		const bool use = (!a.mask || a.mask[k]) && !(a.a0is0 && k == 0);
-		if (use) {
-			const double lv = log(v);
-			se = dadd(se, v), sl = dadd(sl, lv), sel = dfma(v, lv, sel);
-			cnt++;
+		if (sidx < slices)
+			for (int r = sidx; r < a.nblocks; r += slices) v = dadd(v, a.partials[(size_t) r * n + k]);
+		r_e[t] = v;
+		__syncthreads();
+		if (t < n) {
+			double tot = 0.;
+			for (int q = 0; q < slices; q++) tot = dadd(tot, r_e[q * n + t]);
+			finish_mode(a, t, tot, se, sl, sel, cnt);
+		}
+		__syncthreads();
+	} else {
+		for (int k = t; k < n; k += kFinishThreads) {
+			double v = 0.;
+			for (int r = 0; r < a.nblocks; r++) v = dadd(v, a.partials[(size_t) r * n + k]);
+			finish_mode(a, k, v, se, sl, sel, cnt);
 		}
 	}
 	r_e[t] = se, r_l[t] = sl, r_el[t] = sel, r_c[t] = cnt;
@@ -166,21 +188,25 @@ cudaError_t launch_linenergies_finish(const FinishArgs &a, cudaStream_t stream) 
 	return cudaGetLastError();
 }
 
-// FP64 FMA probe: 8 independent chains per thread; one FMA = 2 flops.
-__global__ void fp64_probe_kernel(double *out, int iters) {
-	double x0 = threadIdx.x * 1e-3, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3, x4 = x0 + 4, x5 = x0 + 5,
-	       x6 = x0 + 6, x7 = x0 + 7;
-	const double a = 0.999999, b = 1e-7;
+// FP64 FMA probe: 8 independent chains per thread, 4x unrolled; one FMA = 2 flops.
+__global__ void fp64_probe_kernel(double *out, int iters, double a, double b) {
+	double x[8];
+#pragma unroll
+	for (int j = 0; j < 8; j++) x[j] = threadIdx.x * 1e-3 + j;
+#pragma unroll 4
 	for (int i = 0; i < iters; i++) {
-		x0 = dfma(x0, a, b), x1 = dfma(x1, a, b), x2 = dfma(x2, a, b), x3 = dfma(x3, a, b);
-		x4 = dfma(x4, a, b), x5 = dfma(x5, a, b), x6 = dfma(x6, a, b), x7 = dfma(x7, a, b);
+#pragma unroll
+		for (int j = 0; j < 8; j++) x[j] = dfma(x[j], a, b);
 	}
-	out[blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+	double s = 0.;
+#pragma unroll
+	for (int j = 0; j < 8; j++) s += x[j];
+	out[blockIdx.x * blockDim.x + threadIdx.x] = s;
 }
 
 cudaError_t launch_fp64_probe(double *out, int blocks, int threads, int iters, cudaStream_t stream) {
 	count_launch();
-	fp64_probe_kernel<<<blocks, threads, 0, stream>>>(out, iters);
+	fp64_probe_kernel<<<blocks, threads, 0, stream>>>(out, iters, 0.999999, 1e-7);
 	return cudaGetLastError();
 }
 

@@ -23,10 +23,8 @@ int set_error(int code, const std::string &msg) {
 
 int cuda_status(cudaError_t e, const char *what) {
 	if (e == cudaSuccess) return NLC_OK;
-	if (e == cudaErrorMemoryAllocation) {
-		cudaGetLastError();
-		return set_error(NLC_ENOMEM, std::string(what) + ": " + cudaGetErrorString(e));
-	}
+	cudaGetLastError();   // a reported failure must not resurface at the next launch check
+	if (e == cudaErrorMemoryAllocation) return set_error(NLC_ENOMEM, std::string(what) + ": " + cudaGetErrorString(e));
 	return set_error(NLC_ECUDA, std::string(what) + ": " + cudaGetErrorString(e));
 }
 
@@ -50,9 +48,14 @@ const void *real_move_kernel(int model, int variant, int sites) {
 cudaError_t launch_real_move(int model, int variant, const RealShape &shape, double *state, const RealArgs &args,
                              cudaStream_t stream) {
 	const void *k = real_move_kernel(model, variant, shape.sites);
-	if (!k) return cudaErrorInvalidDeviceFunction;
+	if (!k || shape.lanes < 1 || (shape.lanes & (shape.lanes - 1)) || shape.threads < 32 || shape.threads % 32 ||
+	    shape.threads % shape.lanes || (shape.lanes > 32 && shape.threads != shape.lanes) || shape.blocks < 1)
+		return cudaErrorInvalidConfiguration;
 	double2 *st = reinterpret_cast<double2 *>(state);
+	if ((args.n + uint32_t(shape.lanes) - 1) / uint32_t(shape.lanes) != uint32_t(shape.sites) || !args.copies)
+		return cudaErrorInvalidConfiguration;   // every lane must hold sites or sites - 1 >= 1 sites
 	RealArgs a = args;
+	a.lanes = shape.lanes;   // the lane count of the shape is the one the kernel must use
 	void *params[] = {&st, &a};
 	count_launch();
 	return cudaLaunchKernel(k, dim3(shape.blocks), dim3(shape.threads), params, shape.smem, stream);
@@ -329,9 +332,16 @@ int setup_diagnostics(nlc_plan &P) {
 	return NLC_OK;
 }
 
-int set_smem_attr(const void *k, size_t smem) {
+// Raise the kernel's dynamic shared-memory limit to the device maximum (never lowered, so plans
+// created earlier with larger chains keep launching).
+int set_smem_attr(const void *k, size_t smem, const cudaDeviceProp &prop) {
 	if (smem <= 48 * 1024) return NLC_OK;
-	return cuda_status(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)),
+	cudaFuncAttributes attr{};
+	int rc = cuda_status(cudaFuncGetAttributes(&attr, k), "cudaFuncGetAttributes");
+	if (rc) return rc;
+	const size_t room = prop.sharedMemPerBlockOptin - attr.sharedSizeBytes;   // static shared memory counts too
+	if (smem > room) return set_error(NLC_EUNSUPPORTED, "chain_length too large for the shared-memory kernels");
+	return cuda_status(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(room)),
 	                   "cudaFuncSetAttribute");
 }
 
@@ -426,7 +436,7 @@ extern "C" int nlc_plan_create(const nlc_model *model, nlc_plan **out) {
 		if (P->dnls_smem > size_t(P->prop.sharedMemPerBlockOptin))
 			return set_error(NLC_EUNSUPPORTED, "chain_length too large for the shared-memory DNLS integrator");
 		const void *k = dnls_kernel_ptr(P->dnls_team_block);
-		if ((rc = set_smem_attr(k, P->dnls_smem))) return rc;
+		if ((rc = set_smem_attr(k, P->dnls_smem, P->prop))) return rc;
 		int per_sm = 0;
 		if ((rc = cuda_status(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, P->dnls_threads, P->dnls_smem),
 		                      "occupancy")))
@@ -491,7 +501,7 @@ extern "C" int nlc_plan_create(const nlc_model *model, nlc_plan **out) {
 	if ((rc = setup_diagnostics(*P))) return rc;
 	{
 		const void *k = lin_kernel_ptr(mdl, P->diag_team_block);
-		if ((rc = set_smem_attr(k, P->diag_smem))) return rc;
+		if ((rc = set_smem_attr(k, P->diag_smem, P->prop))) return rc;
 	}
 	*out = P.release();
 	return NLC_OK;
@@ -592,7 +602,7 @@ extern "C" int nlc_fp64_peak(double ms, double *tflops) {
 	cudaEventCreate(&e1);
 	int iters = 1000;
 	float t = 0;
-	// grow the loop until one launch lasts about `ms`
+	// grow the loop until one launch lasts about `ms` (this also brings the clocks up)
 	for (int rep = 0; rep < 12; rep++) {
 		cudaEventRecord(e0);
 		launch_fp64_probe(out, blocks, threads, iters, 0);
@@ -602,6 +612,17 @@ extern "C" int nlc_fp64_peak(double ms, double *tflops) {
 		if (t >= ms * 0.8) break;
 		iters = int(std::min(1e8, iters * std::max(2.0, ms / std::max(t, 0.01f))));
 	}
+	// best of three timed launches at that size
+	float best = t;
+	for (int rep = 0; rep < 3 && !rc; rep++) {
+		cudaEventRecord(e0);
+		launch_fp64_probe(out, blocks, threads, iters, 0);
+		cudaEventRecord(e1);
+		if ((rc = cuda_status(cudaEventSynchronize(e1), "fp64 probe"))) break;
+		cudaEventElapsedTime(&t, e0, e1);
+		best = std::min(best, t);
+	}
+	t = best;
 	if (!rc) *tflops = double(blocks) * threads * iters * 8 * 2 / (t * 1e-3) / 1e12;
 	cudaEventDestroy(e0);
 	cudaEventDestroy(e1);

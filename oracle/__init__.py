@@ -138,7 +138,7 @@ def entropies(lin, a0is0_flag, mask=None):
         mask = np.ascontiguousarray(mask, dtype=np.uint8)
         mp = mask.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8))
     if _lib().nlo_entropies(_dp(lin), lin.size, int(a0is0_flag), mp, ctypes.byref(wt), ctypes.byref(inf)) != 0:
-        raise ValueError("too few modes for entropy")
+        raise ValueError("nlo_entropies rejected its arguments")
     return wt.value, inf.value
 
 

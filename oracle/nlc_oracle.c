@@ -96,7 +96,7 @@ void nlo_exp_table(double scale, double table[256]) {
 	}
 }
 
-/* The exact FP64 sequence of the device exp (see csrc/nlc_math.cuh). */
+/* The exact FP64 sequence of the device exp (nlchains_gb300/csrc/nlc_device.cuh, exp_scaled). */
 double nlo_exp_scaled(double x, const double table[256]) {
 	const double shifter = 0x1.8p52, inv_l = 256. / 0x1.62e42fefa39efp-1;
 	const double l1 = 0x1.62e42fefa39efp-9, l2 = 0x1.abc9e3b39803fp-64;
@@ -196,7 +196,7 @@ static void move_chain_reference(const nlo_model *M, const consts *K, double *re
 	for (uint32_t s = 0; s < n; s++) phi[s + 1] += K->dtc[7] * pi[s];
 }
 
-/* One launch of `batching` steps on one chain in the device operation order (csrc/nlc_real.cu):
+/* One launch of `batching` steps on one chain in the device operation order (nlchains_gb300/csrc/nlc_real.cuh):
  *   drift   q = fma(cd, p, q)
  *   DNKG    t = fma(beta*c, c, mp2); u = fma(c, t, -l); v = u - r; p = fma(-ck, v, p)
  *   FPUT    bond d = q[s+1]-q[s]; g = d*fma(fma(beta, d, alpha), d, 1); p = fma(ck, g[s]-g[s-1], p)
@@ -487,7 +487,7 @@ int nlo_entropies(const double *e, uint32_t n, int a0is0, const uint8_t *mask, d
 		totale += x, totalloge += lx, totaleloge += x * lx;
 		modes++;
 	}
-	if (modes < 2) return -1;
+	/* like results::calc_entropies, any mode count is accepted (the < 2 check is the mask's) */
 	double normalization = modes / totale, lognormalization = log(normalization);
 	*wt = -(totalloge + modes * lognormalization);
 	*inf = normalization * (totaleloge + lognormalization * totale);
