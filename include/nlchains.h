@@ -115,6 +115,25 @@ int nlc_move(nlc_plan *plan, void *state_dev, uint32_t steps, void *stream);
 int nlc_linenergies(nlc_plan *plan, const void *state_dev, double *lin_dev, double *entropies_dev,
                     void *stream);
 
+/*
+ * Allocation-free variant of nlc_linenergies, for callers that cannot allocate device memory when
+ * they need the diagnostics: a thread recording a CUDA graph (cudaMalloc is refused during stream
+ * capture), an application whose device memory is owned by its own pool or framework allocator,
+ * or a service that reserves all memory at start-up.  No counterpart in the reference (which
+ * allocates its FFT buffers, plans and work areas up front).
+ *
+ * Inputs and outputs are the caller's: state_dev (reference layout), an optional device mask of
+ * chain_length bytes (NULL = all modes; it must select at least two modes), lin_dev[chain_length]
+ * and entropies_dev[2] (may be NULL), all device memory, ordered on `stream`.  Models DNKG (m is
+ * its -m), FPUT, Toda (m ignored) and DNLS; chain_length <= 4096, larger sizes are rejected with
+ * NLC_EINVAL.  Nothing is allocated: every temporary lives in one 4 MiB static device array that
+ * each GPU loading the library holds until exit.  The first call on a device looks up that array's
+ * device address and sets kernel attributes, so make the first call before any stream capture.
+ * All calls share the array: calls that overlap on the GPU race and must be ordered by the caller.
+ */
+int nlc_linenergies_noalloc(int32_t model, uint32_t chain_length, uint32_t copies, double m, const void *state_dev,
+                            const uint8_t *entropy_mask_dev, double *lin_dev, double *entropies_dev, void *stream);
+
 /* DNLS elementwise operators with the reference's semantics (DNLS.hpp:16-20, DNLS.cu:11-43), for
  * callers that drive their own FFTs: psi *= exp(-i coef |psi|^2); psi_k *= table[k % n]. */
 int nlc_dnls_evolve_nonlinear(nlc_plan *plan, void *psi_dev, double beta_dt_symplectic, void *stream);

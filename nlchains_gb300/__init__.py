@@ -34,7 +34,7 @@ EXPORTS = (
     "nlc_dnls_evolve_linear", "nlc_plan_shape", "nlc_plan_omegas", "nlc_create", "nlc_destroy",
     "nlc_job_create", "nlc_job_destroy", "nlc_job_upload", "nlc_job_advance", "nlc_job_linenergies",
     "nlc_job_download", "nlc_job_wait", "nlc_job_state_ptr", "nlc_program_run", "nlc_last_error",
-    "nlc_version", "nlc_kernel_launches", "nlc_fp64_peak",
+    "nlc_version", "nlc_kernel_launches", "nlc_fp64_peak", "nlc_linenergies_noalloc",
 )
 
 
@@ -94,6 +94,7 @@ def lib():
         "nlc_version": ([], ctypes.c_char_p),
         "nlc_kernel_launches": ([], u64),
         "nlc_fp64_peak": ([ctypes.c_double, dp], i32),
+        "nlc_linenergies_noalloc": ([i32, u32, u32, ctypes.c_double, vp, vp, vp, vp, vp], i32),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -263,6 +264,14 @@ class Job:
         p = ctypes.c_void_p()
         _check(lib().nlc_job_state_ptr(self.ctx._h, self.id, ctypes.byref(p)))
         return p.value
+
+
+def linenergies_noalloc(model, chain_length, copies, m, state_ptr, lin_ptr, entropies_ptr=0, mask_ptr=0, stream=0):
+    """nlc_linenergies_noalloc on caller device pointers (no device allocation inside)."""
+    mid = MODELS[model] if isinstance(model, str) else int(model)
+    _check(lib().nlc_linenergies_noalloc(mid, chain_length, copies, m, ctypes.c_void_p(state_ptr),
+                                         ctypes.c_void_p(mask_ptr or None), ctypes.c_void_p(lin_ptr),
+                                         ctypes.c_void_p(entropies_ptr or None), ctypes.c_void_p(stream)))
 
 
 def run_program(argv):
