@@ -40,13 +40,32 @@ WORKLOAD = dict(name="DNKG N=128 copies=65536 (register-resident tier)", model="
                 dt=0.05, params=dict(m=1.0, beta=1.0), batching=100, eps=0.5, fraction=0.08, include_zero=True)
 TODA = dict(name="Toda N=128 copies=65536", model="Toda", n=128, copies=65536, dt=0.05,
             params=dict(alpha=0.5), batching=100, eps=0.5, fraction=0.08, include_zero=False)
-FLOPS_PER_SITE_STEP = {"DNKG": 70, "dDNKG": 70, "FPUT": 91, "Toda": 56}
+FLOPS_PER_SITE_STEP = {"DNKG": 70, "dDNKG": 70, "FPUT": 91, "Toda": 56, "DNLS": 812}
+# the other workloads of the reference's benchmark list, measured as secondary line items
+OTHERS = [
+    dict(name="FPUT-beta N=64 copies=1024 (small ensemble)", model="FPUT", n=64, copies=1024, dt=0.1,
+         params=dict(alpha=0.0, beta=1.0), batching=100, eps=0.1, kmax=4, include_zero=False),
+    dict(name="DNLS N=1024 copies=8192", model="DNLS", n=1024, copies=8192, dt=0.01, params=dict(beta=1.0),
+         batching=10, eps=1.0, fraction=0.1, include_zero=True),
+    dict(name="dDNKG N=256 copies=4096", model="dDNKG", n=256, copies=4096, dt=0.05, params=dict(beta=1.0),
+         batching=100, eps=0.5, nmodes=20, include_zero=True),
+]
 L2_FLUSH_BYTES = 256 << 20
+
+
+def masses(w):
+    from nlchains_gb300 import ic
+    return ic.masses_uniform(w["n"], seed=777) if w["model"] == "dDNKG" else None
 
 
 def initial_state(w, copies, first_copy, seed=12345):
     from nlchains_gb300 import ic
-    modes = ic.low_modes(w["n"], w["fraction"], include_zero=w["include_zero"])
+    if w["model"] == "dDNKG":
+        return ic.ddnkg_ensemble(masses(w), copies, w["eps"], w["nmodes"], seed=seed, first_copy=first_copy)
+    modes = ic.low_modes(w["n"], w.get("fraction"), kmax=w.get("kmax"), include_zero=w["include_zero"])
+    if w["model"] == "DNLS":
+        psi = ic.dnls_ensemble(w["n"], copies, w["eps"], modes, seed=seed, first_copy=first_copy)
+        return np.ascontiguousarray(psi).view(np.float64).reshape(copies, w["n"], 2)
     return ic.real_ensemble(w["n"], copies, w["eps"], modes, m=w["params"].get("m", 0.0), seed=seed,
                             first_copy=first_copy)
 
@@ -136,7 +155,7 @@ def measure_engine(w, steps, warmup, rank, world, local):
     nlc.lib()
     n, copies, b = w["n"], w["copies"], w["batching"]
     state = initial_state(w, copies, first_copy=rank * copies)
-    model = nlc.Model(w["model"], n, copies, w["dt"], **w["params"])
+    model = nlc.Model(w["model"], n, copies, w["dt"], masses=masses(w), **w["params"])
     plan = nlc.Plan(model)
     stream = torch.cuda.current_stream()
     sp = stream.cuda_stream
@@ -217,6 +236,97 @@ def measure_e2e(w, steps, warmup, rank, local):
     return dict(value=float(n) * copies * b * steps / t, h2d=bi, d2h=bo)
 
 
+SERVED_PARAMS = {"FPUT": (0.1, dict(alpha=0.0, beta=1.0)), "Toda": (0.05, dict(alpha=0.5)),
+                 "DNKG": (0.05, dict(m=1.0, beta=1.0)), "dDNKG": (0.05, dict(beta=1.0)), "DNLS": (0.01, dict(beta=1.0))}
+
+
+def served_stream(count=48, seed=2024, n_range=(32, 1024), copies_range=(64, 4096), steps_range=(100, 2000),
+                  batching=100, mean_gap_ms=15.0):
+    """A seeded mixed request stream: model uniform over the five, chain length, copies and steps
+    log-uniform, energy density U[0.1, 1], Poisson arrivals (the reference's served mix scaled to a
+    bench run: N <= 1024, copies <= 4096, steps <= 2000)."""
+    from nlchains_gb300 import ic
+    rng = np.random.default_rng(seed)
+    names = ["FPUT", "Toda", "DNKG", "dDNKG", "DNLS"]
+    reqs, t = [], 0.0
+    for i in range(count):
+        name = names[rng.integers(len(names))]
+        n = int(round(np.exp(rng.uniform(*np.log(n_range)))))
+        copies = int(round(np.exp(rng.uniform(*np.log(copies_range)))))
+        steps = max(batching, int(round(np.exp(rng.uniform(*np.log(steps_range))) / batching)) * batching)
+        eps = rng.uniform(0.1, 1.0)
+        dt, params = SERVED_PARAMS[name]
+        masses = ic.masses_uniform(n, seed=seed + i) if name == "dDNKG" else None
+        if name == "DNLS":
+            st = np.ascontiguousarray(ic.dnls_ensemble(n, copies, eps, ic.low_modes(n, 0.1), seed=seed + i))
+            st = st.view(np.float64).reshape(copies, n, 2)
+        elif name == "dDNKG":
+            st = ic.ddnkg_ensemble(masses, copies, eps, max(1, n // 10), seed=seed + i)
+        else:
+            st = ic.real_ensemble(n, copies, eps, ic.low_modes(n, 0.1, include_zero=params.get("m", 0) > 0),
+                                  m=params.get("m", 0.0), seed=seed + i)
+        t += rng.exponential(mean_gap_ms)
+        reqs.append(dict(name=name, n=n, copies=copies, steps=steps, b=batching, dt=dt, params=params,
+                         masses=masses, state=st, arrival_ms=t))
+    return reqs
+
+
+def measure_served(local):
+    """Continuous batching (nlc_server) against the same requests run alone, one after the other."""
+    import nlchains_gb300 as nlc
+    reqs = served_stream()
+    site_steps = sum(float(r["n"]) * r["copies"] * r["steps"] for r in reqs)
+
+    def model(r):
+        return nlc.Model(r["name"], r["n"], r["copies"], r["dt"], masses=r["masses"], **r["params"])
+
+    # warm the plans' code paths once
+    srv = nlc.Server(local)
+    w = reqs[0]
+    srv.wait(srv.submit(model(w), w["b"], w["b"], w["state"]), 120000)
+    srv.close()
+
+    srv = nlc.Server(local)
+    ids = []
+    t0 = time.perf_counter()
+    for r in reqs:
+        delay = r["arrival_ms"] / 1e3 - (time.perf_counter() - t0)
+        if delay > 0:
+            time.sleep(delay)
+        ids.append(srv.submit(model(r), r["b"], r["steps"], r["state"]))
+    lat = []
+    for rid in ids:
+        srv.wait(rid, 600000)
+        st = srv.poll(rid)
+        lat.append(st["finish_ms"] - st["submit_ms"])
+        srv.result(rid)
+    makespan = time.perf_counter() - t0
+    srv.close()
+
+    # the same requests alone: one ensemble at a time through the job API (plain per-model path)
+    ctx = nlc.Context(local)
+    alone_s = 0.0
+    for r in reqs:
+        job = ctx.job(model(r), r["b"])
+        t1 = time.perf_counter()
+        job.upload(r["state"])
+        job.linenergies()
+        for _ in range(r["steps"] // r["b"]):
+            job.advance(r["b"])
+            job.linenergies()
+        job.download()
+        alone_s += time.perf_counter() - t1
+        job.close()
+    ctx.close()
+    return {"value": site_steps / makespan, "unit": "site-steps/s", "alone_value": site_steps / alone_s,
+            "speedup_vs_alone": alone_s / makespan, "p50_ms": float(np.percentile(lat, 50)),
+            "p99_ms": float(np.percentile(lat, 99)), "requests": len(reqs), "makespan_s": makespan,
+            "alone_s": alone_s,
+            "stream": "48 requests, model uniform over FPUT/Toda/DNKG/dDNKG/DNLS, N log-uniform [32, 1024], "
+                      "copies log-uniform [64, 4096], steps log-uniform [100, 2000] (multiples of 100), "
+                      "kernel_batching 100, Poisson arrivals (mean gap 15 ms), seed 2024"}
+
+
 def cpu_baseline(w, target_s=10.0, threads=None, sample_copies=None, steps_per_call=None):
     """The reference CPU algorithm (oracle port, reference arithmetic) on a bounded sample."""
     import oracle as O
@@ -243,7 +353,7 @@ def cpu_baseline(w, target_s=10.0, threads=None, sample_copies=None, steps_per_c
 def energy_drift(w, before, after):
     import oracle as O
     sel = slice(0, 2048)
-    mdl = O.Model(w["model"], w["n"], 2048, w["dt"], **w["params"])
+    mdl = O.Model(w["model"], w["n"], 2048, w["dt"], masses=masses(w), **w["params"])
     e0 = O.energies(mdl, np.ascontiguousarray(before[sel]))
     e1 = O.energies(mdl, np.ascontiguousarray(after[sel]))
     return float(np.abs(e1 / e0 - 1).max())
@@ -274,6 +384,14 @@ def run_engine(args):
     r = measure_engine(w, args.steps, args.warmup, rank, world, local)
     e2e = measure_e2e(w, max(2, args.steps // 2), 1, rank, local)
     toda = measure_engine(TODA, max(2, args.steps // 2), 2, rank, world, local)
+    others = {}
+    for ow in OTHERS:
+        o = measure_engine(ow, max(3, args.steps // 2), 3, rank, world, local)
+        others[ow["model"]] = {"workload": ow["name"], "value": o["value"], "unit": "site-steps/s",
+                               "ms_per_step": o["step_ms"], "kernel_ms": o["move_ms"],
+                               "steps_per_launch": ow["batching"], "shape": o["shape"],
+                               "fp64_frac_of_peak": FLOPS_PER_SITE_STEP[ow["model"]] * ow["n"] * ow["copies"] *
+                               ow["batching"] / (o["move_ms"] * 1e-3) / 1e12 / peak}
     flops = FLOPS_PER_SITE_STEP[w["model"]] * w["n"] * w["copies"] * w["batching"]
     achieved = flops / (r["move_ms"] * 1e-3) / 1e12
     out = {
@@ -309,7 +427,10 @@ def run_engine(args):
                  "roofline_frac": FLOPS_PER_SITE_STEP["Toda"] * TODA["n"] * TODA["copies"] * TODA["batching"] /
                  (toda["move_ms"] * 1e-3) / 1e12 / peak, "kernel_ms": toda["move_ms"],
                  "shape": toda["shape"]},
+        "other_workloads": others,
     }
+    if world == 1:
+        out["served"] = measure_served(local)
     if rank == 0 and world == 1:
         out["cpu_baseline"] = cpu_baseline(w)
     if rank == 0:

@@ -54,8 +54,12 @@ enum {
 
 /* flags of nlc_model.flags */
 enum {
-	NLC_FLAG_SPLIT_KERNEL = 1, /* --split_kernel: force the streamed tier (DNKG_FPUT_Toda.cpp:43) */
-	NLC_FLAG_NO_TUNE = 2       /* skip the autotuner, use the heuristic launch shape */
+	NLC_FLAG_SPLIT_KERNEL = 1,    /* --split_kernel (DNKG_FPUT_Toda.cpp:43): accepted; every length up to
+	                                 16384 runs the resident integrator */
+	NLC_FLAG_NO_TUNE = 2,         /* skip the autotuner, use the heuristic launch shape */
+	NLC_FLAG_CANONICAL_SHAPE = 4, /* launch shape from the chain length alone (up to 8 sites per lane), so
+	                                 ensembles of equal length can share batched launches */
+	NLC_FLAG_COMPACT_DIAG = 8     /* fewer partial rows in the diagnostics (less device memory per plan) */
 };
 
 /*
@@ -172,6 +176,58 @@ int nlc_job_download(nlc_ctx *ctx, uint64_t job, void *host_state);
 int nlc_job_wait(nlc_ctx *ctx, uint64_t job, int32_t timeout_ms);
 /* device pointer of the job's state, for callers that mix levels 1 and 2 */
 int nlc_job_state_ptr(nlc_ctx *ctx, uint64_t job, void **state_dev);
+
+/* ---------------------------------------------------------------------------------------------
+ * Serving: continuous batching of ensemble-integration requests
+ * -------------------------------------------------------------------------------------------*/
+
+/*
+ * A request server on one GPU.  Requests (model, chain length, copies, kernel_batching, steps,
+ * initial state) are queued on submit and admitted while the HBM budget and the active-request
+ * limit allow.  Once admitted, a request's state stays on the device until it completes, and it
+ * advances in rounds of its own kernel_batching steps followed by one diagnostics sample, exactly as
+ * the reference's main loop does for one ensemble.  In every round, requests of the same kernel
+ * class (model, parameters, launch shape) are packed into one persistent batched launch, and
+ * different classes run concurrently on a stream pool.  When a request completes or blows up, its
+ * memory is released and queued requests are admitted (continuous batching).  Results are identical
+ * to running each request alone.  No counterpart in the reference, which runs one ensemble per
+ * process; it covers the served workload of the engine.
+ */
+typedef struct nlc_server nlc_server;
+
+typedef struct nlc_server_config {
+	int32_t device;              /* CUDA device */
+	uint64_t hbm_budget_bytes;   /* device memory for admitted requests (0 = 60% of free memory) */
+	int32_t max_active;          /* requests integrated at the same time (0 = 256) */
+	int32_t streams;             /* CUDA streams in the pool (0 = 8) */
+} nlc_server_config;
+
+enum { NLC_REQ_QUEUED = 0, NLC_REQ_RUNNING = 1, NLC_REQ_DONE = 2, NLC_REQ_FAILED = 3 };
+
+typedef struct nlc_request_status {
+	int32_t state;               /* NLC_REQ_* */
+	int32_t error;               /* status code of a failed request (NLC_EBLOWUP: non-finite entropy) */
+	uint64_t steps_done;
+	uint64_t samples;            /* diagnostics samples taken so far (t = 0 included) */
+	double submit_ms, start_ms, finish_ms;   /* server clock, ms since nlc_server_create */
+} nlc_request_status;
+
+int nlc_server_create(const nlc_server_config *config, nlc_server **server);
+/* stops admitting, finishes or abandons running work (bounded wait), frees everything */
+int nlc_server_destroy(nlc_server *server);
+/* queue a request; host_state (reference layout) is copied before return */
+int nlc_server_submit(nlc_server *server, const nlc_model *model, uint32_t kernel_batching, uint64_t steps,
+                      const void *host_state, uint64_t *request);
+int nlc_server_poll(nlc_server *server, uint64_t request, nlc_request_status *status);   /* non-blocking */
+/* wait until the request is DONE or FAILED, at most timeout_ms (< 0: no limit); NLC_ETIMEDOUT otherwise */
+int nlc_server_wait(nlc_server *server, uint64_t request, int32_t timeout_ms);
+/*
+ * Results of a finished request, then forget it: final state (may be NULL), final linear energies
+ * lin[chain_length] (may be NULL), the entropy series {WT, INF} per sample (entropies[2 * samples],
+ * may be NULL; samples at t = 0, b, 2b, ...) and the sample count.
+ */
+int nlc_server_result(nlc_server *server, uint64_t request, void *host_state, double *lin, double *entropies,
+                      uint64_t *samples);
 
 /* ---------------------------------------------------------------------------------------------
  * Level 3: the reference command line

@@ -26,7 +26,8 @@ MODELS = {"DNKG": DNKG, "FPUT": FPUT, "Toda": TODA, "dDNKG": DDNKG, "DNLS": DNLS
 MODEL_NAMES = {v: k for k, v in MODELS.items()}
 
 OK, EINVAL, ECUDA, ENOMEM, EIO, ETIMEDOUT, ENOTFOUND, EBLOWUP, EUNSUPPORTED = 0, -1, -2, -3, -4, -5, -6, -7, -8
-FLAG_SPLIT_KERNEL, FLAG_NO_TUNE = 1, 2
+FLAG_SPLIT_KERNEL, FLAG_NO_TUNE, FLAG_CANONICAL_SHAPE, FLAG_COMPACT_DIAG = 1, 2, 4, 8
+REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_FAILED = 0, 1, 2, 3
 
 # the exported symbols, as declared in include/nlchains.h
 EXPORTS = (
@@ -35,6 +36,8 @@ EXPORTS = (
     "nlc_job_create", "nlc_job_destroy", "nlc_job_upload", "nlc_job_advance", "nlc_job_linenergies",
     "nlc_job_download", "nlc_job_wait", "nlc_job_state_ptr", "nlc_program_run", "nlc_last_error",
     "nlc_version", "nlc_kernel_launches", "nlc_fp64_peak", "nlc_linenergies_noalloc",
+    "nlc_server_create", "nlc_server_destroy", "nlc_server_submit", "nlc_server_poll", "nlc_server_wait",
+    "nlc_server_result",
 )
 
 
@@ -49,6 +52,17 @@ class _CModel(ctypes.Structure):
                 ("dt", ctypes.c_double), ("m", ctypes.c_double), ("alpha", ctypes.c_double),
                 ("beta", ctypes.c_double), ("masses", ctypes.POINTER(ctypes.c_double)),
                 ("entropy_mask", ctypes.POINTER(ctypes.c_uint8)), ("flags", ctypes.c_uint32)]
+
+
+class _CServerConfig(ctypes.Structure):
+    _fields_ = [("device", ctypes.c_int32), ("hbm_budget_bytes", ctypes.c_uint64), ("max_active", ctypes.c_int32),
+                ("streams", ctypes.c_int32)]
+
+
+class _CRequestStatus(ctypes.Structure):
+    _fields_ = [("state", ctypes.c_int32), ("error", ctypes.c_int32), ("steps_done", ctypes.c_uint64),
+                ("samples", ctypes.c_uint64), ("submit_ms", ctypes.c_double), ("start_ms", ctypes.c_double),
+                ("finish_ms", ctypes.c_double)]
 
 
 _lib = None
@@ -95,6 +109,12 @@ def lib():
         "nlc_kernel_launches": ([], u64),
         "nlc_fp64_peak": ([ctypes.c_double, dp], i32),
         "nlc_linenergies_noalloc": ([i32, u32, u32, ctypes.c_double, vp, vp, vp, vp, vp], i32),
+        "nlc_server_create": ([P(_CServerConfig), P(vp)], i32),
+        "nlc_server_destroy": ([vp], i32),
+        "nlc_server_submit": ([vp, P(_CModel), u32, u64, vp, P(u64)], i32),
+        "nlc_server_poll": ([vp, u64, P(_CRequestStatus)], i32),
+        "nlc_server_wait": ([vp, u64, i32], i32),
+        "nlc_server_result": ([vp, u64, vp, dp, dp, P(u64)], i32),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -272,6 +292,60 @@ def linenergies_noalloc(model, chain_length, copies, m, state_ptr, lin_ptr, entr
     _check(lib().nlc_linenergies_noalloc(mid, chain_length, copies, m, ctypes.c_void_p(state_ptr),
                                          ctypes.c_void_p(mask_ptr or None), ctypes.c_void_p(lin_ptr),
                                          ctypes.c_void_p(entropies_ptr or None), ctypes.c_void_p(stream)))
+
+
+class Server:
+    """Continuous-batching request server on one GPU (nlc_server_* in include/nlchains.h)."""
+
+    def __init__(self, device=0, hbm_budget_bytes=0, max_active=0, streams=0):
+        cfg = _CServerConfig(device, hbm_budget_bytes, max_active, streams)
+        self._h = ctypes.c_void_p()
+        _check(lib().nlc_server_create(ctypes.byref(cfg), ctypes.byref(self._h)))
+        self._models = {}
+
+    def close(self):
+        if self._h:
+            lib().nlc_server_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def submit(self, model, kernel_batching, steps, state):
+        state = np.ascontiguousarray(state, dtype=np.float64)
+        assert state.size == 2 * model.chain_length * model.copies
+        c = model.c_struct()
+        rid = ctypes.c_uint64()
+        _check(lib().nlc_server_submit(self._h, ctypes.byref(c), int(kernel_batching), int(steps),
+                                       state.ctypes.data_as(ctypes.c_void_p), ctypes.byref(rid)))
+        self._models[rid.value] = (model, int(steps), int(kernel_batching))
+        return rid.value
+
+    def poll(self, rid):
+        st = _CRequestStatus()
+        _check(lib().nlc_server_poll(self._h, rid, ctypes.byref(st)))
+        return {"state": st.state, "error": st.error, "steps_done": st.steps_done, "samples": st.samples,
+                "submit_ms": st.submit_ms, "start_ms": st.start_ms, "finish_ms": st.finish_ms}
+
+    def wait(self, rid, timeout_ms=-1):
+        _check(lib().nlc_server_wait(self._h, rid, int(timeout_ms)))
+
+    def result(self, rid):
+        """(final state, final linenergies, entropies[samples, 2], error code); forgets the request."""
+        model, steps, b = self._models.pop(rid)
+        state = np.empty((model.copies, model.chain_length, 2))
+        lin = np.zeros(model.chain_length)
+        ent = np.zeros(2 * (steps // b + 1))
+        ns = ctypes.c_uint64()
+        rc = lib().nlc_server_result(self._h, rid, state.ctypes.data_as(ctypes.c_void_p),
+                                     lin.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                     ent.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), ctypes.byref(ns))
+        if rc not in (OK, EBLOWUP):
+            _check(rc)
+        return state, lin, ent[:2 * ns.value].reshape(-1, 2), rc
 
 
 def run_program(argv):

@@ -23,7 +23,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU_SOURCES = ["nlc_real_dnkg.cu", "nlc_real_fput.cu", "nlc_real_toda.cu", "nlc_real_ddnkg.cu",
               "nlc_diag.cu", "nlc_dnls.cu", "nlc_noalloc.cu"]
-CPP_SOURCES = ["nlc_plan.cpp", "nlc_tables.cpp", "nlc_job.cpp"]
+CPP_SOURCES = ["nlc_plan.cpp", "nlc_tables.cpp", "nlc_job.cpp", "nlc_server.cpp"]
 HEADERS = ["nlc_device.cuh", "nlc_real.cuh", "nlc_fft.cuh", "nlc_internal.h", "nlc_host.h"]
 
 
@@ -63,7 +63,7 @@ def build(verbose=False):
         raise RuntimeError("compilation failed: " + ", ".join(failed))
     if _newer(LIB, objs):
         tmp = LIB + ".tmp"
-        cmd = [NVCC, "-shared", *ARCH, "-Xcompiler", "-fPIC", "-o", tmp, *objs]
+        cmd = [NVCC, "-shared", *ARCH, "-Xcompiler", "-fPIC", "-o", tmp, *objs, "-lpthread"]
         if verbose:
             print(" ".join(cmd), flush=True)
         subprocess.check_call(cmd)

@@ -11,6 +11,8 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "nlc_internal.h"
+
 namespace nlc {
 
 __device__ __forceinline__ double dfma(double a, double b, double c) { return __fma_rn(a, b, c); }
@@ -18,27 +20,37 @@ __device__ __forceinline__ double dadd(double a, double b) { return __dadd_rn(a,
 __device__ __forceinline__ double dsub(double a, double b) { return __dsub_rn(a, b); }
 __device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a, b); }
 
+// On GB300 the FP64 pipe issues DFMA at 600 G lane-ops/s but DADD / DMUL at 506 G (measured with
+// runtime operands, independent of the values).  Adds, subtractions and multiplications on the hot
+// paths are therefore issued as FMAs with the exact same result: a + b = fma(a, 1, b),
+// a - b = fma(b, -1, a), a * b = fma(a, b, -0) (the -0 addend keeps the sign of a zero product).
+// The constants reach the kernels as parameters (FpOnes in nlc_internal.h), so the compiler cannot
+// fold them back into DADD / DMUL, and they are parameter-bank operands rather than registers.
+__device__ __forceinline__ double fadd(double a, double b, const FpOnes &k) { return __fma_rn(a, k.one, b); }
+__device__ __forceinline__ double fsub(double a, double b, const FpOnes &k) { return __fma_rn(b, k.mone, a); }
+__device__ __forceinline__ double fmul(double a, double b, const FpOnes &k) { return __fma_rn(a, b, k.mzero); }
+
 // Table-driven exp (Tang, ACM TOMS 15(2) 1989): x = (n/256) ln2 + r, |r| <= ln2/512,
 // scale*exp(x) = 2^(n>>8) * T[n&255] * (1 + r + r^2/2 + r^3/6 + r^4/24), T[j] = scale * 2^(j/256).
-// Nine FP64 operations on the fast path against ~22 DFMA-equivalents for the library exp.  The
+// Nine FP64 operations (all issued as FMAs) on the fast path against ~22 DFMA-equivalents for the
+// library exp.  The
 // range checks use the integer high word of x, which costs no FP64 issue slot.
-__device__ __forceinline__ double exp_scaled(double x, const double *__restrict__ table) {
-	const double shifter = 0x1.8p52, inv_l = 256. / 0x1.62e42fefa39efp-1;
-	const double l1 = 0x1.62e42fefa39efp-9, l2 = 0x1.abc9e3b39803fp-64;
+__device__ __forceinline__ double exp_scaled(double x, const double *__restrict__ table, const FpOnes &k1,
+                                             const ExpConsts &c) {
 	const int hi = __double2hiint(x);
 	if ((hi & 0x7fffffff) >= 0x40f00000) {   // |x| >= 65536, inf or NaN
 		if (x != x) return x;
 		return hi > 0 ? dmul(table[0], __longlong_as_double(0x7ff0000000000000LL)) : dmul(table[0], 0.);
 	}
-	const double t = dfma(x, inv_l, shifter);
+	const double t = dfma(x, c.inv_l, c.shifter);
 	const int n = __double2loint(t);
-	const double nf = dsub(t, shifter);
-	double r = dfma(-nf, l1, x);
-	r = dfma(-nf, l2, r);
-	double q = dfma(r, 1. / 24, 1. / 6);
-	q = dfma(q, r, 0.5);
-	q = dfma(q, r, 1.);
-	const double p = dmul(q, r);
+	const double nf = fsub(t, c.shifter, k1);
+	double r = dfma(-nf, c.l1, x);
+	r = dfma(-nf, c.l2, r);
+	double q = dfma(r, c.c4, c.c3);
+	q = dfma(q, r, c.c2);
+	q = dfma(q, r, k1.one);
+	const double p = fmul(q, r, k1);
 	const double tj = table[n & 255];
 	double v = dfma(tj, p, tj);
 	const int k = n >> 8;

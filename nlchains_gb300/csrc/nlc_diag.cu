@@ -29,11 +29,13 @@ __global__ void lin_fft_kernel(const double2 *__restrict__ state, const DiagArgs
 	const int t = BLOCK ? threadIdx.x : (threadIdx.x & 31);
 	const int team = BLOCK ? 0 : (threadIdx.x >> 5);
 	const int teams = BLOCK ? 1 : (blockDim.x >> 5);
-	double2 *x = sm + (size_t) team * 2 * n, *y = x + n;
+	const int len = a.fft.len;
+	double2 *x = sm + (size_t) team * 2 * len, *y = x + len;
 	double *acc = a.partials + ((size_t) blockIdx.x * teams + team) * n;
 	for (int k = t; k < n; k += T) acc[k] = 0.;
 
 	const bool dnls = a.model == NLC_DNLS;
+	const FpOnes &k1 = a.fft.k1;
 	for (unsigned long long chain = (unsigned long long) blockIdx.x * teams + team; chain < a.copies;
 	     chain += (unsigned long long) gridDim.x * teams) {
 		const double2 *src = state + chain * (unsigned long long) n;
@@ -43,15 +45,15 @@ __global__ void lin_fft_kernel(const double2 *__restrict__ state, const DiagArgs
 		if (dnls) {
 			for (int k = t; k < n; k += T) {
 				const double2 z = Z[k];
-				acc[k] = dadd(acc[k], dfma(z.x, z.x, dmul(z.y, z.y)));
+				acc[k] = fadd(acc[k], dfma(z.x, z.x, fmul(z.y, z.y, k1)), k1);
 			}
 		} else {
 			for (int k = t; k < n; k += T) {
 				const double2 zk = Z[k], zm = Z[k ? n - k : 0];
 				const double ak = a.coef_a[k], bk = a.coef_b[k];
-				const double re = dfma(ak, zk.x, dmul(bk, zm.x));
-				const double im = dfma(ak, zk.y, -dmul(bk, zm.y));
-				acc[k] = dadd(acc[k], dfma(re, re, dmul(im, im)));
+				const double re = dfma(ak, zk.x, fmul(bk, zm.x, k1));
+				const double im = dfma(ak, zk.y, -fmul(bk, zm.y, k1));
+				acc[k] = fadd(acc[k], dfma(re, re, fmul(im, im, k1)), k1);
 			}
 		}
 		team_sync<BLOCK>();
@@ -93,8 +95,8 @@ __global__ void lin_ddnkg_kernel(const double2 *__restrict__ state, const DiagAr
 			double s = acc[k];
 #pragma unroll
 			for (int c = 0; c < kProjChains; c++) {
-				const double v = dmul(om, dphi[c]);
-				s = dadd(s, dfma(v, v, dmul(dpi[c], dpi[c])));
+				const double v = fmul(om, dphi[c], a.fft.k1);
+				s = fadd(s, dfma(v, v, fmul(dpi[c], dpi[c], a.fft.k1)), a.fft.k1);
 			}
 			acc[k] = s;
 		}

@@ -15,11 +15,11 @@
 
 namespace nlc {
 
-__device__ __forceinline__ double2 nonlinear_rotate(double2 v, double neg_coef) {
-	const double norm = dfma(v.x, v.x, dmul(v.y, v.y));
+__device__ __forceinline__ double2 nonlinear_rotate(double2 v, double neg_coef, const FpOnes &k) {
+	const double norm = dfma(v.x, v.x, fmul(v.y, v.y, k));
 	double s, c;
-	sincos(dmul(neg_coef, norm), &s, &c);
-	return make_double2(dfma(v.x, c, -dmul(v.y, s)), dfma(v.x, s, dmul(v.y, c)));
+	sincos(fmul(neg_coef, norm, k), &s, &c);
+	return make_double2(dfma(v.x, c, -fmul(v.y, s, k)), dfma(v.x, s, fmul(v.y, c, k)));
 }
 
 template <bool BLOCK>
@@ -30,7 +30,8 @@ __global__ void dnls_move_kernel(double2 *__restrict__ psi, const DnlsArgs a) {
 	const int T = BLOCK ? blockDim.x : 32;
 	const int t = BLOCK ? threadIdx.x : (threadIdx.x & 31);
 	const int team = BLOCK ? 0 : (threadIdx.x >> 5);
-	double2 *buf0 = sm + (size_t) team * 2 * n, *buf1 = buf0 + n;
+	const int len = a.fft.len;
+	double2 *buf0 = sm + (size_t) team * 2 * len, *buf1 = buf0 + len;
 
 	for (;;) {
 		// team leader takes the next chain from the self-resetting counter
@@ -55,18 +56,18 @@ __global__ void dnls_move_kernel(double2 *__restrict__ psi, const DnlsArgs a) {
 		for (uint32_t i = 0; i < a.steps; i++) {
 			for (int k = 0; k < 7; k++) {
 				const double coef = (k == 0 && i != 0) ? a.nl[7] : a.nl[k];
-				for (int j = t; j < n; j += T) x[j] = nonlinear_rotate(x[j], -coef);
+				for (int j = t; j < n; j += T) x[j] = nonlinear_rotate(x[j], -coef, a.fft.k1);
 				team_sync<BLOCK>();
 				double2 *r = fft_team<BLOCK, false>(a.fft, x, y, t, T);
 				double2 *o = r == x ? y : x;
 				const double2 *tab = a.lin_tables + (size_t) k * n;
-				for (int j = t; j < n; j += T) r[j] = cmul(r[j], tab[j]);
+				for (int j = t; j < n; j += T) r[j] = cmul(r[j], tab[j], a.fft.k1);
 				team_sync<BLOCK>();
 				x = fft_team<BLOCK, true>(a.fft, r, o, t, T);
 				y = x == buf0 ? buf1 : buf0;
 			}
 		}
-		for (int j = t; j < n; j += T) g[j] = nonlinear_rotate(x[j], -a.nl_final);
+		for (int j = t; j < n; j += T) g[j] = nonlinear_rotate(x[j], -a.nl_final, a.fft.k1);
 		team_sync<BLOCK>();
 	}
 
@@ -92,20 +93,21 @@ cudaError_t launch_dnls_move(const DnlsArgs &a, double2 *psi, int blocks, int th
 
 // Elementwise operators with the reference's semantics (DNLS.cu:11-25), for callers that keep
 // their own FFT loop.
-__global__ void dnls_nonlinear_kernel(double2 *psi, unsigned long long elements, double neg_coef) {
+__global__ void dnls_nonlinear_kernel(double2 *psi, unsigned long long elements, double neg_coef, const FpOnes k) {
 	const unsigned long long i = (unsigned long long) blockIdx.x * blockDim.x + threadIdx.x;
-	if (i < elements) psi[i] = nonlinear_rotate(psi[i], neg_coef);
+	if (i < elements) psi[i] = nonlinear_rotate(psi[i], neg_coef, k);
 }
 
-__global__ void dnls_linear_kernel(double2 *psi, unsigned long long elements, uint32_t n, const double2 *table) {
+__global__ void dnls_linear_kernel(double2 *psi, unsigned long long elements, uint32_t n, const double2 *table,
+                                   const FpOnes k) {
 	const unsigned long long i = (unsigned long long) blockIdx.x * blockDim.x + threadIdx.x;
-	if (i < elements) psi[i] = cmul(psi[i], table[i % n]);
+	if (i < elements) psi[i] = cmul(psi[i], table[i % n], k);
 }
 
 cudaError_t launch_dnls_nonlinear(double2 *psi, uint64_t elements, double coef, cudaStream_t stream) {
 	count_launch();
 	const unsigned long long blocks = (elements + 255) / 256;
-	dnls_nonlinear_kernel<<<(unsigned) blocks, 256, 0, stream>>>(psi, elements, -coef);
+	dnls_nonlinear_kernel<<<(unsigned) blocks, 256, 0, stream>>>(psi, elements, -coef, FpOnes{});
 	return cudaGetLastError();
 }
 
@@ -113,7 +115,7 @@ cudaError_t launch_dnls_linear(double2 *psi, uint64_t elements, uint32_t n, cons
                                cudaStream_t stream) {
 	count_launch();
 	const unsigned long long blocks = (elements + 255) / 256;
-	dnls_linear_kernel<<<(unsigned) blocks, 256, 0, stream>>>(psi, elements, n, table);
+	dnls_linear_kernel<<<(unsigned) blocks, 256, 0, stream>>>(psi, elements, n, table, FpOnes{});
 	return cudaGetLastError();
 }
 

@@ -23,11 +23,16 @@ __device__ __forceinline__ void team_sync() {
 	else __syncwarp();
 }
 
-__device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_double2(dadd(a.x, b.x), dadd(a.y, b.y)); }
-__device__ __forceinline__ double2 csub(double2 a, double2 b) { return make_double2(dsub(a.x, b.x), dsub(a.y, b.y)); }
+// complex add / subtract / multiply, every FP64 operation issued as an FMA (nlc_device.cuh)
+__device__ __forceinline__ double2 cadd(double2 a, double2 b, const FpOnes &k) {
+	return make_double2(fadd(a.x, b.x, k), fadd(a.y, b.y, k));
+}
+__device__ __forceinline__ double2 csub(double2 a, double2 b, const FpOnes &k) {
+	return make_double2(fsub(a.x, b.x, k), fsub(a.y, b.y, k));
+}
 // a * w
-__device__ __forceinline__ double2 cmul(double2 a, double2 w) {
-	return make_double2(dfma(a.x, w.x, -dmul(a.y, w.y)), dfma(a.x, w.y, dmul(a.y, w.x)));
+__device__ __forceinline__ double2 cmul(double2 a, double2 w, const FpOnes &k) {
+	return make_double2(dfma(a.x, w.x, -fmul(a.y, w.y, k)), dfma(a.x, w.y, fmul(a.y, w.x, k)));
 }
 // twiddle exp(-+2 pi i e / n) from the forward table
 template <bool INV>
@@ -41,12 +46,13 @@ __device__ __forceinline__ double2 rot_mi(double2 a) {
 	return INV ? make_double2(-a.y, a.x) : make_double2(a.y, -a.x);
 }
 
-// In-place transform of one chain held in x (shared memory, n complex), y the ping-pong buffer.
-// t / T: this thread's index / size of the team.  Returns the buffer holding the result.
+// Stockham pass of length P.len on x (shared memory), y the ping-pong buffer.  t / T: this
+// thread's index / size of the team.  Returns the buffer holding the result.
 template <bool BLOCK, bool INV>
-__device__ double2 *fft_team(const FftPlanDev &P, double2 *x, double2 *y, int t, int T) {
-	const int n = P.n;
+__device__ double2 *stockham_team(const FftPlanDev &P, double2 *x, double2 *y, int t, int T) {
+	const int n = P.len;
 	const double2 *__restrict__ tw = P.tw;
+	const FpOnes &k = P.k1;
 	int L = n, s = 1;
 	for (int r = 0; r < P.nradix; r++) {
 		const int p = P.radix[r];
@@ -58,17 +64,17 @@ __device__ double2 *fft_team(const FftPlanDev &P, double2 *x, double2 *y, int t,
 				const int q = b / s, tt = b - q * s;
 				const double2 a0 = x[tt + s * q], a1 = x[tt + s * (q + m)], a2 = x[tt + s * (q + 2 * m)],
 				              a3 = x[tt + s * (q + 3 * m)];
-				const double2 b0 = cadd(a0, a2), b1 = csub(a0, a2), b2 = cadd(a1, a3), b3 = rot_mi<INV>(csub(a1, a3));
+				const double2 b0 = cadd(a0, a2, k), b1 = csub(a0, a2, k), b2 = cadd(a1, a3, k), b3 = rot_mi<INV>(csub(a1, a3, k));
 				double2 *o = y + tt + s * 4 * q;
-				o[0] = cadd(b0, b2);
+				o[0] = cadd(b0, b2, k);
 				if (q == 0) {
-					o[s] = cadd(b1, b3);
-					o[2 * s] = csub(b0, b2);
-					o[3 * s] = csub(b1, b3);
+					o[s] = cadd(b1, b3, k);
+					o[2 * s] = csub(b0, b2, k);
+					o[3 * s] = csub(b1, b3, k);
 				} else {
-					o[s] = cmul(cadd(b1, b3), twiddle<INV>(tw, q * tws));
-					o[2 * s] = cmul(csub(b0, b2), twiddle<INV>(tw, 2 * q * tws));
-					o[3 * s] = cmul(csub(b1, b3), twiddle<INV>(tw, 3 * q * tws));
+					o[s] = cmul(cadd(b1, b3, k), twiddle<INV>(tw, q * tws), k);
+					o[2 * s] = cmul(csub(b0, b2, k), twiddle<INV>(tw, 2 * q * tws), k);
+					o[3 * s] = cmul(csub(b1, b3, k), twiddle<INV>(tw, 3 * q * tws), k);
 				}
 			}
 		} else if (p == 2) {
@@ -76,25 +82,27 @@ __device__ double2 *fft_team(const FftPlanDev &P, double2 *x, double2 *y, int t,
 				const int q = b / s, tt = b - q * s;
 				const double2 a0 = x[tt + s * q], a1 = x[tt + s * (q + m)];
 				double2 *o = y + tt + s * 2 * q;
-				o[0] = cadd(a0, a1);
-				o[s] = q == 0 ? csub(a0, a1) : cmul(csub(a0, a1), twiddle<INV>(tw, q * tws));
+				o[0] = cadd(a0, a1, k);
+				o[s] = q == 0 ? csub(a0, a1, k) : cmul(csub(a0, a1, k), twiddle<INV>(tw, q * tws), k);
 			}
 		} else if (p == 3) {
-			const double sn = 0.86602540378443864676;   // sin(2 pi / 3)
+			const double sn = P.sin60;   // sin(2 pi / 3), a parameter-bank operand
 			for (int b = t; b < nb; b += T) {
 				const int q = b / s, tt = b - q * s;
 				const double2 a0 = x[tt + s * q], a1 = x[tt + s * (q + m)], a2 = x[tt + s * (q + 2 * m)];
-				const double2 t1 = cadd(a1, a2);
-				const double2 t2 = make_double2(dfma(t1.x, -0.5, a0.x), dfma(t1.y, -0.5, a0.y));
-				const double2 d = csub(a1, a2);
-				const double2 u = make_double2(dmul(sn, d.x), dmul(sn, d.y));
+				const double2 t1 = cadd(a1, a2, k);
+				const double2 t2 = make_double2(dfma(t1.x, -P.half, a0.x), dfma(t1.y, -P.half, a0.y));
+				const double2 d = csub(a1, a2, k);
+				const double2 u = make_double2(fmul(sn, d.x, k), fmul(sn, d.y, k));
 				// forward: X1 = t2 - i u, X2 = t2 + i u
-				const double2 x1 = INV ? make_double2(dsub(t2.x, u.y), dadd(t2.y, u.x)) : make_double2(dadd(t2.x, u.y), dsub(t2.y, u.x));
-				const double2 x2 = INV ? make_double2(dadd(t2.x, u.y), dsub(t2.y, u.x)) : make_double2(dsub(t2.x, u.y), dadd(t2.y, u.x));
+				const double2 x1 = INV ? make_double2(fsub(t2.x, u.y, k), fadd(t2.y, u.x, k))
+				                       : make_double2(fadd(t2.x, u.y, k), fsub(t2.y, u.x, k));
+				const double2 x2 = INV ? make_double2(fadd(t2.x, u.y, k), fsub(t2.y, u.x, k))
+				                       : make_double2(fsub(t2.x, u.y, k), fadd(t2.y, u.x, k));
 				double2 *o = y + tt + s * 3 * q;
-				o[0] = cadd(a0, t1);
-				o[s] = q == 0 ? x1 : cmul(x1, twiddle<INV>(tw, q * tws));
-				o[2 * s] = q == 0 ? x2 : cmul(x2, twiddle<INV>(tw, 2 * q * tws));
+				o[0] = cadd(a0, t1, k);
+				o[s] = q == 0 ? x1 : cmul(x1, twiddle<INV>(tw, q * tws), k);
+				o[2 * s] = q == 0 ? x2 : cmul(x2, twiddle<INV>(tw, 2 * q * tws), k);
 			}
 		} else {
 			// direct p-point DFT: X_v = sum_u a_u W_p^{uv}, W_p^e = tw[(e mod p) n/p]
@@ -110,7 +118,7 @@ __device__ double2 *fft_team(const FftPlanDev &P, double2 *x, double2 *y, int t,
 						im = dfma(a.x, w.y, dfma(a.y, w.x, im));
 					}
 					double2 out = make_double2(re, im);
-					if (q != 0 && v != 0) out = cmul(out, twiddle<INV>(tw, q * v * tws));
+					if (q != 0 && v != 0) out = cmul(out, twiddle<INV>(tw, q * v * tws), k);
 					y[tt + s * (p * q + v)] = out;
 				}
 			}
@@ -121,6 +129,42 @@ __device__ double2 *fft_team(const FftPlanDev &P, double2 *x, double2 *y, int t,
 		L = m, s *= p;
 	}
 	return x;
+}
+
+__device__ __forceinline__ double2 conj2(double2 a) { return make_double2(a.x, -a.y); }
+
+// Transform of one chain of length P.n held in x[0, n); x and y hold P.len elements each.
+// Lengths with a prime factor above 47 go through Bluestein's chirp-z identity
+//   X_k = w_k sum_j (x_j w_j) conj(w)_{k-j},  w_j = exp(-i pi j^2 / n)
+// (L. Bluestein, IEEE Trans. Audio Electroacoust. 18, 1970), the convolution evaluated as a cyclic
+// convolution of smooth length m >= 2n - 1 by two Stockham passes; the backward transform uses the
+// conjugate chirp.  Returns the buffer holding X[0, n).
+template <bool BLOCK, bool INV>
+__device__ double2 *fft_team(const FftPlanDev &P, double2 *x, double2 *y, int t, int T) {
+	if (!P.bluestein) return stockham_team<BLOCK, INV>(P, x, y, t, T);
+	const int n = P.n, m = P.len;
+	const FpOnes &k = P.k1;
+	for (int j = t; j < m; j += T) {
+		if (j < n) {
+			const double2 w = P.chirp[j];
+			y[j] = cmul(x[j], INV ? conj2(w) : w, k);
+		} else {
+			y[j] = make_double2(0., 0.);
+		}
+	}
+	team_sync<BLOCK>();
+	double2 *r = stockham_team<BLOCK, false>(P, y, x, t, T);
+	double2 *o = r == y ? x : y;
+	const double2 *__restrict__ b = INV ? P.bi : P.bf;
+	for (int j = t; j < m; j += T) r[j] = cmul(r[j], b[j], k);
+	team_sync<BLOCK>();
+	double2 *c = stockham_team<BLOCK, true>(P, r, o, t, T);
+	for (int j = t; j < n; j += T) {
+		const double2 w = P.chirp[j];
+		c[j] = cmul(c[j], INV ? conj2(w) : w, k);
+	}
+	team_sync<BLOCK>();
+	return c;
 }
 
 }  // namespace nlc

@@ -31,6 +31,17 @@ std::vector<int> fft_radices(uint32_t n);
 // forward twiddles exp(-2 pi i e / n), e < n, interleaved re/im
 std::vector<double> fft_twiddles(uint32_t n);
 
+// Host tables of a chain FFT: Stockham radices/twiddles of the pass length, plus the Bluestein
+// chirp and convolution kernels when n has a prime factor above 47 and the convolution fits
+// max_len (the caller's shared-memory budget).
+struct FftTables {
+	uint32_t n = 0, len = 0;
+	bool bluestein = false;
+	std::vector<int> radices;
+	std::vector<double> tw, chirp, bf, bi;   // interleaved re/im
+};
+FftTables fft_tables(uint32_t n, uint32_t max_len);
+
 // Symmetric eigensystem of the periodic dDNKG operator diag(mp2) - shift(+-1) (eigensystem.cpp:
 // 15-18): ascending eigenvalues, omegas = sqrt(eigenvalues), eigenvectors column-major
 // (eigvec[k*n + s] = component s of eigenvector k), as Armadillo's eig_sym would return them.
@@ -38,5 +49,18 @@ std::vector<double> fft_twiddles(uint32_t n);
 // shifts (Golub and Van Loan, Matrix Computations, algorithms 8.3.1 and 8.3.3).
 bool eigensystem_periodic(const std::vector<double> &mp2, std::vector<double> &omegas,
                           std::vector<double> &eigvec);
+
+// What the request server needs to know about a plan (nlc_plan.cpp).
+struct PlanInfo {
+	int model = 0, variant = 0;
+	RealShape shape;
+	RealArgs args;          // integrator constants (device pointers included)
+	size_t device_bytes = 0;  // device memory held by the plan
+	int sms = 0;
+};
+bool plan_info(const nlc_plan *plan, PlanInfo *info);
+// a batched launch of the resident integrator (args.batch / nbatch / batch_units set)
+cudaError_t launch_real_move_batch(int model, int variant, const RealShape &shape, const RealArgs &args,
+                                   cudaStream_t stream);
 
 }  // namespace nlc

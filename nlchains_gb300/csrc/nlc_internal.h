@@ -10,8 +10,32 @@
 
 namespace nlc {
 
+// FP64 constants that reach the kernels as parameters rather than literals: on GB300 an FMA whose
+// constant operands come from the parameter bank issues faster than one with literal operands or
+// than DADD / DMUL, so the hot paths issue adds and products as FMAs with these (see nlc_device.cuh).
+struct FpOnes {
+	double one = 1., mone = -1., mzero = -0.;
+};
+// Constants of the table-driven exp (nlc_device.cuh exp_scaled).
+struct ExpConsts {
+	double shifter = 0x1.8p52;                    // 1.5 * 2^52: round-to-integer shifter
+	double inv_l = 256. / 0x1.62e42fefa39efp-1;   // 256 / ln 2
+	double l1 = 0x1.62e42fefa39efp-9;             // ln 2 / 256, leading part
+	double l2 = 0x1.abc9e3b39803fp-64;            // ln 2 / 256, trailing part
+	double c4 = 1. / 24, c3 = 1. / 6, c2 = 0.5;   // Taylor coefficients of exp(r) - 1 - r
+};
+
 constexpr int kMaxSitesPerLane = 16;   // E: sites of a chain held in registers by one thread
 constexpr int kMaxLanesPerChain = 1024;
+
+// One ensemble inside a batched launch of the resident integrator (device table, see RealArgs).
+struct BatchJob {
+	double2 *state;
+	const double *mp2_site;          // dDNKG per-site m_x + 2
+	unsigned long long unit_begin;   // first work unit of this ensemble in the launch
+	uint32_t n, copies, steps;
+	uint32_t pad;
+};
 
 // Kernel arguments of the real-model integrators, passed by value (kernel parameter bank).
 struct RealArgs {
@@ -30,6 +54,14 @@ struct RealArgs {
 	uint32_t copies;
 	uint32_t steps;
 	int32_t lanes;         // G: lanes per chain (power of two)
+	FpOnes k1;
+	ExpConsts ek;
+	// batched launch: when `batch` is set, the launch integrates every ensemble of the table (same
+	// model, constants, lanes and sites per lane; its own state, length, copies and step count);
+	// n / copies / steps / mp2_site above are then unused
+	const BatchJob *batch;
+	int32_t nbatch;
+	unsigned long long batch_units;
 };
 
 // Launch shape of the resident integrator.
@@ -53,11 +85,19 @@ const void *real_move_kernel(int model, int variant, int sites);
 
 constexpr int kMaxRadices = 24;
 
+// Device plan of the shared-memory FFT of one chain (nlc_fft.cuh).
 struct FftPlanDev {
-	int n;
+	int n;                 // transform length
+	int len;               // length of the Stockham pass: n, or the Bluestein convolution length m
 	int nradix;
-	int radix[kMaxRadices];
-	const double2 *tw;     // tw[e] = exp(-2 pi i e / n), device
+	int radix[kMaxRadices];  // radices of len
+	const double2 *tw;     // tw[e] = exp(-2 pi i e / len), device
+	int bluestein;         // 1: chirp-z transform through a length-m cyclic convolution
+	const double2 *chirp;  // exp(-i pi j^2 / n), j < n
+	const double2 *bf;     // FFT_m(b) / m, b_j = exp(+i pi j^2 / n) wrapped (forward transforms)
+	const double2 *bi;     // FFT_m(conj b) / m (backward transforms)
+	FpOnes k1;
+	double half = 0.5, sin60 = 0.86602540378443864676;   // radix-3 butterfly constants
 };
 
 struct DiagArgs {

@@ -134,6 +134,7 @@ extern "C" int nlc_linenergies_noalloc(int32_t model, uint32_t chain_length, uin
 	DiagArgs g{};
 	g.n = n, g.copies = copies, g.model = model;
 	g.fft.n = int(n);
+	g.fft.len = int(n);   // direct passes only: the static scratch holds no Bluestein tables
 	if (fill_radices(n, g.fft)) return set_error(NLC_EINVAL, "nlc_linenergies_noalloc: too many prime factors");
 	// scratch layout: [twiddles 2n][coef a n][coef b n][partial rows rows x n]
 	double *base = S->scratch;

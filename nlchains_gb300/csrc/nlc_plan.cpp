@@ -61,6 +61,21 @@ cudaError_t launch_real_move(int model, int variant, const RealShape &shape, dou
 	return cudaLaunchKernel(k, dim3(shape.blocks), dim3(shape.threads), params, shape.smem, stream);
 }
 
+cudaError_t launch_real_move_batch(int model, int variant, const RealShape &shape, const RealArgs &args,
+                                   cudaStream_t stream) {
+	const void *k = real_move_kernel(model, variant, shape.sites);
+	if (!k || shape.lanes < 1 || (shape.lanes & (shape.lanes - 1)) || shape.threads < 32 || shape.threads % 32 ||
+	    shape.threads % shape.lanes || (shape.lanes > 32 && shape.threads != shape.lanes) || shape.blocks < 1 ||
+	    !args.batch || args.nbatch < 1 || !args.batch_units)
+		return cudaErrorInvalidConfiguration;
+	double2 *st = nullptr;
+	RealArgs a = args;
+	a.lanes = shape.lanes;
+	void *params[] = {&st, &a};
+	count_launch();
+	return cudaLaunchKernel(k, dim3(shape.blocks), dim3(shape.threads), params, shape.smem, stream);
+}
+
 }  // namespace nlc
 
 using namespace nlc;
@@ -81,6 +96,7 @@ struct nlc_plan {
 
 	// device allocations, freed by the destructor
 	std::vector<void *> allocs;
+	size_t device_bytes = 0;
 	unsigned long long *d_counter = nullptr;
 	double *d_partials = nullptr;
 	uint8_t *d_mask = nullptr;
@@ -105,6 +121,7 @@ struct nlc_plan {
 		const cudaError_t e = cudaMalloc(&q, std::max<size_t>(count, 1) * sizeof(T));
 		if (e != cudaSuccess) return cuda_status(e, "cudaMalloc");
 		allocs.push_back(q);
+		device_bytes += std::max<size_t>(count, 1) * sizeof(T);
 		*p = static_cast<T *>(q);
 		return NLC_OK;
 	}
@@ -163,6 +180,17 @@ bool finish_shape(const nlc_plan &P, int model, int variant, RealShape &s, int t
 	s.smem = 0;
 	s.blocks = int(std::min<unsigned long long>(units, (unsigned long long) per_sm * P.prop.multiProcessorCount));
 	return s.blocks > 0;
+}
+
+// Canonical: the smallest group whose lanes hold at most 8 sites, from the chain length alone.
+RealShape canonical_shape(const nlc_plan &P, int model, int variant) {
+	for (auto c : shape_candidates(P.m.chain_length)) {
+		if (c.second > 8) continue;
+		RealShape s{};
+		s.lanes = c.first, s.sites = c.second;
+		if (finish_shape(P, model, variant, s, 128)) return s;
+	}
+	return RealShape{};
 }
 
 // Heuristic: fewest lanes per chain (largest E) that still gives every SM >= 8 warps of work,
@@ -256,16 +284,27 @@ RealShape autotune_shape(nlc_plan &P, int model, int variant) {
 
 int setup_fft(nlc_plan &P, FftPlanDev &f) {
 	const uint32_t n = P.m.chain_length;
-	const auto rad = fft_radices(n);
-	if (rad.size() > size_t(kMaxRadices)) return set_error(NLC_EINVAL, "chain_length has too many prime factors");
+	// the largest pass the shared-memory kernels can hold: one team of 2 x len complex per block
+	const uint32_t max_len = uint32_t(P.prop.sharedMemPerBlockOptin / (2 * sizeof(double2))) - 64;
+	const FftTables T = fft_tables(n, max_len);
+	if (T.radices.size() > size_t(kMaxRadices)) return set_error(NLC_EINVAL, "chain_length has too many prime factors");
 	f.n = int(n);
-	f.nradix = int(rad.size());
-	for (size_t i = 0; i < rad.size(); i++) f.radix[i] = rad[i];
-	const auto tw = fft_twiddles(n);
+	f.len = int(T.len);
+	f.nradix = int(T.radices.size());
+	for (size_t i = 0; i < T.radices.size(); i++) f.radix[i] = T.radices[i];
+	f.bluestein = T.bluestein;
 	double2 *d = nullptr;
-	int rc = P.upload(&d, reinterpret_cast<const double2 *>(tw.data()), n);
+	int rc = P.upload(&d, reinterpret_cast<const double2 *>(T.tw.data()), T.len);
+	if (rc) return rc;
 	f.tw = d;
-	return rc;
+	if (T.bluestein) {
+		double2 *c = nullptr, *bf = nullptr, *bi = nullptr;
+		if ((rc = P.upload(&c, reinterpret_cast<const double2 *>(T.chirp.data()), n))) return rc;
+		if ((rc = P.upload(&bf, reinterpret_cast<const double2 *>(T.bf.data()), T.len))) return rc;
+		if ((rc = P.upload(&bi, reinterpret_cast<const double2 *>(T.bi.data()), T.len))) return rc;
+		f.chirp = c, f.bf = bf, f.bi = bi;
+	}
+	return NLC_OK;
 }
 
 int setup_diagnostics(nlc_plan &P) {
@@ -303,20 +342,21 @@ int setup_diagnostics(nlc_plan &P) {
 			if ((rc = P.upload(&d_b, cb.data(), n))) return rc;
 			g.coef_a = d_a, g.coef_b = d_b;
 		}
-		// a warp per chain up to 1024 sites (2 x 16 KiB ping-pong), else a 256-thread block per chain
-		if (n <= 1024) {
+		// a warp per chain up to a 1024-point pass (2 x 16 KiB ping-pong), else a 256-thread block
+		const uint32_t len = uint32_t(g.fft.len);
+		if (len <= 1024) {
 			P.diag_team_block = 0;
 			P.diag_threads = 128;
 			const int teams = 4;
-			P.diag_smem = size_t(teams) * 2 * n * sizeof(double2);
+			P.diag_smem = size_t(teams) * 2 * len * sizeof(double2);
 			const unsigned long long groups = (P.m.copies + teams - 1) / teams;
-			P.diag_blocks = int(std::min<unsigned long long>(groups, 4ull * sms));
+			P.diag_blocks = int(std::min<unsigned long long>(groups, (P.m.flags & NLC_FLAG_COMPACT_DIAG ? 1ull : 4ull) * sms));
 			P.diag_rows = P.diag_blocks * teams;
 		} else {
 			P.diag_team_block = 1;
 			P.diag_threads = 256;
-			P.diag_smem = size_t(2) * n * sizeof(double2);
-			P.diag_blocks = int(std::min<unsigned long long>(P.m.copies, 2ull * sms));
+			P.diag_smem = size_t(2) * len * sizeof(double2);
+			P.diag_blocks = int(std::min<unsigned long long>(P.m.copies, (P.m.flags & NLC_FLAG_COMPACT_DIAG ? 1ull : 2ull) * sms));
 			P.diag_rows = P.diag_blocks;
 		}
 		if (P.diag_smem > size_t(P.prop.sharedMemPerBlockOptin))
@@ -422,16 +462,17 @@ extern "C" int nlc_plan_create(const nlc_model *model, nlc_plan **out) {
 		if ((rc = P->upload(&d_tab, reinterpret_cast<const double2 *>(tab.data()), 7 * size_t(n)))) return rc;
 		d.lin_tables = d_tab;
 		d.work_counter = P->d_counter;
-		// team: a warp per chain up to 256 sites, else a block of up to 256 threads per chain
+		// team: a warp per chain up to a 256-point pass, else a block of up to 256 threads per chain
 		const int sms = P->prop.multiProcessorCount;
-		if (n <= 256) {
+		const uint32_t len = uint32_t(d.fft.len);
+		if (len <= 256) {
 			P->dnls_team_block = 0;
 			P->dnls_threads = 128;
-			P->dnls_smem = 4 * 2 * size_t(n) * sizeof(double2);
+			P->dnls_smem = 4 * 2 * size_t(len) * sizeof(double2);
 		} else {
 			P->dnls_team_block = 1;
-			P->dnls_threads = int(std::min<uint32_t>(256, std::max<uint32_t>(64, (n / 4 + 31) / 32 * 32)));
-			P->dnls_smem = 2 * size_t(n) * sizeof(double2);
+			P->dnls_threads = int(std::min<uint32_t>(256, std::max<uint32_t>(64, (len / 4 + 31) / 32 * 32)));
+			P->dnls_smem = 2 * size_t(len) * sizeof(double2);
 		}
 		if (P->dnls_smem > size_t(P->prop.sharedMemPerBlockOptin))
 			return set_error(NLC_EUNSUPPORTED, "chain_length too large for the shared-memory DNLS integrator");
@@ -490,6 +531,9 @@ extern "C" int nlc_plan_create(const nlc_model *model, nlc_plan **out) {
 				if (finish_shape(*P, mdl, P->variant, s, 128)) P->rs = s;
 			}
 			if (!P->rs.blocks) return set_error(NLC_EINVAL, "NLC_FORCE_LANES does not give a launchable shape");
+		} else if (model->flags & NLC_FLAG_CANONICAL_SHAPE) {
+			P->rs = canonical_shape(*P, mdl, P->variant);
+			if (!P->rs.blocks) P->rs = heuristic_shape(*P, mdl, P->variant);
 		} else {
 			P->rs = (model->flags & NLC_FLAG_NO_TUNE) ? heuristic_shape(*P, mdl, P->variant)
 			                                          : autotune_shape(*P, mdl, P->variant);
@@ -505,6 +549,18 @@ extern "C" int nlc_plan_create(const nlc_model *model, nlc_plan **out) {
 	}
 	*out = P.release();
 	return NLC_OK;
+}
+
+bool nlc::plan_info(const nlc_plan *P, PlanInfo *info) {
+	if (!P || !info) return false;
+	info->model = P->m.model;
+	info->variant = P->variant;
+	info->shape = P->rs;
+	info->args = P->ra;
+	info->args.lanes = P->rs.lanes;
+	info->device_bytes = P->device_bytes;
+	info->sms = P->prop.multiProcessorCount;
+	return true;
 }
 
 extern "C" int nlc_plan_destroy(nlc_plan *plan) {

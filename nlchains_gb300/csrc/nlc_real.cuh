@@ -11,11 +11,16 @@
 //   chain and warp-boundary halos go through double-buffered shared memory, one barrier per exchange;
 // * the grid is persistent: each block takes units of work (one chain per group) from a
 //   self-resetting device counter, which balances the FP64 pipes of all SMs to within one unit;
+// * a batched launch packs several ensembles of one kernel class (model, constants, G, E) into the
+//   same persistent grid through a device table (BatchJob): units are numbered across the table and
+//   each block looks up the ensemble of its unit, so small requests share the GPU without extra
+//   launches and every chain still sees exactly the arithmetic of a launch of its own;
 // * bond-based forces (FPUT, Toda) compute each bond once: a lane computes its own right bonds and
 //   receives the left bond of its first site from its left neighbour by shuffle, instead of
 //   recomputing it as the reference's RHS constructor does;
 // * every FP64 operation is an explicit round-to-nearest intrinsic in the order the CPU oracle
-//   replays (oracle/nlc_oracle.c, move_chain_device).
+//   replays (oracle/nlc_oracle.c, move_chain_device); adds and products are issued as FMAs with
+//   parameter-bank constants (bit-identical, faster issue on GB300, see nlc_device.cuh).
 //
 // FP64 operations per site and sub-step (GB300 is FP64-pipe bound, see nlc_device.cuh):
 //   DNKG / dDNKG 6 (5 with beta == 1), FPUT 7 (6 with alpha == 0 and beta == 1),
@@ -86,11 +91,11 @@ __device__ __forceinline__ double bond_force(double d, const RealArgs &a, const 
 	if constexpr (MODEL == NLC_FPUT) {
 		// d + alpha d^2 + beta d^3 = d * (1 + d * (alpha + beta d))
 		const double h = VAR ? d : dfma(a.beta, d, a.alpha);
-		const double w = dfma(h, d, 1.);
-		return dmul(d, w);
+		const double w = dfma(h, d, a.k1.one);
+		return fmul(d, w, a.k1);
 	} else {
 		// (exp(2 alpha d) - 1) / (2 alpha) up to the constant, which cancels in g[s] - g[s-1]
-		return exp_scaled(VAR ? d : dmul(a.alpha2, d), tab);
+		return exp_scaled(VAR ? d : fmul(a.alpha2, d, a.k1), tab, a.k1, a.ek);
 	}
 }
 
@@ -99,41 +104,73 @@ __global__ void real_move_kernel_t(double2 *__restrict__ state, const RealArgs a
 	__shared__ double xbuf[4 * 32];
 	__shared__ double s_tab[MODEL == NLC_TODA ? 256 : 1];
 	__shared__ unsigned long long s_unit;
+	__shared__ int s_job;
 
 	const int G = a.lanes;
 	const int tid = threadIdx.x;
 	const int lane = tid & (G - 1);
 	const int gib = tid / G;                 // group (chain) in block
 	const int gpb = blockDim.x / G;          // groups per block
-	const int n = int(a.n);
-	const int full = n - G * (E - 1);       // lanes [0, full) hold E sites, the others E - 1
-	const bool fl = lane < full;
-	const int ne = fl ? E : E - 1;
-	const int first = fl ? lane * E : full * E + (lane - full) * (E - 1);
 
 	Ring ring{G, lane, tid & 31, tid >> 5, G > 32 ? G >> 5 : 1, xbuf, 0};
 
 	if constexpr (MODEL == NLC_TODA) {
 		for (int i = tid; i < 256; i += blockDim.x) s_tab[i] = a.exptab[i];
 	}
-	double mv[MODEL == NLC_DDNKG ? E : 1];
-	if constexpr (MODEL == NLC_DDNKG) {
-#pragma unroll
-		for (int j = 0; j < E; j++) mv[j] = j < ne ? a.mp2_site[first + j] : 2.;
-	}
 
-	const unsigned long long units = (a.copies + gpb - 1) / gpb;
+	// the ensemble of the current unit: the launch's own, or one entry of the batch table
+	int cur_job = -1;
+	double2 *st = state;
+	uint32_t n = a.n, copies = a.copies, steps = a.steps;
+	const double *mp2_site = a.mp2_site;
+	unsigned long long unit_base = 0;
+	int full = 0, ne = 0, first = 0;
+	bool fl = false;
+	double mv[MODEL == NLC_DDNKG ? E : 1];
+	auto layout = [&]() {
+		full = int(n) - G * (E - 1);       // lanes [0, full) hold E sites, the others E - 1
+		fl = lane < full;
+		ne = fl ? E : E - 1;
+		first = fl ? lane * E : full * E + (lane - full) * (E - 1);
+		if constexpr (MODEL == NLC_DDNKG) {
+#pragma unroll
+			for (int j = 0; j < E; j++) mv[j] = j < ne ? mp2_site[first + j] : 2.;
+		}
+	};
+	if (!a.batch) layout();
+
+	const unsigned long long units = a.batch ? a.batch_units : (copies + gpb - 1) / gpb;
 	for (;;) {
 		__syncthreads();
-		if (tid == 0) s_unit = atomicAdd(&a.work_counter[0], 1ull);
+		if (tid == 0) {
+			const unsigned long long u = atomicAdd(&a.work_counter[0], 1ull);
+			s_unit = u;
+			if (a.batch && u < units) {
+				// last table entry whose first unit is <= u
+				int lo = 0, hi = a.nbatch - 1;
+				while (lo < hi) {
+					const int mid = (lo + hi + 1) >> 1;
+					if (a.batch[mid].unit_begin <= u) lo = mid;
+					else hi = mid - 1;
+				}
+				s_job = lo;
+			}
+		}
 		__syncthreads();
 		const unsigned long long u = s_unit;
 		if (u >= units) break;
+		if (a.batch && s_job != cur_job) {
+			cur_job = s_job;
+			const BatchJob &J = a.batch[cur_job];
+			st = J.state, n = J.n, copies = J.copies, steps = J.steps, mp2_site = J.mp2_site;
+			unit_base = J.unit_begin;
+			layout();
+		}
 
-		unsigned long long chain = u * gpb + gib;
-		const bool active = chain < a.copies;
-		if (!active) chain = a.copies - 1;   // redundant work keeps shuffles and barriers convergent
-		double2 *cp = state + chain * (unsigned long long) n + first;
+		unsigned long long chain = (u - unit_base) * gpb + gib;
+		const bool active = chain < copies;
+		if (!active) chain = copies - 1;   // redundant work keeps shuffles and barriers convergent
+		double2 *cp = st + chain * (unsigned long long) n + first;
 
 		double x[E + 2], p[E];
 #pragma unroll
@@ -146,7 +183,7 @@ __global__ void real_move_kernel_t(double2 *__restrict__ state, const RealArgs a
 			}
 		}
 
-		for (uint32_t i = 0; i < a.steps; i++) {
+		for (uint32_t i = 0; i < steps; i++) {
 #pragma unroll
 			for (int k = 0; k < 7; k++) {
 				// the trailing drift of step i-1 (c[7]) merged with the leading drift of step i (c[0])
@@ -162,13 +199,13 @@ __global__ void real_move_kernel_t(double2 *__restrict__ state, const RealArgs a
 #pragma unroll
 					for (int j = 1; j <= E; j++) {
 						const double c = x[j];
-						const double bc = VAR ? c : dmul(a.beta, c);
+						const double bc = VAR ? c : fmul(a.beta, c, a.k1);
 						double mp2x;
 						if constexpr (MODEL == NLC_DDNKG) mp2x = mv[j - 1];
 						else mp2x = a.mp2;
 						const double t = dfma(bc, c, mp2x);
 						const double uu = dfma(c, t, -x[j - 1]);
-						const double v = dsub(uu, x[j + 1]);
+						const double v = fsub(uu, x[j + 1], a.k1);
 						p[j - 1] = dfma(a.nck[k], v, p[j - 1]);
 					}
 				} else {
@@ -177,10 +214,10 @@ __global__ void real_move_kernel_t(double2 *__restrict__ state, const RealArgs a
 					if (!fl) x[E] = r;
 					double g[E + 1];
 #pragma unroll
-					for (int j = 1; j <= E; j++) g[j] = bond_force<MODEL, VAR>(dsub(x[j + 1], x[j]), a, s_tab);
+					for (int j = 1; j <= E; j++) g[j] = bond_force<MODEL, VAR>(fsub(x[j + 1], x[j], a.k1), a, s_tab);
 					g[0] = ring.from_left(fl ? g[E] : g[E - 1]);
 #pragma unroll
-					for (int j = 1; j <= E; j++) p[j - 1] = dfma(a.ck[k], dsub(g[j], g[j - 1]), p[j - 1]);
+					for (int j = 1; j <= E; j++) p[j - 1] = dfma(a.ck[k], fsub(g[j], g[j - 1], a.k1), p[j - 1]);
 				}
 				if (!fl) p[E - 1] = 0.;   // the slot past a short lane's last site stays inert
 			}

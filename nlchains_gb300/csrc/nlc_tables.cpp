@@ -3,7 +3,12 @@
 // written here on both x86-64 and aarch64 hosts.
 #include <algorithm>
 #include <cmath>
+#include <complex>
+#include <condition_variable>
 #include <cstring>
+#include <functional>
+#include <mutex>
+#include <thread>
 
 #include "nlc_host.h"
 
@@ -104,9 +109,164 @@ std::vector<double> fft_twiddles(uint32_t n) {
 	return tw;
 }
 
+namespace {
+
+// Fork-join pool for the O(n^3) loops of the eigensolver: the calling thread plus helpers, each
+// call splits [0, count) into contiguous chunks, one per thread.
+class Pool {
+public:
+	explicit Pool(unsigned threads) {
+		for (unsigned t = 1; t < threads; t++) helpers_.emplace_back([this, t] { run(t); });
+		size_ = threads;
+	}
+	~Pool() {
+		{
+			std::lock_guard<std::mutex> lk(mu_);
+			stop_ = true;
+			gen_++;
+		}
+		cv_.notify_all();
+		for (auto &h : helpers_) h.join();
+	}
+	void parallel_for(size_t count, const std::function<void(size_t, size_t)> &fn) {
+		if (size_ == 1 || count < 64) {
+			fn(0, count);
+			return;
+		}
+		{
+			std::lock_guard<std::mutex> lk(mu_);
+			fn_ = &fn, count_ = count, pending_ = size_ - 1;
+			gen_++;
+		}
+		cv_.notify_all();
+		chunk(0, fn, count);
+		std::unique_lock<std::mutex> lk(mu_);
+		done_.wait(lk, [&] { return pending_ == 0; });
+	}
+
+private:
+	void chunk(unsigned t, const std::function<void(size_t, size_t)> &fn, size_t count) {
+		const size_t b = count * t / size_, e = count * (t + 1) / size_;
+		if (b < e) fn(b, e);
+	}
+	void run(unsigned t) {
+		uint64_t seen = 0;
+		for (;;) {
+			const std::function<void(size_t, size_t)> *fn;
+			size_t count;
+			{
+				std::unique_lock<std::mutex> lk(mu_);
+				cv_.wait(lk, [&] { return gen_ != seen; });
+				seen = gen_;
+				if (stop_) return;
+				fn = fn_, count = count_;
+			}
+			chunk(t, *fn, count);
+			std::lock_guard<std::mutex> lk(mu_);
+			if (--pending_ == 0) done_.notify_one();
+		}
+	}
+	std::vector<std::thread> helpers_;
+	unsigned size_ = 1;
+	std::mutex mu_;
+	std::condition_variable cv_, done_;
+	const std::function<void(size_t, size_t)> *fn_ = nullptr;
+	size_t count_ = 0;
+	unsigned pending_ = 0;
+	uint64_t gen_ = 0;
+	bool stop_ = false;
+};
+
+}  // namespace
+
+namespace {
+
+uint32_t largest_prime_factor(uint32_t n) {
+	uint32_t p = 1;
+	for (uint32_t f = 2; f * f <= n; f++)
+		while (n % f == 0) p = f, n /= f;
+	return n > 1 ? std::max(p, n) : p;
+}
+
+// smallest 2^a 3^b 5^c >= x
+uint32_t smooth_at_least(uint32_t x) {
+	uint32_t best = 1u << 31;
+	for (uint64_t a = 1; a < 2ull * x; a *= 2)
+		for (uint64_t b = a; b < 2ull * x; b *= 3)
+			for (uint64_t c = b; c < 2ull * x; c *= 5)
+				if (c >= x && c < best) best = uint32_t(c);
+	return best;
+}
+
+// in-place recursive mixed-radix DFT (sign -1 forward), for host table set-up only
+void host_dft(std::vector<std::complex<double>> &z, int sign) {
+	const size_t n = z.size();
+	if (n <= 1) return;
+	size_t p = 2;
+	while (n % p) p++;
+	if (p == n) {
+		std::vector<std::complex<double>> out(n);
+		for (size_t k = 0; k < n; k++) {
+			std::complex<double> acc = 0;
+			for (size_t j = 0; j < n; j++) acc += z[j] * std::polar(1., sign * 2 * M_PI * double(j * k % n) / n);
+			out[k] = acc;
+		}
+		z = out;
+		return;
+	}
+	const size_t m = n / p;
+	std::vector<std::vector<std::complex<double>>> sub(p, std::vector<std::complex<double>>(m));
+	for (size_t r = 0; r < p; r++) {
+		for (size_t j = 0; j < m; j++) sub[r][j] = z[j * p + r];
+		host_dft(sub[r], sign);
+	}
+	for (size_t k = 0; k < n; k++) {
+		std::complex<double> acc = 0;
+		for (size_t r = 0; r < p; r++) acc += sub[r][k % m] * std::polar(1., sign * 2 * M_PI * double(r * k % n) / n);
+		z[k] = acc;
+	}
+}
+
+}  // namespace
+
+FftTables fft_tables(uint32_t n, uint32_t max_len) {
+	FftTables T;
+	T.n = n;
+	T.len = n;
+	if (n >= 2 && largest_prime_factor(n) > 47) {
+		const uint32_t m = smooth_at_least(2 * n - 1);
+		if (m <= max_len) T.bluestein = true, T.len = m;
+	}
+	T.radices = fft_radices(T.len);
+	T.tw = fft_twiddles(T.len);
+	if (!T.bluestein) return T;
+	const uint32_t m = T.len;
+	T.chirp.resize(2 * size_t(n));
+	std::vector<std::complex<double>> b(m, 0.), bc(m, 0.);
+	for (uint32_t j = 0; j < n; j++) {
+		// exp(-i pi j^2 / n) with j^2 reduced mod 2n exactly
+		const double ang = M_PI * double((uint64_t(j) * j) % (2ull * n)) / n;
+		T.chirp[2 * j] = std::cos(ang), T.chirp[2 * j + 1] = -std::sin(ang);
+		const std::complex<double> bj(std::cos(ang), std::sin(ang));   // exp(+i pi j^2 / n)
+		b[j] = bj, bc[j] = std::conj(bj);
+		if (j) b[m - j] = bj, bc[m - j] = std::conj(bj);
+	}
+	host_dft(b, -1);
+	host_dft(bc, -1);
+	T.bf.resize(2 * size_t(m));
+	T.bi.resize(2 * size_t(m));
+	for (uint32_t k = 0; k < m; k++) {
+		T.bf[2 * k] = b[k].real() / m, T.bf[2 * k + 1] = b[k].imag() / m;
+		T.bi[2 * k] = bc[k].real() / m, T.bi[2 * k + 1] = bc[k].imag() / m;
+	}
+	return T;
+}
+
 bool eigensystem_periodic(const std::vector<double> &mp2, std::vector<double> &omegas, std::vector<double> &eigvec) {
 	const size_t n = mp2.size();
 	if (n < 2) return false;
+	const unsigned hw = std::max(1u, std::min(32u, std::thread::hardware_concurrency()));
+	Pool pool(n >= 512 ? hw : 1);
 	// dense symmetric matrix, column-major A[j*n + i]
 	std::vector<double> A(n * n, 0.), Q(n * n, 0.);
 	auto a = [&](size_t i, size_t j) -> double & { return A[j * n + i]; };
@@ -136,35 +296,54 @@ bool eigensystem_periodic(const std::vector<double> &mp2, std::vector<double> &o
 		if (vn2 == 0.) continue;
 		const double vinv = 1. / std::sqrt(vn2);
 		for (size_t i = k + 1; i < n; i++) v[i] *= vinv;
-		// p = A v over the trailing block (rows/cols k..n-1; column k interacts too)
-		for (size_t i = k; i < n; i++) {
-			double s = 0.;
-			for (size_t j = k + 1; j < n; j++) s += a(i, j) * v[j];
-			p[i] = s;
-		}
+		// p = A v over the trailing block; A is symmetric, so p[i] = sum_j A(j, i) v[j] reads column i
+		pool.parallel_for(n - k, [&](size_t b, size_t e) {
+			for (size_t i = k + b; i < k + e; i++) {
+				const double *col = &A[i * n];
+				double s = 0.;
+				for (size_t j = k + 1; j < n; j++) s += col[j] * v[j];
+				p[i] = s;
+			}
+		});
 		double K = 0.;
 		for (size_t i = k + 1; i < n; i++) K += v[i] * p[i];
 		// A <- A - v w^T - w v^T with w = 2 (p - K v)
 		for (size_t i = k; i < n; i++) w[i] = 2. * (p[i] - K * v[i]);
-		for (size_t j = k; j < n; j++)
-			for (size_t i = k; i < n; i++) a(i, j) -= v[i] * w[j] + w[i] * v[j];
+		pool.parallel_for(n - k, [&](size_t b, size_t e) {
+			for (size_t j = k + b; j < k + e; j++) {
+				double *col = &A[j * n];
+				const double vj = v[j], wj = w[j];
+				for (size_t i = k; i < n; i++) col[i] -= v[i] * wj + w[i] * vj;
+			}
+		});
 		// exact zeros below the subdiagonal of column k
 		a(k + 1, k) = a(k, k + 1) = alpha;
 		for (size_t i = k + 2; i < n; i++) a(i, k) = a(k, i) = 0.;
-		// Q <- Q H, H = I - 2 v v^T
-		for (size_t i = 0; i < n; i++) {
-			double s = 0.;
-			for (size_t j = k + 1; j < n; j++) s += q(i, j) * v[j];
-			s *= 2.;
-			for (size_t j = k + 1; j < n; j++) q(i, j) -= s * v[j];
-		}
+		// Q <- Q H, H = I - 2 v v^T: s = Q v (rows in parallel), then a rank-1 update (columns)
+		pool.parallel_for(n, [&](size_t b, size_t e) {
+			for (size_t i = b; i < e; i++) p[i] = 0.;
+			for (size_t j = k + 1; j < n; j++) {
+				const double *col = &Q[j * n];
+				const double vj = v[j];
+				for (size_t i = b; i < e; i++) p[i] += col[i] * vj;
+			}
+		});
+		pool.parallel_for(n - k - 1, [&](size_t b, size_t e) {
+			for (size_t j = k + 1 + b; j < k + 1 + e; j++) {
+				double *col = &Q[j * n];
+				const double vj2 = 2. * v[j];
+				for (size_t i = 0; i < n; i++) col[i] -= p[i] * vj2;
+			}
+		});
 	}
 	std::vector<double> d(n), e(n, 0.);
 	for (size_t i = 0; i < n; i++) d[i] = a(i, i);
 	for (size_t i = 0; i + 1 < n; i++) e[i] = a(i + 1, i);
 
-	// implicit symmetric QR with Wilkinson shift, deflating from the bottom
+	// implicit symmetric QR with Wilkinson shift, deflating from the bottom; the rotations of one
+	// sweep are recorded and then applied to Q by row blocks in parallel
 	const double eps = 2.220446049250313e-16;
+	std::vector<double> rc(n), rs(n);
 	size_t iter = 0, hi = n - 1;
 	while (hi > 0) {
 		if (std::fabs(e[hi - 1]) <= eps * (std::fabs(d[hi - 1]) + std::fabs(d[hi]))) {
@@ -193,13 +372,20 @@ bool eigensystem_periodic(const std::vector<double> &mp2, std::vector<double> &o
 				e[k + 1] = c * e[k + 1];
 				x = e[k];
 			}
-			// Q <- Q P^T on columns k, k+1
-			for (size_t i = 0; i < n; i++) {
-				const double qk = q(i, k), qk1 = q(i, k + 1);
-				q(i, k) = c * qk + s * qk1;
-				q(i, k + 1) = -s * qk + c * qk1;
-			}
+			rc[k] = c, rs[k] = s;
 		}
+		// Q <- Q P^T on columns (k, k+1), k = lo .. hi-1 in order
+		pool.parallel_for(n, [&](size_t b, size_t e2) {
+			for (size_t k = lo; k < hi; k++) {
+				const double c = rc[k], s = rs[k];
+				double *qk = &Q[k * n], *qk1 = &Q[(k + 1) * n];
+				for (size_t i = b; i < e2; i++) {
+					const double x0 = qk[i], x1 = qk1[i];
+					qk[i] = c * x0 + s * x1;
+					qk1[i] = -s * x0 + c * x1;
+				}
+			}
+		});
 	}
 	// ascending order with vectors
 	std::vector<size_t> idx(n);

@@ -46,9 +46,13 @@ def uniform(seed, copies, count, stream=0, first_copy=0):
 
 
 def low_modes(n, fraction=None, kmax=None, include_zero=True):
-    """Wave numbers 0 (optional), +-1 .. +-kmax as DFT indices; kmax = floor(fraction * n) if not given."""
+    """Wave numbers 0 (optional), +-1 .. +-kmax as DFT indices.
+
+    With `fraction` instead of kmax, the lowest fraction of all n modes is taken, each frequency
+    counting twice (+k and -k): kmax = floor(fraction * n / 2), e.g. 10% of n = 1024 gives |k| <= 51.
+    """
     if kmax is None:
-        kmax = int(np.floor(fraction * n))
+        kmax = int(np.floor(fraction * n / 2))
     kmax = max(1, min(kmax, (n - 1) // 2 if n > 2 else 1))
     ks = [0] if include_zero else []
     for k in range(1, kmax + 1):

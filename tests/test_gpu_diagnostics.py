@@ -35,7 +35,7 @@ def check(lin, wt, inf, exp_lin, a0is0, mask=None):
     assert abs(inf - einf) <= TOL * max(1.0, abs(einf))
 
 
-@pytest.mark.parametrize("n", [2, 3, 7, 12, 64, 100, 128, 1024, 1536, 4096])
+@pytest.mark.parametrize("n", [2, 3, 7, 12, 64, 86, 100, 101, 128, 509, 1021, 1024, 1536, 3583, 4096])
 @pytest.mark.parametrize("model,params", [("FPUT", dict(alpha=0.0, beta=1.0)), ("DNKG", dict(m=1.0, beta=1.0)),
                                           ("Toda", dict(alpha=0.5))])
 def test_real_models(gpu, model, params, n):
@@ -47,7 +47,7 @@ def test_real_models(gpu, model, params, n):
     check(lin, wt, inf, O.linenergies(mdl, state), O.a0is0(mdl))
 
 
-@pytest.mark.parametrize("n", [4, 16, 64, 100, 1024, 2048])
+@pytest.mark.parametrize("n", [4, 16, 64, 100, 211, 1024, 2048, 2477])
 def test_dnls(gpu, n):
     copies = 29
     # a full spectrum: the WT entropy sums log e_k and is ill-conditioned for modes at rounding level

@@ -19,13 +19,18 @@ def run(nlc, n, copies, dt, beta, psi, steps, batching):
     return out
 
 
-@pytest.mark.parametrize("n", [2, 8, 12, 64, 100, 256, 512, 1024, 2048])
+# 86 = 2 x 43 (direct radix-43 pass), 97 / 211 / 997 / 3001 prime (Bluestein) and
+# 1000 smooth: every FFT path of the shared-memory transform
+@pytest.mark.parametrize("n", [2, 8, 12, 64, 86, 97, 100, 211, 256, 512, 997, 1000, 1024, 2048, 3001])
 def test_against_oracle(gpu, n):
     copies, dt = 11, 0.01
+    steps, b = (20, 10) if n <= 2048 else (4, 2)   # the oracle's prime-length DFT is O(n^2)
+    if n > 2048:
+        copies = 3
     psi = ic.dnls_ensemble(n, copies, 1.0, ic.low_modes(n, 0.1), seed=n)
-    out = run(gpu, n, copies, dt, 1.0, psi, 20, 10)
+    out = run(gpu, n, copies, dt, 1.0, psi, steps, b)
     mdl = O.Model("DNLS", n, copies, dt, beta=1.0)
-    exp = O.advance(mdl, psi.view(np.float64), 20, 10).view(np.complex128).reshape(copies, n)
+    exp = O.advance(mdl, psi.view(np.float64), steps, b).view(np.complex128).reshape(copies, n)
     # different FFT algorithms and sincos implementations: agreement to rounding
     assert np.abs(out - exp).max() <= 1e-12 * np.abs(exp).max()
 
