@@ -22,31 +22,40 @@ __device__ __forceinline__ double2 nonlinear_rotate(double2 v, double neg_coef, 
 	return make_double2(dfma(v.x, c, -fmul(v.y, s, k)), dfma(v.x, s, fmul(v.y, c, k)));
 }
 
+// BLOCK: one chain per block.  Otherwise teams of a.team lanes (a power of two, 4 .. 32) inside each
+// warp, 32 / a.team chains per warp: short chains keep every lane busy.  A warp takes its chains as
+// one unit from the self-resetting counter, so all its teams run the same control flow (a team
+// past the last chain repeats the last one and does not store).
 template <bool BLOCK>
 __global__ void dnls_move_kernel(double2 *__restrict__ psi, const DnlsArgs a) {
 	extern __shared__ double2 sm[];
 	__shared__ unsigned long long s_chain[32];
 	const int n = int(a.n);
-	const int T = BLOCK ? blockDim.x : 32;
-	const int t = BLOCK ? threadIdx.x : (threadIdx.x & 31);
-	const int team = BLOCK ? 0 : (threadIdx.x >> 5);
+	const int T = BLOCK ? blockDim.x : a.team;
+	const int t = BLOCK ? threadIdx.x : (threadIdx.x & (T - 1));
+	const int team = BLOCK ? 0 : (threadIdx.x / T);
+	const int per_warp = BLOCK ? 1 : 32 / T;
 	const int len = a.fft.len;
 	double2 *buf0 = sm + (size_t) team * 2 * len, *buf1 = buf0 + len;
+	const unsigned long long units = (a.copies + per_warp - 1) / per_warp;
 
 	for (;;) {
-		// team leader takes the next chain from the self-resetting counter
-		unsigned long long chain;
+		// the next unit from the self-resetting counter: a chain (BLOCK) or a warp's chains
+		unsigned long long u;
 		if (BLOCK) {
 			__syncthreads();
 			if (t == 0) s_chain[0] = atomicAdd(&a.work_counter[0], 1ull);
 			__syncthreads();
-			chain = s_chain[0];
+			u = s_chain[0];
 		} else {
 			unsigned long long c = 0;
-			if (t == 0) c = atomicAdd(&a.work_counter[0], 1ull);
-			chain = __shfl_sync(0xffffffffu, c, 0);
+			if ((threadIdx.x & 31) == 0) c = atomicAdd(&a.work_counter[0], 1ull);
+			u = __shfl_sync(0xffffffffu, c, 0);
 		}
-		if (chain >= a.copies) break;
+		if (u >= units) break;
+		unsigned long long chain = u * per_warp + (BLOCK ? 0 : (threadIdx.x & 31) / T);
+		const bool active = chain < a.copies;
+		if (!active) chain = a.copies - 1;
 
 		double2 *g = psi + chain * (unsigned long long) n;
 		double2 *x = buf0, *y = buf1;
@@ -67,7 +76,8 @@ __global__ void dnls_move_kernel(double2 *__restrict__ psi, const DnlsArgs a) {
 				y = x == buf0 ? buf1 : buf0;
 			}
 		}
-		for (int j = t; j < n; j += T) g[j] = nonlinear_rotate(x[j], -a.nl_final, a.fft.k1);
+		if (active)
+			for (int j = t; j < n; j += T) g[j] = nonlinear_rotate(x[j], -a.nl_final, a.fft.k1);
 		team_sync<BLOCK>();
 	}
 

@@ -32,7 +32,7 @@ std::vector<int> fft_radices(uint32_t n);
 std::vector<double> fft_twiddles(uint32_t n);
 
 // Host tables of a chain FFT: Stockham radices/twiddles of the pass length, plus the Bluestein
-// chirp and convolution kernels when n has a prime factor above 47 and the convolution fits
+// chirp and convolution kernels when n has a prime factor above 7 and the convolution fits
 // max_len (the caller's shared-memory budget).
 struct FftTables {
 	uint32_t n = 0, len = 0;

@@ -136,6 +136,7 @@ struct DnlsArgs {
 	double nl_final;           // beta*dt*c[7]
 	const double2 *lin_tables; // [7][n] exp(-i dt d_k omega_j)/n
 	unsigned long long *work_counter;
+	int team;                  // lanes per chain of the warp-team variant (power of two, 4 .. 32)
 };
 cudaError_t launch_dnls_move(const DnlsArgs &a, double2 *psi, int blocks, int threads, size_t smem,
                              int team_block, cudaStream_t stream);

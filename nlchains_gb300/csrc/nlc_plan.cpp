@@ -462,13 +462,17 @@ extern "C" int nlc_plan_create(const nlc_model *model, nlc_plan **out) {
 		if ((rc = P->upload(&d_tab, reinterpret_cast<const double2 *>(tab.data()), 7 * size_t(n)))) return rc;
 		d.lin_tables = d_tab;
 		d.work_counter = P->d_counter;
-		// team: a warp per chain up to a 256-point pass, else a block of up to 256 threads per chain
+		// team: up to a 256-point pass, len/4 lanes (4 .. 32, a power of two) per chain and several
+		// chains per warp; beyond, a block of up to 256 threads per chain
 		const int sms = P->prop.multiProcessorCount;
 		const uint32_t len = uint32_t(d.fft.len);
 		if (len <= 256) {
+			int T = 4;
+			while (T < 32 && uint32_t(T) * 4 < len) T <<= 1;
+			d.team = T;
 			P->dnls_team_block = 0;
 			P->dnls_threads = 128;
-			P->dnls_smem = 4 * 2 * size_t(len) * sizeof(double2);
+			P->dnls_smem = size_t(128 / T) * 2 * len * sizeof(double2);
 		} else {
 			P->dnls_team_block = 1;
 			P->dnls_threads = int(std::min<uint32_t>(256, std::max<uint32_t>(64, (len / 4 + 31) / 32 * 32)));
@@ -483,7 +487,7 @@ extern "C" int nlc_plan_create(const nlc_model *model, nlc_plan **out) {
 		                      "occupancy")))
 			return rc;
 		if (per_sm < 1) return set_error(NLC_EUNSUPPORTED, "DNLS kernel does not fit an SM");
-		const int teams = P->dnls_team_block ? 1 : P->dnls_threads / 32;
+		const int teams = P->dnls_team_block ? 1 : P->dnls_threads / d.team;
 		P->dnls_blocks = int(std::min<unsigned long long>((model->copies + teams - 1) / teams, (unsigned long long) per_sm * sms));
 		P->tier = 3;
 	} else {
@@ -570,7 +574,7 @@ extern "C" int nlc_plan_destroy(nlc_plan *plan) {
 
 extern "C" int nlc_plan_shape(const nlc_plan *P, int32_t *lanes, int32_t *sites, int32_t *threads, int32_t *tier) {
 	if (!P) return set_error(NLC_EINVAL, "plan is NULL");
-	if (lanes) *lanes = P->m.model == NLC_DNLS ? (P->dnls_team_block ? P->dnls_threads : 32) : P->rs.lanes;
+	if (lanes) *lanes = P->m.model == NLC_DNLS ? (P->dnls_team_block ? P->dnls_threads : P->da.team) : P->rs.lanes;
 	if (sites) *sites = P->m.model == NLC_DNLS ? 0 : P->rs.sites;
 	if (threads) *threads = P->m.model == NLC_DNLS ? P->dnls_threads : P->rs.threads;
 	if (tier) *tier = P->tier;

@@ -1,17 +1,18 @@
 // Request server: continuous batching of ensemble-integration requests on one GPU.
 //
-// A background scheduler thread repeats rounds.  A round:
-//   1. admits queued requests while the HBM budget and the active limit allow (plan with the
-//      canonical launch shape, device state, upload, diagnostics sample at t = 0);
-//   2. groups the active real-model requests by kernel class (model, parameters, dt, launch shape)
-//      and advances every class with one persistent batched launch of the resident integrator
-//      (each request by its own kernel_batching steps), DNLS requests with their own launches, all
-//      classes concurrently on a pool of streams;
-//   3. takes one diagnostics sample per request (linear energies + entropies) on its class stream;
-//   4. waits for the round, appends the entropies, retires finished or blown-up requests (final
-//      state and energies copied out, device memory released), and loops.
-// A request's chains see exactly the arithmetic of a launch of their own (the batched kernel only
-// changes which block integrates which chain), so results are identical alone and in the mix.
+// Requests move queue -> admitted (by HBM budget) -> prepared -> running -> finished:
+//   * a preparer thread builds each admitted request's plan (canonical launch shape; for dDNKG the
+//     host eigensolve), allocates and uploads its state and takes the t = 0 diagnostics sample;
+//   * the scheduler thread groups idle prepared requests by kernel class (model, parameters, dt,
+//     launch shape) and launches each group on a free stream slot: one persistent batched launch of
+//     the resident integrator advancing every member by its own kernel_batching steps (DNLS
+//     requests run their own fused launch), then one diagnostics sample per member, then an event;
+//   * completed events return their requests to idle (entropies appended, blow-ups flagged);
+//     requests with all steps done are retired (final state and energies copied out, device memory
+//     released), which lets queued requests in.
+// There is no round barrier: fast groups keep cycling while slow ones run.  A request's chains see
+// exactly the arithmetic of a launch of their own (the batched kernel only changes which block
+// integrates which chain), so results are identical alone and in the mix.
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -56,6 +57,7 @@ struct Request {
 	int state = NLC_REQ_QUEUED;
 	int error = NLC_OK;
 	bool prepared = false;          // plan, state and t = 0 sample ready (set by the scheduler)
+	bool in_flight = false;         // a launch group with this request is on the GPU
 	double submit_ms = 0, start_ms = 0, finish_ms = 0;
 
 	void release_device() {
@@ -104,11 +106,12 @@ struct nlc_server {
 	cudaStream_t prep_stream = nullptr;
 	std::vector<cudaStream_t> streams;
 	std::vector<cudaEvent_t> events;
-	// per-class device job tables, reused across rounds (grown on demand)
+	// per stream slot: the launch group on the GPU, its device job table and pinned staging
+	std::vector<std::vector<Request *>> slot_reqs;
 	std::vector<BatchJob *> d_tables;
 	std::vector<size_t> d_table_cap;
-	BatchJob *h_tables = nullptr;   // pinned staging, one slice per class slot
-	size_t h_table_cap = 0;
+	std::vector<BatchJob *> h_slot;
+	std::vector<size_t> h_slot_cap;
 	std::string fatal;
 
 	double now_ms() const { return std::chrono::duration<double, std::milli>(Clock::now() - t0).count(); }
@@ -195,29 +198,99 @@ void preparer_loop(nlc_server *S) {
 	}
 }
 
+// Launch the next kernel_batching steps plus one sample for a group of idle requests of one class
+// (several: one packed launch; one: its own plan's launch) on stream slot `slot`.
+int launch_group(nlc_server *S, size_t slot, const std::vector<Request *> &reqs) {
+	cudaStream_t st = S->streams[slot];
+	int rc = NLC_OK;
+	if (reqs.size() == 1 || reqs[0]->model.model == NLC_DNLS) {
+		for (Request *R : reqs)
+			if (!rc) rc = nlc_move(R->plan, R->d_state, R->batching, st);
+	} else {
+		if (S->h_slot_cap[slot] < reqs.size()) {
+			cudaFreeHost(S->h_slot[slot]);
+			S->h_slot[slot] = nullptr;
+			S->h_slot_cap[slot] = 0;
+			const size_t cap = std::max<size_t>(reqs.size(), 64);
+			if ((rc = cuda_status(cudaMallocHost(&S->h_slot[slot], cap * sizeof(BatchJob)), "cudaMallocHost"))) return rc;
+			S->h_slot_cap[slot] = cap;
+		}
+		BatchJob *h = S->h_slot[slot];
+		unsigned long long units = 0;
+		const int gpb = reqs[0]->info.shape.threads / reqs[0]->info.shape.lanes;
+		for (size_t i = 0; i < reqs.size(); i++) {
+			Request *R = reqs[i];
+			h[i].state = R->d_state;
+			h[i].mp2_site = R->info.args.mp2_site;
+			h[i].unit_begin = units;
+			h[i].n = R->model.chain_length;
+			h[i].copies = R->model.copies;
+			h[i].steps = R->batching;
+			h[i].pad = 0;
+			units += (R->model.copies + gpb - 1) / gpb;
+		}
+		BatchJob *d = class_table(S, slot, reqs.size());
+		if (!d) return set_error(NLC_ENOMEM, "batch table");
+		if ((rc = cuda_status(cudaMemcpyAsync(d, h, reqs.size() * sizeof(BatchJob), cudaMemcpyHostToDevice, st),
+		                      "batch table copy")))
+			return rc;
+		RealArgs a = reqs[0]->info.args;
+		a.batch = d, a.nbatch = int(reqs.size()), a.batch_units = units;
+		RealShape sh = reqs[0]->info.shape;
+		int per_sm = 0;
+		cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+		    &per_sm, real_move_kernel(reqs[0]->info.model, reqs[0]->info.variant, sh.sites), sh.threads, 0);
+		sh.blocks = int(std::min<unsigned long long>(units, (unsigned long long) std::max(per_sm, 1) * reqs[0]->info.sms));
+		if ((rc = cuda_status(launch_real_move_batch(reqs[0]->info.model, reqs[0]->info.variant, sh, a, st),
+		                      "batched move launch")))
+			return rc;
+	}
+	for (Request *R : reqs)
+		if (!rc) rc = sample(S, *R, st);
+	if (!rc) rc = cuda_status(cudaEventRecord(S->events[slot], st), "cudaEventRecord");
+	return rc;
+}
+
+// Event-driven scheduler: admits requests, launches every group of idle same-class requests on a
+// free stream slot, and retires groups whose event has completed.  No round barrier: a group of
+// small fast requests goes round after round while a large one is still on the GPU.
 void worker_loop(nlc_server *S) {
 	cudaSetDevice(S->cfg.device);
+	const size_t nslots = S->streams.size();
 	for (;;) {
-		std::vector<Request *> fresh;
+		bool progressed = false;
 		{
 			std::unique_lock<std::mutex> lk(S->mu);
-			auto runnable = [&] {
-				for (auto &kv : S->active)
-					if (kv.second->prepared) return true;
-				return false;
-			};
 			auto admissible = [&] {
 				if (S->queue.empty() || S->active.size() >= size_t(S->cfg.max_active)) return false;
 				return S->active.empty() || S->used_bytes + S->queue.front()->need_bytes <= S->cfg.hbm_budget_bytes;
 			};
-			S->cv_work.wait(lk, [&] { return S->stop || admissible() || !S->ready.empty() || runnable(); });
+			auto in_flight = [&] {
+				for (auto &g : S->slot_reqs)
+					if (!g.empty()) return true;
+				return false;
+			};
+			auto idle_work = [&] {
+				for (auto &kv : S->active) {
+					const Request &R = *kv.second;
+					if (R.prepared && !R.in_flight) return true;
+				}
+				return false;
+			};
+			auto free_slot = [&] {
+				for (auto &g : S->slot_reqs)
+					if (g.empty()) return true;
+				return false;
+			};
+			// idle requests only need the scheduler when a slot is free (or they are to be retired)
+			auto wake = [&] { return S->stop || admissible() || !S->ready.empty() || (idle_work() && free_slot()); };
+			if (in_flight()) S->cv_work.wait_for(lk, std::chrono::microseconds(100), wake);
+			else S->cv_work.wait(lk, wake);
 			if (S->stop) return;
 			// admission by HBM budget (first come, first served; a request larger than the whole
 			// budget is admitted alone when nothing else is admitted)
 			bool admitted = false;
-			while (!S->queue.empty() && S->active.size() < size_t(S->cfg.max_active)) {
-				Request &R = *S->queue.front();
-				if (S->used_bytes + R.need_bytes > S->cfg.hbm_budget_bytes && !S->active.empty()) break;
+			while (admissible()) {
 				std::unique_ptr<Request> P = std::move(S->queue.front());
 				S->queue.pop_front();
 				S->used_bytes += P->need_bytes;
@@ -229,23 +302,48 @@ void worker_loop(nlc_server *S) {
 				admitted = true;
 			}
 			if (admitted) S->cv_prepare.notify_all();
-			for (Request *R : S->ready) R->prepared = true, fresh.push_back(R);
+			for (Request *R : S->ready) R->prepared = true;
 			S->ready.clear();
-			if (!runnable() && fresh.empty()) continue;
 		}
-		// group the prepared requests that still have steps to run (the fresh ones ran their t = 0
-		// sample in the preparer and start with the next round)
+
+		// 1. completed groups: record their samples
+		std::vector<Request *> finished;
+		for (size_t slot = 0; slot < nslots; slot++) {
+			auto &g = S->slot_reqs[slot];
+			if (g.empty()) continue;
+			const cudaError_t e = cudaEventQuery(S->events[slot]);
+			if (e == cudaErrorNotReady) continue;
+			std::lock_guard<std::mutex> lk(S->mu);
+			if (e != cudaSuccess) {
+				S->fatal = cudaGetErrorString(e);
+				for (Request *R : g) R->error = NLC_ECUDA;
+			}
+			for (Request *R : g) {
+				R->in_flight = false;
+				if (R->error) continue;
+				const size_t n = R->model.chain_length;
+				R->t += R->batching;
+				R->entropies.push_back(R->h_diag[n]), R->entropies.push_back(R->h_diag[n + 1]);
+				if (!std::isfinite(R->h_diag[n]) || !std::isfinite(R->h_diag[n + 1])) R->error = NLC_EBLOWUP;
+			}
+			g.clear();
+			progressed = true;
+		}
+
+		// 2. retire finished / failed idle requests, and group the idle ones with steps left
 		std::map<ClassKey, std::vector<Request *>> classes;
-		std::vector<Request *> dnls, running;
+		std::vector<std::vector<Request *>> singles;
 		{
 			std::lock_guard<std::mutex> lk(S->mu);
 			for (auto &kv : S->active) {
 				Request *R = kv.second.get();
-				if (!R->prepared || R->error || R->t >= R->steps) continue;
-				if (std::find(fresh.begin(), fresh.end(), R) != fresh.end()) continue;
-				running.push_back(R);
+				if (!R->prepared || R->in_flight) continue;
+				if (R->error || R->t >= R->steps) {
+					finished.push_back(R);
+					continue;
+				}
 				if (R->model.model == NLC_DNLS) {
-					dnls.push_back(R);
+					singles.push_back({R});
 					continue;
 				}
 				const PlanInfo &I = R->info;
@@ -254,115 +352,43 @@ void worker_loop(nlc_server *S) {
 				classes[key].push_back(R);
 			}
 		}
-		// one round: batched integrator launches per class, then one sample per request
-		size_t slot = 0, staged = 0;
-		size_t need_stage = 0;
-		for (auto &kv : classes) need_stage += kv.second.size();
-		if (need_stage > S->h_table_cap) {
-			cudaFreeHost(S->h_tables);
-			S->h_tables = nullptr;
-			S->h_table_cap = 0;
-			if (cudaMallocHost(&S->h_tables, std::max<size_t>(need_stage, 64) * sizeof(BatchJob)) == cudaSuccess)
-				S->h_table_cap = std::max<size_t>(need_stage, 64);
-		}
-		for (auto &kv : classes) {
-			auto &reqs = kv.second;
-			cudaStream_t st = S->streams[slot % S->streams.size()];
-			// the class runs on one stream: make it wait for each member's upload / previous sample
-			for (Request *R : reqs) {
-				if (S->streams[R->stream_slot] != st) {
-					cudaEventRecord(S->events[R->stream_slot], S->streams[R->stream_slot]);
-					cudaStreamWaitEvent(st, S->events[R->stream_slot], 0);
-				}
-			}
-			int rc = NLC_OK;
-			if (reqs.size() == 1 || !S->h_tables) {
-				for (Request *R : reqs)
-					if (!rc) rc = nlc_move(R->plan, R->d_state, R->batching, st);
-			} else {
-				BatchJob *h = S->h_tables + staged;
-				unsigned long long units = 0;
-				const int gpb = reqs[0]->info.shape.threads / reqs[0]->info.shape.lanes;
-				for (size_t i = 0; i < reqs.size(); i++) {
-					Request *R = reqs[i];
-					h[i].state = R->d_state;
-					h[i].mp2_site = R->info.args.mp2_site;
-					h[i].unit_begin = units;
-					h[i].n = R->model.chain_length;
-					h[i].copies = R->model.copies;
-					h[i].steps = R->batching;
-					h[i].pad = 0;
-					units += (R->model.copies + gpb - 1) / gpb;
-				}
-				BatchJob *d = class_table(S, slot, reqs.size());
-				if (!d) rc = set_error(NLC_ENOMEM, "batch table");
-				if (!rc) rc = cuda_status(cudaMemcpyAsync(d, h, reqs.size() * sizeof(BatchJob), cudaMemcpyHostToDevice, st),
-				                          "batch table copy");
-				if (!rc) {
-					RealArgs a = reqs[0]->info.args;
-					a.batch = d, a.nbatch = int(reqs.size()), a.batch_units = units;
-					RealShape sh = reqs[0]->info.shape;
-					int per_sm = 0;
-					cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-					    &per_sm, real_move_kernel(reqs[0]->info.model, reqs[0]->info.variant, sh.sites), sh.threads, 0);
-					sh.blocks = int(std::min<unsigned long long>(units, (unsigned long long) std::max(per_sm, 1) *
-					                                                        reqs[0]->info.sms));
-					rc = cuda_status(launch_real_move_batch(reqs[0]->info.model, reqs[0]->info.variant, sh, a, st),
-					                 "batched move launch");
-				}
-				staged += reqs.size();
-			}
-			for (Request *R : reqs)
-				if (!rc) rc = sample(S, *R, st);
-			if (rc)
-				for (Request *R : reqs) R->error = rc;
-			// later rounds of these requests follow this stream
-			for (Request *R : reqs) R->stream_slot = int(slot % S->streams.size());
-			slot++;
-		}
-		for (Request *R : dnls) {
-			cudaStream_t st = S->streams[R->stream_slot];
-			int rc = nlc_move(R->plan, R->d_state, R->batching, st);
-			if (!rc) rc = sample(S, *R, st);
-			if (rc) R->error = rc;
-		}
-		for (cudaStream_t st : S->streams) {
-			const cudaError_t e = cudaStreamSynchronize(st);
-			if (e != cudaSuccess) {
-				std::lock_guard<std::mutex> lk(S->mu);
-				S->fatal = cudaGetErrorString(e);
-			}
-		}
-		// bookkeeping
-		std::lock_guard<std::mutex> lk(S->mu);
-		std::vector<uint64_t> done;
-		for (Request *R : fresh)
-			if (R->steps == 0 || R->error) done.push_back(R->id);
-		for (Request *R : running) {
-			if (R->error) continue;
-			const size_t n = R->model.chain_length;
-			R->t += R->batching;
-			R->entropies.push_back(R->h_diag[n]), R->entropies.push_back(R->h_diag[n + 1]);
-			if (!std::isfinite(R->h_diag[n]) || !std::isfinite(R->h_diag[n + 1])) R->error = NLC_EBLOWUP;
-			if (R->t >= R->steps || R->error) done.push_back(R->id);
-		}
-		for (auto &kv : S->active)
-			if (kv.second->prepared && kv.second->error && std::find(done.begin(), done.end(), kv.first) == done.end())
-				done.push_back(kv.first);
-		for (uint64_t id : done) {
-			auto it = S->active.find(id);
-			if (it == S->active.end()) continue;
-			std::unique_ptr<Request> R = std::move(it->second);
-			S->active.erase(it);
+		for (Request *R : finished) {
+			// final state and energies; copies outside the lock
 			const size_t n = R->model.chain_length;
 			if (R->d_state && R->error != NLC_ECUDA) {
 				cudaMemcpy(R->host_in.data(), R->d_state, R->state_bytes, cudaMemcpyDeviceToHost);
 				R->lin.assign(R->h_diag, R->h_diag + n);
 			}
-			const int err = R->error;
-			retire(S, std::move(R), err && err != NLC_EBLOWUP ? NLC_REQ_FAILED : (err ? NLC_REQ_FAILED : NLC_REQ_DONE), err);
+			std::lock_guard<std::mutex> lk(S->mu);
+			auto it = S->active.find(R->id);
+			std::unique_ptr<Request> P = std::move(it->second);
+			S->active.erase(it);
+			const int err = P->error;
+			retire(S, std::move(P), err ? NLC_REQ_FAILED : NLC_REQ_DONE, err);
+			progressed = true;
 		}
-		S->cv_done.notify_all();
+		if (!finished.empty()) S->cv_done.notify_all();
+
+		// 3. launch the groups on free slots (largest groups first)
+		std::vector<std::vector<Request *>> groups;
+		for (auto &kv : classes) groups.push_back(kv.second);
+		for (auto &g : singles) groups.push_back(g);
+		std::stable_sort(groups.begin(), groups.end(),
+		                 [](const std::vector<Request *> &a, const std::vector<Request *> &b) { return a.size() > b.size(); });
+		size_t next = 0;
+		for (size_t slot = 0; slot < nslots && next < groups.size(); slot++) {
+			if (!S->slot_reqs[slot].empty()) continue;
+			auto &g = groups[next++];
+			const int rc = launch_group(S, slot, g);
+			std::lock_guard<std::mutex> lk(S->mu);
+			for (Request *R : g) {
+				R->in_flight = true;
+				if (rc) R->error = rc;
+			}
+			S->slot_reqs[slot] = g;
+			progressed = true;
+		}
+		if (!progressed) std::this_thread::yield();
 	}
 }
 
@@ -373,7 +399,7 @@ extern "C" int nlc_server_create(const nlc_server_config *config, nlc_server **o
 	std::unique_ptr<nlc_server> S(new nlc_server);
 	if (config) S->cfg = *config;
 	if (S->cfg.max_active <= 0) S->cfg.max_active = 256;
-	if (S->cfg.streams <= 0) S->cfg.streams = 8;
+	if (S->cfg.streams <= 0) S->cfg.streams = 16;
 	int rc = cuda_status(cudaSetDevice(S->cfg.device), "cudaSetDevice");
 	if (rc) return rc;
 	if (!S->cfg.hbm_budget_bytes) {
@@ -391,6 +417,11 @@ extern "C" int nlc_server_create(const nlc_server_config *config, nlc_server **o
 	}
 	if ((rc = cuda_status(cudaStreamCreateWithFlags(&S->prep_stream, cudaStreamNonBlocking), "cudaStreamCreate")))
 		return rc;
+	S->slot_reqs.resize(S->streams.size());
+	S->d_tables.assign(S->streams.size(), nullptr);
+	S->d_table_cap.assign(S->streams.size(), 0);
+	S->h_slot.assign(S->streams.size(), nullptr);
+	S->h_slot_cap.assign(S->streams.size(), 0);
 	S->t0 = Clock::now();
 	nlc_server *raw = S.get();
 	S->worker = std::thread([raw] { worker_loop(raw); });
@@ -414,7 +445,7 @@ extern "C" int nlc_server_destroy(nlc_server *S) {
 	for (cudaStream_t st : S->streams) cudaStreamSynchronize(st);
 	for (auto &kv : S->active) kv.second->release_device();
 	for (BatchJob *p : S->d_tables) cudaFree(p);
-	cudaFreeHost(S->h_tables);
+	for (BatchJob *p : S->h_slot) cudaFreeHost(p);
 	for (cudaStream_t st : S->streams) cudaStreamDestroy(st);
 	for (cudaEvent_t ev : S->events) cudaEventDestroy(ev);
 	delete S;

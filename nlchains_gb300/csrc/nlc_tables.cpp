@@ -233,7 +233,7 @@ FftTables fft_tables(uint32_t n, uint32_t max_len) {
 	FftTables T;
 	T.n = n;
 	T.len = n;
-	if (n >= 2 && largest_prime_factor(n) > 47) {
+	if (n >= 2 && largest_prime_factor(n) > 7) {
 		const uint32_t m = smooth_at_least(2 * n - 1);
 		if (m <= max_len) T.bluestein = true, T.len = m;
 	}

@@ -19,9 +19,9 @@ def run(nlc, n, copies, dt, beta, psi, steps, batching):
     return out
 
 
-# 86 = 2 x 43 (direct radix-43 pass), 97 / 211 / 997 / 3001 prime (Bluestein) and
-# 1000 smooth: every FFT path of the shared-memory transform
-@pytest.mark.parametrize("n", [2, 8, 12, 64, 86, 97, 100, 211, 256, 512, 997, 1000, 1024, 2048, 3001])
+# 70 = 2 x 5 x 7 (direct radix-5 and radix-7 passes), 39 / 86 (factors 13, 43) and 97 / 211 / 997 /
+# 3001 prime (Bluestein), 1000 smooth: every FFT path and every team width of the shared-memory step
+@pytest.mark.parametrize("n", [2, 8, 12, 39, 64, 70, 86, 97, 100, 211, 256, 512, 997, 1000, 1024, 2048, 3001])
 def test_against_oracle(gpu, n):
     copies, dt = 11, 0.01
     steps, b = (20, 10) if n <= 2048 else (4, 2)   # the oracle's prime-length DFT is O(n^2)
