@@ -59,7 +59,9 @@ enum {
 	NLC_FLAG_NO_TUNE = 2,         /* skip the autotuner, use the heuristic launch shape */
 	NLC_FLAG_CANONICAL_SHAPE = 4, /* launch shape from the chain length alone (up to 8 sites per lane), so
 	                                 ensembles of equal length can share batched launches */
-	NLC_FLAG_COMPACT_DIAG = 8     /* fewer partial rows in the diagnostics (less device memory per plan) */
+	NLC_FLAG_COMPACT_DIAG = 8,    /* fewer partial rows in the diagnostics (less device memory per plan) */
+	NLC_FLAG_SHARED_GPU = 16      /* one work unit per block instead of a persistent grid: blocks retire as
+	                                 they finish, so launches on other streams interleave with this plan's */
 };
 
 /*
@@ -199,7 +201,11 @@ typedef struct nlc_server_config {
 	int32_t device;              /* CUDA device */
 	uint64_t hbm_budget_bytes;   /* device memory for admitted requests (0 = 60% of free memory) */
 	int32_t max_active;          /* requests integrated at the same time (0 = 256) */
-	int32_t streams;             /* CUDA streams in the pool (0 = 8) */
+	int32_t streams;             /* CUDA streams in the pool (0 = 16) */
+	/* longest wanted block lifetime of one launch: a round of kernel_batching steps is integrated
+	   by launches of fewer steps when one block would run longer, so that newly arrived work finds
+	   free SMs soon (0 = 3 ms; < 0 = every round in one launch).  Results are bit-identical. */
+	double quantum_ms;
 } nlc_server_config;
 
 enum { NLC_REQ_QUEUED = 0, NLC_REQ_RUNNING = 1, NLC_REQ_DONE = 2, NLC_REQ_FAILED = 3 };
@@ -209,7 +215,10 @@ typedef struct nlc_request_status {
 	int32_t error;               /* status code of a failed request (NLC_EBLOWUP: non-finite entropy) */
 	uint64_t steps_done;
 	uint64_t samples;            /* diagnostics samples taken so far (t = 0 included) */
-	double submit_ms, start_ms, finish_ms;   /* server clock, ms since nlc_server_create */
+	double submit_ms;            /* server clock, ms since nlc_server_create: submitted */
+	double start_ms;             /* admitted (HBM budget available) */
+	double ready_ms;             /* plan, device state and t = 0 sample ready */
+	double finish_ms;            /* done or failed */
 } nlc_request_status;
 
 int nlc_server_create(const nlc_server_config *config, nlc_server **server);

@@ -56,13 +56,13 @@ class _CModel(ctypes.Structure):
 
 class _CServerConfig(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int32), ("hbm_budget_bytes", ctypes.c_uint64), ("max_active", ctypes.c_int32),
-                ("streams", ctypes.c_int32)]
+                ("streams", ctypes.c_int32), ("quantum_ms", ctypes.c_double)]
 
 
 class _CRequestStatus(ctypes.Structure):
     _fields_ = [("state", ctypes.c_int32), ("error", ctypes.c_int32), ("steps_done", ctypes.c_uint64),
                 ("samples", ctypes.c_uint64), ("submit_ms", ctypes.c_double), ("start_ms", ctypes.c_double),
-                ("finish_ms", ctypes.c_double)]
+                ("ready_ms", ctypes.c_double), ("finish_ms", ctypes.c_double)]
 
 
 _lib = None
@@ -297,8 +297,8 @@ def linenergies_noalloc(model, chain_length, copies, m, state_ptr, lin_ptr, entr
 class Server:
     """Continuous-batching request server on one GPU (nlc_server_* in include/nlchains.h)."""
 
-    def __init__(self, device=0, hbm_budget_bytes=0, max_active=0, streams=0):
-        cfg = _CServerConfig(device, hbm_budget_bytes, max_active, streams)
+    def __init__(self, device=0, hbm_budget_bytes=0, max_active=0, streams=0, quantum_ms=0.0):
+        cfg = _CServerConfig(device, hbm_budget_bytes, max_active, streams, quantum_ms)
         self._h = ctypes.c_void_p()
         _check(lib().nlc_server_create(ctypes.byref(cfg), ctypes.byref(self._h)))
         self._models = {}
@@ -328,7 +328,8 @@ class Server:
         st = _CRequestStatus()
         _check(lib().nlc_server_poll(self._h, rid, ctypes.byref(st)))
         return {"state": st.state, "error": st.error, "steps_done": st.steps_done, "samples": st.samples,
-                "submit_ms": st.submit_ms, "start_ms": st.start_ms, "finish_ms": st.finish_ms}
+                "submit_ms": st.submit_ms, "start_ms": st.start_ms, "ready_ms": st.ready_ms,
+                "finish_ms": st.finish_ms}
 
     def wait(self, rid, timeout_ms=-1):
         _check(lib().nlc_server_wait(self._h, rid, int(timeout_ms)))

@@ -64,7 +64,7 @@ __global__ void dnls_move_kernel(double2 *__restrict__ psi, const DnlsArgs a) {
 
 		for (uint32_t i = 0; i < a.steps; i++) {
 			for (int k = 0; k < 7; k++) {
-				const double coef = (k == 0 && i != 0) ? a.nl[7] : a.nl[k];
+				const double coef = (k == 0 && (i != 0 || (a.seg & NLC_SEG_CONTINUE))) ? a.nl[7] : a.nl[k];
 				for (int j = t; j < n; j += T) x[j] = nonlinear_rotate(x[j], -coef, a.fft.k1);
 				team_sync<BLOCK>();
 				double2 *r = fft_team<BLOCK, false>(a.fft, x, y, t, T);
@@ -76,8 +76,12 @@ __global__ void dnls_move_kernel(double2 *__restrict__ psi, const DnlsArgs a) {
 				y = x == buf0 ? buf1 : buf0;
 			}
 		}
-		if (active)
-			for (int j = t; j < n; j += T) g[j] = nonlinear_rotate(x[j], -a.nl_final, a.fft.k1);
+		if (active) {
+			if (a.seg & NLC_SEG_OPEN)
+				for (int j = t; j < n; j += T) g[j] = x[j];
+			else
+				for (int j = t; j < n; j += T) g[j] = nonlinear_rotate(x[j], -a.nl_final, a.fft.k1);
+		}
 		team_sync<BLOCK>();
 	}
 

@@ -57,8 +57,14 @@ struct PlanInfo {
 	RealArgs args;          // integrator constants (device pointers included)
 	size_t device_bytes = 0;  // device memory held by the plan
 	int sms = 0;
+	double unit_step_us = 0;  // estimated time of one block's step with its SM fully shared
 };
 bool plan_info(const nlc_plan *plan, PlanInfo *info);
+// free a plan's device memory in the order of `stream` (after the work already queued there),
+// without the device-wide wait of nlc_plan_destroy
+void plan_destroy_ordered(nlc_plan *plan, cudaStream_t stream);
+// nlc_move of one segment of a round (seg: NLC_SEG_* flags)
+int move_segment(nlc_plan *plan, void *state, uint32_t steps, uint32_t seg, cudaStream_t stream);
 // a batched launch of the resident integrator (args.batch / nbatch / batch_units set)
 cudaError_t launch_real_move_batch(int model, int variant, const RealShape &shape, const RealArgs &args,
                                    cudaStream_t stream);

@@ -34,8 +34,15 @@ struct BatchJob {
 	const double *mp2_site;          // dDNKG per-site m_x + 2
 	unsigned long long unit_begin;   // first work unit of this ensemble in the launch
 	uint32_t n, copies, steps;
-	uint32_t pad;
+	uint32_t seg;                    // NLC_SEG_* of this ensemble's segment
 };
+
+// Segments: one round of kernel_batching steps may be integrated by several launches.  A launch
+// that continues a round starts with the merged drift (DNLS: merged nonlinear rotation) instead of
+// the round's leading c[0] sub-step, and a launch that leaves the round open stores the state
+// without the closing c[7] sub-step.  The operations and their order are those of the single
+// launch, so a round split into segments gives bit-identical results.
+enum : uint32_t { NLC_SEG_CONTINUE = 1, NLC_SEG_OPEN = 2 };
 
 // Kernel arguments of the real-model integrators, passed by value (kernel parameter bank).
 struct RealArgs {
@@ -62,6 +69,7 @@ struct RealArgs {
 	const BatchJob *batch;
 	int32_t nbatch;
 	unsigned long long batch_units;
+	uint32_t seg;          // NLC_SEG_* of an unbatched launch (batched: per table entry)
 };
 
 // Launch shape of the resident integrator.
@@ -137,6 +145,7 @@ struct DnlsArgs {
 	const double2 *lin_tables; // [7][n] exp(-i dt d_k omega_j)/n
 	unsigned long long *work_counter;
 	int team;                  // lanes per chain of the warp-team variant (power of two, 4 .. 32)
+	uint32_t seg;              // NLC_SEG_*
 };
 cudaError_t launch_dnls_move(const DnlsArgs &a, double2 *psi, int blocks, int threads, size_t smem,
                              int team_block, cudaStream_t stream);

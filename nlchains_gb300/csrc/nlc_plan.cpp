@@ -110,16 +110,20 @@ struct nlc_plan {
 	int diag_blocks = 0, diag_threads = 0, diag_team_block = 0, diag_rows = 0;
 	size_t diag_smem = 0;
 	int tier = 0;   // 1 = resident lanes (G <= 32), 2 = resident block (G > 32), 3 = DNLS shared-memory
+	double unit_step_us = 0;   // estimated time of one block's step with its SM fully shared
 
+	// Device memory comes from the stream-ordered allocator, so that creating and destroying plans
+	// (the request server does it per request) never synchronises the whole device.
+	cudaStream_t free_stream = nullptr;   // stream the allocations are returned on
 	~nlc_plan() {
-		for (void *p : allocs) cudaFree(p);
+		for (void *p : allocs) cudaFreeAsync(p, free_stream);
 	}
 
 	template <typename T>
 	int dalloc(T **p, size_t count) {
 		void *q = nullptr;
-		const cudaError_t e = cudaMalloc(&q, std::max<size_t>(count, 1) * sizeof(T));
-		if (e != cudaSuccess) return cuda_status(e, "cudaMalloc");
+		const cudaError_t e = cudaMallocAsync(&q, std::max<size_t>(count, 1) * sizeof(T), cudaStreamLegacy);
+		if (e != cudaSuccess) return cuda_status(e, "cudaMallocAsync");
 		allocs.push_back(q);
 		device_bytes += std::max<size_t>(count, 1) * sizeof(T);
 		*p = static_cast<T *>(q);
@@ -282,6 +286,32 @@ RealShape autotune_shape(nlc_plan &P, int model, int variant) {
 	return best;
 }
 
+// Time of one step of one block (chains_per_block chains) when its SM also runs per_sm - 1 other
+// such blocks: work in FP64 lane operations (an FMA is one) over the SM's FP64 rate at the fraction
+// of peak the kernel reaches when the SM is full.  Work per site and step (7 sub-steps): the real
+// models' drift, neighbour terms and kick, the Toda exponential (~22 operations), the DNLS phase
+// rotation (sincos ~31) and two Stockham transforms (~3 operations per element and radix-2 level;
+// a Bluestein transform is two passes of the padded length plus the chirp products).  Used by the
+// request server to split long rounds into launches of bounded length.
+double unit_step_estimate(int model, uint32_t n, uint32_t len, bool bluestein, int chains_per_block, int per_sm) {
+	double per_site, eff;
+	switch (model) {
+		case NLC_TODA: per_site = 7 * 32.; eff = 0.8; break;
+		case NLC_FPUT: per_site = 7 * 8.; eff = 0.85; break;
+		case NLC_DNLS: {
+			const double lg = std::log2(double(std::max<uint32_t>(len, 2)));
+			const double fft = bluestein ? (2 * 3 * lg * len + 4. * len) / n + 8 : 3 * lg;
+			per_site = 7 * (44 + 2 * fft);
+			eff = 0.5;
+			break;
+		}
+		default: per_site = 7 * 6.; eff = 0.85;
+	}
+	// 600 G FP64 lane operations per second on 152 SMs: ~3950 per SM and microsecond
+	const double sm_ops_per_us = 3950.;
+	return per_site * double(n) * chains_per_block * per_sm / (eff * sm_ops_per_us);
+}
+
 int setup_fft(nlc_plan &P, FftPlanDev &f) {
 	const uint32_t n = P.m.chain_length;
 	// the largest pass the shared-memory kernels can hold: one team of 2 x len complex per block
@@ -381,8 +411,17 @@ int set_smem_attr(const void *k, size_t smem, const cudaDeviceProp &prop) {
 	if (rc) return rc;
 	const size_t room = prop.sharedMemPerBlockOptin - attr.sharedSizeBytes;   // static shared memory counts too
 	if (smem > room) return set_error(NLC_EUNSUPPORTED, "chain_length too large for the shared-memory kernels");
-	return cuda_status(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(room)),
-	                   "cudaFuncSetAttribute");
+	// once per (device, kernel) for the process: the limit only ever goes to the device maximum
+	static std::mutex mu;
+	static std::map<std::pair<int, const void *>, bool> done;
+	int dev = 0;
+	cudaGetDevice(&dev);
+	std::lock_guard<std::mutex> lk(mu);
+	if (done[{dev, k}]) return NLC_OK;
+	rc = cuda_status(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(room)),
+	                 "cudaFuncSetAttribute");
+	if (!rc) done[{dev, k}] = true;
+	return rc;
 }
 
 }  // namespace
@@ -439,8 +478,10 @@ extern "C" int nlc_plan_create(const nlc_model *model, nlc_plan **out) {
 		P->norm = (0.5 / model->copies) / n;   // DNKG_FPUT_Toda.cpp:129
 	}
 
-	if ((rc = P->dalloc(&P->d_counter, 2))) return rc;
-	if ((rc = cuda_status(cudaMemset(P->d_counter, 0, 2 * sizeof(unsigned long long)), "cudaMemset"))) return rc;
+	{   // zeroed by a copy, not a memset kernel, so that plan creation needs no free SM
+		const unsigned long long zero[2] = {0, 0};
+		if ((rc = P->upload(&P->d_counter, zero, 2))) return rc;
+	}
 
 	if (mdl == NLC_DNLS) {
 		DnlsArgs &d = P->da;
@@ -488,7 +529,12 @@ extern "C" int nlc_plan_create(const nlc_model *model, nlc_plan **out) {
 			return rc;
 		if (per_sm < 1) return set_error(NLC_EUNSUPPORTED, "DNLS kernel does not fit an SM");
 		const int teams = P->dnls_team_block ? 1 : P->dnls_threads / d.team;
+		P->unit_step_us = unit_step_estimate(NLC_DNLS, n, len, d.fft.bluestein, teams, per_sm);
 		P->dnls_blocks = int(std::min<unsigned long long>((model->copies + teams - 1) / teams, (unsigned long long) per_sm * sms));
+		if (model->flags & NLC_FLAG_SHARED_GPU)   // one block per unit of work: a warp's chains per unit
+			P->dnls_blocks = int(std::min<unsigned long long>(
+			    P->dnls_team_block ? model->copies : (model->copies + (32 / d.team) - 1) / (32 / d.team) / 4 + 1,
+			    0x7fffffffull));
 		P->tier = 3;
 	} else {
 		RealArgs &a = P->ra;
@@ -543,14 +589,25 @@ extern "C" int nlc_plan_create(const nlc_model *model, nlc_plan **out) {
 			                                          : autotune_shape(*P, mdl, P->variant);
 		}
 		if (!P->rs.blocks) return set_error(NLC_EUNSUPPORTED, "no launchable integrator shape for this chain_length");
+		if (model->flags & NLC_FLAG_SHARED_GPU) {
+			const unsigned long long gpb = P->rs.threads / P->rs.lanes;
+			P->rs.blocks = int(std::min<unsigned long long>((model->copies + gpb - 1) / gpb, 0x7fffffffull));
+		}
 		a.lanes = P->rs.lanes;
 		P->tier = P->rs.lanes > 32 ? 2 : 1;
+		int per_sm = 1;
+		cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, real_move_kernel(mdl, P->variant, P->rs.sites),
+		                                              P->rs.threads, 0);
+		P->unit_step_us = unit_step_estimate(mdl, n, 0, false, P->rs.threads / P->rs.lanes, std::max(per_sm, 1));
 	}
 	if ((rc = setup_diagnostics(*P))) return rc;
 	{
 		const void *k = lin_kernel_ptr(mdl, P->diag_team_block);
 		if ((rc = set_smem_attr(k, P->diag_smem, P->prop))) return rc;
 	}
+	// every allocation and upload above is ordered on the legacy stream: complete them before the
+	// plan is used from other streams
+	if ((rc = cuda_status(cudaStreamSynchronize(cudaStreamLegacy), "plan set-up"))) return rc;
 	*out = P.release();
 	return NLC_OK;
 }
@@ -564,12 +621,22 @@ bool nlc::plan_info(const nlc_plan *P, PlanInfo *info) {
 	info->args.lanes = P->rs.lanes;
 	info->device_bytes = P->device_bytes;
 	info->sms = P->prop.multiProcessorCount;
+	info->unit_step_us = P->unit_step_us;
 	return true;
 }
 
 extern "C" int nlc_plan_destroy(nlc_plan *plan) {
+	if (!plan) return NLC_OK;
+	// the caller may still have work using the plan on any stream: wait for the device, as cudaFree did
+	cudaDeviceSynchronize();
 	delete plan;
 	return NLC_OK;
+}
+
+void nlc::plan_destroy_ordered(nlc_plan *plan, cudaStream_t stream) {
+	if (!plan) return;
+	plan->free_stream = stream;
+	delete plan;
 }
 
 extern "C" int nlc_plan_shape(const nlc_plan *P, int32_t *lanes, int32_t *sites, int32_t *threads, int32_t *tier) {
@@ -588,18 +655,23 @@ extern "C" int nlc_plan_omegas(const nlc_plan *P, double *omegas) {
 }
 
 extern "C" int nlc_move(nlc_plan *P, void *state, uint32_t steps, void *stream) {
+	return nlc::move_segment(P, state, steps, 0, static_cast<cudaStream_t>(stream));
+}
+
+int nlc::move_segment(nlc_plan *P, void *state, uint32_t steps, uint32_t seg, cudaStream_t st) {
 	if (!P || !state) return set_error(NLC_EINVAL, "NULL argument");
 	if (!steps) return NLC_OK;
-	cudaStream_t st = static_cast<cudaStream_t>(stream);
 	if (P->m.model == NLC_DNLS) {
 		DnlsArgs a = P->da;
 		a.steps = steps;
+		a.seg = seg;
 		return cuda_status(launch_dnls_move(a, static_cast<double2 *>(state), P->dnls_blocks, P->dnls_threads,
 		                                    P->dnls_smem, P->dnls_team_block, st),
 		                   "DNLS move launch");
 	}
 	RealArgs a = P->ra;
 	a.steps = steps;
+	a.seg = seg;
 	return cuda_status(launch_real_move(P->m.model, P->variant, P->rs, static_cast<double *>(state), a, st), "move launch");
 }
 

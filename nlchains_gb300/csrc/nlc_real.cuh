@@ -121,7 +121,7 @@ __global__ void real_move_kernel_t(double2 *__restrict__ state, const RealArgs a
 	// the ensemble of the current unit: the launch's own, or one entry of the batch table
 	int cur_job = -1;
 	double2 *st = state;
-	uint32_t n = a.n, copies = a.copies, steps = a.steps;
+	uint32_t n = a.n, copies = a.copies, steps = a.steps, seg = a.seg;
 	const double *mp2_site = a.mp2_site;
 	unsigned long long unit_base = 0;
 	int full = 0, ne = 0, first = 0;
@@ -162,7 +162,7 @@ __global__ void real_move_kernel_t(double2 *__restrict__ state, const RealArgs a
 		if (a.batch && s_job != cur_job) {
 			cur_job = s_job;
 			const BatchJob &J = a.batch[cur_job];
-			st = J.state, n = J.n, copies = J.copies, steps = J.steps, mp2_site = J.mp2_site;
+			st = J.state, n = J.n, copies = J.copies, steps = J.steps, mp2_site = J.mp2_site, seg = J.seg;
 			unit_base = J.unit_begin;
 			layout();
 		}
@@ -183,11 +183,12 @@ __global__ void real_move_kernel_t(double2 *__restrict__ state, const RealArgs a
 			}
 		}
 
+		const double cd_lead = (seg & NLC_SEG_CONTINUE) ? a.cd0_merged : a.cd[0];
 		for (uint32_t i = 0; i < steps; i++) {
 #pragma unroll
 			for (int k = 0; k < 7; k++) {
 				// the trailing drift of step i-1 (c[7]) merged with the leading drift of step i (c[0])
-				const double cd = (k == 0 && i != 0) ? a.cd0_merged : a.cd[k];
+				const double cd = k == 0 ? (i != 0 ? a.cd0_merged : cd_lead) : a.cd[k];
 #pragma unroll
 				for (int j = 0; j < E; j++) x[j + 1] = dfma(cd, p[j], x[j + 1]);
 
@@ -224,9 +225,10 @@ __global__ void real_move_kernel_t(double2 *__restrict__ state, const RealArgs a
 		}
 
 		if (active) {
+			const bool open = seg & NLC_SEG_OPEN;
 #pragma unroll
 			for (int j = 0; j < E; j++)
-				if (j < ne) cp[j] = make_double2(dfma(a.cd_final, p[j], x[j + 1]), p[j]);
+				if (j < ne) cp[j] = make_double2(open ? x[j + 1] : dfma(a.cd_final, p[j], x[j + 1]), p[j]);
 		}
 	}
 

@@ -49,22 +49,29 @@ struct Request {
 	double2 *d_state = nullptr;
 	double *d_diag = nullptr;       // [n] linenergies + [2] entropies
 	double *h_diag = nullptr;       // pinned
-	int stream_slot = 0;
+	int stream_slot = -1;           // slot of the request's last launch group (-1: the preparer's stream)
 
-	uint64_t t = 0;
+	uint64_t t = 0;                 // steps integrated
+	uint32_t round_pos = 0;         // steps of the current round of `batching` steps already integrated
+	uint32_t seg_steps = 0;         // steps of the launch in flight
+	bool seg_samples = false;       // the launch in flight closes a round and takes its sample
 	std::vector<double> entropies;  // {WT, INF} per sample
 	std::vector<double> lin;
 	int state = NLC_REQ_QUEUED;
 	int error = NLC_OK;
 	bool prepared = false;          // plan, state and t = 0 sample ready (set by the scheduler)
 	bool in_flight = false;         // a launch group with this request is on the GPU
-	double submit_ms = 0, start_ms = 0, finish_ms = 0;
+	bool sampled0 = false;          // the t = 0 diagnostics sample has been taken
+	double submit_ms = 0, start_ms = 0, ready_ms = 0, finish_ms = 0;
 
-	void release_device() {
-		if (plan) nlc_plan_destroy(plan), plan = nullptr;
-		cudaFree(d_state), d_state = nullptr;
-		cudaFree(d_diag), d_diag = nullptr;
-		cudaFreeHost(h_diag), h_diag = nullptr;
+	// device memory goes back in the order of `stream`: no device-wide wait.  The server passes a
+	// stream with no queued work once the host has seen the request's last event complete, so the
+	// memory is reusable at once; a free queued behind another group's kernel would hold up every
+	// later allocation that reuses it.
+	void release_device(cudaStream_t stream) {
+		if (plan) plan_destroy_ordered(plan, stream), plan = nullptr;
+		if (d_state) cudaFreeAsync(d_state, stream), d_state = nullptr;
+		if (d_diag) cudaFreeAsync(d_diag, stream), d_diag = nullptr;
 	}
 };
 
@@ -101,38 +108,71 @@ struct nlc_server {
 	uint64_t next_id = 1;
 	uint64_t used_bytes = 0;
 	bool stop = false;
-	std::thread worker, preparer;
+	std::thread worker;
+	std::vector<std::thread> preparers;
+	int prio_high = 0;
 	std::condition_variable cv_prepare;
-	cudaStream_t prep_stream = nullptr;
+	cudaStream_t free_stream = nullptr;   // final read-backs and frees only: never holds queued kernels
+	double quantum_us = 3000;
 	std::vector<cudaStream_t> streams;
 	std::vector<cudaEvent_t> events;
 	// per stream slot: the launch group on the GPU, its device job table and pinned staging
 	std::vector<std::vector<Request *>> slot_reqs;
+	std::vector<char> slot_sample_only;   // the group only takes the t = 0 samples
 	std::vector<BatchJob *> d_tables;
 	std::vector<size_t> d_table_cap;
 	std::vector<BatchJob *> h_slot;
 	std::vector<size_t> h_slot_cap;
 	std::string fatal;
+	// pinned read-back buffers, reused (cudaFreeHost would wait for the whole device)
+	std::multimap<size_t, double *> pinned_free;
+	std::vector<double *> pinned_all;
 
 	double now_ms() const { return std::chrono::duration<double, std::milli>(Clock::now() - t0).count(); }
 };
 
 namespace {
 
-int admit(nlc_server *S, Request &R) {
+double *pinned_get(nlc_server *S, size_t count) {
+	size_t cap = 64;
+	while (cap < count) cap <<= 1;
+	{
+		std::lock_guard<std::mutex> lk(S->mu);
+		auto it = S->pinned_free.find(cap);
+		if (it != S->pinned_free.end()) {
+			double *p = it->second;
+			S->pinned_free.erase(it);
+			return p;
+		}
+	}
+	double *p = nullptr;
+	if (cudaMallocHost(&p, cap * sizeof(double)) != cudaSuccess) return nullptr;
+	std::lock_guard<std::mutex> lk(S->mu);
+	S->pinned_all.push_back(p);
+	return p;
+}
+
+// caller holds S->mu
+void pinned_put(nlc_server *S, double *p, size_t count) {
+	if (!p) return;
+	size_t cap = 64;
+	while (cap < count) cap <<= 1;
+	S->pinned_free.emplace(cap, p);
+}
+
+int admit(nlc_server *S, Request &R, cudaStream_t st) {
 	int rc = cudaSetDevice(S->cfg.device) == cudaSuccess ? NLC_OK : set_error(NLC_ECUDA, "cudaSetDevice");
 	if (rc) return rc;
 	nlc_model m = R.model;
 	m.masses = R.masses.empty() ? nullptr : R.masses.data();
 	m.entropy_mask = R.mask.empty() ? nullptr : R.mask.data();
-	m.flags |= NLC_FLAG_CANONICAL_SHAPE | NLC_FLAG_COMPACT_DIAG | NLC_FLAG_NO_TUNE;
+	m.flags |= NLC_FLAG_CANONICAL_SHAPE | NLC_FLAG_COMPACT_DIAG | NLC_FLAG_NO_TUNE | NLC_FLAG_SHARED_GPU;
 	if ((rc = nlc_plan_create(&m, &R.plan))) return rc;
 	plan_info(R.plan, &R.info);
 	const size_t n = m.chain_length;
-	if ((rc = cuda_status(cudaMalloc(&R.d_state, R.state_bytes), "cudaMalloc state"))) return rc;
-	if ((rc = cuda_status(cudaMalloc(&R.d_diag, (n + 2) * sizeof(double)), "cudaMalloc"))) return rc;
-	if ((rc = cuda_status(cudaMallocHost(&R.h_diag, (n + 2) * sizeof(double)), "cudaMallocHost"))) return rc;
-	cudaStream_t st = S->prep_stream;
+	if ((rc = cuda_status(cudaMallocAsync(&R.d_state, R.state_bytes, st), "cudaMallocAsync state"))) return rc;
+	if ((rc = cuda_status(cudaMallocAsync(&R.d_diag, (n + 2) * sizeof(double), st), "cudaMallocAsync"))) return rc;
+	if (!(R.h_diag = pinned_get(S, n + 2))) return set_error(NLC_ENOMEM, "pinned read-back buffer");
 	if ((rc = cuda_status(cudaMemcpyAsync(R.d_state, R.host_in.data(), R.state_bytes, cudaMemcpyHostToDevice, st),
 	                      "upload")))
 		return rc;
@@ -151,7 +191,9 @@ void retire(nlc_server *S, std::unique_ptr<Request> R, int state, int error) {
 	R->state = state;
 	R->error = error;
 	R->finish_ms = S->now_ms();
-	R->release_device();
+	R->release_device(S->free_stream);
+	pinned_put(S, R->h_diag, R->model.chain_length + 2);
+	R->h_diag = nullptr;
 	if (R->need_bytes <= S->used_bytes) S->used_bytes -= R->need_bytes;
 	S->where[R->id] = state;
 	S->finished[R->id] = std::move(R);
@@ -173,39 +215,57 @@ BatchJob *class_table(nlc_server *S, size_t slot, size_t count) {
 // state and takes the t = 0 sample, off the scheduler thread so that rounds keep running.
 void preparer_loop(nlc_server *S) {
 	cudaSetDevice(S->cfg.device);
+	cudaStream_t st = nullptr;
+	if (cudaStreamCreateWithPriority(&st, cudaStreamNonBlocking, S->prio_high) != cudaSuccess) st = nullptr;
 	for (;;) {
 		Request *R;
 		{
 			std::unique_lock<std::mutex> lk(S->mu);
 			S->cv_prepare.wait(lk, [&] { return S->stop || !S->to_prepare.empty(); });
-			if (S->stop) return;
+			if (S->stop) {
+				if (st) cudaStreamSynchronize(st), cudaStreamDestroy(st);
+				return;
+			}
 			R = S->to_prepare.front();
 			S->to_prepare.pop_front();
 		}
-		int rc = admit(S, *R);
-		if (!rc) rc = sample(S, *R, S->prep_stream);
-		if (!rc) rc = cuda_status(cudaStreamSynchronize(S->prep_stream), "request set-up");
+		int rc = st ? admit(S, *R, st) : set_error(NLC_ECUDA, "preparer stream");
+		if (!rc) rc = cuda_status(cudaStreamSynchronize(st), "request set-up");
 		std::lock_guard<std::mutex> lk(S->mu);
-		if (rc) {
-			R->error = rc;
-		} else {
-			const size_t n = R->model.chain_length;
-			R->entropies.push_back(R->h_diag[n]), R->entropies.push_back(R->h_diag[n + 1]);
-			if (!std::isfinite(R->h_diag[n]) || !std::isfinite(R->h_diag[n + 1])) R->error = NLC_EBLOWUP;
-		}
+		if (rc) R->error = rc;
+		R->ready_ms = S->now_ms();
 		S->ready.push_back(R);
 		S->cv_work.notify_all();
 	}
 }
 
-// Launch the next kernel_batching steps plus one sample for a group of idle requests of one class
-// (several: one packed launch; one: its own plan's launch) on stream slot `slot`.
+// Steps of the next launch of R: the rest of its round, or, when one block would then run longer
+// than the quantum, an equal share of the rest that does not.
+uint32_t segment_steps(const nlc_server *S, const Request &R) {
+	const uint32_t left = R.batching - R.round_pos;
+	const double est = R.info.unit_step_us;
+	if (S->quantum_us <= 0 || !(est > 0) || est * left <= S->quantum_us) return left;
+	const uint32_t cap = uint32_t(std::max(1., std::floor(S->quantum_us / est)));
+	const uint32_t parts = (left + cap - 1) / cap;
+	return (left + parts - 1) / parts;
+}
+
+// Launch the next segment of every request of a group of idle requests of one class (several: one
+// packed launch; one: its own plan's launch) on stream slot `slot`, plus the sample of each request
+// whose round the segment closes.
 int launch_group(nlc_server *S, size_t slot, const std::vector<Request *> &reqs) {
 	cudaStream_t st = S->streams[slot];
 	int rc = NLC_OK;
+	for (Request *R : reqs) {
+		R->seg_steps = segment_steps(S, *R);
+		R->seg_samples = R->round_pos + R->seg_steps == R->batching;
+	}
+	auto seg_flags = [](const Request &R) {
+		return (R.round_pos ? NLC_SEG_CONTINUE : 0u) | (R.seg_samples ? 0u : NLC_SEG_OPEN);
+	};
 	if (reqs.size() == 1 || reqs[0]->model.model == NLC_DNLS) {
 		for (Request *R : reqs)
-			if (!rc) rc = nlc_move(R->plan, R->d_state, R->batching, st);
+			if (!rc) rc = move_segment(R->plan, R->d_state, R->seg_steps, seg_flags(*R), st);
 	} else {
 		if (S->h_slot_cap[slot] < reqs.size()) {
 			cudaFreeHost(S->h_slot[slot]);
@@ -225,8 +285,8 @@ int launch_group(nlc_server *S, size_t slot, const std::vector<Request *> &reqs)
 			h[i].unit_begin = units;
 			h[i].n = R->model.chain_length;
 			h[i].copies = R->model.copies;
-			h[i].steps = R->batching;
-			h[i].pad = 0;
+			h[i].steps = R->seg_steps;
+			h[i].seg = seg_flags(*R);
 			units += (R->model.copies + gpb - 1) / gpb;
 		}
 		BatchJob *d = class_table(S, slot, reqs.size());
@@ -237,16 +297,14 @@ int launch_group(nlc_server *S, size_t slot, const std::vector<Request *> &reqs)
 		RealArgs a = reqs[0]->info.args;
 		a.batch = d, a.nbatch = int(reqs.size()), a.batch_units = units;
 		RealShape sh = reqs[0]->info.shape;
-		int per_sm = 0;
-		cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-		    &per_sm, real_move_kernel(reqs[0]->info.model, reqs[0]->info.variant, sh.sites), sh.threads, 0);
-		sh.blocks = int(std::min<unsigned long long>(units, (unsigned long long) std::max(per_sm, 1) * reqs[0]->info.sms));
+		// one block per unit: blocks retire as they finish, so the groups on other streams interleave
+		sh.blocks = int(std::min<unsigned long long>(units, 0x7fffffffull));
 		if ((rc = cuda_status(launch_real_move_batch(reqs[0]->info.model, reqs[0]->info.variant, sh, a, st),
 		                      "batched move launch")))
 			return rc;
 	}
 	for (Request *R : reqs)
-		if (!rc) rc = sample(S, *R, st);
+		if (!rc && R->seg_samples) rc = sample(S, *R, st);
 	if (!rc) rc = cuda_status(cudaEventRecord(S->events[slot], st), "cudaEventRecord");
 	return rc;
 }
@@ -318,11 +376,19 @@ void worker_loop(nlc_server *S) {
 				S->fatal = cudaGetErrorString(e);
 				for (Request *R : g) R->error = NLC_ECUDA;
 			}
+			const bool sample_only = S->slot_sample_only[slot];
 			for (Request *R : g) {
 				R->in_flight = false;
 				if (R->error) continue;
 				const size_t n = R->model.chain_length;
-				R->t += R->batching;
+				if (sample_only) {
+					R->sampled0 = true;
+				} else {
+					R->t += R->seg_steps;
+					R->round_pos += R->seg_steps;
+					if (!R->seg_samples) continue;
+					R->round_pos = 0;
+				}
 				R->entropies.push_back(R->h_diag[n]), R->entropies.push_back(R->h_diag[n + 1]);
 				if (!std::isfinite(R->h_diag[n]) || !std::isfinite(R->h_diag[n + 1])) R->error = NLC_EBLOWUP;
 			}
@@ -333,11 +399,16 @@ void worker_loop(nlc_server *S) {
 		// 2. retire finished / failed idle requests, and group the idle ones with steps left
 		std::map<ClassKey, std::vector<Request *>> classes;
 		std::vector<std::vector<Request *>> singles;
+		std::vector<Request *> first_samples;
 		{
 			std::lock_guard<std::mutex> lk(S->mu);
 			for (auto &kv : S->active) {
 				Request *R = kv.second.get();
 				if (!R->prepared || R->in_flight) continue;
+				if (!R->error && !R->sampled0) {
+					first_samples.push_back(R);
+					continue;
+				}
 				if (R->error || R->t >= R->steps) {
 					finished.push_back(R);
 					continue;
@@ -356,7 +427,8 @@ void worker_loop(nlc_server *S) {
 			// final state and energies; copies outside the lock
 			const size_t n = R->model.chain_length;
 			if (R->d_state && R->error != NLC_ECUDA) {
-				cudaMemcpy(R->host_in.data(), R->d_state, R->state_bytes, cudaMemcpyDeviceToHost);
+				cudaMemcpyAsync(R->host_in.data(), R->d_state, R->state_bytes, cudaMemcpyDeviceToHost, S->free_stream);
+				cudaStreamSynchronize(S->free_stream);
 				R->lin.assign(R->h_diag, R->h_diag + n);
 			}
 			std::lock_guard<std::mutex> lk(S->mu);
@@ -376,13 +448,26 @@ void worker_loop(nlc_server *S) {
 		std::stable_sort(groups.begin(), groups.end(),
 		                 [](const std::vector<Request *> &a, const std::vector<Request *> &b) { return a.size() > b.size(); });
 		size_t next = 0;
-		for (size_t slot = 0; slot < nslots && next < groups.size(); slot++) {
+		for (size_t slot = 0; slot < nslots && (next < groups.size() || !first_samples.empty()); slot++) {
 			if (!S->slot_reqs[slot].empty()) continue;
-			auto &g = groups[next++];
-			const int rc = launch_group(S, slot, g);
+			std::vector<Request *> g;
+			int rc = NLC_OK;
+			// the t = 0 samples of newly prepared requests go first, all in one group
+			const bool sample_only = !first_samples.empty();
+			if (sample_only) {
+				g.swap(first_samples);
+				for (Request *R : g)
+					if (!rc) rc = sample(S, *R, S->streams[slot]);
+				if (!rc) rc = cuda_status(cudaEventRecord(S->events[slot], S->streams[slot]), "cudaEventRecord");
+			} else {
+				g = groups[next++];
+				rc = launch_group(S, slot, g);
+			}
+			S->slot_sample_only[slot] = sample_only;
 			std::lock_guard<std::mutex> lk(S->mu);
 			for (Request *R : g) {
 				R->in_flight = true;
+				R->stream_slot = int(slot);
 				if (rc) R->error = rc;
 			}
 			S->slot_reqs[slot] = g;
@@ -400,6 +485,7 @@ extern "C" int nlc_server_create(const nlc_server_config *config, nlc_server **o
 	if (config) S->cfg = *config;
 	if (S->cfg.max_active <= 0) S->cfg.max_active = 256;
 	if (S->cfg.streams <= 0) S->cfg.streams = 16;
+	S->quantum_us = S->cfg.quantum_ms > 0 ? S->cfg.quantum_ms * 1e3 : S->cfg.quantum_ms < 0 ? 0. : 3000.;
 	int rc = cuda_status(cudaSetDevice(S->cfg.device), "cudaSetDevice");
 	if (rc) return rc;
 	if (!S->cfg.hbm_budget_bytes) {
@@ -415,17 +501,38 @@ extern "C" int nlc_server_create(const nlc_server_config *config, nlc_server **o
 		if ((rc = cuda_status(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "cudaEventCreate"))) return rc;
 		S->events.push_back(ev);
 	}
-	if ((rc = cuda_status(cudaStreamCreateWithFlags(&S->prep_stream, cudaStreamNonBlocking), "cudaStreamCreate")))
+	// request set-up (plan, upload) runs on preparer streams of the highest priority: it gates latency
+	int prio_low = 0, prio_high = 0;
+	cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high);
+	S->prio_high = prio_high;
+	if ((rc = cuda_status(cudaStreamCreateWithFlags(&S->free_stream, cudaStreamNonBlocking), "cudaStreamCreate")))
 		return rc;
+	// keep the memory returned by cudaFreeAsync cached in the device's pool between requests, and
+	// never let an allocation silently wait for another stream's pending free (the pool grows instead)
+	cudaMemPool_t pool;
+	if (cudaDeviceGetDefaultMemPool(&pool, S->cfg.device) == cudaSuccess) {
+		uint64_t threshold = UINT64_MAX;
+		cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &threshold);
+		int internal = 0;
+		cudaMemPoolSetAttribute(pool, cudaMemPoolReuseAllowInternalDependencies, &internal);
+	}
 	S->slot_reqs.resize(S->streams.size());
+	S->slot_sample_only.assign(S->streams.size(), 0);
 	S->d_tables.assign(S->streams.size(), nullptr);
 	S->d_table_cap.assign(S->streams.size(), 0);
 	S->h_slot.assign(S->streams.size(), nullptr);
 	S->h_slot_cap.assign(S->streams.size(), 0);
+	// job tables sized for max_active members up front: growing them later would synchronise
+	for (size_t i = 0; i < S->streams.size(); i++) {
+		const size_t cap = size_t(S->cfg.max_active);
+		if ((rc = cuda_status(cudaMalloc(&S->d_tables[i], cap * sizeof(BatchJob)), "cudaMalloc"))) return rc;
+		if ((rc = cuda_status(cudaMallocHost(&S->h_slot[i], cap * sizeof(BatchJob)), "cudaMallocHost"))) return rc;
+		S->d_table_cap[i] = S->h_slot_cap[i] = cap;
+	}
 	S->t0 = Clock::now();
 	nlc_server *raw = S.get();
 	S->worker = std::thread([raw] { worker_loop(raw); });
-	S->preparer = std::thread([raw] { preparer_loop(raw); });
+	for (int i = 0; i < 4; i++) S->preparers.emplace_back([raw] { preparer_loop(raw); });
 	*out = S.release();
 	return NLC_OK;
 }
@@ -439,11 +546,14 @@ extern "C" int nlc_server_destroy(nlc_server *S) {
 	S->cv_work.notify_all();
 	S->cv_prepare.notify_all();
 	if (S->worker.joinable()) S->worker.join();
-	if (S->preparer.joinable()) S->preparer.join();
+	for (auto &th : S->preparers)
+		if (th.joinable()) th.join();
 	cudaSetDevice(S->cfg.device);
-	if (S->prep_stream) cudaStreamSynchronize(S->prep_stream), cudaStreamDestroy(S->prep_stream);
 	for (cudaStream_t st : S->streams) cudaStreamSynchronize(st);
-	for (auto &kv : S->active) kv.second->release_device();
+	for (auto &kv : S->active) kv.second->release_device(S->free_stream);
+	cudaDeviceSynchronize();
+	if (S->free_stream) cudaStreamDestroy(S->free_stream);
+	for (double *p : S->pinned_all) cudaFreeHost(p);
 	for (BatchJob *p : S->d_tables) cudaFree(p);
 	for (BatchJob *p : S->h_slot) cudaFreeHost(p);
 	for (cudaStream_t st : S->streams) cudaStreamDestroy(st);
@@ -504,7 +614,7 @@ extern "C" int nlc_server_poll(nlc_server *S, uint64_t id, nlc_request_status *s
 	st->error = R->error;
 	st->steps_done = R->t;
 	st->samples = R->entropies.size() / 2;
-	st->submit_ms = R->submit_ms, st->start_ms = R->start_ms, st->finish_ms = R->finish_ms;
+	st->submit_ms = R->submit_ms, st->start_ms = R->start_ms, st->ready_ms = R->ready_ms, st->finish_ms = R->finish_ms;
 	return NLC_OK;
 }
 

@@ -79,6 +79,18 @@ def test_mixed_results_equal_alone(gpu):
         assert st["submit_ms"] <= st["start_ms"] <= st["finish_ms"]
 
 
+@pytest.mark.parametrize("quantum_ms", [1e-6, -1.0])
+def test_segmented_rounds_equal_alone(gpu, quantum_ms):
+    # 1e-6 ms: every round is integrated one step per launch (open segments, merged drift between
+    # them); -1: every round in one launch.  Both equal the run alone bit for bit.
+    reqs, results = run_mix(gpu, MIX, quantum_ms=quantum_ms)
+    for (rid, model, b, steps, state), (st, fstate, flin, ents, rc) in zip(reqs, results):
+        assert rc == gpu.OK and st["steps_done"] == steps and len(ents) == steps // b + 1
+        out, lin, aents = alone(gpu, model, b, steps, state)
+        assert np.array_equal(fstate, out), f"{model.name} n={model.chain_length}: segmented run differs"
+        assert np.abs(ents - aents).max() <= 1e-10 * max(1.0, np.abs(aents).max())
+
+
 def test_budget_admission_serialises(gpu):
     # a budget of one byte admits one request at a time (a request larger than the budget runs
     # alone when nothing else is active); all still complete with the same results
