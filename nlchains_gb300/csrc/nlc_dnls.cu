@@ -9,7 +9,8 @@
 //   psi <- psi exp(-i beta dt c_k |psi|^2)       (DNLS.cu:11-17; c_0 doubled when merged, DNLS.cpp:162)
 //   psi_k <- FFT(psi) * exp(-i dt d_k omega_k)/n  (DNLS/dispersion.cpp:19-26, DNLS.cu:19-25)
 //   psi <- IFFT(psi_k)
-// and finally psi <- psi exp(-i beta dt c_7 |psi|^2) (DNLS.cpp:175).  The FFTs are the Stockham
+// (for a length with a prime factor above 7 the last two lines are one zero-padded cyclic
+// convolution of smooth length len >= 2n - 1: the propagator is circulant, nlc_host.h), and finally psi <- psi exp(-i beta dt c_7 |psi|^2) (DNLS.cpp:175).  The FFTs are the Stockham
 // shared-memory transforms of nlc_fft.cuh; state is read once and written once per launch.
 #include "nlc_fft.cuh"
 
@@ -65,6 +66,19 @@ __global__ void dnls_move_kernel(double2 *__restrict__ psi, const DnlsArgs a) {
 		for (uint32_t i = 0; i < a.steps; i++) {
 			for (int k = 0; k < 7; k++) {
 				const double coef = (k == 0 && (i != 0 || (a.seg & NLC_SEG_CONTINUE))) ? a.nl[7] : a.nl[k];
+				if (a.conv_tables) {
+					// rotation, zero padding to len, then FFT_len, product with G_k, IFFT_len
+					for (int j = t; j < len; j += T) x[j] = j < n ? nonlinear_rotate(x[j], -coef, a.fft.k1) : make_double2(0., 0.);
+					team_sync<BLOCK>();
+					double2 *r = stockham_team<BLOCK, false>(a.fft, x, y, t, T);
+					double2 *o = r == x ? y : x;
+					const double2 *tab = a.conv_tables + (size_t) k * len;
+					for (int j = t; j < len; j += T) r[j] = cmul(r[j], tab[j], a.fft.k1);
+					team_sync<BLOCK>();
+					x = stockham_team<BLOCK, true>(a.fft, r, o, t, T);
+					y = x == buf0 ? buf1 : buf0;
+					continue;
+				}
 				for (int j = t; j < n; j += T) x[j] = nonlinear_rotate(x[j], -coef, a.fft.k1);
 				team_sync<BLOCK>();
 				double2 *r = fft_team<BLOCK, false>(a.fft, x, y, t, T);

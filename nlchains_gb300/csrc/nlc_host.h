@@ -42,6 +42,13 @@ struct FftTables {
 };
 FftTables fft_tables(uint32_t n, uint32_t max_len);
 
+// The DNLS linear propagators IFFT_n diag(L_k) FFT_n (lin: 7 tables of n interleaved complex L_k,
+// the 1/n included) are circulant: x -> x (*) h_k with h_k = sum_q L_k[q] exp(+2 pi i q t / n).  A
+// cyclic convolution of length n equals the first n outputs of a cyclic convolution of length
+// m >= 2n - 1 with g_k[t mod m] = h_k[t mod n], |t| < n, and x zero-padded to m.  Returns the 7
+// spectra FFT_m(g_k) / m (interleaved), so that x (*) h_k = IFFT_m(FFT_m(x) G_k) on [0, n).
+std::vector<double> dnls_conv_tables(const std::vector<double> &lin, uint32_t n, uint32_t m);
+
 // Symmetric eigensystem of the periodic dDNKG operator diag(mp2) - shift(+-1) (eigensystem.cpp:
 // 15-18): ascending eigenvalues, omegas = sqrt(eigenvalues), eigenvectors column-major
 // (eigvec[k*n + s] = component s of eigenvector k), as Armadillo's eig_sym would return them.
@@ -57,7 +64,10 @@ struct PlanInfo {
 	RealArgs args;          // integrator constants (device pointers included)
 	size_t device_bytes = 0;  // device memory held by the plan
 	int sms = 0;
-	double unit_step_us = 0;  // estimated time of one block's step with its SM fully shared
+	// cost model of the move kernel: FP64 work of one block's step over the sustained fraction of
+	// peak, resident blocks per SM, warps per block, and the plan's own grid
+	double block_ops = 0;
+	int per_sm = 1, block_warps = 1, grid = 0;
 };
 bool plan_info(const nlc_plan *plan, PlanInfo *info);
 // free a plan's device memory in the order of `stream` (after the work already queued there),

@@ -143,6 +143,7 @@ struct DnlsArgs {
 	double nl[8];              // nonlinear coefficient of sub-step k: beta*dt*c[k]; nl[7]: beta*dt*2*c[0] (merged)
 	double nl_final;           // beta*dt*c[7]
 	const double2 *lin_tables; // [7][n] exp(-i dt d_k omega_j)/n
+	const double2 *conv_tables;  // [7][len] when set: the linear sub-steps as length-len cyclic convolutions
 	unsigned long long *work_counter;
 	int team;                  // lanes per chain of the warp-team variant (power of two, 4 .. 32)
 	uint32_t seg;              // NLC_SEG_*

@@ -110,7 +110,8 @@ struct nlc_plan {
 	int diag_blocks = 0, diag_threads = 0, diag_team_block = 0, diag_rows = 0;
 	size_t diag_smem = 0;
 	int tier = 0;   // 1 = resident lanes (G <= 32), 2 = resident block (G > 32), 3 = DNLS shared-memory
-	double unit_step_us = 0;   // estimated time of one block's step with its SM fully shared
+	double block_ops = 0;      // FP64 work of one block's step over the sustained fraction of peak
+	int per_sm = 1, block_warps = 1;   // resident blocks per SM, warps per block of the move kernel
 
 	// Device memory comes from the stream-ordered allocator, so that creating and destroying plans
 	// (the request server does it per request) never synchronises the whole device.
@@ -286,30 +287,28 @@ RealShape autotune_shape(nlc_plan &P, int model, int variant) {
 	return best;
 }
 
-// Time of one step of one block (chains_per_block chains) when its SM also runs per_sm - 1 other
-// such blocks: work in FP64 lane operations (an FMA is one) over the SM's FP64 rate at the fraction
-// of peak the kernel reaches when the SM is full.  Work per site and step (7 sub-steps): the real
-// models' drift, neighbour terms and kick, the Toda exponential (~22 operations), the DNLS phase
-// rotation (sincos ~31) and two Stockham transforms (~3 operations per element and radix-2 level;
-// a Bluestein transform is two passes of the padded length plus the chirp products).  Used by the
-// request server to split long rounds into launches of bounded length.
-double unit_step_estimate(int model, uint32_t n, uint32_t len, bool bluestein, int chains_per_block, int per_sm) {
+// FP64 lane operations of one step of one block of chains_per_block chains, divided by the fraction
+// of the FP64 peak the kernel sustains (an FMA is one operation).  Work per site and step (7
+// sub-steps): the real models' drift, neighbour terms and kick, the Toda exponential (~22
+// operations), the DNLS phase rotation (sincos ~31) and two Stockham transforms (~3 operations per
+// element and radix-2 level).  The request server turns it into a block lifetime to split long rounds.
+double block_step_ops(int model, uint32_t n, uint32_t len, bool bluestein, int chains_per_block) {
 	double per_site, eff;
 	switch (model) {
 		case NLC_TODA: per_site = 7 * 32.; eff = 0.8; break;
 		case NLC_FPUT: per_site = 7 * 8.; eff = 0.85; break;
 		case NLC_DNLS: {
+			// a linear sub-step: two passes of n, or with a large prime factor two passes of the
+			// padded convolution length plus its product
 			const double lg = std::log2(double(std::max<uint32_t>(len, 2)));
-			const double fft = bluestein ? (2 * 3 * lg * len + 4. * len) / n + 8 : 3 * lg;
-			per_site = 7 * (44 + 2 * fft);
-			eff = 0.5;
+			const double pair = bluestein ? (6 * lg * len + 6. * len) / n : 6 * lg + 6;
+			per_site = 7 * (40 + pair);
+			eff = 0.4;
 			break;
 		}
 		default: per_site = 7 * 6.; eff = 0.85;
 	}
-	// 600 G FP64 lane operations per second on 152 SMs: ~3950 per SM and microsecond
-	const double sm_ops_per_us = 3950.;
-	return per_site * double(n) * chains_per_block * per_sm / (eff * sm_ops_per_us);
+	return per_site * double(n) * chains_per_block / eff;
 }
 
 int setup_fft(nlc_plan &P, FftPlanDev &f) {
@@ -502,6 +501,16 @@ extern "C" int nlc_plan_create(const nlc_model *model, nlc_plan **out) {
 		double2 *d_tab = nullptr;
 		if ((rc = P->upload(&d_tab, reinterpret_cast<const double2 *>(tab.data()), 7 * size_t(n)))) return rc;
 		d.lin_tables = d_tab;
+		if (d.fft.bluestein) {
+			// lengths with a prime factor above 7: each linear sub-step as one zero-padded cyclic
+			// convolution of the smooth length len (two passes) instead of two Bluestein transforms
+			// (four passes and three chirp products)
+			const uint32_t m = uint32_t(d.fft.len);
+			const std::vector<double> conv = dnls_conv_tables(tab, n, m);
+			double2 *d_conv = nullptr;
+			if ((rc = P->upload(&d_conv, reinterpret_cast<const double2 *>(conv.data()), 7 * size_t(m)))) return rc;
+			d.conv_tables = d_conv;
+		}
 		d.work_counter = P->d_counter;
 		// team: up to a 256-point pass, len/4 lanes (4 .. 32, a power of two) per chain and several
 		// chains per warp; beyond, a block of up to 256 threads per chain
@@ -529,7 +538,9 @@ extern "C" int nlc_plan_create(const nlc_model *model, nlc_plan **out) {
 			return rc;
 		if (per_sm < 1) return set_error(NLC_EUNSUPPORTED, "DNLS kernel does not fit an SM");
 		const int teams = P->dnls_team_block ? 1 : P->dnls_threads / d.team;
-		P->unit_step_us = unit_step_estimate(NLC_DNLS, n, len, d.fft.bluestein, teams, per_sm);
+		P->block_ops = block_step_ops(NLC_DNLS, n, len, d.fft.bluestein, teams);
+		P->per_sm = per_sm;
+		P->block_warps = P->dnls_threads / 32;
 		P->dnls_blocks = int(std::min<unsigned long long>((model->copies + teams - 1) / teams, (unsigned long long) per_sm * sms));
 		if (model->flags & NLC_FLAG_SHARED_GPU)   // one block per unit of work: a warp's chains per unit
 			P->dnls_blocks = int(std::min<unsigned long long>(
@@ -598,7 +609,9 @@ extern "C" int nlc_plan_create(const nlc_model *model, nlc_plan **out) {
 		int per_sm = 1;
 		cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, real_move_kernel(mdl, P->variant, P->rs.sites),
 		                                              P->rs.threads, 0);
-		P->unit_step_us = unit_step_estimate(mdl, n, 0, false, P->rs.threads / P->rs.lanes, std::max(per_sm, 1));
+		P->block_ops = block_step_ops(mdl, n, 0, false, P->rs.threads / P->rs.lanes);
+		P->per_sm = std::max(per_sm, 1);
+		P->block_warps = P->rs.threads / 32;
 	}
 	if ((rc = setup_diagnostics(*P))) return rc;
 	{
@@ -621,7 +634,10 @@ bool nlc::plan_info(const nlc_plan *P, PlanInfo *info) {
 	info->args.lanes = P->rs.lanes;
 	info->device_bytes = P->device_bytes;
 	info->sms = P->prop.multiProcessorCount;
-	info->unit_step_us = P->unit_step_us;
+	info->block_ops = P->block_ops;
+	info->per_sm = P->per_sm;
+	info->block_warps = P->block_warps;
+	info->grid = P->m.model == NLC_DNLS ? P->dnls_blocks : P->rs.blocks;
 	return true;
 }
 

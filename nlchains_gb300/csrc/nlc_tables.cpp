@@ -205,10 +205,11 @@ void host_dft(std::vector<std::complex<double>> &z, int sign) {
 	size_t p = 2;
 	while (n % p) p++;
 	if (p == n) {
-		std::vector<std::complex<double>> out(n);
+		std::vector<std::complex<double>> w(n), out(n);
+		for (size_t e = 0; e < n; e++) w[e] = std::polar(1., sign * 2 * M_PI * double(e) / n);
 		for (size_t k = 0; k < n; k++) {
 			std::complex<double> acc = 0;
-			for (size_t j = 0; j < n; j++) acc += z[j] * std::polar(1., sign * 2 * M_PI * double(j * k % n) / n);
+			for (size_t j = 0, e = 0; j < n; j++, e = e + k < n ? e + k : e + k - n) acc += z[j] * w[e];
 			out[k] = acc;
 		}
 		z = out;
@@ -228,6 +229,23 @@ void host_dft(std::vector<std::complex<double>> &z, int sign) {
 }
 
 }  // namespace
+
+std::vector<double> dnls_conv_tables(const std::vector<double> &lin, uint32_t n, uint32_t m) {
+	std::vector<double> out(2 * 7 * size_t(m));
+	for (int k = 0; k < 7; k++) {
+		std::vector<std::complex<double>> h(n), g(m, 0.);
+		for (uint32_t q = 0; q < n; q++) h[q] = {lin[2 * (k * size_t(n) + q)], lin[2 * (k * size_t(n) + q) + 1]};
+		host_dft(h, +1);   // h[t] = sum_q L_k[q] exp(+2 pi i q t / n): the propagator's kernel in site space
+		for (uint32_t t = 0; t < n; t++) g[t] = h[t];
+		for (uint32_t t = 1; t < n; t++) g[m - t] = h[n - t];   // g[-t mod m] = h[-t mod n]
+		host_dft(g, -1);
+		for (uint32_t j = 0; j < m; j++) {
+			out[2 * (k * size_t(m) + j)] = g[j].real() / m;
+			out[2 * (k * size_t(m) + j) + 1] = g[j].imag() / m;
+		}
+	}
+	return out;
+}
 
 FftTables fft_tables(uint32_t n, uint32_t max_len) {
 	FftTables T;

@@ -35,8 +35,10 @@ def test_against_oracle(gpu, n):
     assert np.abs(out - exp).max() <= 1e-12 * np.abs(exp).max()
 
 
-def test_linear_exact_phase_advance(gpu):
-    n, copies, dt, steps = 128, 5, 0.05, 40
+# 128: direct passes; 97, 211, 1021 (prime): the linear sub-steps as padded cyclic convolutions
+@pytest.mark.parametrize("n", [128, 97, 211, 1021])
+def test_linear_exact_phase_advance(gpu, n):
+    copies, dt, steps = 5, 0.05, 40
     rng = np.random.default_rng(1)
     psi = rng.standard_normal((copies, n)) + 1j * rng.standard_normal((copies, n))
     out = run(gpu, n, copies, dt, 0.0, psi, steps, 20)
