@@ -195,12 +195,12 @@ def measure_engine(w, steps, warmup, rank, world, local):
     step_ms = float(allreduce([step_ms], "max")[0])
     site_steps = float(n) * copies * b * steps * world
     value = site_steps / (step_ms * 1e-3)
-    lin_h = lin.cpu().numpy()
-    # ensemble average over ranks: the reference's all_reduce of linenergies (equal shards)
-    lin_all = allreduce(lin_h) / world
+    # ensemble average over ranks and its entropies: the reference's all_reduce of linenergies
+    from nlchains_gb300 import shards
+    lin_all, wt, inf = shards.sample(lin.cpu().numpy(), copies, copies * world, model.a0is0)
     shape = plan.shape()
     return dict(value=value, step_ms=step_ms / steps, move_ms=move_ms, wall_s=wall, launches=launches,
-                clocks=clk.summary(), shape=shape, plan=plan, lin=lin_all, entropies=ent.cpu().numpy().tolist(),
+                clocks=clk.summary(), shape=shape, plan=plan, lin=lin_all, entropies=[wt, inf],
                 state_after=dev.cpu().numpy(), state_before=state)
 
 

@@ -255,6 +255,18 @@ int nlc_program_run(int argc, char **argv);
  * Misc
  * -------------------------------------------------------------------------------------------*/
 
+/*
+ * The reference's results::calc_entropies (results_entropy.cpp:21-46) on host memory: {WT entropy,
+ * information entropy} of the linear energies lin[chain_length] into out[2], over every mode, every
+ * mode but 0 when a0is0 (zero-frequency mode 0: m = 0 for DNKG, always for FPUT, Toda and DNLS,
+ * never for dDNKG; results.cpp:8), or the modes whose entropy_mask byte is non-zero.  For linear
+ * energies combined on the host, e.g. all-reduced over processes that each integrate a shard of the
+ * copies, as the reference's MPI ranks do (results_entropy.cpp:13).  NLC_EBLOWUP when a result is
+ * not finite (results::check_entropy, results.cpp:63-68); out[] is written either way.  Needs no GPU.
+ */
+int nlc_entropies(const double *lin, uint32_t chain_length, int32_t a0is0, const uint8_t *entropy_mask,
+                  double *out);
+
 const char *nlc_last_error(void);
 const char *nlc_version(void);
 

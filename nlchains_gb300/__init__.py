@@ -37,7 +37,7 @@ EXPORTS = (
     "nlc_job_download", "nlc_job_wait", "nlc_job_state_ptr", "nlc_program_run", "nlc_last_error",
     "nlc_version", "nlc_kernel_launches", "nlc_fp64_peak", "nlc_linenergies_noalloc",
     "nlc_server_create", "nlc_server_destroy", "nlc_server_submit", "nlc_server_poll", "nlc_server_wait",
-    "nlc_server_result",
+    "nlc_server_result", "nlc_entropies",
 )
 
 
@@ -115,6 +115,7 @@ def lib():
         "nlc_server_poll": ([vp, u64, P(_CRequestStatus)], i32),
         "nlc_server_wait": ([vp, u64, i32], i32),
         "nlc_server_result": ([vp, u64, vp, dp, dp, P(u64)], i32),
+        "nlc_entropies": ([dp, u32, i32, vp, dp], i32),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -127,6 +128,17 @@ def _check(rc):
     if rc != OK:
         raise NlcError(rc, lib().nlc_last_error().decode(errors="replace"))
     return rc
+
+
+def entropies(lin, a0is0, entropy_mask=None):
+    """(WT, INF) of host linear energies (nlc_entropies); NlcError(EBLOWUP) when not finite."""
+    lin = np.ascontiguousarray(lin, dtype=np.float64)
+    out = np.zeros(2)
+    mask = None if entropy_mask is None else np.ascontiguousarray(entropy_mask, dtype=np.uint8)
+    _check(lib().nlc_entropies(lin.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), lin.size, int(bool(a0is0)),
+                               None if mask is None else mask.ctypes.data_as(ctypes.c_void_p),
+                               out.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
+    return float(out[0]), float(out[1])
 
 
 def last_error():
@@ -157,6 +169,15 @@ class Model:
     @property
     def name(self):
         return MODEL_NAMES[self.model]
+
+    @property
+    def a0is0(self):
+        """Mode 0 has zero frequency and is left out of the entropies (results.cpp:8)."""
+        if self.model == MODELS["DNLS"]:
+            return True
+        if self.model == MODELS["dDNKG"]:
+            return False
+        return self.model != MODELS["DNKG"] or self.m == 0.0
 
     @property
     def state_shape(self):

@@ -488,3 +488,28 @@ extern "C" int nlc_program_run(int argc, char **argv) {
 	std::signal(SIGTERM, prev_term);
 	return ret;
 }
+
+// Host entropies of the linear energies e over the selected modes M (|M| = count):
+// e' = e |M| / sum e, WT = -sum log e', INF = sum e' log e' (results_entropy.cpp:21-46), written
+// with the normalisation taken out of the sums: WT = -(sum log e + |M| log r), INF =
+// r (sum e log e + log r sum e), r = |M| / sum e.
+extern "C" int nlc_entropies(const double *lin, uint32_t n, int32_t a0is0, const uint8_t *mask, double *out) {
+	if (!lin || !out) return set_error(NLC_EINVAL, "nlc_entropies: NULL argument");
+	double sum_e = 0, sum_log = 0, sum_elog = 0;
+	uint32_t count = 0;
+	for (uint32_t k = 0; k < n; k++) {
+		if ((mask && !mask[k]) || (a0is0 && k == 0)) continue;
+		const double lk = std::log(lin[k]);
+		sum_e += lin[k];
+		sum_log += lk;
+		sum_elog += lin[k] * lk;
+		count++;
+	}
+	if (!count) return set_error(NLC_EINVAL, "nlc_entropies: no mode selected");
+	const double r = count / sum_e, lr = std::log(r);
+	out[0] = -(sum_log + count * lr);
+	out[1] = r * (sum_elog + lr * sum_e);
+	if (!std::isfinite(out[0]) || !std::isfinite(out[1]))
+		return set_error(NLC_EBLOWUP, "non-finite entropy");
+	return NLC_OK;
+}
