@@ -16,10 +16,11 @@
 
 namespace nlc {
 
-__device__ __forceinline__ double2 nonlinear_rotate(double2 v, double neg_coef, const FpOnes &k) {
+__device__ __forceinline__ double2 nonlinear_rotate(double2 v, double neg_coef, const double2 *__restrict__ sctab,
+                                                    const SinCosConsts &sc, const FpOnes &k) {
 	const double norm = dfma(v.x, v.x, fmul(v.y, v.y, k));
 	double s, c;
-	sincos(fmul(neg_coef, norm, k), &s, &c);
+	sincos_table(fmul(neg_coef, norm, k), sctab, sc, k, &s, &c);
 	return make_double2(dfma(v.x, c, -fmul(v.y, s, k)), dfma(v.x, s, fmul(v.y, c, k)));
 }
 
@@ -68,7 +69,7 @@ __global__ void dnls_move_kernel(double2 *__restrict__ psi, const DnlsArgs a) {
 				const double coef = (k == 0 && (i != 0 || (a.seg & NLC_SEG_CONTINUE))) ? a.nl[7] : a.nl[k];
 				if (a.conv_tables) {
 					// rotation, zero padding to len, then FFT_len, product with G_k, IFFT_len
-					for (int j = t; j < len; j += T) x[j] = j < n ? nonlinear_rotate(x[j], -coef, a.fft.k1) : make_double2(0., 0.);
+					for (int j = t; j < len; j += T) x[j] = j < n ? nonlinear_rotate(x[j], -coef, a.sctab, a.sc, a.fft.k1) : make_double2(0., 0.);
 					team_sync<BLOCK>();
 					double2 *r = stockham_team<BLOCK, false>(a.fft, x, y, t, T);
 					double2 *o = r == x ? y : x;
@@ -79,7 +80,7 @@ __global__ void dnls_move_kernel(double2 *__restrict__ psi, const DnlsArgs a) {
 					y = x == buf0 ? buf1 : buf0;
 					continue;
 				}
-				for (int j = t; j < n; j += T) x[j] = nonlinear_rotate(x[j], -coef, a.fft.k1);
+				for (int j = t; j < n; j += T) x[j] = nonlinear_rotate(x[j], -coef, a.sctab, a.sc, a.fft.k1);
 				team_sync<BLOCK>();
 				double2 *r = fft_team<BLOCK, false>(a.fft, x, y, t, T);
 				double2 *o = r == x ? y : x;
@@ -94,7 +95,7 @@ __global__ void dnls_move_kernel(double2 *__restrict__ psi, const DnlsArgs a) {
 			if (a.seg & NLC_SEG_OPEN)
 				for (int j = t; j < n; j += T) g[j] = x[j];
 			else
-				for (int j = t; j < n; j += T) g[j] = nonlinear_rotate(x[j], -a.nl_final, a.fft.k1);
+				for (int j = t; j < n; j += T) g[j] = nonlinear_rotate(x[j], -a.nl_final, a.sctab, a.sc, a.fft.k1);
 		}
 		team_sync<BLOCK>();
 	}
@@ -121,9 +122,10 @@ cudaError_t launch_dnls_move(const DnlsArgs &a, double2 *psi, int blocks, int th
 
 // Elementwise operators with the reference's semantics (DNLS.cu:11-25), for callers that keep
 // their own FFT loop.
-__global__ void dnls_nonlinear_kernel(double2 *psi, unsigned long long elements, double neg_coef, const FpOnes k) {
+__global__ void dnls_nonlinear_kernel(double2 *psi, unsigned long long elements, double neg_coef,
+                                      const double2 *sctab, const SinCosConsts sc, const FpOnes k) {
 	const unsigned long long i = (unsigned long long) blockIdx.x * blockDim.x + threadIdx.x;
-	if (i < elements) psi[i] = nonlinear_rotate(psi[i], neg_coef, k);
+	if (i < elements) psi[i] = nonlinear_rotate(psi[i], neg_coef, sctab, sc, k);
 }
 
 __global__ void dnls_linear_kernel(double2 *psi, unsigned long long elements, uint32_t n, const double2 *table,
@@ -132,10 +134,11 @@ __global__ void dnls_linear_kernel(double2 *psi, unsigned long long elements, ui
 	if (i < elements) psi[i] = cmul(psi[i], table[i % n], k);
 }
 
-cudaError_t launch_dnls_nonlinear(double2 *psi, uint64_t elements, double coef, cudaStream_t stream) {
+cudaError_t launch_dnls_nonlinear(double2 *psi, uint64_t elements, double coef, const double2 *sctab,
+                                  cudaStream_t stream) {
 	count_launch();
 	const unsigned long long blocks = (elements + 255) / 256;
-	dnls_nonlinear_kernel<<<(unsigned) blocks, 256, 0, stream>>>(psi, elements, -coef, FpOnes{});
+	dnls_nonlinear_kernel<<<(unsigned) blocks, 256, 0, stream>>>(psi, elements, -coef, sctab, SinCosConsts{}, FpOnes{});
 	return cudaGetLastError();
 }
 

@@ -5,9 +5,8 @@
 // sub-length L (L = n before the first stage) and stride s (s = 1), every butterfly (q, t),
 // q < L/p, t < s, reads a_u = x[t + s (q + u L/p)], forms the p-point DFT, multiplies output v by
 // exp(-+2 pi i q v / L) and writes y[t + s (p q + v)]; then L /= p, s *= p.  The result lands in
-// natural order after the last stage, with no bit reversal.  Radices 4, 2, 3 have dedicated
-// butterflies; any other prime radix uses a direct p-point DFT (the linear-energy diagnostics are
-// the only users of those, and they run once per sample).
+// natural order after the last stage, with no bit reversal.  Radices 4, 2, 3, 5 have dedicated
+// butterflies; any other prime radix uses a direct p-point DFT.
 //
 // Forward = exp(-2 pi i jk/n), unnormalised, as cuFFT / FFTW forward transforms in the reference.
 #pragma once
@@ -103,6 +102,43 @@ __device__ double2 *stockham_team(const FftPlanDev &P, double2 *x, double2 *y, i
 				o[0] = cadd(a0, t1, k);
 				o[s] = q == 0 ? x1 : cmul(x1, twiddle<INV>(tw, q * tws), k);
 				o[2 * s] = q == 0 ? x2 : cmul(x2, twiddle<INV>(tw, 2 * q * tws), k);
+			}
+		} else if (p == 5) {
+			// t1 = a1 + a4, t2 = a2 + a3, t3 = a1 - a4, t4 = a2 - a3;
+			// X1,4 = a0 + c1 t1 + c2 t2 -+ i (s1 t3 + s2 t4), X2,3 = a0 + c2 t1 + c1 t2 -+ i (s2 t3 - s1 t4)
+			// (forward; the inverse swaps the signs of i), c_j = cos(2 pi j/5), s_j = sin(2 pi j/5)
+			for (int b = t; b < nb; b += T) {
+				const int q = b / s, tt = b - q * s;
+				const double2 a0 = x[tt + s * q], a1 = x[tt + s * (q + m)], a2 = x[tt + s * (q + 2 * m)],
+				              a3 = x[tt + s * (q + 3 * m)], a4 = x[tt + s * (q + 4 * m)];
+				const double2 t1 = cadd(a1, a4, k), t2 = cadd(a2, a3, k), t3 = csub(a1, a4, k), t4 = csub(a2, a3, k);
+				const double2 b1 = make_double2(dfma(P.c52, t2.x, dfma(P.c51, t1.x, a0.x)),
+				                                dfma(P.c52, t2.y, dfma(P.c51, t1.y, a0.y)));
+				const double2 b2 = make_double2(dfma(P.c51, t2.x, dfma(P.c52, t1.x, a0.x)),
+				                                dfma(P.c51, t2.y, dfma(P.c52, t1.y, a0.y)));
+				const double2 u1 = make_double2(dfma(P.s52, t4.x, fmul(P.s51, t3.x, k)),
+				                                dfma(P.s52, t4.y, fmul(P.s51, t3.y, k)));
+				const double2 u2 = make_double2(dfma(-P.s51, t4.x, fmul(P.s52, t3.x, k)),
+				                                dfma(-P.s51, t4.y, fmul(P.s52, t3.y, k)));
+				// b -+ i u: forward X1 = b1 - i u1 = (b1.x + u1.y, b1.y - u1.x)
+				const double2 x1 = INV ? make_double2(fsub(b1.x, u1.y, k), fadd(b1.y, u1.x, k))
+				                       : make_double2(fadd(b1.x, u1.y, k), fsub(b1.y, u1.x, k));
+				const double2 x4 = INV ? make_double2(fadd(b1.x, u1.y, k), fsub(b1.y, u1.x, k))
+				                       : make_double2(fsub(b1.x, u1.y, k), fadd(b1.y, u1.x, k));
+				const double2 x2 = INV ? make_double2(fsub(b2.x, u2.y, k), fadd(b2.y, u2.x, k))
+				                       : make_double2(fadd(b2.x, u2.y, k), fsub(b2.y, u2.x, k));
+				const double2 x3 = INV ? make_double2(fadd(b2.x, u2.y, k), fsub(b2.y, u2.x, k))
+				                       : make_double2(fsub(b2.x, u2.y, k), fadd(b2.y, u2.x, k));
+				double2 *o = y + tt + s * 5 * q;
+				o[0] = cadd(a0, cadd(t1, t2, k), k);
+				if (q == 0) {
+					o[s] = x1, o[2 * s] = x2, o[3 * s] = x3, o[4 * s] = x4;
+				} else {
+					o[s] = cmul(x1, twiddle<INV>(tw, q * tws), k);
+					o[2 * s] = cmul(x2, twiddle<INV>(tw, 2 * q * tws), k);
+					o[3 * s] = cmul(x3, twiddle<INV>(tw, 3 * q * tws), k);
+					o[4 * s] = cmul(x4, twiddle<INV>(tw, 4 * q * tws), k);
+				}
 			}
 		} else {
 			// direct p-point DFT: X_v = sum_u a_u W_p^{uv}, W_p^e = tw[(e mod p) n/p]

@@ -21,6 +21,10 @@ extern const double kYoshidaD[8];
 // scale * 2^(j/256), j < 256, in double-double arithmetic (identical bits on every IEEE host)
 void exp_table(double scale, double table[256]);
 
+// (cos, sin)(2 pi j / 256), j < 256, interleaved, in double-double arithmetic (identical bits on
+// every IEEE host): the table of the device's sincos_table
+void sincos_table(double table[512]);
+
 // dispersion of the real models, sqrt(m + 4 sin^2(pi k / n)) (DNKG_FPUT_Toda/dispersion.cpp:9-16)
 std::vector<double> dispersion_real(uint32_t n, double m);
 // dispersion of DNLS, 4 sin^2(pi k / n) (DNLS/dispersion.cpp:10-17)

@@ -25,6 +25,17 @@ struct ExpConsts {
 	double c4 = 1. / 24, c3 = 1. / 6, c2 = 0.5;   // Taylor coefficients of exp(r) - 1 - r
 };
 
+// Constants of the table-driven sincos (nlc_device.cuh sincos_table): Cody-Waite reduction by
+// 2 pi / 256 = pi / 128 (split as the double-double value of pi, scaled) and Taylor coefficients
+struct SinCosConsts {
+	double shifter = 0x1.8p52;                      // 1.5 * 2^52: round-to-integer shifter
+	double inv = 128. / 3.141592653589793116;       // 256 / (2 pi)
+	double p1 = 3.141592653589793116 / 128;         // pi / 128, leading part
+	double p2 = 1.2246467991473532072e-16 / 128;    // pi / 128, trailing part
+	double s3 = -1. / 6, s5 = 1. / 120, s7 = -1. / 5040;   // sin r = r + r^3 (s3 + r^2 (s5 + r^2 s7))
+	double c2 = -1. / 2, c4 = 1. / 24, c6 = -1. / 720;     // cos r - 1 = r^2 (c2 + r^2 (c4 + r^2 c6))
+};
+
 constexpr int kMaxSitesPerLane = 16;   // E: sites of a chain held in registers by one thread
 constexpr int kMaxLanesPerChain = 1024;
 
@@ -106,6 +117,9 @@ struct FftPlanDev {
 	const double2 *bi;     // FFT_m(conj b) / m (backward transforms)
 	FpOnes k1;
 	double half = 0.5, sin60 = 0.86602540378443864676;   // radix-3 butterfly constants
+	// radix-5 butterfly constants: cos(2 pi/5), cos(4 pi/5), sin(2 pi/5), sin(4 pi/5)
+	double c51 = 0.30901699437494742410, c52 = -0.80901699437494742410;
+	double s51 = 0.95105651629515357212, s52 = 0.58778525229247312917;
 };
 
 struct DiagArgs {
@@ -147,10 +161,13 @@ struct DnlsArgs {
 	unsigned long long *work_counter;
 	int team;                  // lanes per chain of the warp-team variant (power of two, 4 .. 32)
 	uint32_t seg;              // NLC_SEG_*
+	const double2 *sctab;      // (cos, sin)(2 pi j / 256), j < 256 (device)
+	SinCosConsts sc;
 };
 cudaError_t launch_dnls_move(const DnlsArgs &a, double2 *psi, int blocks, int threads, size_t smem,
                              int team_block, cudaStream_t stream);
-cudaError_t launch_dnls_nonlinear(double2 *psi, uint64_t elements, double coef, cudaStream_t stream);
+cudaError_t launch_dnls_nonlinear(double2 *psi, uint64_t elements, double coef, const double2 *sctab,
+                                  cudaStream_t stream);
 cudaError_t launch_dnls_linear(double2 *psi, uint64_t elements, uint32_t n, const double2 *table,
                                cudaStream_t stream);
 

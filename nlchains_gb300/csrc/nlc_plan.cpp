@@ -404,11 +404,12 @@ int setup_diagnostics(nlc_plan &P) {
 // Raise the kernel's dynamic shared-memory limit to the device maximum (never lowered, so plans
 // created earlier with larger chains keep launching).
 int set_smem_attr(const void *k, size_t smem, const cudaDeviceProp &prop) {
-	if (smem <= 48 * 1024) return NLC_OK;
 	cudaFuncAttributes attr{};
 	int rc = cuda_status(cudaFuncGetAttributes(&attr, k), "cudaFuncGetAttributes");
 	if (rc) return rc;
-	const size_t room = prop.sharedMemPerBlockOptin - attr.sharedSizeBytes;   // static shared memory counts too
+	// static shared memory counts against both the 48 KiB default and the opt-in maximum
+	if (smem + attr.sharedSizeBytes <= 48 * 1024) return NLC_OK;
+	const size_t room = prop.sharedMemPerBlockOptin - attr.sharedSizeBytes;
 	if (smem > room) return set_error(NLC_EUNSUPPORTED, "chain_length too large for the shared-memory kernels");
 	// once per (device, kernel) for the process: the limit only ever goes to the device maximum
 	static std::mutex mu;
@@ -501,6 +502,13 @@ extern "C" int nlc_plan_create(const nlc_model *model, nlc_plan **out) {
 		double2 *d_tab = nullptr;
 		if ((rc = P->upload(&d_tab, reinterpret_cast<const double2 *>(tab.data()), 7 * size_t(n)))) return rc;
 		d.lin_tables = d_tab;
+		{
+			double sct[512];
+			sincos_table(sct);
+			double2 *d_sct = nullptr;
+			if ((rc = P->upload(&d_sct, reinterpret_cast<const double2 *>(sct), 256))) return rc;
+			d.sctab = d_sct;
+		}
 		if (d.fft.bluestein) {
 			// lengths with a prime factor above 7: each linear sub-step as one zero-padded cyclic
 			// convolution of the smooth length len (two passes) instead of two Bluestein transforms
@@ -716,7 +724,7 @@ extern "C" int nlc_dnls_evolve_nonlinear(nlc_plan *P, void *psi, double coef, vo
 	if (!P || !psi) return set_error(NLC_EINVAL, "NULL argument");
 	if (P->m.model != NLC_DNLS) return set_error(NLC_EINVAL, "not a DNLS plan");
 	return cuda_status(launch_dnls_nonlinear(static_cast<double2 *>(psi), uint64_t(P->m.copies) * P->m.chain_length, coef,
-	                                         static_cast<cudaStream_t>(stream)),
+	                                         P->da.sctab, static_cast<cudaStream_t>(stream)),
 	                   "evolve_nonlinear launch");
 }
 

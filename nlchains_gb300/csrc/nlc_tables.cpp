@@ -59,7 +59,46 @@ DD dd_exp_small(DD y) {
 	return sum;
 }
 
+// sin and cos of x in [0, pi/4] by their Taylor series in double-double
+void dd_sincos_small(DD x, DD &s, DD &c) {
+	const DD x2 = dd_mul(x, x);
+	DD term = x;
+	s = x;
+	for (unsigned k = 1; k < 40; k++) {   // term_k = (-1)^k x^(2k+1) / (2k+1)!
+		term = dd_div_u(dd_mul(term, x2), (2 * k) * (2 * k + 1));
+		term = {-term.hi, -term.lo};
+		s = dd_add(s, term);
+		if (std::fabs(term.hi) < 1e-40) break;
+	}
+	term = {1., 0.};
+	c = term;
+	for (unsigned k = 1; k < 40; k++) {   // (-1)^k x^(2k) / (2k)!
+		term = dd_div_u(dd_mul(term, x2), (2 * k - 1) * (2 * k));
+		term = {-term.hi, -term.lo};
+		c = dd_add(c, term);
+		if (std::fabs(term.hi) < 1e-40) break;
+	}
+}
+
 }  // namespace
+
+void sincos_table(double table[512]) {
+	// octant values m pi/128, m = 0..32, then quarter-turn symmetries (exact sign and swap)
+	const DD pi{3.141592653589793116, 1.2246467991473532072e-16};
+	double cs[33], sn[33];
+	for (unsigned m = 0; m <= 32; m++) {
+		DD s, c;
+		dd_sincos_small(dd_div_u(dd_mul(pi, DD{double(m), 0.}), 128), s, c);
+		sn[m] = s.hi + s.lo, cs[m] = c.hi + c.lo;
+	}
+	for (unsigned j = 0; j < 256; j++) {
+		const unsigned q = j / 64, jj = j % 64;
+		const double c0 = jj <= 32 ? cs[jj] : sn[64 - jj], s0 = jj <= 32 ? sn[jj] : cs[64 - jj];
+		const double c = q == 0 ? c0 : q == 1 ? -s0 : q == 2 ? -c0 : s0;
+		const double s = q == 0 ? s0 : q == 1 ? c0 : q == 2 ? -s0 : -c0;
+		table[2 * j] = c, table[2 * j + 1] = s;
+	}
+}
 
 void exp_table(double scale, double table[256]) {
 	const DD ln2{0x1.62e42fefa39efp-1, 0x1.abc9e3b39803fp-56};
@@ -188,13 +227,35 @@ uint32_t largest_prime_factor(uint32_t n) {
 	return n > 1 ? std::max(p, n) : p;
 }
 
-// smallest 2^a 3^b 5^c >= x
-uint32_t smooth_at_least(uint32_t x) {
-	uint32_t best = 1u << 31;
-	for (uint64_t a = 1; a < 2ull * x; a *= 2)
-		for (uint64_t b = a; b < 2ull * x; b *= 3)
-			for (uint64_t c = b; c < 2ull * x; c *= 5)
-				if (c >= x && c < best) best = uint32_t(c);
+// FP64 operations per element of one Stockham pass of radix r (nlc_fft.cuh): the radix-4 butterfly
+// (16 for the additions and 12 for three twiddle products per 4 points), radix 2, 3 and 5, and the
+// direct p-point DFT of any other radix (4p for the sums plus a twiddle product)
+double pass_cost(int r) {
+	switch (r) {
+		case 4: return 7.;
+		case 2: return 4.;
+		case 3: return 26. / 3;
+		case 5: return 52. / 5;
+		default: return 4. * r + 4;
+	}
+}
+
+// The length in [x, max_len] of the form 2^a 3^b 5^c 7^d whose transform takes the fewest FP64
+// operations (length x sum of pass costs), not merely the smallest: 384 = 4^3 2 3 costs less than
+// 360 = 4 2 3^2 5.  0 when there is none.
+uint32_t cheapest_length(uint32_t x, uint32_t max_len) {
+	uint32_t best = 0;
+	double best_cost = 0;
+	for (uint64_t a = 1; a <= max_len; a *= 2)
+		for (uint64_t b = a; b <= max_len; b *= 3)
+			for (uint64_t c = b; c <= max_len; c *= 5)
+				for (uint64_t d = c; d <= max_len; d *= 7) {
+					if (d < x) continue;
+					double cost = 0;
+					for (int r : fft_radices(uint32_t(d))) cost += pass_cost(r);
+					cost *= double(d);
+					if (!best || cost < best_cost) best = uint32_t(d), best_cost = cost;
+				}
 	return best;
 }
 
@@ -252,8 +313,8 @@ FftTables fft_tables(uint32_t n, uint32_t max_len) {
 	T.n = n;
 	T.len = n;
 	if (n >= 2 && largest_prime_factor(n) > 7) {
-		const uint32_t m = smooth_at_least(2 * n - 1);
-		if (m <= max_len) T.bluestein = true, T.len = m;
+		const uint32_t m = cheapest_length(2 * n - 1, max_len);
+		if (m) T.bluestein = true, T.len = m;
 	}
 	T.radices = fft_radices(T.len);
 	T.tw = fft_twiddles(T.len);

@@ -47,7 +47,7 @@ def test_real_models(gpu, model, params, n):
     check(lin, wt, inf, O.linenergies(mdl, state), O.a0is0(mdl))
 
 
-@pytest.mark.parametrize("n", [4, 16, 64, 100, 211, 1024, 2048, 2477])
+@pytest.mark.parametrize("n", [4, 16, 64, 100, 211, 664, 1024, 2048, 2477])
 def test_dnls(gpu, n):
     copies = 29
     # a full spectrum: the WT entropy sums log e_k and is ill-conditioned for modes at rounding level

@@ -21,7 +21,8 @@ def run(nlc, n, copies, dt, beta, psi, steps, batching):
 
 # 70 = 2 x 5 x 7 (direct radix-5 and radix-7 passes), 39 / 86 (factors 13, 43) and 97 / 211 / 997 /
 # 3001 prime (Bluestein), 1000 smooth: every FFT path and every team width of the shared-memory step
-@pytest.mark.parametrize("n", [2, 8, 12, 39, 64, 70, 86, 97, 100, 211, 256, 512, 997, 1000, 1024, 2048, 3001])
+# 664 pads to 1536 points: exactly 48 KiB of dynamic shared memory per block, plus the static part
+@pytest.mark.parametrize("n", [2, 8, 12, 39, 64, 70, 86, 97, 100, 211, 256, 512, 664, 997, 1000, 1024, 2048, 3001])
 def test_against_oracle(gpu, n):
     copies, dt = 11, 0.01
     steps, b = (20, 10) if n <= 2048 else (4, 2)   # the oracle's prime-length DFT is O(n^2)
@@ -74,3 +75,22 @@ def test_elementwise_operators(gpu):
     plan.dnls_evolve_linear(dev.data_ptr(), tdev.data_ptr(), torch.cuda.current_stream().cuda_stream)
     torch.cuda.synchronize()
     assert np.abs(dev.cpu().numpy() - exp * table[None, :]).max() < 1e-14 * np.abs(exp).max()
+
+
+def test_phase_rotation_accuracy(gpu):
+    """The table-driven sincos of the phase rotation against numpy for |theta| from 1e-8 to 1e7 (the
+    library sincos takes |theta| >= 2^20): psi = (x, 0) with x a 13-bit dyadic number in [0.5, 2],
+    so |psi|^2 is exact, theta = -coef x^2 is rounded once on both sides, and the result must be
+    x (cos theta, sin theta) to a few ulp."""
+    torch = pytest.importorskip("torch")
+    n, copies = 64, 64
+    x = np.round(np.random.default_rng(4).uniform(0.5, 2.0, n * copies) * 2 ** 12) / 2 ** 12
+    plan = gpu.Plan(gpu.Model("DNLS", n, copies, 0.01, beta=1.0))
+    for coef in (1e-8, 1e-3, 0.37, 3.0, 123.0, 4.1e4, 3e6):
+        dev = torch.from_numpy(np.stack([x, np.zeros_like(x)], axis=1).copy()).cuda()
+        plan.dnls_evolve_nonlinear(dev.data_ptr(), coef, torch.cuda.current_stream().cuda_stream)
+        torch.cuda.synchronize()
+        out = dev.cpu().numpy()
+        theta = -coef * (x * x)
+        err = max(np.abs(out[:, 0] - x * np.cos(theta)).max(), np.abs(out[:, 1] - x * np.sin(theta)).max())
+        assert err <= 4 * 2.0 ** -52, (coef, err)
