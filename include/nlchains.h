@@ -145,7 +145,11 @@ int nlc_linenergies_noalloc(int32_t model, uint32_t chain_length, uint32_t copie
 int nlc_dnls_evolve_nonlinear(nlc_plan *plan, void *psi_dev, double beta_dt_symplectic, void *stream);
 int nlc_dnls_evolve_linear(nlc_plan *plan, void *psi_k_dev, const void *table_dev, void *stream);
 
-/* Launch shape chosen for the integrator: lanes per chain, sites per lane, threads per block. */
+/* Launch shape chosen for the integrator: lanes per chain, sites per lane, threads per block, and
+ * the tier: 1 = register-resident, a chain on G <= 32 lanes of a warp; 2 = register-resident, a
+ * chain on one block of G > 32 lanes; 3 = DNLS, chains resident in shared memory (or, beyond it, in
+ * per-block global scratch); 4 = windowed, chains longer than one block holds, integrated in
+ * overlapping windows of G x E sites (lanes x sites per lane) between two state buffers. */
 int nlc_plan_shape(const nlc_plan *plan, int32_t *lanes_per_chain, int32_t *sites_per_lane,
                    int32_t *threads_per_block, int32_t *tier);
 

@@ -30,7 +30,8 @@ __global__ void lin_fft_kernel(const double2 *__restrict__ state, const DiagArgs
 	const int team = BLOCK ? 0 : (threadIdx.x >> 5);
 	const int teams = BLOCK ? 1 : (blockDim.x >> 5);
 	const int len = a.fft.len;
-	double2 *x = sm + (size_t) team * 2 * len, *y = x + len;
+	double2 *x = BLOCK && a.gscratch ? a.gscratch + (size_t) blockIdx.x * 2 * len : sm + (size_t) team * 2 * len;
+	double2 *y = x + len;
 	double *acc = a.partials + ((size_t) blockIdx.x * teams + team) * n;
 	for (int k = t; k < n; k += T) acc[k] = 0.;
 

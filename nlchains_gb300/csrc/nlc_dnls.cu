@@ -38,7 +38,8 @@ __global__ void dnls_move_kernel(double2 *__restrict__ psi, const DnlsArgs a) {
 	const int team = BLOCK ? 0 : (threadIdx.x / T);
 	const int per_warp = BLOCK ? 1 : 32 / T;
 	const int len = a.fft.len;
-	double2 *buf0 = sm + (size_t) team * 2 * len, *buf1 = buf0 + len;
+	double2 *buf0 = BLOCK && a.gscratch ? a.gscratch + (size_t) blockIdx.x * 2 * len : sm + (size_t) team * 2 * len;
+	double2 *buf1 = buf0 + len;
 	const unsigned long long units = (a.copies + per_warp - 1) / per_warp;
 
 	for (;;) {

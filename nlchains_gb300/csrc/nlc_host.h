@@ -36,15 +36,20 @@ std::vector<int> fft_radices(uint32_t n);
 std::vector<double> fft_twiddles(uint32_t n);
 
 // Host tables of a chain FFT: Stockham radices/twiddles of the pass length, plus the Bluestein
-// chirp and convolution kernels when n has a prime factor above 7 and the convolution fits
-// max_len (the caller's shared-memory budget).
+// chirp and convolution kernels when the padded length m >= 2n - 1 (at most max_len) takes fewer
+// FP64 operations than direct passes of n with its prime factors (convolution: the DNLS linear
+// sub-step, two transforms; otherwise one transform).  smem_len: the longest pass length whose two
+// buffers fit shared memory; longer ones run from global memory.
 struct FftTables {
 	uint32_t n = 0, len = 0;
 	bool bluestein = false;
 	std::vector<int> radices;
 	std::vector<double> tw, chirp, bf, bi;   // interleaved re/im
 };
-FftTables fft_tables(uint32_t n, uint32_t max_len);
+FftTables fft_tables(uint32_t n, uint32_t smem_len, uint32_t max_len, bool convolution);
+// the longest padded length of the FFT tables (2^18 >= 2 x 65535 - 1: any chain length of the
+// reference's 16-bit --chain_length)
+constexpr uint32_t kMaxFftLen = 1u << 18;
 
 // The DNLS linear propagators IFFT_n diag(L_k) FFT_n (lin: 7 tables of n interleaved complex L_k,
 // the 1/n included) are circulant: x -> x (*) h_k with h_k = sum_q L_k[q] exp(+2 pi i q t / n).  A
@@ -72,6 +77,7 @@ struct PlanInfo {
 	// peak, resident blocks per SM, warps per block, and the plan's own grid
 	double block_ops = 0;
 	int per_sm = 1, block_warps = 1, grid = 0;
+	bool windowed = false;   // windowed tier: its own launches only, never in a batched launch
 };
 bool plan_info(const nlc_plan *plan, PlanInfo *info);
 // free a plan's device memory in the order of `stream` (after the work already queued there),

@@ -81,6 +81,12 @@ struct RealArgs {
 	int32_t nbatch;
 	unsigned long long batch_units;
 	uint32_t seg;          // NLC_SEG_* of an unbatched launch (batched: per table entry)
+	// windowed tier (chains longer than one block's registers hold): when win_len is set, each unit
+	// is one window of win_len = G E consecutive sites (mod n) of one chain, integrated as a ring;
+	// the sites that the wrong ring closure can reach, win_halo = 7 x steps at each end, are
+	// discarded and the interior (at most win_inner sites) is written to win_out
+	uint32_t win_len, win_halo, win_inner, win_count;
+	double2 *win_out;
 };
 
 // Launch shape of the resident integrator.
@@ -98,7 +104,7 @@ enum Variant { kGeneric = 0, kSpecial = 1 };
 cudaError_t launch_real_move(int model, int variant, const RealShape &shape, double *state,
                              const RealArgs &args, cudaStream_t stream);
 // Function pointer for occupancy / attribute queries of one instantiation.
-const void *real_move_kernel(int model, int variant, int sites);
+const void *real_move_kernel(int model, int variant, int sites, bool windowed = false);
 
 // Diagnostics ---------------------------------------------------------------------------------
 
@@ -131,6 +137,7 @@ struct DiagArgs {
 	const double *omega;     // DNLS omega_k, dDNKG omegas
 	const double *eigT;      // dDNKG: eigenvectors, row-major by site: eigT[s*n + k] = e_k[s]
 	double *partials;        // [blocks][n]
+	double2 *gscratch;       // block teams whose buffers exceed shared memory: [blocks][2][len]
 };
 
 cudaError_t launch_linenergies_partials(const DiagArgs &a, const void *state, int blocks, int threads,
@@ -163,6 +170,7 @@ struct DnlsArgs {
 	uint32_t seg;              // NLC_SEG_*
 	const double2 *sctab;      // (cos, sin)(2 pi j / 256), j < 256 (device)
 	SinCosConsts sc;
+	double2 *gscratch;         // block teams whose buffers exceed shared memory: [blocks][2][len]
 };
 cudaError_t launch_dnls_move(const DnlsArgs &a, double2 *psi, int blocks, int threads, size_t smem,
                              int team_block, cudaStream_t stream);

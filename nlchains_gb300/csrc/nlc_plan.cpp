@@ -30,30 +30,37 @@ int cuda_status(cudaError_t e, const char *what) {
 
 void count_launch(uint64_t k) { g_launches += k; }
 
-const void *real_kernel_dnkg(int variant, int sites);
-const void *real_kernel_fput(int variant, int sites);
-const void *real_kernel_toda(int variant, int sites);
-const void *real_kernel_ddnkg(int variant, int sites);
+const void *real_kernel_dnkg(int variant, int sites, bool win);
+const void *real_kernel_fput(int variant, int sites, bool win);
+const void *real_kernel_toda(int variant, int sites, bool win);
+const void *real_kernel_ddnkg(int variant, int sites, bool win);
 
-const void *real_move_kernel(int model, int variant, int sites) {
+const void *real_move_kernel(int model, int variant, int sites, bool win) {
 	switch (model) {
-		case NLC_DNKG: return real_kernel_dnkg(variant, sites);
-		case NLC_FPUT: return real_kernel_fput(variant, sites);
-		case NLC_TODA: return real_kernel_toda(variant, sites);
-		case NLC_DDNKG: return real_kernel_ddnkg(variant, sites);
+		case NLC_DNKG: return real_kernel_dnkg(variant, sites, win);
+		case NLC_FPUT: return real_kernel_fput(variant, sites, win);
+		case NLC_TODA: return real_kernel_toda(variant, sites, win);
+		case NLC_DDNKG: return real_kernel_ddnkg(variant, sites, win);
 		default: return nullptr;
 	}
 }
 
 cudaError_t launch_real_move(int model, int variant, const RealShape &shape, double *state, const RealArgs &args,
                              cudaStream_t stream) {
-	const void *k = real_move_kernel(model, variant, shape.sites);
+	const void *k = real_move_kernel(model, variant, shape.sites, args.win_len != 0);
 	if (!k || shape.lanes < 1 || (shape.lanes & (shape.lanes - 1)) || shape.threads < 32 || shape.threads % 32 ||
 	    shape.threads % shape.lanes || (shape.lanes > 32 && shape.threads != shape.lanes) || shape.blocks < 1)
 		return cudaErrorInvalidConfiguration;
 	double2 *st = reinterpret_cast<double2 *>(state);
-	if ((args.n + uint32_t(shape.lanes) - 1) / uint32_t(shape.lanes) != uint32_t(shape.sites) || !args.copies)
+	if (args.win_len) {
+		// a window fills every lane, lies strictly inside the chain, and keeps a non-empty interior
+		if (args.win_len != uint32_t(shape.lanes) * uint32_t(shape.sites) || args.n <= args.win_len ||
+		    !args.win_inner || 2ull * args.win_halo + args.win_inner > args.win_len || !args.win_out ||
+		    args.win_count != (args.n + args.win_inner - 1) / args.win_inner || !args.copies)
+			return cudaErrorInvalidConfiguration;
+	} else if ((args.n + uint32_t(shape.lanes) - 1) / uint32_t(shape.lanes) != uint32_t(shape.sites) || !args.copies) {
 		return cudaErrorInvalidConfiguration;   // every lane must hold sites or sites - 1 >= 1 sites
+	}
 	RealArgs a = args;
 	a.lanes = shape.lanes;   // the lane count of the shape is the one the kernel must use
 	void *params[] = {&st, &a};
@@ -109,7 +116,9 @@ struct nlc_plan {
 	DiagArgs ga{};
 	int diag_blocks = 0, diag_threads = 0, diag_team_block = 0, diag_rows = 0;
 	size_t diag_smem = 0;
-	int tier = 0;   // 1 = resident lanes (G <= 32), 2 = resident block (G > 32), 3 = DNLS shared-memory
+	int tier = 0;   // 1 = resident lanes (G <= 32), 2 = resident block (G > 32), 3 = DNLS, 4 = windowed
+	uint32_t win_len = 0, win_steps = 0;   // windowed tier: sites per window, steps per launch
+	double2 *d_win = nullptr;              // windowed tier: the second state buffer
 	double block_ops = 0;      // FP64 work of one block's step over the sustained fraction of peak
 	int per_sm = 1, block_warps = 1;   // resident blocks per SM, warps per block of the move kernel
 
@@ -166,8 +175,8 @@ std::vector<std::pair<int, int>> shape_candidates(uint32_t n) {
 }
 
 // Complete a shape (threads, blocks) for the device; false if not launchable.
-bool finish_shape(const nlc_plan &P, int model, int variant, RealShape &s, int threads_hint) {
-	const void *k = real_move_kernel(model, variant, s.sites);
+bool finish_shape(const nlc_plan &P, int model, int variant, RealShape &s, int threads_hint, bool win = false) {
+	const void *k = real_move_kernel(model, variant, s.sites, win);
 	if (!k) return false;
 	cudaFuncAttributes attr{};
 	if (cudaFuncGetAttributes(&attr, k) != cudaSuccess) return false;
@@ -311,11 +320,33 @@ double block_step_ops(int model, uint32_t n, uint32_t len, bool bluestein, int c
 	return per_site * double(n) * chains_per_block / eff;
 }
 
-int setup_fft(nlc_plan &P, FftPlanDev &f) {
+// Windowed tier: the launchable block shape (G > 32 lanes of E sites, one window per block) with
+// the most sites G E.  Longer windows waste less on their discarded ends.
+RealShape window_shape(const nlc_plan &P, int model, int variant, int only_lanes) {
+	RealShape best{};
+	for (int G = kMaxLanesPerChain; G > 32; G >>= 1)
+		for (int E = kMaxSitesPerLane; E >= 2; E--) {
+			if (only_lanes && G != only_lanes) break;
+			if (uint64_t(G) * E <= uint64_t(best.lanes) * best.sites) break;
+			if (uint64_t(G) * E >= P.m.chain_length) continue;
+			RealShape s{};
+			s.lanes = G, s.sites = E;
+			if (finish_shape(P, model, variant, s, G, true)) {
+				best = s;
+				break;
+			}
+		}
+	return best;
+}
+
+// the longest pass length whose two buffers (2 x len complex) fit one block's shared memory
+uint32_t smem_fft_len(const nlc_plan &P) {
+	return uint32_t(P.prop.sharedMemPerBlockOptin / (2 * sizeof(double2))) - 64;
+}
+
+int setup_fft(nlc_plan &P, FftPlanDev &f, bool convolution) {
 	const uint32_t n = P.m.chain_length;
-	// the largest pass the shared-memory kernels can hold: one team of 2 x len complex per block
-	const uint32_t max_len = uint32_t(P.prop.sharedMemPerBlockOptin / (2 * sizeof(double2))) - 64;
-	const FftTables T = fft_tables(n, max_len);
+	const FftTables T = fft_tables(n, smem_fft_len(P), kMaxFftLen, convolution);
 	if (T.radices.size() > size_t(kMaxRadices)) return set_error(NLC_EINVAL, "chain_length has too many prime factors");
 	f.n = int(n);
 	f.len = int(T.len);
@@ -358,7 +389,7 @@ int setup_diagnostics(nlc_plan &P) {
 		P.diag_blocks = int(std::min<unsigned long long>(tiles, 2ull * sms));
 		P.diag_rows = P.diag_blocks;
 	} else {
-		if ((rc = setup_fft(P, g.fft))) return rc;
+		if ((rc = setup_fft(P, g.fft, false))) return rc;
 		if (P.m.model == NLC_DNLS) {
 			double *d_om = nullptr;
 			if ((rc = P.upload(&d_om, P.omega_host.data(), n))) return rc;
@@ -387,9 +418,13 @@ int setup_diagnostics(nlc_plan &P) {
 			P.diag_smem = size_t(2) * len * sizeof(double2);
 			P.diag_blocks = int(std::min<unsigned long long>(P.m.copies, (P.m.flags & NLC_FLAG_COMPACT_DIAG ? 1ull : 2ull) * sms));
 			P.diag_rows = P.diag_blocks;
+			if (len > smem_fft_len(P)) {
+				// the two buffers of each block in global memory (L2-resident at these sizes)
+				P.diag_threads = 512;
+				P.diag_smem = 0;
+				if ((rc = P.dalloc(&g.gscratch, size_t(P.diag_blocks) * 2 * len))) return rc;
+			}
 		}
-		if (P.diag_smem > size_t(P.prop.sharedMemPerBlockOptin))
-			return set_error(NLC_EUNSUPPORTED, "chain_length too large for the shared-memory diagnostics");
 	}
 	if (P.diag_smem > size_t(P.prop.sharedMemPerBlockOptin))
 		return set_error(NLC_EUNSUPPORTED, "chain_length too large for the shared-memory diagnostics");
@@ -486,7 +521,7 @@ extern "C" int nlc_plan_create(const nlc_model *model, nlc_plan **out) {
 	if (mdl == NLC_DNLS) {
 		DnlsArgs &d = P->da;
 		d.n = n, d.copies = model->copies;
-		if ((rc = setup_fft(*P, d.fft))) return rc;
+		if ((rc = setup_fft(*P, d.fft, true))) return rc;
 		const double bdt = model->beta * model->dt;
 		for (int k = 0; k < 7; k++) d.nl[k] = bdt * 1. * kYoshidaC[k];
 		d.nl[7] = bdt * 2. * kYoshidaC[0];   // merged c7 + c0 (DNLS.cpp:162)
@@ -536,8 +571,8 @@ extern "C" int nlc_plan_create(const nlc_model *model, nlc_plan **out) {
 			P->dnls_threads = int(std::min<uint32_t>(256, std::max<uint32_t>(64, (len / 4 + 31) / 32 * 32)));
 			P->dnls_smem = 2 * size_t(len) * sizeof(double2);
 		}
-		if (P->dnls_smem > size_t(P->prop.sharedMemPerBlockOptin))
-			return set_error(NLC_EUNSUPPORTED, "chain_length too large for the shared-memory DNLS integrator");
+		const bool global = len > smem_fft_len(*P);   // the chain's two buffers in global memory
+		if (global) P->dnls_threads = 512, P->dnls_smem = 0;
 		const void *k = dnls_kernel_ptr(P->dnls_team_block);
 		if ((rc = set_smem_attr(k, P->dnls_smem, P->prop))) return rc;
 		int per_sm = 0;
@@ -546,14 +581,18 @@ extern "C" int nlc_plan_create(const nlc_model *model, nlc_plan **out) {
 			return rc;
 		if (per_sm < 1) return set_error(NLC_EUNSUPPORTED, "DNLS kernel does not fit an SM");
 		const int teams = P->dnls_team_block ? 1 : P->dnls_threads / d.team;
-		P->block_ops = block_step_ops(NLC_DNLS, n, len, d.fft.bluestein, teams);
+		P->block_ops = block_step_ops(NLC_DNLS, n, len, d.fft.bluestein, teams) * (global ? 2 : 1);
 		P->per_sm = per_sm;
 		P->block_warps = P->dnls_threads / 32;
 		P->dnls_blocks = int(std::min<unsigned long long>((model->copies + teams - 1) / teams, (unsigned long long) per_sm * sms));
-		if (model->flags & NLC_FLAG_SHARED_GPU)   // one block per unit of work: a warp's chains per unit
+		if ((model->flags & NLC_FLAG_SHARED_GPU) && !global)   // one block per unit of work: a warp's chains per unit
 			P->dnls_blocks = int(std::min<unsigned long long>(
 			    P->dnls_team_block ? model->copies : (model->copies + (32 / d.team) - 1) / (32 / d.team) / 4 + 1,
 			    0x7fffffffull));
+		if (global) {
+			// scratch for the resident blocks of the persistent grid
+			if ((rc = P->dalloc(&d.gscratch, size_t(P->dnls_blocks) * 2 * len))) return rc;
+		}
 		P->tier = 3;
 	} else {
 		RealArgs &a = P->ra;
@@ -588,8 +627,6 @@ extern "C" int nlc_plan_create(const nlc_model *model, nlc_plan **out) {
 			case NLC_FPUT: P->variant = model->alpha == 0. && model->beta == 1.; break;
 			case NLC_TODA: P->variant = a.alpha2 == 1.; break;
 		}
-		if (n > uint32_t(kMaxSitesPerLane) * kMaxLanesPerChain)
-			return set_error(NLC_EUNSUPPORTED, "chain_length above 16384 needs the streamed tier (not built)");
 		P->rs = RealShape{};
 		// NLC_FORCE_LANES=<G> pins the lanes per chain (used by the tests to cover every tier)
 		if (const char *force = std::getenv("NLC_FORCE_LANES")) {
@@ -607,17 +644,30 @@ extern "C" int nlc_plan_create(const nlc_model *model, nlc_plan **out) {
 			P->rs = (model->flags & NLC_FLAG_NO_TUNE) ? heuristic_shape(*P, mdl, P->variant)
 			                                          : autotune_shape(*P, mdl, P->variant);
 		}
-		if (!P->rs.blocks) return set_error(NLC_EUNSUPPORTED, "no launchable integrator shape for this chain_length");
+		// NLC_FORCE_WINDOW=<G> integrates in windows of G lanes even where one block holds the chain
+		// (used by the tests to cover the windowed tier on short chains)
+		const char *force_win = std::getenv("NLC_FORCE_WINDOW");
+		if (force_win) P->rs = RealShape{};
+		if (!P->rs.blocks) {
+			// longer than one block's registers hold: windows of the chain, ping-ponging between the
+			// caller's buffer and a second one of the same size
+			P->rs = window_shape(*P, mdl, P->variant, force_win ? std::atoi(force_win) : 0);
+			if (!P->rs.blocks) return set_error(NLC_EUNSUPPORTED, "no launchable integrator shape for this chain_length");
+			P->win_len = uint32_t(P->rs.lanes) * P->rs.sites;
+			P->win_steps = std::max<uint32_t>(1, P->win_len / 140);   // discarded ends: 5% of a window each
+			if ((rc = P->dalloc(&P->d_win, size_t(model->copies) * n))) return rc;
+			P->rs.blocks = std::max(1, P->rs.blocks);
+		}
 		if (model->flags & NLC_FLAG_SHARED_GPU) {
 			const unsigned long long gpb = P->rs.threads / P->rs.lanes;
 			P->rs.blocks = int(std::min<unsigned long long>((model->copies + gpb - 1) / gpb, 0x7fffffffull));
 		}
 		a.lanes = P->rs.lanes;
-		P->tier = P->rs.lanes > 32 ? 2 : 1;
+		P->tier = P->win_len ? 4 : P->rs.lanes > 32 ? 2 : 1;
 		int per_sm = 1;
-		cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, real_move_kernel(mdl, P->variant, P->rs.sites),
+		cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, real_move_kernel(mdl, P->variant, P->rs.sites, P->win_len != 0),
 		                                              P->rs.threads, 0);
-		P->block_ops = block_step_ops(mdl, n, 0, false, P->rs.threads / P->rs.lanes);
+		P->block_ops = block_step_ops(mdl, P->win_len ? P->win_len : n, 0, false, P->rs.threads / P->rs.lanes);
 		P->per_sm = std::max(per_sm, 1);
 		P->block_warps = P->rs.threads / 32;
 	}
@@ -646,6 +696,7 @@ bool nlc::plan_info(const nlc_plan *P, PlanInfo *info) {
 	info->per_sm = P->per_sm;
 	info->block_warps = P->block_warps;
 	info->grid = P->m.model == NLC_DNLS ? P->dnls_blocks : P->rs.blocks;
+	info->windowed = P->win_len != 0;
 	return true;
 }
 
@@ -694,6 +745,39 @@ int nlc::move_segment(nlc_plan *P, void *state, uint32_t steps, uint32_t seg, cu
 		                   "DNLS move launch");
 	}
 	RealArgs a = P->ra;
+	if (P->win_len) {
+		// windowed tier: launches of at most win_steps steps (open segments in between), each reading
+		// one buffer and writing the interiors of its windows to the other
+		const uint32_t n = P->m.chain_length;
+		double2 *in = static_cast<double2 *>(state), *out = P->d_win;
+		RealShape sh = P->rs;
+		for (uint32_t done = 0; done < steps;) {
+			const uint32_t s = std::min(steps - done, P->win_steps);
+			a.steps = s;
+			a.seg = ((done || (seg & NLC_SEG_CONTINUE)) ? NLC_SEG_CONTINUE : 0u) |
+			        ((done + s < steps || (seg & NLC_SEG_OPEN)) ? NLC_SEG_OPEN : 0u);
+			a.win_len = P->win_len;
+			a.win_halo = 7 * s;
+			a.win_inner = P->win_len - 2 * a.win_halo;
+			a.win_count = (n + a.win_inner - 1) / a.win_inner;
+			a.win_out = out;
+			const unsigned long long units = (unsigned long long) P->m.copies * a.win_count;
+			// persistent grid of the resident blocks, or one block per window for a shared GPU
+			sh.blocks = int(std::min<unsigned long long>(
+			    units, (P->m.flags & NLC_FLAG_SHARED_GPU) ? 0x7fffffffull
+			                                              : (unsigned long long) P->per_sm * P->prop.multiProcessorCount));
+			int rc = cuda_status(launch_real_move(P->m.model, P->variant, sh, reinterpret_cast<double *>(in), a, st),
+			                     "windowed move launch");
+			if (rc) return rc;
+			std::swap(in, out);
+			done += s;
+		}
+		if (in != state)
+			return cuda_status(cudaMemcpyAsync(state, in, size_t(P->m.copies) * n * sizeof(double2),
+			                                   cudaMemcpyDeviceToDevice, st),
+			                   "windowed state copy");
+		return NLC_OK;
+	}
 	a.steps = steps;
 	a.seg = seg;
 	return cuda_status(launch_real_move(P->m.model, P->variant, P->rs, static_cast<double *>(state), a, st), "move launch");

@@ -99,7 +99,7 @@ __device__ __forceinline__ double bond_force(double d, const RealArgs &a, const 
 	}
 }
 
-template <int MODEL, int E, int VAR>
+template <int MODEL, int E, int VAR, bool WIN>
 __global__ void real_move_kernel_t(double2 *__restrict__ state, const RealArgs a) {
 	__shared__ double xbuf[4 * 32];
 	__shared__ double s_tab[MODEL == NLC_TODA ? 256 : 1];
@@ -127,19 +127,25 @@ __global__ void real_move_kernel_t(double2 *__restrict__ state, const RealArgs a
 	int full = 0, ne = 0, first = 0;
 	bool fl = false;
 	double mv[MODEL == NLC_DDNKG ? E : 1];
+	constexpr bool windowed = WIN;
 	auto layout = [&]() {
-		full = int(n) - G * (E - 1);       // lanes [0, full) hold E sites, the others E - 1
+		// lanes [0, full) hold E sites, the others E - 1 (a window: G E sites, every lane E)
+		full = int(windowed ? a.win_len : n) - G * (E - 1);
 		fl = lane < full;
 		ne = fl ? E : E - 1;
 		first = fl ? lane * E : full * E + (lane - full) * (E - 1);
 		if constexpr (MODEL == NLC_DDNKG) {
+			if (!windowed) {
 #pragma unroll
-			for (int j = 0; j < E; j++) mv[j] = j < ne ? mp2_site[first + j] : 2.;
+				for (int j = 0; j < E; j++) mv[j] = j < ne ? mp2_site[first + j] : 2.;
+			}
 		}
 	};
 	if (!a.batch) layout();
 
-	const unsigned long long units = a.batch ? a.batch_units : (copies + gpb - 1) / gpb;
+	const unsigned long long units =
+	    a.batch ? a.batch_units
+	            : ((windowed ? (unsigned long long) copies * a.win_count : (unsigned long long) copies) + gpb - 1) / gpb;
 	for (;;) {
 		__syncthreads();
 		if (tid == 0) {
@@ -168,15 +174,29 @@ __global__ void real_move_kernel_t(double2 *__restrict__ state, const RealArgs a
 		}
 
 		unsigned long long chain = (u - unit_base) * gpb + gib;
+		uint32_t win = 0, wsite = 0;   // windowed: window index, chain site of this lane's first site
+		if (windowed) {
+			const unsigned long long item = chain;
+			chain = item / a.win_count;
+			win = uint32_t(item - chain * a.win_count);
+			// the window starts win_halo sites before its interior; n > win_len >= first + E
+			wsite = uint32_t((win * (unsigned long long) a.win_inner + n - a.win_halo + first) % n);
+		}
 		const bool active = chain < copies;
 		if (!active) chain = copies - 1;   // redundant work keeps shuffles and barriers convergent
-		double2 *cp = st + chain * (unsigned long long) n + first;
+		double2 *cp = st + chain * (unsigned long long) n + (windowed ? 0 : first);
 
 		double x[E + 2], p[E];
 #pragma unroll
 		for (int j = 0; j < E; j++) {
+			uint32_t sj = j;
+			if (windowed) {
+				sj = wsite + j;
+				if (sj >= n) sj -= n;
+				if constexpr (MODEL == NLC_DDNKG) mv[j] = mp2_site[sj];
+			}
 			if (j < ne) {
-				const double2 v = cp[j];
+				const double2 v = cp[sj];
 				x[j + 1] = v.x, p[j] = v.y;
 			} else {
 				x[j + 1] = 0., p[j] = 0.;
@@ -226,9 +246,24 @@ __global__ void real_move_kernel_t(double2 *__restrict__ state, const RealArgs a
 
 		if (active) {
 			const bool open = seg & NLC_SEG_OPEN;
+			double2 *dst = cp;
+			uint32_t lo = 0, hi = E;   // window offsets of the interior, relative to this lane's first site
+			if (windowed) {
+				dst = a.win_out + chain * (unsigned long long) n;
+				const uint32_t inner = min(a.win_inner, n - win * a.win_inner);
+				lo = a.win_halo > uint32_t(first) ? a.win_halo - first : 0;
+				hi = a.win_halo + inner > uint32_t(first) ? a.win_halo + inner - first : 0;
+			}
 #pragma unroll
-			for (int j = 0; j < E; j++)
-				if (j < ne) cp[j] = make_double2(open ? x[j + 1] : dfma(a.cd_final, p[j], x[j + 1]), p[j]);
+			for (int j = 0; j < E; j++) {
+				uint32_t sj = j;
+				if (windowed) {
+					sj = wsite + j;
+					if (sj >= n) sj -= n;
+				}
+				if (j < ne && uint32_t(j) >= lo && uint32_t(j) < hi)
+					dst[sj] = make_double2(open ? x[j + 1] : dfma(a.cd_final, p[j], x[j + 1]), p[j]);
+			}
 		}
 	}
 
@@ -244,15 +279,26 @@ __global__ void real_move_kernel_t(double2 *__restrict__ state, const RealArgs a
 	}
 }
 
-// Kernel table of one model: [variant][E]
+// Kernel table of one model: [variant][E], and the windowed tier's kernels for a few E (the window
+// bookkeeping costs registers, so it has its own instantiations)
 template <int MODEL>
 struct RealKernels {
 	using K = void (*)(double2 *, const RealArgs);
-	template <int E>
+	template <int E, bool WIN = false>
 	static constexpr K get(int variant) {
-		return variant ? real_move_kernel_t<MODEL, E, 1> : real_move_kernel_t<MODEL, E, 0>;
+		return variant ? real_move_kernel_t<MODEL, E, 1, WIN> : real_move_kernel_t<MODEL, E, 0, WIN>;
 	}
-	static K lookup(int variant, int e) {
+	static K lookup(int variant, int e, bool win) {
+		if (win) {
+			switch (e) {
+				case 4: return get<4, true>(variant);
+				case 8: return get<8, true>(variant);
+				case 12: return get<12, true>(variant);
+				case 14: return get<14, true>(variant);
+				case 16: return get<16, true>(variant);
+				default: return nullptr;
+			}
+		}
 		switch (e) {
 			case 2: return get<2>(variant);
 			case 3: return get<3>(variant);

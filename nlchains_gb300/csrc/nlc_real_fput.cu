@@ -3,7 +3,7 @@
 #include "nlc_real.cuh"
 
 namespace nlc {
-const void *real_kernel_fput(int variant, int sites) {
-	return (const void *) RealKernels<NLC_FPUT>::lookup(variant, sites);
+const void *real_kernel_fput(int variant, int sites, bool win) {
+	return (const void *) RealKernels<NLC_FPUT>::lookup(variant, sites, win);
 }
 }  // namespace nlc

@@ -274,7 +274,7 @@ int launch_group(nlc_server *S, size_t slot, const std::vector<Request *> &reqs)
 	auto seg_flags = [](const Request &R) {
 		return (R.round_pos ? NLC_SEG_CONTINUE : 0u) | (R.seg_samples ? 0u : NLC_SEG_OPEN);
 	};
-	if (reqs.size() == 1 || reqs[0]->model.model == NLC_DNLS) {
+	if (reqs.size() == 1 || reqs[0]->model.model == NLC_DNLS || reqs[0]->info.windowed) {
 		for (Request *R : reqs)
 			if (!rc) rc = move_segment(R->plan, R->d_state, R->seg_steps, seg_flags(*R), st);
 	} else {
@@ -424,7 +424,7 @@ void worker_loop(nlc_server *S) {
 					finished.push_back(R);
 					continue;
 				}
-				if (R->model.model == NLC_DNLS) {
+				if (R->model.model == NLC_DNLS || R->info.windowed) {
 					singles.push_back({R});
 					continue;
 				}
@@ -595,6 +595,7 @@ extern "C" int nlc_server_submit(nlc_server *S, const nlc_model *model, uint32_t
 	// state + diagnostics partial rows (<= one row block per SM) + tables
 	R->need_bytes = R->state_bytes + size_t(4 * 160) * n * sizeof(double) + 16 * n * sizeof(double) +
 	                (model->model == NLC_DDNKG ? n * n * sizeof(double) : 0) + (1 << 16);
+	if (n > 4096) R->need_bytes += R->state_bytes + size_t(2 * 1024) * 4 * n * sizeof(double2);   // windows / FFT scratch
 	std::lock_guard<std::mutex> lk(S->mu);
 	if (!S->fatal.empty()) return set_error(NLC_ECUDA, "server stopped after a CUDA error: " + S->fatal);
 	R->id = S->next_id++;

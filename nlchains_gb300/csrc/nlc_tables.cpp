@@ -291,12 +291,37 @@ void host_dft(std::vector<std::complex<double>> &z, int sign) {
 
 }  // namespace
 
+// host_dft for any length: lengths with a prime factor above 7 through Bluestein's identity on a
+// 2^a 3^b 5^c length >= 2n - 1 (O(n log n) instead of the O(n^2) direct prime pass)
+void host_fft_any(std::vector<std::complex<double>> &z, int sign) {
+	const uint32_t n = uint32_t(z.size());
+	if (n < 2 || largest_prime_factor(n) <= 7) return host_dft(z, sign);
+	uint32_t m = 1u << 31;
+	for (uint64_t a = 1; a < 4ull * n; a *= 2)
+		for (uint64_t b = a; b < 4ull * n; b *= 3)
+			for (uint64_t c = b; c < 4ull * n; c *= 5)
+				if (c >= 2ull * n - 1 && c < m) m = uint32_t(c);
+	std::vector<std::complex<double>> w(n), a(m, 0.), b(m, 0.);
+	for (uint32_t j = 0; j < n; j++) {
+		const double ang = M_PI * double((uint64_t(j) * j) % (2ull * n)) / n;
+		w[j] = std::polar(1., sign * ang);   // exp(sign i pi j^2 / n)
+		a[j] = z[j] * w[j];
+		b[j] = std::conj(w[j]);
+		if (j) b[m - j] = b[j];
+	}
+	host_dft(a, -1);
+	host_dft(b, -1);
+	for (uint32_t k = 0; k < m; k++) a[k] *= b[k] / double(m);
+	host_dft(a, +1);
+	for (uint32_t k = 0; k < n; k++) z[k] = w[k] * a[k];
+}
+
 std::vector<double> dnls_conv_tables(const std::vector<double> &lin, uint32_t n, uint32_t m) {
 	std::vector<double> out(2 * 7 * size_t(m));
 	for (int k = 0; k < 7; k++) {
 		std::vector<std::complex<double>> h(n), g(m, 0.);
 		for (uint32_t q = 0; q < n; q++) h[q] = {lin[2 * (k * size_t(n) + q)], lin[2 * (k * size_t(n) + q) + 1]};
-		host_dft(h, +1);   // h[t] = sum_q L_k[q] exp(+2 pi i q t / n): the propagator's kernel in site space
+		host_fft_any(h, +1);   // h[t] = sum_q L_k[q] exp(+2 pi i q t / n): the propagator's kernel in site space
 		for (uint32_t t = 0; t < n; t++) g[t] = h[t];
 		for (uint32_t t = 1; t < n; t++) g[m - t] = h[n - t];   // g[-t mod m] = h[-t mod n]
 		host_dft(g, -1);
@@ -308,13 +333,28 @@ std::vector<double> dnls_conv_tables(const std::vector<double> &lin, uint32_t n,
 	return out;
 }
 
-FftTables fft_tables(uint32_t n, uint32_t max_len) {
+FftTables fft_tables(uint32_t n, uint32_t smem_len, uint32_t max_len, bool convolution) {
 	FftTables T;
 	T.n = n;
 	T.len = n;
-	if (n >= 2 && largest_prime_factor(n) > 7) {
+	if (n >= 2 && largest_prime_factor(n) > 5) {
+		// FP64 operations of the direct form against the padded form of length m; a transform whose
+		// two buffers do not fit shared memory (len > smem_len) runs from global memory at about half
+		// the rate.  DNLS (convolution): two passes of n and the propagator product, or two passes of
+		// m, the kernel product and the zero padding.  Diagnostics: one pass of n, or Bluestein's two
+		// passes of m with the kernel and chirp products.
+		auto cost = [](uint32_t len) {
+			double c = 0;
+			for (int r : fft_radices(len)) c += pass_cost(r);
+			return c * len;
+		};
+		auto slow = [&](uint32_t len) { return len > smem_len ? 2. : 1.; };
 		const uint32_t m = cheapest_length(2 * n - 1, max_len);
-		if (m) T.bluestein = true, T.len = m;
+		if (m) {
+			const double direct = convolution ? (2 * cost(n) + 4. * n) * slow(n) : cost(n) * slow(n);
+			const double padded = convolution ? (2 * cost(m) + 6. * m) * slow(m) : (2 * cost(m) + 4. * m + 8. * n) * slow(m);
+			if (padded < direct) T.bluestein = true, T.len = m;
+		}
 	}
 	T.radices = fft_radices(T.len);
 	T.tw = fft_twiddles(T.len);
