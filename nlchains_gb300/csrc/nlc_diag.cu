@@ -61,49 +61,59 @@ __global__ void lin_fft_kernel(const double2 *__restrict__ state, const DiagArgs
 	}
 }
 
-// dDNKG projection: a block holds CH chains in shared memory; thread k accumulates
-// sum_c (omega_k e_k.phi_c)^2 + (e_k.pi_c)^2 for its modes.
+// dDNKG projection: a block takes CH chains at a time; thread k of a block of modes accumulates
+// sum_c (omega_k e_k.phi_c)^2 + (e_k.pi_c)^2 over its chains.  The chains' sites pass through shared
+// memory in chunks of a.proj_chunk (whole chains when they fit), the eigenvector matrix is read
+// site-major (a warp reads 32 consecutive modes of one site), and each block accumulates into its
+// own row of partial sums in global memory.  Sums over sites run in site order for every length.
 constexpr int kProjChains = 8;
 
 __global__ void lin_ddnkg_kernel(const double2 *__restrict__ state, const DiagArgs a) {
 	extern __shared__ double2 sm[];
-	const int n = int(a.n);
-	double2 *tile = sm;                                              // [CH][n]
-	double *acc = reinterpret_cast<double *>(sm + (size_t) kProjChains * n);   // [n]
+	const int n = int(a.n), SC = a.proj_chunk;
+	double2 *tile = sm;   // [CH][SC]
+	double *acc = a.partials + (size_t) blockIdx.x * n;
 	for (int k = threadIdx.x; k < n; k += blockDim.x) acc[k] = 0.;
 	for (unsigned long long base = (unsigned long long) blockIdx.x * kProjChains; base < a.copies;
 	     base += (unsigned long long) gridDim.x * kProjChains) {
-		__syncthreads();
-		for (int i = threadIdx.x; i < kProjChains * n; i += blockDim.x) {
-			const unsigned long long c = base + i / n;
-			tile[i] = c < a.copies ? state[c * n + i % n] : make_double2(0., 0.);
-		}
-		__syncthreads();
-		for (int k = threadIdx.x; k < n; k += blockDim.x) {
+		for (int kb = 0; kb < n; kb += blockDim.x) {
+			const int k = kb + threadIdx.x;
 			double dphi[kProjChains], dpi[kProjChains];
 #pragma unroll
 			for (int c = 0; c < kProjChains; c++) dphi[c] = 0., dpi[c] = 0.;
-			for (int s = 0; s < n; s++) {
-				const double e = a.eigT[(size_t) s * n + k];
+			for (int s0 = 0; s0 < n; s0 += SC) {
+				const int cs = min(SC, n - s0);
+				__syncthreads();
+				for (int i = threadIdx.x; i < kProjChains * cs; i += blockDim.x) {
+					const int c = i / cs, sl = i - c * cs;
+					const unsigned long long ch = base + c;
+					tile[c * SC + sl] = ch < a.copies ? state[ch * n + s0 + sl] : make_double2(0., 0.);
+				}
+				__syncthreads();
+				if (k < n) {
+					for (int sl = 0; sl < cs; sl++) {
+						const double e = a.eigT[(size_t) (s0 + sl) * n + k];
 #pragma unroll
-				for (int c = 0; c < kProjChains; c++) {
-					const double2 v = tile[c * n + s];
-					dphi[c] = dfma(v.x, e, dphi[c]);
-					dpi[c] = dfma(v.y, e, dpi[c]);
+						for (int c = 0; c < kProjChains; c++) {
+							const double2 v = tile[c * SC + sl];
+							dphi[c] = dfma(v.x, e, dphi[c]);
+							dpi[c] = dfma(v.y, e, dpi[c]);
+						}
+					}
 				}
 			}
-			const double om = a.omega[k];
-			double s = acc[k];
+			if (k < n) {
+				const double om = a.omega[k];
+				double s = acc[k];
 #pragma unroll
-			for (int c = 0; c < kProjChains; c++) {
-				const double v = fmul(om, dphi[c], a.fft.k1);
-				s = fadd(s, dfma(v, v, fmul(dpi[c], dpi[c], a.fft.k1)), a.fft.k1);
+				for (int c = 0; c < kProjChains; c++) {
+					const double v = fmul(om, dphi[c], a.fft.k1);
+					s = fadd(s, dfma(v, v, fmul(dpi[c], dpi[c], a.fft.k1)), a.fft.k1);
+				}
+				acc[k] = s;
 			}
-			acc[k] = s;
 		}
 	}
-	__syncthreads();
-	for (int k = threadIdx.x; k < n; k += blockDim.x) a.partials[(size_t) blockIdx.x * n + k] = acc[k];
 }
 
 cudaError_t launch_linenergies_partials(const DiagArgs &a, const void *state, int blocks, int threads,

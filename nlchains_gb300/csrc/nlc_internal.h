@@ -138,6 +138,7 @@ struct DiagArgs {
 	const double *eigT;      // dDNKG: eigenvectors, row-major by site: eigT[s*n + k] = e_k[s]
 	double *partials;        // [blocks][n]
 	double2 *gscratch;       // block teams whose buffers exceed shared memory: [blocks][2][len]
+	int proj_chunk;          // dDNKG: sites per shared-memory chunk of the projection
 };
 
 cudaError_t launch_linenergies_partials(const DiagArgs &a, const void *state, int blocks, int threads,

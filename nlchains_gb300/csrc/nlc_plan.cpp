@@ -383,7 +383,8 @@ int setup_diagnostics(nlc_plan &P) {
 		if ((rc = P.upload(&d_om, P.omega_host.data(), n))) return rc;
 		g.eigT = d_eigT, g.omega = d_om;
 		P.diag_threads = int(std::min<uint32_t>(256, (n + 31) / 32 * 32));
-		P.diag_smem = size_t(8) * n * sizeof(double2) + n * sizeof(double);
+		g.proj_chunk = int(std::min<uint32_t>(n, 512));
+		P.diag_smem = size_t(8) * g.proj_chunk * sizeof(double2);
 		P.diag_team_block = 1;
 		const unsigned long long tiles = (P.m.copies + 7) / 8;
 		P.diag_blocks = int(std::min<unsigned long long>(tiles, 2ull * sms));
