@@ -178,6 +178,18 @@ int nlc_job_advance(nlc_ctx *ctx, uint64_t job, uint64_t steps);
  * is not finite (the reference's quit condition, results.cpp:64-68). */
 int nlc_job_linenergies(nlc_ctx *ctx, uint64_t job, double *lin, double *wt, double *inf);
 int nlc_job_download(nlc_ctx *ctx, uint64_t job, void *host_state);
+/*
+ * Pipelined sampling, as the reference's main loop keeps up to two batches in flight
+ * (loop_control.hpp, DNKG_FPUT_Toda.cpp:108-151): nlc_job_sample_async enqueues the diagnostics of
+ * the job's current state into result slot 0 or 1 (with copy_state, also a copy of the state into
+ * the slot's pinned host buffer) and returns at once, so the job can advance before the slot is
+ * read.  nlc_job_sample_wait waits for the slot (at most timeout_ms, < 0: no limit; NLC_ETIMEDOUT)
+ * and returns what nlc_job_linenergies returns, plus the state copy into host_state when it is not
+ * NULL (the slot must have been filled with copy_state).  The `nlchains` command line runs on these.
+ */
+int nlc_job_sample_async(nlc_ctx *ctx, uint64_t job, int32_t slot, int32_t copy_state);
+int nlc_job_sample_wait(nlc_ctx *ctx, uint64_t job, int32_t slot, double *lin, double *wt, double *inf,
+                        void *host_state, int32_t timeout_ms);
 /* wait for the job's queued work, at most timeout_ms (< 0: no limit); NLC_ETIMEDOUT if not done */
 int nlc_job_wait(nlc_ctx *ctx, uint64_t job, int32_t timeout_ms);
 /* device pointer of the job's state, for callers that mix levels 1 and 2 */

@@ -37,7 +37,7 @@ EXPORTS = (
     "nlc_job_download", "nlc_job_wait", "nlc_job_state_ptr", "nlc_program_run", "nlc_last_error",
     "nlc_version", "nlc_kernel_launches", "nlc_fp64_peak", "nlc_linenergies_noalloc",
     "nlc_server_create", "nlc_server_destroy", "nlc_server_submit", "nlc_server_poll", "nlc_server_wait",
-    "nlc_server_result", "nlc_entropies",
+    "nlc_server_result", "nlc_entropies", "nlc_job_sample_async", "nlc_job_sample_wait",
 )
 
 
@@ -116,6 +116,8 @@ def lib():
         "nlc_server_wait": ([vp, u64, i32], i32),
         "nlc_server_result": ([vp, u64, vp, dp, dp, P(u64)], i32),
         "nlc_entropies": ([dp, u32, i32, vp, dp], i32),
+        "nlc_job_sample_async": ([vp, u64, i32, i32], i32),
+        "nlc_job_sample_wait": ([vp, u64, i32, dp, dp, dp, vp, i32], i32),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -294,6 +296,21 @@ class Job:
         _check(lib().nlc_job_linenergies(self.ctx._h, self.id, lin.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
                                          ctypes.byref(wt), ctypes.byref(inf)))
         return lin, wt.value, inf.value
+
+    def sample_async(self, slot, copy_state=False):
+        """Enqueue the diagnostics (and optionally a state copy) of the current state into slot 0/1."""
+        _check(lib().nlc_job_sample_async(self.ctx._h, self.id, int(slot), int(bool(copy_state))))
+
+    def sample_wait(self, slot, with_state=False, timeout_ms=-1):
+        """(linenergies, WT, INF, state or None) of a slot filled by sample_async; EBLOWUP raises."""
+        lin = np.zeros(self.model.chain_length)
+        wt, inf = ctypes.c_double(), ctypes.c_double()
+        state = np.empty((self.model.copies, self.model.chain_length, 2)) if with_state else None
+        _check(lib().nlc_job_sample_wait(self.ctx._h, self.id, int(slot),
+                                         lin.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), ctypes.byref(wt),
+                                         ctypes.byref(inf), None if state is None else state.ctypes.data_as(ctypes.c_void_p),
+                                         int(timeout_ms)))
+        return lin, wt.value, inf.value, state
 
     def download(self, out=None):
         dtype_shape = (self.model.copies, self.model.chain_length, 2)

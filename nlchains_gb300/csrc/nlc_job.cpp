@@ -28,6 +28,11 @@ struct Job {
 	double *h_diag = nullptr;   // pinned copy
 	cudaStream_t stream = nullptr;
 	size_t state_bytes = 0;
+	// pipelined sampling: two result slots (device diagnostics, pinned copies, optional pinned state)
+	double *d_slot[2] = {nullptr, nullptr}, *h_slot[2] = {nullptr, nullptr};
+	double2 *h_state_slot[2] = {nullptr, nullptr};
+	cudaEvent_t ev_slot[2] = {nullptr, nullptr};
+	bool slot_state[2] = {false, false};
 
 	~Job() {
 		if (stream) cudaStreamSynchronize(stream);
@@ -35,6 +40,12 @@ struct Job {
 		cudaFree(d_state);
 		cudaFree(d_diag);
 		cudaFreeHost(h_diag);
+		for (int i = 0; i < 2; i++) {
+			cudaFree(d_slot[i]);
+			cudaFreeHost(h_slot[i]);
+			cudaFreeHost(h_state_slot[i]);
+			if (ev_slot[i]) cudaEventDestroy(ev_slot[i]);
+		}
 		if (stream) cudaStreamDestroy(stream);
 	}
 };
@@ -142,6 +153,61 @@ extern "C" int nlc_job_linenergies(nlc_ctx *ctx, uint64_t id, double *lin, doubl
 	if (wt) *wt = J->h_diag[n];
 	if (inf) *inf = J->h_diag[n + 1];
 	if (!std::isfinite(J->h_diag[n]) || !std::isfinite(J->h_diag[n + 1]))
+		return set_error(NLC_EBLOWUP, "non-finite entropy (blow-up or vanishing mode energy)");
+	return NLC_OK;
+}
+
+extern "C" int nlc_job_sample_async(nlc_ctx *ctx, uint64_t id, int32_t slot, int32_t copy_state) {
+	Job *J = find_job(ctx, id);
+	if (!J) return set_error(NLC_ENOTFOUND, "no such job");
+	if (slot < 0 || slot > 1) return set_error(NLC_EINVAL, "slot must be 0 or 1");
+	const size_t n = J->model.chain_length;
+	int rc;
+	if (!J->d_slot[slot]) {
+		if ((rc = cuda_status(cudaMalloc(&J->d_slot[slot], (n + 2) * sizeof(double)), "cudaMalloc"))) return rc;
+		if ((rc = cuda_status(cudaMallocHost(&J->h_slot[slot], (n + 2) * sizeof(double)), "cudaMallocHost"))) return rc;
+		if ((rc = cuda_status(cudaEventCreateWithFlags(&J->ev_slot[slot], cudaEventDisableTiming), "cudaEventCreate")))
+			return rc;
+	}
+	if (copy_state && !J->h_state_slot[slot] &&
+	    (rc = cuda_status(cudaMallocHost(&J->h_state_slot[slot], J->state_bytes), "cudaMallocHost")))
+		return rc;
+	if ((rc = nlc_linenergies(J->plan, J->d_state, J->d_slot[slot], J->d_slot[slot] + n, J->stream))) return rc;
+	if ((rc = cuda_status(cudaMemcpyAsync(J->h_slot[slot], J->d_slot[slot], (n + 2) * sizeof(double),
+	                                      cudaMemcpyDeviceToHost, J->stream),
+	                      "diagnostics copy")))
+		return rc;
+	J->slot_state[slot] = copy_state != 0;
+	if (copy_state &&
+	    (rc = cuda_status(cudaMemcpyAsync(J->h_state_slot[slot], J->d_state, J->state_bytes, cudaMemcpyDeviceToHost,
+	                                      J->stream),
+	                      "state copy")))
+		return rc;
+	return cuda_status(cudaEventRecord(J->ev_slot[slot], J->stream), "cudaEventRecord");
+}
+
+extern "C" int nlc_job_sample_wait(nlc_ctx *ctx, uint64_t id, int32_t slot, double *lin, double *wt, double *inf,
+                                   void *host_state, int32_t timeout_ms) {
+	Job *J = find_job(ctx, id);
+	if (!J) return set_error(NLC_ENOTFOUND, "no such job");
+	if (slot < 0 || slot > 1 || !J->ev_slot[slot]) return set_error(NLC_EINVAL, "slot was never filled");
+	if (host_state && !J->slot_state[slot]) return set_error(NLC_EINVAL, "slot holds no state copy");
+	const auto t0 = std::chrono::steady_clock::now();
+	for (;;) {
+		const cudaError_t e = cudaEventQuery(J->ev_slot[slot]);
+		if (e == cudaSuccess) break;
+		if (e != cudaErrorNotReady) return cuda_status(e, "sample");
+		if (timeout_ms >= 0 && std::chrono::steady_clock::now() - t0 >= std::chrono::milliseconds(timeout_ms))
+			return set_error(NLC_ETIMEDOUT, "sample not ready");
+		std::this_thread::sleep_for(std::chrono::microseconds(50));
+	}
+	const size_t n = J->model.chain_length;
+	const double *h = J->h_slot[slot];
+	if (lin) std::memcpy(lin, h, n * sizeof(double));
+	if (wt) *wt = h[n];
+	if (inf) *inf = h[n + 1];
+	if (host_state) std::memcpy(host_state, J->h_state_slot[slot], J->state_bytes);
+	if (!std::isfinite(h[n]) || !std::isfinite(h[n + 1]))
 		return set_error(NLC_EBLOWUP, "non-finite entropy (blow-up or vanishing mode energy)");
 	return NLC_OK;
 }
@@ -442,21 +508,42 @@ int run_program(int argc, char **argv) {
 			write_file(prefix + "-" + std::to_string(t), host_state, state_bytes, "dump");
 		}
 	};
+	// Pipelined like the reference's loop (DNKG_FPUT_Toda.cpp:108-151, loop_control.hpp): the next
+	// batch and its sample are enqueued before the host handles the current sample (entropy line,
+	// limit checks, dumps), so the GPU integrates while the files are written.  A quit request (signal,
+	// entropy limit, non-finite entropy: results.cpp:63-73) stops the loop at the step of the sample
+	// already in flight, within the reference's own range (it stops at its main loop's step, up to
+	// two batches past the sample that asked).
 	uint64_t t = offset;
+	int slot = 0;
+	if ((rc = nlc_job_sample_async(ctx, job, slot, t % dump_interval == 0))) throw CliError{2, nlc_last_error()};
+	bool quit = false, in_flight = false;
 	for (;;) {
+		const bool last = (steps && t == steps) || quit;
+		in_flight = false;
+		if (!last) {
+			if ((rc = nlc_job_advance(ctx, job, batching))) throw CliError{2, nlc_last_error()};
+			const uint64_t tn = t + batching;
+			if ((rc = nlc_job_sample_async(ctx, job, slot ^ 1, tn % dump_interval == 0))) throw CliError{2, nlc_last_error()};
+			in_flight = true;
+		}
 		double wt = 0, inf = 0;
-		rc = nlc_job_linenergies(ctx, job, lin.data(), &wt, &inf);
-		bool quit = g_quit != 0;
+		const bool full_dump = t % dump_interval == 0;
+		rc = nlc_job_sample_wait(ctx, job, slot, lin.data(), &wt, &inf, full_dump ? host_state : nullptr, -1);
 		if (rc == NLC_EBLOWUP) quit = true;   // results.cpp:64-68
 		else if (rc) throw CliError{2, nlc_last_error()};
+		if (g_quit) quit = true;
 		const double triplet[3] = {t * M.dt, wt, inf};
 		entropy_file.write(reinterpret_cast<const char *>(triplet), sizeof(triplet)).flush();
 		if (verbose) std::cout << "Entropy step " << t << ": " << wt << '/' << inf << std::endl;
 		if (has_entropy && (wt_limit ? wt : inf) < entropy_limit) quit = true;   // results.cpp:69-72
-		if (t % dump_interval == 0) dump(t, true);
-		if ((steps && t == steps) || quit) break;
-		if ((rc = nlc_job_advance(ctx, job, batching))) throw CliError{2, nlc_last_error()};
+		if (full_dump) {
+			write_file(prefix + "-linenergies-" + std::to_string(t), lin.data(), n * sizeof(double), "linenergies");
+			write_file(prefix + "-" + std::to_string(t), host_state, state_bytes, "dump");
+		}
+		if (!in_flight) break;   // after a quit request the sample in flight is handled, then the loop stops
 		t += batching;
+		slot ^= 1;
 	}
 	if (t % dump_interval != 0) dump(t, true);
 	return 0;

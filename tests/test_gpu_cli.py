@@ -71,5 +71,8 @@ def test_entropy_limit_stops_early(gpu, tmp_path):
                       "-s", "0", "-p", "o", "--alpha", "0", "--beta", "1", "-e", "1e9"], tmp_path)
     assert r.returncode == 0, r.stderr
     ent = np.fromfile(tmp_path / "o-entropy").reshape(-1, 3)
-    assert ent.shape[0] == 1
+    # the reference stops at its main loop's step, up to two batches past the sample that asked
+    # (loop_control.hpp); the engine keeps one batch in flight, so it stops at t = 0 or t = 10
+    assert 1 <= ent.shape[0] <= 3
     assert os.path.exists(tmp_path / "o-0")
+    assert os.path.exists(tmp_path / f"o-{10 * (ent.shape[0] - 1)}")

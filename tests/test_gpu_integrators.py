@@ -137,3 +137,32 @@ def test_zero_steps_is_a_no_op(gpu):
     state = ic.real_ensemble(n, copies, 0.1, ic.low_modes(n, kmax=2, include_zero=False), seed=1)
     out = gpu_run(gpu, "FPUT", n, copies, 0.1, dict(alpha=0.0, beta=1.0), state, 0, 10)
     assert np.array_equal(out, state)
+
+
+def test_pipelined_sampling_equals_synchronous(gpu):
+    """Two result slots with the next batch enqueued before the previous sample is read give the
+    same samples and states as the synchronous loop."""
+    n, copies, b, rounds = 64, 96, 10, 6
+    model = gpu.Model("FPUT", n, copies, 0.1, alpha=0.0, beta=1.0)
+    state = ic.real_ensemble(n, copies, 0.1, ic.low_modes(n, kmax=4, include_zero=False), seed=5)
+    ctx = gpu.Context(0)
+    sync = ctx.job(model, b)
+    sync.upload(state)
+    exp = []
+    for r in range(rounds):
+        lin, wt, inf = sync.linenergies()
+        exp.append((lin, wt, inf, sync.download()))
+        sync.advance(b)
+    pipe = ctx.job(model, b)
+    pipe.upload(state)
+    pipe.sample_async(0, copy_state=True)
+    got = []
+    for r in range(rounds):
+        pipe.advance(b)
+        pipe.sample_async((r + 1) % 2, copy_state=True)
+        got.append(pipe.sample_wait(r % 2, with_state=True))
+    for (el, ew, ei, es), (gl, gw, gi, gs) in zip(exp, got):
+        assert np.array_equal(el, gl) and ew == gw and ei == gi and np.array_equal(es, gs)
+    sync.close()
+    pipe.close()
+    ctx.close()
