@@ -163,6 +163,10 @@ def measure_engine(w, steps, warmup, rank, world, local):
     lin = torch.zeros(n, dtype=torch.float64, device="cuda")
     ent = torch.zeros(2, dtype=torch.float64, device="cuda")
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    # per-chain energies before and after the run (nlc_energies): the drift of the integrator
+    e_before = torch.zeros(copies, dtype=torch.float64, device="cuda")
+    e_after = torch.zeros(copies, dtype=torch.float64, device="cuda")
+    plan.energies(dev.data_ptr(), e_before.data_ptr(), sp)
 
     def one_step():
         plan.move(dev.data_ptr(), b, sp)
@@ -199,7 +203,9 @@ def measure_engine(w, steps, warmup, rank, world, local):
     from nlchains_gb300 import shards
     lin_all, wt, inf = shards.sample(lin.cpu().numpy(), copies, copies * world, model.a0is0)
     shape = plan.shape()
-    return dict(value=value, step_ms=step_ms / steps, move_ms=move_ms, wall_s=wall, launches=launches,
+    plan.energies(dev.data_ptr(), e_after.data_ptr(), sp)
+    drift = float((e_after / e_before - 1).abs().max().item())
+    return dict(value=value, step_ms=step_ms / steps, move_ms=move_ms, wall_s=wall, launches=launches, energy_drift=drift,
                 clocks=clk.summary(), shape=shape, plan=plan, lin=lin_all, entropies=[wt, inf],
                 state_after=dev.cpu().numpy(), state_before=state)
 
@@ -350,15 +356,6 @@ def cpu_baseline(w, target_s=10.0, threads=None, sample_copies=None, steps_per_c
                       f"({t:.1f} s), oracle reference-order port, OpenMP over copies"}
 
 
-def energy_drift(w, before, after):
-    import oracle as O
-    sel = slice(0, 2048)
-    mdl = O.Model(w["model"], w["n"], 2048, w["dt"], masses=masses(w), **w["params"])
-    e0 = O.energies(mdl, np.ascontiguousarray(before[sel]))
-    e1 = O.energies(mdl, np.ascontiguousarray(after[sel]))
-    return float(np.abs(e1 / e0 - 1).max())
-
-
 def read_traffic(kernel_key):
     """DRAM bytes per launch from the committed ncu summary (profiles/traffic.tsv), or None."""
     path = os.path.join(ROOT, "profiles", "traffic.tsv")
@@ -422,7 +419,7 @@ def run_engine(args):
                 "d2h_bytes_per_step": e2e["d2h"]},
         "gpu_launches": r["launches"],
         "clocks": r["clocks"],
-        "energy_drift": energy_drift(w, r["state_before"], r["state_after"]) if rank == 0 else None,
+        "energy_drift": r["energy_drift"] if rank == 0 else None,
         "toda": {"value": toda["value"], "unit": "site-steps/s", "workload": TODA["name"],
                  "roofline_frac": FLOPS_PER_SITE_STEP["Toda"] * TODA["n"] * TODA["copies"] * TODA["batching"] /
                  (toda["move_ms"] * 1e-3) / 1e12 / peak, "kernel_ms": toda["move_ms"],
@@ -445,7 +442,6 @@ def run_reference(args):
     w = WORKLOAD
     threads = os.cpu_count() or 1
     copies = max(threads * 64, 1024)   # a bounded sample of the 65536 copies per step
-    import oracle as O
     for _ in range(args.warmup):
         cpu_baseline(w, threads=threads, sample_copies=copies, steps_per_call=1)
     t0 = time.perf_counter()

@@ -140,6 +140,13 @@ int nlc_linenergies(nlc_plan *plan, const void *state_dev, double *lin_dev, doub
 int nlc_linenergies_noalloc(int32_t model, uint32_t chain_length, uint32_t copies, double m, const void *state_dev,
                             const uint8_t *entropy_mask_dev, double *lin_dev, double *entropies_dev, void *stream);
 
+/*
+ * Energy (Hamiltonian) of every chain into energies_dev[copies] (device memory), ordered on
+ * `stream`: the definitions of the reference's post-processing (supporting-material/
+ * post-processing/nlchains.m:40-48), for energy-drift checks.  The reference C++ has no equivalent.
+ */
+int nlc_energies(nlc_plan *plan, const void *state_dev, double *energies_dev, void *stream);
+
 /* DNLS elementwise operators with the reference's semantics (DNLS.hpp:16-20, DNLS.cu:11-43), for
  * callers that drive their own FFTs: psi *= exp(-i coef |psi|^2); psi_k *= table[k % n]. */
 int nlc_dnls_evolve_nonlinear(nlc_plan *plan, void *psi_dev, double beta_dt_symplectic, void *stream);
@@ -178,6 +185,8 @@ int nlc_job_advance(nlc_ctx *ctx, uint64_t job, uint64_t steps);
  * is not finite (the reference's quit condition, results.cpp:64-68). */
 int nlc_job_linenergies(nlc_ctx *ctx, uint64_t job, double *lin, double *wt, double *inf);
 int nlc_job_download(nlc_ctx *ctx, uint64_t job, void *host_state);
+/* energies of every chain of the job's current state into host_energies[copies] (blocking) */
+int nlc_job_energies(nlc_ctx *ctx, uint64_t job, double *host_energies);
 /*
  * Pipelined sampling, as the reference's main loop keeps up to two batches in flight
  * (loop_control.hpp, DNKG_FPUT_Toda.cpp:108-151): nlc_job_sample_async enqueues the diagnostics of

@@ -37,7 +37,8 @@ EXPORTS = (
     "nlc_job_download", "nlc_job_wait", "nlc_job_state_ptr", "nlc_program_run", "nlc_last_error",
     "nlc_version", "nlc_kernel_launches", "nlc_fp64_peak", "nlc_linenergies_noalloc",
     "nlc_server_create", "nlc_server_destroy", "nlc_server_submit", "nlc_server_poll", "nlc_server_wait",
-    "nlc_server_result", "nlc_entropies", "nlc_job_sample_async", "nlc_job_sample_wait",
+    "nlc_server_result", "nlc_entropies", "nlc_job_sample_async", "nlc_job_sample_wait", "nlc_energies",
+    "nlc_job_energies",
 )
 
 
@@ -118,6 +119,8 @@ def lib():
         "nlc_entropies": ([dp, u32, i32, vp, dp], i32),
         "nlc_job_sample_async": ([vp, u64, i32, i32], i32),
         "nlc_job_sample_wait": ([vp, u64, i32, dp, dp, dp, vp, i32], i32),
+        "nlc_energies": ([vp, vp, vp, vp], i32),
+        "nlc_job_energies": ([vp, u64, dp], i32),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -222,6 +225,10 @@ class Plan:
         _check(lib().nlc_linenergies(self._h, ctypes.c_void_p(state_ptr), ctypes.c_void_p(lin_ptr),
                                      ctypes.c_void_p(entropies_ptr or None), ctypes.c_void_p(stream)))
 
+    def energies(self, state_ptr, energies_ptr, stream=0):
+        _check(lib().nlc_energies(self._h, ctypes.c_void_p(state_ptr), ctypes.c_void_p(energies_ptr),
+                                  ctypes.c_void_p(stream)))
+
     def dnls_evolve_nonlinear(self, psi_ptr, coef, stream=0):
         _check(lib().nlc_dnls_evolve_nonlinear(self._h, ctypes.c_void_p(psi_ptr), coef, ctypes.c_void_p(stream)))
 
@@ -296,6 +303,12 @@ class Job:
         _check(lib().nlc_job_linenergies(self.ctx._h, self.id, lin.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
                                          ctypes.byref(wt), ctypes.byref(inf)))
         return lin, wt.value, inf.value
+
+    def energies(self):
+        """Energy of every chain of the current state (nlchains.m:40-48 definitions)."""
+        out = np.zeros(self.model.copies)
+        _check(lib().nlc_job_energies(self.ctx._h, self.id, out.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
+        return out
 
     def sample_async(self, slot, copy_state=False):
         """Enqueue the diagnostics (and optionally a state copy) of the current state into slot 0/1."""

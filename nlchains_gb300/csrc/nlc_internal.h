@@ -186,4 +186,13 @@ cudaError_t launch_fp64_probe(double *out, int blocks, int threads, int iters, c
 // bookkeeping
 void count_launch(uint64_t k = 1);
 
+// Per-chain energies (nlc_energy.cu)
+struct EnergyArgs {
+	int model;
+	uint32_t n, copies;
+	double m, alpha, beta;
+	const double *mp2_site;   // dDNKG: m_s + 2 (device)
+};
+cudaError_t launch_energies(const EnergyArgs &a, const double2 *state, double *out, cudaStream_t stream);
+
 }  // namespace nlc

@@ -157,6 +157,21 @@ extern "C" int nlc_job_linenergies(nlc_ctx *ctx, uint64_t id, double *lin, doubl
 	return NLC_OK;
 }
 
+extern "C" int nlc_job_energies(nlc_ctx *ctx, uint64_t id, double *host_energies) {
+	Job *J = find_job(ctx, id);
+	if (!J) return set_error(NLC_ENOTFOUND, "no such job");
+	if (!host_energies) return set_error(NLC_EINVAL, "NULL argument");
+	double *d = nullptr;
+	const size_t bytes = size_t(J->model.copies) * sizeof(double);
+	int rc = cuda_status(cudaMallocAsync(reinterpret_cast<void **>(&d), bytes, J->stream), "cudaMallocAsync");
+	if (rc) return rc;
+	rc = nlc_energies(J->plan, J->d_state, d, J->stream);
+	if (!rc) rc = cuda_status(cudaMemcpyAsync(host_energies, d, bytes, cudaMemcpyDeviceToHost, J->stream), "energies copy");
+	cudaFreeAsync(d, J->stream);
+	const int rs = cuda_status(cudaStreamSynchronize(J->stream), "energies");
+	return rc ? rc : rs;
+}
+
 extern "C" int nlc_job_sample_async(nlc_ctx *ctx, uint64_t id, int32_t slot, int32_t copy_state) {
 	Job *J = find_job(ctx, id);
 	if (!J) return set_error(NLC_ENOTFOUND, "no such job");

@@ -784,6 +784,17 @@ int nlc::move_segment(nlc_plan *P, void *state, uint32_t steps, uint32_t seg, cu
 	return cuda_status(launch_real_move(P->m.model, P->variant, P->rs, static_cast<double *>(state), a, st), "move launch");
 }
 
+extern "C" int nlc_energies(nlc_plan *P, const void *state, double *energies, void *stream) {
+	if (!P || !state || !energies) return set_error(NLC_EINVAL, "NULL argument");
+	EnergyArgs e{};
+	e.model = P->m.model;
+	e.n = P->m.chain_length, e.copies = P->m.copies;
+	e.m = P->m.m, e.alpha = P->m.alpha, e.beta = P->m.beta;
+	e.mp2_site = P->ra.mp2_site;
+	return cuda_status(launch_energies(e, static_cast<const double2 *>(state), energies, static_cast<cudaStream_t>(stream)),
+	                   "energies launch");
+}
+
 extern "C" int nlc_linenergies(nlc_plan *P, const void *state, double *lin, double *ent, void *stream) {
 	if (!P || !state || !lin) return set_error(NLC_EINVAL, "NULL argument");
 	cudaStream_t st = static_cast<cudaStream_t>(stream);
