@@ -468,13 +468,17 @@ def run_reference(args):
 
 
 def run_profile_case(args):
-    """Small case of the headline kernels for ncu captures: 16384 copies, 4 launches of 10 steps."""
+    """Small cases of the headline kernels for ncu captures: 4 launches (10 steps; DNLS 2 steps),
+    each followed by one diagnostics sample.  DNKG / Toda: 16384 of the 65536 copies (33.5 MB);
+    DNLS: the full 8192 copies of N = 1024 (134 MB, above the L2)."""
     import torch
 
     import nlchains_gb300 as nlc
-    w = dict(WORKLOAD, copies=16384)
+    w, steps = dict(WORKLOAD, copies=16384), 10
     if args.profile == "toda":
         w = dict(TODA, copies=16384)
+    if args.profile == "dnls":
+        w, steps = dict(OTHERS[1]), 2
     state = initial_state(w, w["copies"], 0)
     plan = nlc.Plan(nlc.Model(w["model"], w["n"], w["copies"], w["dt"], flags=nlc.FLAG_NO_TUNE, **w["params"]))
     dev = torch.from_numpy(state).cuda()
@@ -482,7 +486,7 @@ def run_profile_case(args):
     ent = torch.zeros(2, dtype=torch.float64, device="cuda")
     sp = torch.cuda.current_stream().cuda_stream
     for _ in range(4):
-        plan.move(dev.data_ptr(), 10, sp)
+        plan.move(dev.data_ptr(), steps, sp)
         plan.linenergies(dev.data_ptr(), lin.data_ptr(), ent.data_ptr(), sp)
     torch.cuda.synchronize()
     print(json.dumps({"profile_case": w["name"].replace("65536", str(w["copies"])), "shape": plan.shape(),
@@ -495,7 +499,7 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["engine", "reference"], default="engine")
-    ap.add_argument("--profile", choices=["dnkg", "toda"], default=None,
+    ap.add_argument("--profile", choices=["dnkg", "toda", "dnls"], default=None,
                     help="run only a small case of the integrator + diagnostics (for ncu captures)")
     args = ap.parse_args()
     if args.profile:
