@@ -186,6 +186,24 @@ cudaError_t launch_fp64_probe(double *out, int blocks, int threads, int iters, c
 // bookkeeping
 void count_launch(uint64_t k = 1);
 
+// dDNKG projection on the tensor cores (nlc_tc.cu): 7 BF16 slices of X (rows 2c, 2c + 1 = phi_c,
+// pi_c of chain c) and of the eigenvector matrix E, each padded with zeros to mp / np rows (multiples
+// of 128 / 64) and kp sites (a multiple of 32), slice i at rows [i mp, (i + 1) mp)
+struct TcArgs {
+	uint32_t n, copies;
+	int mp, np, kp;
+	uint16_t *a_slices;        // [7][mp][kp] BF16 bit patterns, written per sample by the split kernel
+	int *row_exp;              // [2 copies] power-of-two exponent of each row of X
+	const int *col_exp;        // [n] exponent of each eigenvector (row of E)
+	const double *omega;       // [n]
+	double *partials;          // [mp / 128][n] weighted squared sums per row tile
+	int *status;               // set on a bounded-wait timeout
+};
+cudaError_t launch_tc_projection(const TcArgs &a, const void *map_a, const void *map_b, const double2 *state,
+                                 cudaStream_t stream);
+size_t tc_projection_smem();
+const void *tc_projection_kernel_ptr();
+
 // Per-chain energies (nlc_energy.cu)
 struct EnergyArgs {
 	int model;

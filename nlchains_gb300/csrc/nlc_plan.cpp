@@ -9,6 +9,8 @@
 #include <mutex>
 #include <tuple>
 
+#include <cuda.h>
+
 #include "nlc_host.h"
 
 namespace nlc {
@@ -117,6 +119,10 @@ struct nlc_plan {
 	int diag_blocks = 0, diag_threads = 0, diag_team_block = 0, diag_rows = 0;
 	size_t diag_smem = 0;
 	int tier = 0;   // 1 = resident lanes (G <= 32), 2 = resident block (G > 32), 3 = DNLS, 4 = windowed
+	// dDNKG projection on the tensor cores
+	bool tc = false;
+	TcArgs tca{};
+	CUtensorMap tc_map_a{}, tc_map_b{};
 	uint32_t win_len = 0, win_steps = 0;   // windowed tier: sites per window, steps per launch
 	double2 *d_win = nullptr;              // windowed tier: the second state buffer
 	double block_ops = 0;      // FP64 work of one block's step over the sustained fraction of peak
@@ -367,6 +373,87 @@ int setup_fft(nlc_plan &P, FftPlanDev &f, bool convolution) {
 	return NLC_OK;
 }
 
+int set_smem_attr(const void *k, size_t smem, const cudaDeviceProp &prop);
+
+// cuTensorMapEncodeTiled from the driver, without linking libcuda
+using EncodeTiledFn = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                   const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_tiled() {
+	static EncodeTiledFn fn = [] {
+		void *p = nullptr;
+		cudaDriverEntryPointQueryResult q{};
+		if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+		    q != cudaDriverEntryPointSuccess)
+			p = nullptr;
+		return reinterpret_cast<EncodeTiledFn>(p);
+	}();
+	return fn;
+}
+
+// 2-D BF16 tensor map of `rows` rows of kp elements, boxes of 32 x box_rows, 64-byte swizzle
+int bf16_map(CUtensorMap *map, void *base, uint64_t kp, uint64_t rows, uint32_t box_rows) {
+	EncodeTiledFn enc = encode_tiled();
+	if (!enc) return set_error(NLC_ECUDA, "cuTensorMapEncodeTiled is not available");
+	const cuuint64_t dims[2] = {kp, rows}, strides[1] = {kp * 2};
+	const cuuint32_t box[2] = {32, box_rows}, es[2] = {1, 1};
+	const CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, base, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+	                       CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+	return r == CUDA_SUCCESS ? NLC_OK : set_error(NLC_ECUDA, "cuTensorMapEncodeTiled failed");
+}
+
+// Tensor-core projection set-up: the 7 BF16 slices of every eigenvector (rows of E, host, once),
+// the per-sample slice buffer of X (zero padding included), and the tensor maps.  Slicing as in
+// nlc_tc.cu: a row scaled by 2^-f (max |e| = m 2^f, 0.5 <= m < 1), v = 256 e 2^-f, then
+// sigma_i = round(v), v <- 256 (v - sigma_i).
+int setup_tc_projection(nlc_plan &P, const double *d_omega) {
+	const uint32_t n = P.m.chain_length;
+	TcArgs &t = P.tca;
+	t.n = n, t.copies = P.m.copies;
+	t.mp = int((2ull * P.m.copies + 127) / 128 * 128);
+	t.np = int((n + 63) / 64 * 64);
+	t.kp = int((n + 31) / 32 * 32);
+	std::vector<uint16_t> b(size_t(7) * t.np * t.kp, 0);
+	std::vector<int> fexp(n, 0);
+	for (uint32_t k = 0; k < n; k++) {
+		const double *e = &P.eig_host[size_t(k) * n];
+		double mx = 0;
+		for (uint32_t s = 0; s < n; s++) mx = std::max(mx, std::fabs(e[s]));
+		int f = 0;
+		if (mx > 0) std::frexp(mx, &f);
+		fexp[k] = f;
+		for (uint32_t s = 0; s < n; s++) {
+			double v = std::ldexp(e[s], 8 - f);
+			for (int i = 0; i < 7; i++) {
+				const double sg = std::nearbyint(v);
+				const float fs = float(sg);   // an integer of at most 9 bits: exact in BF16
+				uint32_t bits;
+				std::memcpy(&bits, &fs, 4);
+				b[(size_t(i) * t.np + k) * t.kp + s] = uint16_t(bits >> 16);
+				v = (v - sg) * 256.;
+			}
+		}
+	}
+	int rc;
+	uint16_t *d_b = nullptr, *d_a = nullptr;
+	int *d_fexp = nullptr, *d_rexp = nullptr, *d_status = nullptr;
+	if ((rc = P.upload(&d_b, b.data(), b.size()))) return rc;
+	if ((rc = P.upload(&d_fexp, fexp.data(), n))) return rc;
+	const std::vector<uint16_t> zeros(size_t(7) * t.mp * t.kp, 0);   // padding rows and sites stay 0
+	if ((rc = P.upload(&d_a, zeros.data(), zeros.size()))) return rc;
+	if ((rc = P.dalloc(&d_rexp, 2ull * P.m.copies))) return rc;
+	const int zero = 0;
+	if ((rc = P.upload(&d_status, &zero, 1))) return rc;
+	t.a_slices = d_a, t.row_exp = d_rexp, t.col_exp = d_fexp, t.omega = d_omega, t.status = d_status;
+	if ((rc = bf16_map(&P.tc_map_a, d_a, uint64_t(t.kp), uint64_t(7) * t.mp, 128))) return rc;
+	if ((rc = bf16_map(&P.tc_map_b, d_b, uint64_t(t.kp), uint64_t(7) * t.np, 64))) return rc;
+	if ((rc = set_smem_attr(tc_projection_kernel_ptr(), tc_projection_smem(), P.prop))) return rc;
+	P.diag_rows = t.mp / 128;
+	P.tc = true;
+	return NLC_OK;
+}
+
 int setup_diagnostics(nlc_plan &P) {
 	const uint32_t n = P.m.chain_length;
 	DiagArgs &g = P.ga;
@@ -389,6 +476,10 @@ int setup_diagnostics(nlc_plan &P) {
 		const unsigned long long tiles = (P.m.copies + 7) / 8;
 		P.diag_blocks = int(std::min<unsigned long long>(tiles, 2ull * sms));
 		P.diag_rows = P.diag_blocks;
+		if (P.m.flags & NLC_FLAG_TENSOR_PROJECTION) {
+			if ((rc = setup_tc_projection(P, d_om))) return rc;   // its own partial rows: one per 64 chains
+			P.diag_smem = 0;
+		}
 	} else {
 		if ((rc = setup_fft(P, g.fft, false))) return rc;
 		if (P.m.model == NLC_DNLS) {
@@ -798,9 +889,17 @@ extern "C" int nlc_energies(nlc_plan *P, const void *state, double *energies, vo
 extern "C" int nlc_linenergies(nlc_plan *P, const void *state, double *lin, double *ent, void *stream) {
 	if (!P || !state || !lin) return set_error(NLC_EINVAL, "NULL argument");
 	cudaStream_t st = static_cast<cudaStream_t>(stream);
-	int rc = cuda_status(launch_linenergies_partials(P->ga, state, P->diag_blocks, P->diag_threads, P->diag_smem,
-	                                                 P->diag_team_block, st),
-	                     "linenergies launch");
+	int rc;
+	if (P->tc) {
+		TcArgs t = P->tca;
+		t.partials = P->d_partials;
+		rc = cuda_status(launch_tc_projection(t, &P->tc_map_a, &P->tc_map_b, static_cast<const double2 *>(state), st),
+		                 "tensor projection launch");
+	} else {
+		rc = cuda_status(launch_linenergies_partials(P->ga, state, P->diag_blocks, P->diag_threads, P->diag_smem,
+		                                             P->diag_team_block, st),
+		                 "linenergies launch");
+	}
 	if (rc) return rc;
 	FinishArgs f{};
 	f.partials = P->d_partials;

@@ -1,0 +1,274 @@
+// dDNKG linear-mode projection on the tensor cores (tcgen05, sm_103a), FP64-accurate.
+//
+// The projection is a matrix product: with X the 2C x n matrix whose rows are the chains' phi and
+// pi (row 2c = phi_c, 2c + 1 = pi_c) and E the eigenvector matrix (E[k][s] = component s of mode
+// k), P = X E^T and e_k = sum_c (omega_k P[2c][k])^2 + P[2c+1][k]^2 (the reference: two
+// cublasDgemm + a reduction kernel, dDNKG.cpp:120-141, dDNKG.cu:237-256).  GB300's FP64 rate is a
+// small fraction of its BF16 tensor rate, so the product runs as an Ozaki-type split (K. Ozaki,
+// T. Ogita, S. Oishi, S. M. Rump, "Error-free transformations of matrix multiplication by using
+// fast routines of matrix multiplication and its applications", Numer. Algorithms 59, 2012):
+//
+//   each row of X and of E is scaled by a power of two 2^e so that |x 2^-e| < 1, then written as
+//   7 slices  x 2^-e = sum_i sigma_i 2^(-8i),  sigma_i integers with |sigma_i| <= 256 (exact in
+//   BF16).  P = 2^(e_r + f_k) sum_{t = 2..8} 2^(-8t) G_t,  G_t = sum_{i + j = t} A_i B_j^T.
+//
+// Every G_t is a sum of integer products below 2^16, accumulated in FP32 in tensor memory; it is
+// read out every 256 sites of K, while the partial sums are still exact or within a few units of
+// 2^-8t, and added in FP64.  The slices beyond t = 8 and the residual of the 7-slice truncation are
+// below 2^-56 of the row and column maxima, so P carries FP64-level error.  The squares, the omega
+// weights and the sum over the tile's 128 rows are fused into the epilogue; a block's column sums
+// go to its row of partial sums, which the linenergies finish kernel adds in a fixed order.
+//
+// One CTA: 128 rows (64 chains) x 64 modes; 4 warps.  Thread 0 drives a two-stage TMA pipeline
+// (64-byte swizzle, 32 sites of K per stage: 7 A tiles of 128 x 32 and 7 B tiles of 64 x 32) and
+// issues 56 tcgen05.mma (M = 128, N = 64, K = 16, BF16 in, FP32 in TMEM) per stage into the seven
+// G_t accumulators (7 x 64 TMEM columns).  Every wait is bounded: on a timeout the block records a
+// status, writes NaN into its partial row (the host then sees a non-finite entropy) and returns
+// after freeing its tensor memory.
+#include <cuda.h>
+#include <cuda_bf16.h>
+
+#include "nlc_device.cuh"
+
+namespace nlc {
+
+namespace {
+
+constexpr int kSlices = 7;
+constexpr int kBM = 128, kBN = 64, kBK = 32;
+constexpr int kChunkK = 256;   // sites of K between two read-outs of the accumulators
+constexpr uint32_t kTmemCols = 512;
+constexpr uint32_t kStageA = kSlices * kBM * kBK * 2, kStageB = kSlices * kBN * kBK * 2;
+constexpr uint32_t kStageBytes = kStageA + kStageB;
+constexpr long long kWaitTries = 1ll << 24;
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t) __cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+	for (long long i = 0; i < kWaitTries; i++) {
+		uint32_t ok;
+		asm volatile("{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
+		             : "=r"(ok) : "r"(bar), "r"(parity) : "memory");
+		if (ok) return true;
+	}
+	return false;
+}
+
+// Shared-memory matrix descriptor of a K-major tile written by TMA with the 64-byte swizzle:
+// 8-row atoms of 512 bytes (stride byte offset), descriptor version 1, layout type 4.
+__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr) {
+	return (uint64_t) ((saddr & 0x3FFFF) >> 4) | ((uint64_t) 1 << 16) | ((uint64_t) (512 >> 4) << 32) |
+	       ((uint64_t) 1 << 46) | ((uint64_t) 4 << 61);
+}
+
+// Instruction descriptor of kind::f16: FP32 accumulator, BF16 A and B, both K-major, N = 64, M = 128.
+constexpr uint32_t kIdesc =
+    (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t) (kBN >> 3) << 17) | ((uint32_t) (kBM >> 4) << 24);
+
+__device__ __forceinline__ void tma_load(uint32_t dst, const CUtensorMap *map, int x, int y, uint32_t bar) {
+	asm volatile("cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
+	             ::"r"(dst), "l"((uint64_t) map), "r"(x), "r"(y), "r"(bar) : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
+	uint32_t r[16];
+	asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+	             : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+	               "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+	             : "r"(taddr));
+	asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+	for (int j = 0; j < 16; j++) v[j] = __uint_as_float(r[j]);
+}
+
+}  // namespace
+
+// Row split of X: one warp per row r < 2C (chain r / 2, component r % 2): the row exponent e_r
+// (max |x| = m 2^e_r, 0.5 <= m < 1) and the 7 slices of x 2^-e_r, into slices[i][r][s].
+__global__ void tc_split_rows_kernel(const double2 *__restrict__ state, TcArgs a) {
+	const unsigned long long r = (unsigned long long) blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+	const int lane = threadIdx.x & 31;
+	if (r >= 2ull * a.copies) return;
+	const uint32_t n = a.n;
+	const double *row = reinterpret_cast<const double *>(state + (r >> 1) * n) + (r & 1);
+	double mx = 0.;
+	for (uint32_t s = lane; s < n; s += 32) mx = fmax(mx, fabs(row[2 * (size_t) s]));
+#pragma unroll
+	for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+	int e = 0;
+	if (mx > 0.) frexp(mx, &e);
+	if (lane == 0) a.row_exp[r] = e;
+	for (uint32_t s = lane; s < n; s += 32) {
+		double v = ldexp(row[2 * (size_t) s], 8 - e);   // x 2^-e 2^8, |v| < 256
+#pragma unroll
+		for (int i = 0; i < kSlices; i++) {
+			const double sg = rint(v);
+			a.a_slices[((size_t) i * a.mp + r) * a.kp + s] = __bfloat16_as_ushort(__double2bfloat16(sg));
+			v = (v - sg) * 256.;   // exact: |v - sg| <= 1/2
+		}
+	}
+}
+
+__global__ void __launch_bounds__(128, 1)
+tc_projection_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b, const TcArgs a) {
+	extern __shared__ __align__(1024) unsigned char smem_raw[];
+	unsigned char *smem = (unsigned char *) (((uintptr_t) smem_raw + 1023) & ~(uintptr_t) 1023);
+	__shared__ __align__(8) unsigned long long bars[5];   // full[2], empty[2], acc
+	__shared__ uint32_t tmem_slot;
+	__shared__ int s_fail;
+	const int tid = threadIdx.x, warp = tid >> 5;
+	const int row0 = blockIdx.x * kBM, col0 = blockIdx.y * kBN;
+	const uint32_t full0 = smem_u32(&bars[0]), empty0 = smem_u32(&bars[2]), accb = smem_u32(&bars[4]);
+	if (tid == 0) {
+		for (int i = 0; i < 5; i++) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&bars[i])));
+		asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+		s_fail = 0;
+	}
+	if (warp == 0) {
+		asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_slot)),
+		             "r"(kTmemCols));
+		asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+	}
+	asm volatile("tcgen05.fence::before_thread_sync;");
+	__syncthreads();
+	asm volatile("tcgen05.fence::after_thread_sync;");
+	const uint32_t tmem = tmem_slot;
+
+	const int nk = a.kp / kBK;   // stages of K
+	const int per_chunk = kChunkK / kBK;
+	auto stage_ptr = [&](int s) { return smem + (size_t) s * kStageBytes; };
+	auto load_stage = [&](int it, int s) {
+		const uint32_t full = full0 + 8 * s;
+		asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(full), "r"(kStageBytes) : "memory");
+		unsigned char *base = stage_ptr(s);
+		for (int i = 0; i < kSlices; i++) {
+			tma_load(smem_u32(base + (size_t) i * kBM * kBK * 2), &map_a, it * kBK, i * a.mp + row0, full);
+			tma_load(smem_u32(base + kStageA + (size_t) i * kBN * kBK * 2), &map_b, it * kBK, i * a.np + col0, full);
+		}
+	};
+
+	double acc[kBN];
+#pragma unroll
+	for (int c = 0; c < kBN; c++) acc[c] = 0.;
+	const uint32_t lane_base = (uint32_t) (warp * 32) << 16;
+	int chunks = 0;
+	for (int c0 = 0; c0 < nk; c0 += per_chunk, chunks++) {
+		const int c1 = min(nk, c0 + per_chunk);
+		if (tid == 0 && !s_fail) {
+			bool ok = true;
+			if (c0 == 0) {
+				load_stage(0, 0);
+				if (nk > 1) load_stage(1, 1);
+			}
+			for (int it = c0; it < c1 && ok; it++) {
+				const int s = it & 1;
+				const uint32_t ph = (it >> 1) & 1;
+				if (!mbar_wait(full0 + 8 * s, ph)) {
+					ok = false;
+					break;
+				}
+				asm volatile("tcgen05.fence::after_thread_sync;");
+				const uint32_t sa = smem_u32(stage_ptr(s)), sb = sa + kStageA;
+#pragma unroll 1
+				for (int t = 2; t <= kSlices + 1; t++) {
+					const uint32_t d = tmem + (uint32_t) (t - 2) * kBN;
+					const int ilo = t - kSlices > 1 ? t - kSlices : 1, ihi = t - 1 < kSlices ? t - 1 : kSlices;
+					for (int i = ilo; i <= ihi; i++) {
+						const int j = t - i;
+						for (int kk = 0; kk < kBK / 16; kk++) {
+							const uint64_t ad = smem_desc(sa + (uint32_t) (i - 1) * kBM * kBK * 2 + kk * 32);
+							const uint64_t bd = smem_desc(sb + (uint32_t) (j - 1) * kBN * kBK * 2 + kk * 32);
+							const uint32_t accum = (it == c0 && i == ilo && kk == 0) ? 0u : 1u;
+							asm volatile(
+							    "{ .reg .pred p; setp.ne.b32 p, %4, 0; tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p; }"
+							    ::"r"(d), "l"(ad), "l"(bd), "r"(kIdesc), "r"(accum));
+						}
+					}
+				}
+				asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(empty0 + 8 * s)
+				             : "memory");
+				if (it + 2 < nk) {
+					// the stage is free once its MMAs are done; then prefetch two stages ahead
+					if (!mbar_wait(empty0 + 8 * s, ph)) {
+						ok = false;
+						break;
+					}
+					load_stage(it + 2, s);
+				}
+			}
+			if (ok)
+				asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(accb)
+				             : "memory");
+			else
+				s_fail = 1;
+		}
+		// every thread: wait for the chunk's MMAs, then add its groups into the FP64 row sums
+		if (!s_fail && !mbar_wait(accb, chunks & 1)) s_fail = 1;
+		__syncthreads();
+		if (s_fail) break;
+		asm volatile("tcgen05.fence::after_thread_sync;");
+#pragma unroll
+		for (int seg = 0; seg < kBN / 16; seg++) {
+			double scale = 1. / 65536.;   // 2^-8t, exact
+#pragma unroll 1
+			for (int t = 2; t <= kSlices + 1; t++, scale *= 1. / 256.) {
+				float v[16];
+				tmem_ld16(tmem + lane_base + (uint32_t) (t - 2) * kBN + seg * 16, v);
+#pragma unroll
+				for (int j = 0; j < 16; j++) acc[seg * 16 + j] = fma((double) v[j], scale, acc[seg * 16 + j]);
+			}
+		}
+		asm volatile("tcgen05.fence::before_thread_sync;");
+		__syncthreads();
+	}
+
+	// epilogue: this thread's row r of P, squared and weighted, summed over the tile's rows
+	double *red = reinterpret_cast<double *>(smem);   // [128][64], over the (finished) stages
+	const int r = row0 + tid;
+	const bool phi = (r & 1) == 0;
+	const int er = r < 2 * (int) a.copies ? a.row_exp[r] : 0;
+	if (!s_fail) {
+#pragma unroll
+		for (int c = 0; c < kBN; c++) {
+			const int k = col0 + c;
+			double p = 0., w = 1.;
+			if (k < (int) a.n) {
+				p = ldexp(acc[c], er + a.col_exp[k]);
+				if (phi) w = a.omega[k] * a.omega[k];
+			}
+			red[tid * kBN + c] = w * p * p;
+		}
+	}
+	__syncthreads();
+	if (tid < kBN) {
+		const int k = col0 + tid;
+		if (k < (int) a.n) {
+			double s = 0.;
+			for (int rr = 0; rr < kBM; rr++) s += red[rr * kBN + tid];
+			a.partials[(size_t) blockIdx.x * a.n + k] = s_fail ? __longlong_as_double(0x7ff8000000000000ll) : s;
+		}
+	}
+	if (tid == 0 && s_fail) atomicOr(a.status, 1);
+	asm volatile("tcgen05.fence::before_thread_sync;");
+	__syncthreads();
+	if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols));
+}
+
+size_t tc_projection_smem() { return 2 * (size_t) kStageBytes + 1024; }
+
+cudaError_t launch_tc_projection(const TcArgs &a, const void *map_a, const void *map_b, const double2 *state,
+                                 cudaStream_t stream) {
+	count_launch(2);
+	const unsigned long long rows = 2ull * a.copies;
+	tc_split_rows_kernel<<<(unsigned) ((rows + 7) / 8), 256, 0, stream>>>(state, a);
+	cudaError_t e = cudaGetLastError();
+	if (e != cudaSuccess) return e;
+	const dim3 grid(a.mp / kBM, a.np / kBN);
+	tc_projection_kernel<<<grid, 128, tc_projection_smem(), stream>>>(*static_cast<const CUtensorMap *>(map_a),
+	                                                                  *static_cast<const CUtensorMap *>(map_b), a);
+	return cudaGetLastError();
+}
+
+const void *tc_projection_kernel_ptr() { return (const void *) tc_projection_kernel; }
+
+}  // namespace nlc

@@ -1,0 +1,61 @@
+"""dDNKG mode projection on the tensor cores (tcgen05, 7-slice BF16 split with FP32 accumulation
+and FP64 recombination) against the FP64 CUDA-core projection and a LAPACK-based reference."""
+import numpy as np
+import pytest
+
+from nlchains_gb300 import ic
+
+pytestmark = pytest.mark.gpu
+
+
+def lin_of(nlc, n, copies, state, masses, flags):
+    ctx = nlc.Context(0)
+    job = ctx.job(nlc.Model("dDNKG", n, copies, 0.05, beta=1.0, masses=masses, flags=flags), 10)
+    job.upload(state)
+    lin, wt, inf = job.linenergies()
+    lin2, wt2, inf2 = job.linenergies()
+    job.close()
+    ctx.close()
+    assert np.array_equal(lin, lin2) and wt == wt2, "not deterministic"
+    return lin, wt, inf
+
+
+# 300 and 700 sites: K in two and three read-out chunks; 4096 copies: 64 row tiles
+@pytest.mark.parametrize("n,copies", [(16, 19), (100, 64), (256, 4096), (300, 33), (700, 11)])
+def test_tensor_projection_matches_fp64(gpu, n, copies):
+    masses = ic.masses_uniform(n, seed=n)
+    state = np.random.default_rng(n + copies).standard_normal((copies, n, 2))
+    l64, w64, i64 = lin_of(gpu, n, copies, state, masses, 0)
+    ltc, wtc, itc = lin_of(gpu, n, copies, state, masses, gpu.FLAG_TENSOR_PROJECTION)
+    assert np.abs(ltc - l64).max() <= 1e-13 * np.abs(l64).max()
+    assert abs(wtc - w64) <= 1e-12 * max(1.0, abs(w64)) and abs(itc - i64) <= 1e-12 * max(1.0, abs(i64))
+
+
+def test_tensor_projection_against_lapack(gpu):
+    n, copies = 256, 512
+    masses = ic.masses_uniform(n, seed=7)
+    state = np.random.default_rng(8).standard_normal((copies, n, 2))
+    lin, _, _ = lin_of(gpu, n, copies, state, masses, gpu.FLAG_TENSOR_PROJECTION)
+    h = np.diag(masses + 2.0)
+    idx = np.arange(n)
+    h[idx, (idx + 1) % n] = -1.0
+    h[(idx + 1) % n, idx] = -1.0
+    w, v = np.linalg.eigh(h)
+    exp = 0.5 / copies * ((state[:, :, 0] @ v * np.sqrt(w)) ** 2 + (state[:, :, 1] @ v) ** 2).sum(0)
+    # eigenvectors of two backward-stable solvers agree to ~ eps |H| / gap on closely spaced modes
+    gap = np.minimum(np.abs(np.diff(w, prepend=-np.inf)), np.abs(np.diff(w, append=np.inf)))
+    tol = (1e-11 + 4 * np.finfo(float).eps * np.abs(w).max() / gap) * np.abs(exp).max()
+    assert (np.abs(lin - exp) <= tol).all()
+
+
+def test_tensor_projection_wide_dynamic_range(gpu):
+    # chains whose amplitudes span twelve orders of magnitude, and an all-zero chain: the per-row
+    # power-of-two scaling keeps the small ones, the zero chain contributes nothing
+    n, copies = 64, 40
+    masses = ic.masses_uniform(n, seed=9)
+    rng = np.random.default_rng(10)
+    state = rng.standard_normal((copies, n, 2)) * 10.0 ** rng.uniform(-6, 6, (copies, 1, 1))
+    state[3] = 0.0
+    l64, _, _ = lin_of(gpu, n, copies, state, masses, 0)
+    ltc, _, _ = lin_of(gpu, n, copies, state, masses, gpu.FLAG_TENSOR_PROJECTION)
+    assert np.abs(ltc - l64).max() <= 1e-13 * np.abs(l64).max()
