@@ -62,9 +62,10 @@ enum {
 	NLC_FLAG_COMPACT_DIAG = 8,    /* fewer partial rows in the diagnostics (less device memory per plan) */
 	NLC_FLAG_SHARED_GPU = 16,     /* one work unit per block instead of a persistent grid: blocks retire as
 	                                 they finish, so launches on other streams interleave with this plan's */
-	NLC_FLAG_TENSOR_PROJECTION = 32 /* dDNKG: the mode projection on the tensor cores (7-slice BF16 split,
-	                                   FP32 accumulation, FP64 recombination: FP64-level error) instead
-	                                   of FP64 CUDA cores */
+	NLC_FLAG_TENSOR_PROJECTION = 32, /* dDNKG: the mode projection on the tensor cores (7-slice BF16
+	                                    split, FP32 accumulation, FP64 recombination: FP64-level error);
+	                                    chosen by default from 128 sites */
+	NLC_FLAG_FP64_PROJECTION = 64    /* dDNKG: the mode projection on the FP64 CUDA cores at any length */
 };
 
 /*

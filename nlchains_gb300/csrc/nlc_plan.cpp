@@ -476,7 +476,10 @@ int setup_diagnostics(nlc_plan &P) {
 		const unsigned long long tiles = (P.m.copies + 7) / 8;
 		P.diag_blocks = int(std::min<unsigned long long>(tiles, 2ull * sms));
 		P.diag_rows = P.diag_blocks;
-		if (P.m.flags & NLC_FLAG_TENSOR_PROJECTION) {
+		// the tensor-core projection is faster from ~128 sites on (3x at 256, 6x at 1024 sites on GB300)
+		const bool tensor = (P.m.flags & NLC_FLAG_TENSOR_PROJECTION) ||
+		                    (n >= 128 && !(P.m.flags & NLC_FLAG_FP64_PROJECTION));
+		if (tensor) {
 			if ((rc = setup_tc_projection(P, d_om))) return rc;   // its own partial rows: one per 64 chains
 			P.diag_smem = 0;
 		}

@@ -41,6 +41,7 @@ constexpr uint32_t kTmemCols = 512;
 constexpr uint32_t kStageA = kSlices * kBM * kBK * 2, kStageB = kSlices * kBN * kBK * 2;
 constexpr uint32_t kStageBytes = kStageA + kStageB;
 constexpr long long kWaitTries = 1ll << 24;
+constexpr int kNonFiniteRow = 0x7fff;   // row exponent of a row holding inf or NaN
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t) __cvta_generic_to_shared(p); }
 
@@ -83,28 +84,74 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
 
 }  // namespace
 
-// Row split of X: one warp per row r < 2C (chain r / 2, component r % 2): the row exponent e_r
-// (max |x| = m 2^e_r, 0.5 <= m < 1) and the 7 slices of x 2^-e_r, into slices[i][r][s].
-__global__ void tc_split_rows_kernel(const double2 *__restrict__ state, TcArgs a) {
-	const unsigned long long r = (unsigned long long) blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
-	const int lane = threadIdx.x & 31;
-	if (r >= 2ull * a.copies) return;
-	const uint32_t n = a.n;
-	const double *row = reinterpret_cast<const double *>(state + (r >> 1) * n) + (r & 1);
-	double mx = 0.;
-	for (uint32_t s = lane; s < n; s += 32) mx = fmax(mx, fabs(row[2 * (size_t) s]));
+// 7 balanced base-256 digits of x 2^(56 - e) (e: the row exponent, |x| < 2^e), in integer
+// arithmetic on the FP64 bit pattern: F = round(x 2^(56 - e)) is a 57-bit signed integer, and
+// F = sum_i sigma_i 2^(8 (7 - i)) with sigma_1 = round(F / 2^48), sigma_2 = round((F - sigma_1 2^48)
+// / 2^40), ...: |sigma_1| <= 256, the others |sigma_i| <= 128, all exact in BF16.  The slices of
+// x 2^-e are sigma_i 2^(-8i): the value to 2^-48 of the row maximum, as the tensor product needs.
+__device__ __forceinline__ void split7(double x, int e, uint16_t (&out)[7]) {
+	const long long bits = __double_as_longlong(x);
+	const int ex = int((bits >> 52) & 0x7ff);
+	long long m = bits & ((1ll << 52) - 1);
+	int E;
+	if (ex) m |= 1ll << 52, E = ex - 1075;
+	else E = -1074;
+	const int shift = E + 56 - e;   // x 2^(56 - e) = m 2^shift, below 2^56 in magnitude
+	long long F;
+	if (shift >= 0) F = m << shift;
+	else if (shift > -63) F = (m + (1ll << (-shift - 1))) >> (-shift);
+	else F = 0;
+	if (bits < 0) F = -F;
 #pragma unroll
-	for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-	int e = 0;
-	if (mx > 0.) frexp(mx, &e);
-	if (lane == 0) a.row_exp[r] = e;
+	for (int i = 0; i < 7; i++) {
+		const int pos = 8 * (6 - i);
+		const long long sg = pos ? (F + (1ll << (pos - 1))) >> pos : F;
+		F -= sg << pos;
+		out[i] = uint16_t(__float_as_uint(float(sg)) >> 16);   // |sg| <= 256: exact in BF16
+	}
+}
+
+// Split of X: one warp per chain c (rows 2c = phi, 2c + 1 = pi): the row exponents e_r (max |x| =
+// m 2^e_r, 0.5 <= m < 1, from the largest magnitude's bit pattern) and the 7 slices of each row,
+// into slices[i][r][s].  Integer arithmetic only (GB300 issues it ~30x faster than FP64), coalesced
+// double2 reads of the state.  A row holding inf or NaN gets the exponent kNonFiniteRow, which the
+// projection turns into NaN energies: a blown-up chain is reported, not hidden.
+__global__ void tc_split_rows_kernel(const double2 *__restrict__ state, TcArgs a) {
+	const unsigned long long c = (unsigned long long) blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+	const int lane = threadIdx.x & 31;
+	if (c >= a.copies) return;
+	const uint32_t n = a.n;
+	const double2 *chain = state + c * n;
+	unsigned long long mphi = 0, mpi = 0;   // |x| bit patterns: ordered like the magnitudes
 	for (uint32_t s = lane; s < n; s += 32) {
-		double v = ldexp(row[2 * (size_t) s], 8 - e);   // x 2^-e 2^8, |v| < 256
+		const double2 v = chain[s];
+		mphi = max(mphi, (unsigned long long) __double_as_longlong(v.x) & 0x7fffffffffffffffull);
+		mpi = max(mpi, (unsigned long long) __double_as_longlong(v.y) & 0x7fffffffffffffffull);
+	}
+#pragma unroll
+	for (int o = 16; o > 0; o >>= 1) {
+		mphi = max(mphi, __shfl_xor_sync(0xffffffffu, mphi, o));
+		mpi = max(mpi, __shfl_xor_sync(0xffffffffu, mpi, o));
+	}
+	auto row_exp = [](unsigned long long mb) {
+		int e = 0;
+		if (mb >= 0x7ff0000000000000ull) e = kNonFiniteRow;   // inf or NaN
+		else if (mb >> 52) e = int(mb >> 52) - 1022;          // normal: (1.f) 2^(ex - 1023) = (0.1f) 2^(ex - 1022)
+		else if (mb) frexp(__longlong_as_double((long long) mb), &e);
+		return e;
+	};
+	const int ephi = row_exp(mphi), epi = row_exp(mpi);
+	const unsigned long long r = 2 * c;
+	if (lane == 0) a.row_exp[r] = ephi, a.row_exp[r + 1] = epi;
+	for (uint32_t s = lane; s < n; s += 32) {
+		const double2 v = chain[s];
+		uint16_t sp[7], sq[7];
+		split7(v.x, ephi, sp);
+		split7(v.y, epi, sq);
 #pragma unroll
 		for (int i = 0; i < kSlices; i++) {
-			const double sg = rint(v);
-			a.a_slices[((size_t) i * a.mp + r) * a.kp + s] = __bfloat16_as_ushort(__double2bfloat16(sg));
-			v = (v - sg) * 256.;   // exact: |v - sg| <= 1/2
+			a.a_slices[((size_t) i * a.mp + r) * a.kp + s] = sp[i];
+			a.a_slices[((size_t) i * a.mp + r + 1) * a.kp + s] = sq[i];
 		}
 	}
 }
@@ -233,7 +280,7 @@ tc_projection_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_con
 			const int k = col0 + c;
 			double p = 0., w = 1.;
 			if (k < (int) a.n) {
-				p = ldexp(acc[c], er + a.col_exp[k]);
+				p = er == kNonFiniteRow ? __longlong_as_double(0x7ff8000000000000ll) : ldexp(acc[c], er + a.col_exp[k]);
 				if (phi) w = a.omega[k] * a.omega[k];
 			}
 			red[tid * kBN + c] = w * p * p;
@@ -259,8 +306,7 @@ size_t tc_projection_smem() { return 2 * (size_t) kStageBytes + 1024; }
 cudaError_t launch_tc_projection(const TcArgs &a, const void *map_a, const void *map_b, const double2 *state,
                                  cudaStream_t stream) {
 	count_launch(2);
-	const unsigned long long rows = 2ull * a.copies;
-	tc_split_rows_kernel<<<(unsigned) ((rows + 7) / 8), 256, 0, stream>>>(state, a);
+	tc_split_rows_kernel<<<(unsigned) ((a.copies + 7) / 8), 256, 0, stream>>>(state, a);
 	cudaError_t e = cudaGetLastError();
 	if (e != cudaSuccess) return e;
 	const dim3 grid(a.mp / kBM, a.np / kBN);

@@ -1,5 +1,6 @@
 """dDNKG mode projection on the tensor cores (tcgen05, 7-slice BF16 split with FP32 accumulation
-and FP64 recombination) against the FP64 CUDA-core projection and a LAPACK-based reference."""
+and FP64 recombination; the default from 128 sites) against the FP64 CUDA-core projection and a
+LAPACK-based reference."""
 import numpy as np
 import pytest
 
@@ -25,7 +26,7 @@ def lin_of(nlc, n, copies, state, masses, flags):
 def test_tensor_projection_matches_fp64(gpu, n, copies):
     masses = ic.masses_uniform(n, seed=n)
     state = np.random.default_rng(n + copies).standard_normal((copies, n, 2))
-    l64, w64, i64 = lin_of(gpu, n, copies, state, masses, 0)
+    l64, w64, i64 = lin_of(gpu, n, copies, state, masses, gpu.FLAG_FP64_PROJECTION)
     ltc, wtc, itc = lin_of(gpu, n, copies, state, masses, gpu.FLAG_TENSOR_PROJECTION)
     assert np.abs(ltc - l64).max() <= 1e-13 * np.abs(l64).max()
     assert abs(wtc - w64) <= 1e-12 * max(1.0, abs(w64)) and abs(itc - i64) <= 1e-12 * max(1.0, abs(i64))
@@ -56,6 +57,23 @@ def test_tensor_projection_wide_dynamic_range(gpu):
     rng = np.random.default_rng(10)
     state = rng.standard_normal((copies, n, 2)) * 10.0 ** rng.uniform(-6, 6, (copies, 1, 1))
     state[3] = 0.0
-    l64, _, _ = lin_of(gpu, n, copies, state, masses, 0)
+    l64, _, _ = lin_of(gpu, n, copies, state, masses, gpu.FLAG_FP64_PROJECTION)
     ltc, _, _ = lin_of(gpu, n, copies, state, masses, gpu.FLAG_TENSOR_PROJECTION)
     assert np.abs(ltc - l64).max() <= 1e-13 * np.abs(l64).max()
+
+
+@pytest.mark.parametrize("bad", [np.nan, np.inf])
+def test_tensor_projection_reports_blowup(gpu, bad):
+    # a non-finite site (a blown-up chain) must surface as NLC_EBLOWUP, the reference's quit condition
+    n, copies = 256, 16
+    masses = ic.masses_uniform(n, seed=11)
+    state = np.random.default_rng(12).standard_normal((copies, n, 2))
+    state[5, 17, 1] = bad
+    ctx = gpu.Context(0)
+    job = ctx.job(gpu.Model("dDNKG", n, copies, 0.05, beta=1.0, masses=masses, flags=gpu.FLAG_TENSOR_PROJECTION), 10)
+    job.upload(state)
+    with pytest.raises(gpu.NlcError) as e:
+        job.linenergies()
+    assert e.value.code == gpu.EBLOWUP
+    job.close()
+    ctx.close()
