@@ -356,6 +356,38 @@ def cpu_baseline(w, target_s=10.0, threads=None, sample_copies=None, steps_per_c
                       f"({t:.1f} s), oracle reference-order port, OpenMP over copies"}
 
 
+def measure_projection(w, local):
+    """One diagnostics sample of the dDNKG workload with the mode projection on the FP64 CUDA cores
+    and on the tensor cores (the default), their times and their largest relative difference."""
+    import torch
+
+    import nlchains_gb300 as nlc
+    n, copies = w["n"], w["copies"]
+    dev = torch.from_numpy(initial_state(w, copies, 0)).cuda()
+    sp = torch.cuda.current_stream().cuda_stream
+    res = {}
+    for name, flag in (("fp64", nlc.FLAG_FP64_PROJECTION), ("tensor", nlc.FLAG_TENSOR_PROJECTION)):
+        plan = nlc.Plan(nlc.Model(w["model"], n, copies, w["dt"], masses=masses(w), flags=flag, **w["params"]))
+        lin = torch.zeros(n, dtype=torch.float64, device="cuda")
+        ent = torch.zeros(2, dtype=torch.float64, device="cuda")
+        for _ in range(3):
+            plan.linenergies(dev.data_ptr(), lin.data_ptr(), ent.data_ptr(), sp)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(20):
+            plan.linenergies(dev.data_ptr(), lin.data_ptr(), ent.data_ptr(), sp)
+        e1.record()
+        torch.cuda.synchronize()
+        res[name] = (e0.elapsed_time(e1) / 20, lin.cpu().numpy())
+        plan.close()
+    diff = float(np.abs(res["tensor"][1] - res["fp64"][1]).max() / np.abs(res["fp64"][1]).max())
+    return {"fp64_ms": res["fp64"][0], "tensor_ms": res["tensor"][0], "speedup": res["fp64"][0] / res["tensor"][0],
+            "max_rel_diff": diff, "flops": 4.0 * copies * n * n,
+            "method": "tcgen05 BF16 MMA, 7-slice split of X and of the eigenvectors, FP32 accumulation in TMEM, "
+                      "FP64 recombination, energy epilogue fused"}
+
+
 def read_traffic(kernel_key):
     """DRAM bytes per launch from the committed ncu summary (profiles/traffic.tsv), or None."""
     path = os.path.join(ROOT, "profiles", "traffic.tsv")
@@ -389,6 +421,8 @@ def run_engine(args):
                                "steps_per_launch": ow["batching"], "shape": o["shape"],
                                "fp64_frac_of_peak": FLOPS_PER_SITE_STEP[ow["model"]] * ow["n"] * ow["copies"] *
                                ow["batching"] / (o["move_ms"] * 1e-3) / 1e12 / peak}
+        if ow["model"] == "dDNKG" and rank == 0:
+            others["dDNKG"]["projection"] = measure_projection(ow, local)
     flops = FLOPS_PER_SITE_STEP[w["model"]] * w["n"] * w["copies"] * w["batching"]
     achieved = flops / (r["move_ms"] * 1e-3) / 1e12
     out = {
@@ -470,7 +504,7 @@ def run_reference(args):
 def run_profile_case(args):
     """Small cases of the headline kernels for ncu captures: 4 launches (10 steps; DNLS 2 steps),
     each followed by one diagnostics sample.  DNKG / Toda: 16384 of the 65536 copies (33.5 MB);
-    DNLS: the full 8192 copies of N = 1024 (134 MB, above the L2)."""
+    DNLS: the full 8192 copies of N = 1024 (134 MB, above the L2); dDNKG: the full 4096 x 256."""
     import torch
 
     import nlchains_gb300 as nlc
@@ -479,8 +513,11 @@ def run_profile_case(args):
         w = dict(TODA, copies=16384)
     if args.profile == "dnls":
         w, steps = dict(OTHERS[1]), 2
+    if args.profile == "ddnkg":   # the full dDNKG workload: 4096 chains of 256 sites, tensor-core projection
+        w = dict(OTHERS[2])
     state = initial_state(w, w["copies"], 0)
-    plan = nlc.Plan(nlc.Model(w["model"], w["n"], w["copies"], w["dt"], flags=nlc.FLAG_NO_TUNE, **w["params"]))
+    plan = nlc.Plan(nlc.Model(w["model"], w["n"], w["copies"], w["dt"], masses=masses(w), flags=nlc.FLAG_NO_TUNE,
+                              **w["params"]))
     dev = torch.from_numpy(state).cuda()
     lin = torch.zeros(w["n"], dtype=torch.float64, device="cuda")
     ent = torch.zeros(2, dtype=torch.float64, device="cuda")
@@ -499,7 +536,7 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["engine", "reference"], default="engine")
-    ap.add_argument("--profile", choices=["dnkg", "toda", "dnls"], default=None,
+    ap.add_argument("--profile", choices=["dnkg", "toda", "dnls", "ddnkg"], default=None,
                     help="run only a small case of the integrator + diagnostics (for ncu captures)")
     args = ap.parse_args()
     if args.profile:
