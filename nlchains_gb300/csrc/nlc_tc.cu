@@ -13,8 +13,8 @@
 //   BF16).  P = 2^(e_r + f_k) sum_{t = 2..8} 2^(-8t) G_t,  G_t = sum_{i + j = t} A_i B_j^T.
 //
 // Every G_t is a sum of integer products below 2^16, accumulated in FP32 in tensor memory; it is
-// read out every 256 sites of K, while the partial sums are still exact or within a few units of
-// 2^-8t, and added in FP64.  The slices beyond t = 8 and the residual of the 7-slice truncation are
+// read out every 128 sites of K, while the partial sums are still exact (below 2^24), and the
+// groups are combined exactly in integers and added in FP64.  The slices beyond t = 8 and the residual of the 7-slice truncation are
 // below 2^-56 of the row and column maxima, so P carries FP64-level error.  The squares, the omega
 // weights and the sum over the tile's 128 rows are fused into the epilogue; a block's column sums
 // go to its row of partial sums, which the linenergies finish kernel adds in a fixed order.
@@ -36,7 +36,10 @@ namespace {
 
 constexpr int kSlices = 7;
 constexpr int kBM = 128, kBN = 64, kBK = 32;
-constexpr int kChunkK = 256;   // sites of K between two read-outs of the accumulators
+// sites of K between two read-outs of the accumulators: 128 keeps every group sum G_t below 2^24
+// (G_2 <= 128 x 256 x 256; the later groups have more pairs of smaller digits), so the FP32
+// accumulation in tensor memory is exact
+constexpr int kChunkK = 128;
 constexpr uint32_t kTmemCols = 512;
 constexpr uint32_t kStageA = kSlices * kBM * kBK * 2, kStageB = kSlices * kBN * kBK * 2;
 constexpr uint32_t kStageBytes = kStageA + kStageB;
@@ -71,15 +74,19 @@ __device__ __forceinline__ void tma_load(uint32_t dst, const CUtensorMap *map, i
 	             ::"r"(dst), "l"((uint64_t) map), "r"(x), "r"(y), "r"(bar) : "memory");
 }
 
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
-	uint32_t r[16];
-	asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-	             : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-	               "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float (&v)[8]) {
+	uint32_t r[8];
+	asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+	             : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
 	             : "r"(taddr));
 	asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-	for (int j = 0; j < 16; j++) v[j] = __uint_as_float(r[j]);
+	for (int j = 0; j < 8; j++) v[j] = __uint_as_float(r[j]);
+}
+
+// 2^k for a normal-range k, built from its bit pattern (an exact scaling, no library call)
+__device__ __forceinline__ double pow2i(int k) {
+	return k >= -1022 && k <= 1023 ? __longlong_as_double((long long) (k + 1023) << 52) : ldexp(1., k);
 }
 
 }  // namespace
@@ -254,15 +261,30 @@ tc_projection_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_con
 		__syncthreads();
 		if (s_fail) break;
 		asm volatile("tcgen05.fence::after_thread_sync;");
+		// the exact integer group sums, folded with shifts into two int64 halves (hi: t = 2..4 in units
+		// of 2^-32, below 2^41; lo: t = 5..8 in units of 2^-64, below 2^49: both exact in FP64), then
+		// two FMAs per column into the FP64 row sums
 #pragma unroll
-		for (int seg = 0; seg < kBN / 16; seg++) {
-			double scale = 1. / 65536.;   // 2^-8t, exact
-#pragma unroll 1
-			for (int t = 2; t <= kSlices + 1; t++, scale *= 1. / 256.) {
-				float v[16];
-				tmem_ld16(tmem + lane_base + (uint32_t) (t - 2) * kBN + seg * 16, v);
+		for (int seg = 0; seg < kBN / 8; seg++) {
+			long long hi[8], lo[8];
 #pragma unroll
-				for (int j = 0; j < 16; j++) acc[seg * 16 + j] = fma((double) v[j], scale, acc[seg * 16 + j]);
+			for (int j = 0; j < 8; j++) hi[j] = 0, lo[j] = 0;
+#pragma unroll
+			for (int t = 2; t <= kSlices + 1; t++) {
+				float v[8];
+				tmem_ld8(tmem + lane_base + (uint32_t) (t - 2) * kBN + seg * 8, v);
+#pragma unroll
+				for (int j = 0; j < 8; j++) {
+					const long long g = __float2ll_rn(v[j]);
+					if (t <= 4) hi[j] += g << (8 * (4 - t));
+					else lo[j] += g << (8 * (8 - t));
+				}
+			}
+#pragma unroll
+			for (int j = 0; j < 8; j++) {
+				double &x = acc[seg * 8 + j];
+				x = fma((double) hi[j], 0x1p-32, x);
+				x = fma((double) lo[j], 0x1p-64, x);
 			}
 		}
 		asm volatile("tcgen05.fence::before_thread_sync;");
@@ -280,7 +302,7 @@ tc_projection_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_con
 			const int k = col0 + c;
 			double p = 0., w = 1.;
 			if (k < (int) a.n) {
-				p = er == kNonFiniteRow ? __longlong_as_double(0x7ff8000000000000ll) : ldexp(acc[c], er + a.col_exp[k]);
+				p = er == kNonFiniteRow ? __longlong_as_double(0x7ff8000000000000ll) : acc[c] * pow2i(er + a.col_exp[k]);
 				if (phi) w = a.omega[k] * a.omega[k];
 			}
 			red[tid * kBN + c] = w * p * p;
