@@ -201,6 +201,11 @@ int nlc_job_energies(nlc_ctx *ctx, uint64_t job, double *host_energies);
  * NULL (the slot must have been filled with copy_state).  The `nlchains` command line runs on these.
  */
 int nlc_job_sample_async(nlc_ctx *ctx, uint64_t job, int32_t slot, int32_t copy_state);
+/* nlc_job_advance(kernel_batching) followed by nlc_job_sample_async(slot, copy_state), replayed as
+ * one CUDA graph (captured on the first call for each slot / copy_state pair): one launch per batch
+ * instead of the batch's kernels, copies and event, for short batches whose host overhead would
+ * otherwise show.  Same results as the two calls. */
+int nlc_job_step_async(nlc_ctx *ctx, uint64_t job, int32_t slot, int32_t copy_state);
 int nlc_job_sample_wait(nlc_ctx *ctx, uint64_t job, int32_t slot, double *lin, double *wt, double *inf,
                         void *host_state, int32_t timeout_ms);
 /* wait for the job's queued work, at most timeout_ms (< 0: no limit); NLC_ETIMEDOUT if not done */

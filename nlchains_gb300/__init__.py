@@ -39,7 +39,7 @@ EXPORTS = (
     "nlc_version", "nlc_kernel_launches", "nlc_fp64_peak", "nlc_linenergies_noalloc",
     "nlc_server_create", "nlc_server_destroy", "nlc_server_submit", "nlc_server_poll", "nlc_server_wait",
     "nlc_server_result", "nlc_entropies", "nlc_job_sample_async", "nlc_job_sample_wait", "nlc_energies",
-    "nlc_job_energies",
+    "nlc_job_energies", "nlc_job_step_async",
 )
 
 
@@ -122,6 +122,7 @@ def lib():
         "nlc_job_sample_wait": ([vp, u64, i32, dp, dp, dp, vp, i32], i32),
         "nlc_energies": ([vp, vp, vp, vp], i32),
         "nlc_job_energies": ([vp, u64, dp], i32),
+        "nlc_job_step_async": ([vp, u64, i32, i32], i32),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -314,6 +315,10 @@ class Job:
     def sample_async(self, slot, copy_state=False):
         """Enqueue the diagnostics (and optionally a state copy) of the current state into slot 0/1."""
         _check(lib().nlc_job_sample_async(self.ctx._h, self.id, int(slot), int(bool(copy_state))))
+
+    def step_async(self, slot, copy_state=False):
+        """advance(kernel_batching) + sample_async(slot, copy_state) as one CUDA graph launch."""
+        _check(lib().nlc_job_step_async(self.ctx._h, self.id, int(slot), int(bool(copy_state))))
 
     def sample_wait(self, slot, with_state=False, timeout_ms=-1):
         """(linenergies, WT, INF, state or None) of a slot filled by sample_async; EBLOWUP raises."""

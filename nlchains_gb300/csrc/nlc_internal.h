@@ -185,6 +185,8 @@ cudaError_t launch_fp64_probe(double *out, int blocks, int threads, int iters, c
 
 // bookkeeping
 void count_launch(uint64_t k = 1);
+void uncount_launch(uint64_t k);   // launches recorded during a stream capture did not run
+uint64_t launch_count();
 
 // dDNKG projection on the tensor cores (nlc_tc.cu): 7 BF16 slices of X (rows 2c, 2c + 1 = phi_c,
 // pi_c of chain c) and of the eigenvector matrix E, each padded with zeros to mp / np rows (multiples

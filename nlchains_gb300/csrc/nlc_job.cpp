@@ -33,9 +33,15 @@ struct Job {
 	double2 *h_state_slot[2] = {nullptr, nullptr};
 	cudaEvent_t ev_slot[2] = {nullptr, nullptr};
 	bool slot_state[2] = {false, false};
+	// one batch + its sample as a CUDA graph, per [slot][copy_state], captured on first use
+	cudaGraphExec_t step_exec[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
+	uint64_t step_kernels[2][2] = {{0, 0}, {0, 0}};
 
 	~Job() {
 		if (stream) cudaStreamSynchronize(stream);
+		for (auto &row : step_exec)
+			for (cudaGraphExec_t g : row)
+				if (g) cudaGraphExecDestroy(g);
 		if (plan) nlc_plan_destroy(plan);
 		cudaFree(d_state);
 		cudaFree(d_diag);
@@ -172,10 +178,10 @@ extern "C" int nlc_job_energies(nlc_ctx *ctx, uint64_t id, double *host_energies
 	return rc ? rc : rs;
 }
 
-extern "C" int nlc_job_sample_async(nlc_ctx *ctx, uint64_t id, int32_t slot, int32_t copy_state) {
-	Job *J = find_job(ctx, id);
-	if (!J) return set_error(NLC_ENOTFOUND, "no such job");
-	if (slot < 0 || slot > 1) return set_error(NLC_EINVAL, "slot must be 0 or 1");
+namespace {
+
+// the result slot's buffers and event, allocated on first use
+int ensure_slot(Job *J, int slot, int copy_state) {
 	const size_t n = J->model.chain_length;
 	int rc;
 	if (!J->d_slot[slot]) {
@@ -187,18 +193,69 @@ extern "C" int nlc_job_sample_async(nlc_ctx *ctx, uint64_t id, int32_t slot, int
 	if (copy_state && !J->h_state_slot[slot] &&
 	    (rc = cuda_status(cudaMallocHost(&J->h_state_slot[slot], J->state_bytes), "cudaMallocHost")))
 		return rc;
+	return NLC_OK;
+}
+
+// diagnostics of the current state into the slot, the read-backs and the slot's event; `external`
+// records the event as an event node of a graph being captured
+int enqueue_sample(Job *J, int slot, int copy_state, bool external) {
+	const size_t n = J->model.chain_length;
+	int rc;
 	if ((rc = nlc_linenergies(J->plan, J->d_state, J->d_slot[slot], J->d_slot[slot] + n, J->stream))) return rc;
 	if ((rc = cuda_status(cudaMemcpyAsync(J->h_slot[slot], J->d_slot[slot], (n + 2) * sizeof(double),
 	                                      cudaMemcpyDeviceToHost, J->stream),
 	                      "diagnostics copy")))
 		return rc;
-	J->slot_state[slot] = copy_state != 0;
 	if (copy_state &&
 	    (rc = cuda_status(cudaMemcpyAsync(J->h_state_slot[slot], J->d_state, J->state_bytes, cudaMemcpyDeviceToHost,
 	                                      J->stream),
 	                      "state copy")))
 		return rc;
-	return cuda_status(cudaEventRecord(J->ev_slot[slot], J->stream), "cudaEventRecord");
+	return cuda_status(cudaEventRecordWithFlags(J->ev_slot[slot], J->stream, external ? cudaEventRecordExternal : 0),
+	                   "cudaEventRecord");
+}
+
+}  // namespace
+
+extern "C" int nlc_job_sample_async(nlc_ctx *ctx, uint64_t id, int32_t slot, int32_t copy_state) {
+	Job *J = find_job(ctx, id);
+	if (!J) return set_error(NLC_ENOTFOUND, "no such job");
+	if (slot < 0 || slot > 1) return set_error(NLC_EINVAL, "slot must be 0 or 1");
+	int rc = ensure_slot(J, slot, copy_state);
+	if (rc) return rc;
+	if ((rc = enqueue_sample(J, slot, copy_state, false))) return rc;
+	J->slot_state[slot] = copy_state != 0;
+	return NLC_OK;
+}
+
+extern "C" int nlc_job_step_async(nlc_ctx *ctx, uint64_t id, int32_t slot, int32_t copy_state) {
+	Job *J = find_job(ctx, id);
+	if (!J) return set_error(NLC_ENOTFOUND, "no such job");
+	if (slot < 0 || slot > 1) return set_error(NLC_EINVAL, "slot must be 0 or 1");
+	int rc = ensure_slot(J, slot, copy_state);
+	if (rc) return rc;
+	const int cs = copy_state ? 1 : 0;
+	if (!J->step_exec[slot][cs]) {
+		// capture the batch (its fused launches) and the sample once; the graph replays them with one
+		// launch per batch.  Nothing in them allocates or synchronises.
+		const uint64_t k0 = launch_count();
+		if ((rc = cuda_status(cudaStreamBeginCapture(J->stream, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture")))
+			return rc;
+		rc = nlc_move(J->plan, J->d_state, J->batching, J->stream);
+		if (!rc) rc = enqueue_sample(J, slot, copy_state, true);
+		cudaGraph_t g = nullptr;
+		const cudaError_t e = cudaStreamEndCapture(J->stream, &g);
+		const uint64_t kernels = launch_count() - k0;
+		uncount_launch(kernels);
+		if (!rc && e != cudaSuccess) rc = cuda_status(e, "cudaStreamEndCapture");
+		if (!rc) rc = cuda_status(cudaGraphInstantiate(&J->step_exec[slot][cs], g, 0), "cudaGraphInstantiate");
+		if (g) cudaGraphDestroy(g);
+		if (rc) return rc;
+		J->step_kernels[slot][cs] = kernels;
+	}
+	J->slot_state[slot] = copy_state != 0;
+	count_launch(J->step_kernels[slot][cs]);
+	return cuda_status(cudaGraphLaunch(J->step_exec[slot][cs], J->stream), "cudaGraphLaunch");
 }
 
 extern "C" int nlc_job_sample_wait(nlc_ctx *ctx, uint64_t id, int32_t slot, double *lin, double *wt, double *inf,
@@ -212,9 +269,11 @@ extern "C" int nlc_job_sample_wait(nlc_ctx *ctx, uint64_t id, int32_t slot, doub
 		const cudaError_t e = cudaEventQuery(J->ev_slot[slot]);
 		if (e == cudaSuccess) break;
 		if (e != cudaErrorNotReady) return cuda_status(e, "sample");
-		if (timeout_ms >= 0 && std::chrono::steady_clock::now() - t0 >= std::chrono::milliseconds(timeout_ms))
+		const auto waited = std::chrono::steady_clock::now() - t0;
+		if (timeout_ms >= 0 && waited >= std::chrono::milliseconds(timeout_ms))
 			return set_error(NLC_ETIMEDOUT, "sample not ready");
-		std::this_thread::sleep_for(std::chrono::microseconds(50));
+		// poll for the first half millisecond (short batches), then yield the core in short naps
+		if (waited >= std::chrono::microseconds(500)) std::this_thread::sleep_for(std::chrono::microseconds(20));
 	}
 	const size_t n = J->model.chain_length;
 	const double *h = J->h_slot[slot];
@@ -537,9 +596,9 @@ int run_program(int argc, char **argv) {
 		const bool last = (steps && t == steps) || quit;
 		in_flight = false;
 		if (!last) {
-			if ((rc = nlc_job_advance(ctx, job, batching))) throw CliError{2, nlc_last_error()};
+			// the next batch and its sample: one graph launch
 			const uint64_t tn = t + batching;
-			if ((rc = nlc_job_sample_async(ctx, job, slot ^ 1, tn % dump_interval == 0))) throw CliError{2, nlc_last_error()};
+			if ((rc = nlc_job_step_async(ctx, job, slot ^ 1, tn % dump_interval == 0))) throw CliError{2, nlc_last_error()};
 			in_flight = true;
 		}
 		double wt = 0, inf = 0;

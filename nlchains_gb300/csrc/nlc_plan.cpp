@@ -31,6 +31,8 @@ int cuda_status(cudaError_t e, const char *what) {
 }
 
 void count_launch(uint64_t k) { g_launches += k; }
+void uncount_launch(uint64_t k) { g_launches -= k; }
+uint64_t launch_count() { return g_launches.load(); }
 
 const void *real_kernel_dnkg(int variant, int sites, bool win);
 const void *real_kernel_fput(int variant, int sites, bool win);

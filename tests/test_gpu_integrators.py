@@ -166,3 +166,47 @@ def test_pipelined_sampling_equals_synchronous(gpu):
     sync.close()
     pipe.close()
     ctx.close()
+
+
+@pytest.mark.parametrize("name,n,params,window", [
+    ("FPUT", 64, dict(alpha=0.0, beta=1.0), None),
+    ("DNLS", 97, dict(beta=1.0), None),
+    ("dDNKG", 256, dict(beta=1.0), None),      # tensor-core projection inside the graph
+    ("DNKG", 600, dict(m=1.0, beta=1.0), 64),  # windowed tier: launches plus a device copy per batch
+])
+def test_graph_steps_equal_plain(gpu, name, n, params, window):
+    """nlc_job_step_async (one CUDA graph launch per batch and sample) gives the same samples and
+    states as nlc_job_advance + nlc_job_sample_async."""
+    copies, b, rounds = 24, 7, 5
+    masses = ic.masses_uniform(n, seed=4) if name == "dDNKG" else None
+    state = 0.3 * np.random.default_rng(n).standard_normal((copies, n, 2))
+    old = os.environ.get("NLC_FORCE_WINDOW")
+    if window:
+        os.environ["NLC_FORCE_WINDOW"] = str(window)
+    try:
+        ctx = gpu.Context(0)
+        runs = []
+        for graphs in (False, True):
+            job = ctx.job(gpu.Model(name, n, copies, 0.01, masses=masses, **params), b)
+            job.upload(state)
+            job.sample_async(0, copy_state=True)
+            got = []
+            for r in range(rounds):
+                if graphs:
+                    job.step_async((r + 1) % 2, copy_state=True)
+                else:
+                    job.advance(b)
+                    job.sample_async((r + 1) % 2, copy_state=True)
+                got.append(job.sample_wait(r % 2, with_state=True))
+            got.append(job.sample_wait(rounds % 2, with_state=True))
+            runs.append(got)
+            job.close()
+        ctx.close()
+    finally:
+        if window:
+            if old is None:
+                del os.environ["NLC_FORCE_WINDOW"]
+            else:
+                os.environ["NLC_FORCE_WINDOW"] = old
+    for (pl, pw, pi, ps), (gl, gw, gi, gs) in zip(*runs):
+        assert np.array_equal(pl, gl) and pw == gw and pi == gi and np.array_equal(ps, gs)
