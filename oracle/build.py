@@ -3,7 +3,9 @@
 Two shared objects are produced under oracle/_build/ from oracle/nlc_oracle.c:
 
 * ``libnlc_oracle.so``  -- the checker: -O2, no FP contraction, single thread;
-* ``libnlc_oracle_mt.so`` -- the timed CPU baseline: -O3, OpenMP over copies, no FP contraction.
+* ``libnlc_oracle_mt.so`` -- the timed CPU baseline: -Ofast with FMA contraction, as the reference
+  builds its CPU code (CMakeLists.txt:62), OpenMP over copies.  Timing only: its arithmetic is not
+  the checker's.
 
 Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use these libraries.
 """
@@ -17,7 +19,7 @@ SRC = os.path.join(HERE, "nlc_oracle.c")
 
 VARIANTS = {
     "libnlc_oracle.so": ["-O2"],
-    "libnlc_oracle_mt.so": ["-O3", "-fopenmp"],
+    "libnlc_oracle_mt.so": ["-Ofast", "-ffp-contract=fast", "-fopenmp"],
 }
 
 
@@ -36,7 +38,8 @@ def build(verbose=False):
         target = os.path.join(OUT, name)
         if not _stale(target, deps):
             continue
-        # -ffp-contract=off: gcc on aarch64 would otherwise fuse a*b+c, changing the rounding
+        # the checker: -ffp-contract=off (gcc on aarch64 would otherwise fuse a*b+c, changing the
+        # rounding); the baseline's own flags come after and override it
         cmd = ["gcc", "-std=c11", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math",
                *flags, "-o", target + ".tmp", SRC, "-lm"]
         if verbose:
