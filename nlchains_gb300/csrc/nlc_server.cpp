@@ -1,18 +1,24 @@
 // Request server: continuous batching of ensemble-integration requests on one GPU.
 //
 // Requests move queue -> admitted (by HBM budget) -> prepared -> running -> finished:
-//   * a preparer thread builds each admitted request's plan (canonical launch shape; for dDNKG the
-//     host eigensolve), allocates and uploads its state and takes the t = 0 diagnostics sample;
+//   * four preparer threads build each admitted request's plan (canonical launch shape, one block
+//     per work unit; for dDNKG the host eigensolve) and allocate and upload its state, each on its own
+//     high-priority stream; the t = 0 samples of newly prepared requests then go out as one group;
 //   * the scheduler thread groups idle prepared requests by kernel class (model, parameters, dt,
-//     launch shape) and launches each group on a free stream slot: one persistent batched launch of
-//     the resident integrator advancing every member by its own kernel_batching steps (DNLS
-//     requests run their own fused launch), then one diagnostics sample per member, then an event;
+//     launch shape) and launches each group on a free stream slot: one batched launch of the
+//     resident integrator advancing every member by its next segment (DNLS and windowed requests run
+//     their own launches), then the diagnostics sample of every member whose round the segment
+//     closes, then an event;
+//   * a round of kernel_batching steps is cut into open segments so that no block lives much longer
+//     than the quantum (3 ms): newly arrived work finds free SMs quickly (NLC_SEG_* flags: the
+//     segments together run exactly the operations of one launch);
 //   * completed events return their requests to idle (entropies appended, blow-ups flagged);
 //     requests with all steps done are retired (final state and energies copied out, device memory
-//     released), which lets queued requests in.
+//     returned on a stream with no queued work), which lets queued requests in.
 // There is no round barrier: fast groups keep cycling while slow ones run.  A request's chains see
 // exactly the arithmetic of a launch of their own (the batched kernel only changes which block
-// integrates which chain), so results are identical alone and in the mix.
+// integrates which chain, segments only where a launch ends), so results are identical alone and
+// in the mix.
 #include <algorithm>
 #include <chrono>
 #include <cmath>
