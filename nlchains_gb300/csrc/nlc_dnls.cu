@@ -9,9 +9,11 @@
 //   psi <- psi exp(-i beta dt c_k |psi|^2)       (DNLS.cu:11-17; c_0 doubled when merged, DNLS.cpp:162)
 //   psi_k <- FFT(psi) * exp(-i dt d_k omega_k)/n  (DNLS/dispersion.cpp:19-26, DNLS.cu:19-25)
 //   psi <- IFFT(psi_k)
-// (for a length with a prime factor above 7 the last two lines are one zero-padded cyclic
-// convolution of smooth length len >= 2n - 1: the propagator is circulant, nlc_host.h), and finally psi <- psi exp(-i beta dt c_7 |psi|^2) (DNLS.cpp:175).  The FFTs are the Stockham
-// shared-memory transforms of nlc_fft.cuh; state is read once and written once per launch.
+// (for a length whose direct passes cost more, i.e. with large prime factors, the last two lines
+// are one zero-padded cyclic convolution of smooth length len >= 2n - 1: the propagator is
+// circulant, nlc_host.h), and finally psi <- psi exp(-i beta dt c_7 |psi|^2) (DNLS.cpp:175).  The
+// FFTs are the Stockham transforms of nlc_fft.cuh, in shared memory (beyond it, in per-block global
+// scratch); the state is read once and written once per launch.
 #include "nlc_fft.cuh"
 
 namespace nlc {

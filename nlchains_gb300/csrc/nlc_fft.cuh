@@ -170,7 +170,8 @@ __device__ double2 *stockham_team(const FftPlanDev &P, double2 *x, double2 *y, i
 __device__ __forceinline__ double2 conj2(double2 a) { return make_double2(a.x, -a.y); }
 
 // Transform of one chain of length P.n held in x[0, n); x and y hold P.len elements each.
-// Lengths with a prime factor above 7 go through Bluestein's chirp-z identity
+// Lengths whose padded form costs fewer operations (large prime factors; the plan decides) go
+// through Bluestein's chirp-z identity
 //   X_k = w_k sum_j (x_j w_j) conj(w)_{k-j},  w_j = exp(-i pi j^2 / n)
 // (L. Bluestein, IEEE Trans. Audio Electroacoust. 18, 1970), the convolution evaluated as a cyclic
 // convolution of smooth length m >= 2n - 1 by two Stockham passes; the backward transform uses the

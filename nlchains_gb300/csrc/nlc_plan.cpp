@@ -642,7 +642,8 @@ extern "C" int nlc_plan_create(const nlc_model *model, nlc_plan **out) {
 			d.sctab = d_sct;
 		}
 		if (d.fft.bluestein) {
-			// lengths with a prime factor above 7: each linear sub-step as one zero-padded cyclic
+			// lengths whose padded form is cheaper (large prime factors): each linear sub-step as one
+			// zero-padded cyclic
 			// convolution of the smooth length len (two passes) instead of two Bluestein transforms
 			// (four passes and three chirp products)
 			const uint32_t m = uint32_t(d.fft.len);
