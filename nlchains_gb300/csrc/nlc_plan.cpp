@@ -643,9 +643,8 @@ extern "C" int nlc_plan_create(const nlc_model *model, nlc_plan **out) {
 		}
 		if (d.fft.bluestein) {
 			// lengths whose padded form is cheaper (large prime factors): each linear sub-step as one
-			// zero-padded cyclic
-			// convolution of the smooth length len (two passes) instead of two Bluestein transforms
-			// (four passes and three chirp products)
+			// zero-padded cyclic convolution of the smooth length len (two passes) instead of two
+			// Bluestein transforms (four passes and three chirp products)
 			const uint32_t m = uint32_t(d.fft.len);
 			const std::vector<double> conv = dnls_conv_tables(tab, n, m);
 			double2 *d_conv = nullptr;
