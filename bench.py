@@ -357,8 +357,9 @@ def cpu_baseline(w, target_s=10.0, threads=None, sample_copies=None, steps_per_c
 
 
 def measure_projection(w, local):
-    """One diagnostics sample of the dDNKG workload with the mode projection on the FP64 CUDA cores
-    and on the tensor cores (the default), their times and their largest relative difference."""
+    """One diagnostics sample of the dDNKG workload with the mode projection on the FP64 CUDA cores,
+    on the tensor cores (7 slices, the default) and as BF16x3 (3 slices): times and largest relative
+    difference of the mode energies against the FP64 projection."""
     import torch
 
     import nlchains_gb300 as nlc
@@ -366,7 +367,8 @@ def measure_projection(w, local):
     dev = torch.from_numpy(initial_state(w, copies, 0)).cuda()
     sp = torch.cuda.current_stream().cuda_stream
     res = {}
-    for name, flag in (("fp64", nlc.FLAG_FP64_PROJECTION), ("tensor", nlc.FLAG_TENSOR_PROJECTION)):
+    for name, flag in (("fp64", nlc.FLAG_FP64_PROJECTION), ("tensor", nlc.FLAG_TENSOR_PROJECTION),
+                       ("bf16x3", nlc.FLAG_BF16X3_PROJECTION)):
         plan = nlc.Plan(nlc.Model(w["model"], n, copies, w["dt"], masses=masses(w), flags=flag, **w["params"]))
         lin = torch.zeros(n, dtype=torch.float64, device="cuda")
         ent = torch.zeros(2, dtype=torch.float64, device="cuda")
@@ -381,9 +383,12 @@ def measure_projection(w, local):
         torch.cuda.synchronize()
         res[name] = (e0.elapsed_time(e1) / 20, lin.cpu().numpy())
         plan.close()
-    diff = float(np.abs(res["tensor"][1] - res["fp64"][1]).max() / np.abs(res["fp64"][1]).max())
+    ref = res["fp64"][1]
+    diff = float(np.abs(res["tensor"][1] - ref).max() / np.abs(ref).max())
+    diff3 = float(np.abs(res["bf16x3"][1] - ref).max() / np.abs(ref).max())
     return {"fp64_ms": res["fp64"][0], "tensor_ms": res["tensor"][0], "speedup": res["fp64"][0] / res["tensor"][0],
-            "max_rel_diff": diff, "flops": 4.0 * copies * n * n,
+            "max_rel_diff": diff, "bf16x3_ms": res["bf16x3"][0], "bf16x3_max_rel_diff": diff3,
+            "flops": 4.0 * copies * n * n,
             "method": "tcgen05 BF16 MMA, 7-slice split of X and of the eigenvectors, FP32 accumulation in TMEM, "
                       "FP64 recombination, energy epilogue fused"}
 

@@ -65,7 +65,9 @@ enum {
 	NLC_FLAG_TENSOR_PROJECTION = 32, /* dDNKG: the mode projection on the tensor cores (7-slice BF16
 	                                    split, FP32 accumulation, FP64 recombination: FP64-level error);
 	                                    chosen by default from 128 sites */
-	NLC_FLAG_FP64_PROJECTION = 64    /* dDNKG: the mode projection on the FP64 CUDA cores at any length */
+	NLC_FLAG_FP64_PROJECTION = 64,   /* dDNKG: the mode projection on the FP64 CUDA cores at any length */
+	NLC_FLAG_BF16X3_PROJECTION = 128 /* dDNKG: the tensor-core projection with 3 BF16 slices: faster, with
+	                                    mode energies to ~1e-7 relative instead of FP64 level */
 };
 
 /*

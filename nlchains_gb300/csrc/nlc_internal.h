@@ -188,12 +188,13 @@ void count_launch(uint64_t k = 1);
 void uncount_launch(uint64_t k);   // launches recorded during a stream capture did not run
 uint64_t launch_count();
 
-// dDNKG projection on the tensor cores (nlc_tc.cu): 7 BF16 slices of X (rows 2c, 2c + 1 = phi_c,
+// dDNKG projection on the tensor cores (nlc_tc.cu): 7 (or 3) BF16 slices of X (rows 2c, 2c + 1 = phi_c,
 // pi_c of chain c) and of the eigenvector matrix E, each padded with zeros to mp / np rows (multiples
 // of 128 / 64) and kp sites (a multiple of 32), slice i at rows [i mp, (i + 1) mp)
 struct TcArgs {
 	uint32_t n, copies;
 	int mp, np, kp;
+	int slices;                // 7 (FP64-accurate) or 3 (BF16x3)
 	uint16_t *a_slices;        // [7][mp][kp] BF16 bit patterns, written per sample by the split kernel
 	int *row_exp;              // [2 copies] power-of-two exponent of each row of X
 	const int *col_exp;        // [n] exponent of each eigenvector (row of E)
@@ -203,8 +204,8 @@ struct TcArgs {
 };
 cudaError_t launch_tc_projection(const TcArgs &a, const void *map_a, const void *map_b, const double2 *state,
                                  cudaStream_t stream);
-size_t tc_projection_smem();
-const void *tc_projection_kernel_ptr();
+size_t tc_projection_smem(int slices);
+const void *tc_projection_kernel_ptr(int slices);
 
 // Per-chain energies (nlc_energy.cu)
 struct EnergyArgs {

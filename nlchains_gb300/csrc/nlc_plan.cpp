@@ -405,18 +405,19 @@ int bf16_map(CUtensorMap *map, void *base, uint64_t kp, uint64_t rows, uint32_t 
 	return r == CUDA_SUCCESS ? NLC_OK : set_error(NLC_ECUDA, "cuTensorMapEncodeTiled failed");
 }
 
-// Tensor-core projection set-up: the 7 BF16 slices of every eigenvector (rows of E, host, once),
+// Tensor-core projection set-up: the 7 (or 3) BF16 slices of every eigenvector (rows of E, host, once),
 // the per-sample slice buffer of X (zero padding included), and the tensor maps.  Slicing as in
 // nlc_tc.cu: a row scaled by 2^-f (max |e| = m 2^f, 0.5 <= m < 1), v = 256 e 2^-f, then
 // sigma_i = round(v), v <- 256 (v - sigma_i).
-int setup_tc_projection(nlc_plan &P, const double *d_omega) {
+int setup_tc_projection(nlc_plan &P, const double *d_omega, int slices) {
 	const uint32_t n = P.m.chain_length;
 	TcArgs &t = P.tca;
 	t.n = n, t.copies = P.m.copies;
+	t.slices = slices;
 	t.mp = int((2ull * P.m.copies + 127) / 128 * 128);
 	t.np = int((n + 63) / 64 * 64);
 	t.kp = int((n + 31) / 32 * 32);
-	std::vector<uint16_t> b(size_t(7) * t.np * t.kp, 0);
+	std::vector<uint16_t> b(size_t(slices) * t.np * t.kp, 0);
 	std::vector<int> fexp(n, 0);
 	for (uint32_t k = 0; k < n; k++) {
 		const double *e = &P.eig_host[size_t(k) * n];
@@ -427,7 +428,7 @@ int setup_tc_projection(nlc_plan &P, const double *d_omega) {
 		fexp[k] = f;
 		for (uint32_t s = 0; s < n; s++) {
 			double v = std::ldexp(e[s], 8 - f);
-			for (int i = 0; i < 7; i++) {
+			for (int i = 0; i < slices; i++) {
 				const double sg = std::nearbyint(v);
 				const float fs = float(sg);   // an integer of at most 9 bits: exact in BF16
 				uint32_t bits;
@@ -442,15 +443,15 @@ int setup_tc_projection(nlc_plan &P, const double *d_omega) {
 	int *d_fexp = nullptr, *d_rexp = nullptr, *d_status = nullptr;
 	if ((rc = P.upload(&d_b, b.data(), b.size()))) return rc;
 	if ((rc = P.upload(&d_fexp, fexp.data(), n))) return rc;
-	const std::vector<uint16_t> zeros(size_t(7) * t.mp * t.kp, 0);   // padding rows and sites stay 0
+	const std::vector<uint16_t> zeros(size_t(slices) * t.mp * t.kp, 0);   // padding rows and sites stay 0
 	if ((rc = P.upload(&d_a, zeros.data(), zeros.size()))) return rc;
 	if ((rc = P.dalloc(&d_rexp, 2ull * P.m.copies))) return rc;
 	const int zero = 0;
 	if ((rc = P.upload(&d_status, &zero, 1))) return rc;
 	t.a_slices = d_a, t.row_exp = d_rexp, t.col_exp = d_fexp, t.omega = d_omega, t.status = d_status;
-	if ((rc = bf16_map(&P.tc_map_a, d_a, uint64_t(t.kp), uint64_t(7) * t.mp, 128))) return rc;
-	if ((rc = bf16_map(&P.tc_map_b, d_b, uint64_t(t.kp), uint64_t(7) * t.np, 64))) return rc;
-	if ((rc = set_smem_attr(tc_projection_kernel_ptr(), tc_projection_smem(), P.prop))) return rc;
+	if ((rc = bf16_map(&P.tc_map_a, d_a, uint64_t(t.kp), uint64_t(slices) * t.mp, 128))) return rc;
+	if ((rc = bf16_map(&P.tc_map_b, d_b, uint64_t(t.kp), uint64_t(slices) * t.np, 64))) return rc;
+	if ((rc = set_smem_attr(tc_projection_kernel_ptr(slices), tc_projection_smem(slices), P.prop))) return rc;
 	P.diag_rows = t.mp / 128;
 	P.tc = true;
 	return NLC_OK;
@@ -479,10 +480,12 @@ int setup_diagnostics(nlc_plan &P) {
 		P.diag_blocks = int(std::min<unsigned long long>(tiles, 2ull * sms));
 		P.diag_rows = P.diag_blocks;
 		// the tensor-core projection is faster from ~128 sites on (3x at 256, 6x at 1024 sites on GB300)
-		const bool tensor = (P.m.flags & NLC_FLAG_TENSOR_PROJECTION) ||
+		const bool bf16x3 = P.m.flags & NLC_FLAG_BF16X3_PROJECTION;
+		const bool tensor = bf16x3 || (P.m.flags & NLC_FLAG_TENSOR_PROJECTION) ||
 		                    (n >= 128 && !(P.m.flags & NLC_FLAG_FP64_PROJECTION));
 		if (tensor) {
-			if ((rc = setup_tc_projection(P, d_om))) return rc;   // its own partial rows: one per 64 chains
+			// its own partial rows: one per 64 chains
+			if ((rc = setup_tc_projection(P, d_om, bf16x3 ? 3 : 7))) return rc;
 			P.diag_smem = 0;
 		}
 	} else {

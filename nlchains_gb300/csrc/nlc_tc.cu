@@ -19,6 +19,9 @@
 // weights and the sum over the tile's 128 rows are fused into the epilogue; a block's column sums
 // go to its row of partial sums, which the linenergies finish kernel adds in a fixed order.
 //
+// With 3 slices instead of 7 (NLC_FLAG_BF16X3_PROJECTION: 6 slice products, t = 2..4) the same
+// kernels give P to ~2^-24 of the maxima: the north star's "split BF16x3" precision, faster.
+//
 // One CTA: 128 rows (64 chains) x 64 modes; 4 warps.  Thread 0 drives a two-stage TMA pipeline
 // (64-byte swizzle, 32 sites of K per stage: 7 A tiles of 128 x 32 and 7 B tiles of 64 x 32) and
 // issues 56 tcgen05.mma (M = 128, N = 64, K = 16, BF16 in, FP32 in TMEM) per stage into the seven
@@ -34,15 +37,17 @@ namespace nlc {
 
 namespace {
 
-constexpr int kSlices = 7;
+constexpr int kSlicesFull = 7;   // FP64-accurate; 3: the BF16x3 option (~2^-24 of the maxima)
 constexpr int kBM = 128, kBN = 64, kBK = 32;
 // sites of K between two read-outs of the accumulators: 128 keeps every group sum G_t below 2^24
 // (G_2 <= 128 x 256 x 256; the later groups have more pairs of smaller digits), so the FP32
 // accumulation in tensor memory is exact
 constexpr int kChunkK = 128;
 constexpr uint32_t kTmemCols = 512;
-constexpr uint32_t kStageA = kSlices * kBM * kBK * 2, kStageB = kSlices * kBN * kBK * 2;
-constexpr uint32_t kStageBytes = kStageA + kStageB;
+template <int S>
+__host__ __device__ constexpr uint32_t stage_a() { return S * kBM * kBK * 2; }
+template <int S>
+__host__ __device__ constexpr uint32_t stage_bytes() { return S * (kBM + kBN) * kBK * 2; }
 constexpr long long kWaitTries = 1ll << 24;
 constexpr int kNonFiniteRow = 0x7fff;   // row exponent of a row holding inf or NaN
 
@@ -123,6 +128,7 @@ __device__ __forceinline__ void split7(double x, int e, uint16_t (&out)[7]) {
 // into slices[i][r][s].  Integer arithmetic only (GB300 issues it ~30x faster than FP64), coalesced
 // double2 reads of the state.  A row holding inf or NaN gets the exponent kNonFiniteRow, which the
 // projection turns into NaN energies: a blown-up chain is reported, not hidden.
+template <int S>
 __global__ void tc_split_rows_kernel(const double2 *__restrict__ state, TcArgs a) {
 	const unsigned long long c = (unsigned long long) blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
 	const int lane = threadIdx.x & 31;
@@ -156,13 +162,14 @@ __global__ void tc_split_rows_kernel(const double2 *__restrict__ state, TcArgs a
 		split7(v.x, ephi, sp);
 		split7(v.y, epi, sq);
 #pragma unroll
-		for (int i = 0; i < kSlices; i++) {
+		for (int i = 0; i < S; i++) {
 			a.a_slices[((size_t) i * a.mp + r) * a.kp + s] = sp[i];
 			a.a_slices[((size_t) i * a.mp + r + 1) * a.kp + s] = sq[i];
 		}
 	}
 }
 
+template <int S>
 __global__ void __launch_bounds__(128, 1)
 tc_projection_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b, const TcArgs a) {
 	extern __shared__ __align__(1024) unsigned char smem_raw[];
@@ -190,12 +197,13 @@ tc_projection_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_con
 
 	const int nk = a.kp / kBK;   // stages of K
 	const int per_chunk = kChunkK / kBK;
+	constexpr uint32_t kStageA = stage_a<S>(), kStageBytes = stage_bytes<S>();
 	auto stage_ptr = [&](int s) { return smem + (size_t) s * kStageBytes; };
 	auto load_stage = [&](int it, int s) {
 		const uint32_t full = full0 + 8 * s;
 		asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(full), "r"(kStageBytes) : "memory");
 		unsigned char *base = stage_ptr(s);
-		for (int i = 0; i < kSlices; i++) {
+		for (int i = 0; i < S; i++) {
 			tma_load(smem_u32(base + (size_t) i * kBM * kBK * 2), &map_a, it * kBK, i * a.mp + row0, full);
 			tma_load(smem_u32(base + kStageA + (size_t) i * kBN * kBK * 2), &map_b, it * kBK, i * a.np + col0, full);
 		}
@@ -224,9 +232,9 @@ tc_projection_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_con
 				asm volatile("tcgen05.fence::after_thread_sync;");
 				const uint32_t sa = smem_u32(stage_ptr(s)), sb = sa + kStageA;
 #pragma unroll 1
-				for (int t = 2; t <= kSlices + 1; t++) {
+				for (int t = 2; t <= S + 1; t++) {
 					const uint32_t d = tmem + (uint32_t) (t - 2) * kBN;
-					const int ilo = t - kSlices > 1 ? t - kSlices : 1, ihi = t - 1 < kSlices ? t - 1 : kSlices;
+					const int ilo = t - S > 1 ? t - S : 1, ihi = t - 1 < S ? t - 1 : S;
 					for (int i = ilo; i <= ihi; i++) {
 						const int j = t - i;
 						for (int kk = 0; kk < kBK / 16; kk++) {
@@ -270,7 +278,7 @@ tc_projection_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_con
 #pragma unroll
 			for (int j = 0; j < 8; j++) hi[j] = 0, lo[j] = 0;
 #pragma unroll
-			for (int t = 2; t <= kSlices + 1; t++) {
+			for (int t = 2; t <= S + 1; t++) {
 				float v[8];
 				tmem_ld8(tmem + lane_base + (uint32_t) (t - 2) * kBN + seg * 8, v);
 #pragma unroll
@@ -284,7 +292,7 @@ tc_projection_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_con
 			for (int j = 0; j < 8; j++) {
 				double &x = acc[seg * 8 + j];
 				x = fma((double) hi[j], 0x1p-32, x);
-				x = fma((double) lo[j], 0x1p-64, x);
+				if constexpr (S + 1 > 4) x = fma((double) lo[j], 0x1p-64, x);
 			}
 		}
 		asm volatile("tcgen05.fence::before_thread_sync;");
@@ -323,20 +331,28 @@ tc_projection_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_con
 	if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols));
 }
 
-size_t tc_projection_smem() { return 2 * (size_t) kStageBytes + 1024; }
+size_t tc_projection_smem(int slices) {
+	return 2 * (size_t) (slices == 3 ? stage_bytes<3>() : stage_bytes<kSlicesFull>()) + 1024;
+}
 
 cudaError_t launch_tc_projection(const TcArgs &a, const void *map_a, const void *map_b, const double2 *state,
                                  cudaStream_t stream) {
 	count_launch(2);
-	tc_split_rows_kernel<<<(unsigned) ((a.copies + 7) / 8), 256, 0, stream>>>(state, a);
-	cudaError_t e = cudaGetLastError();
-	if (e != cudaSuccess) return e;
 	const dim3 grid(a.mp / kBM, a.np / kBN);
-	tc_projection_kernel<<<grid, 128, tc_projection_smem(), stream>>>(*static_cast<const CUtensorMap *>(map_a),
-	                                                                  *static_cast<const CUtensorMap *>(map_b), a);
+	const CUtensorMap &ma = *static_cast<const CUtensorMap *>(map_a), &mb = *static_cast<const CUtensorMap *>(map_b);
+	const unsigned split_blocks = (unsigned) ((a.copies + 7) / 8);
+	if (a.slices == 3) {
+		tc_split_rows_kernel<3><<<split_blocks, 256, 0, stream>>>(state, a);
+		tc_projection_kernel<3><<<grid, 128, tc_projection_smem(3), stream>>>(ma, mb, a);
+	} else {
+		tc_split_rows_kernel<kSlicesFull><<<split_blocks, 256, 0, stream>>>(state, a);
+		tc_projection_kernel<kSlicesFull><<<grid, 128, tc_projection_smem(kSlicesFull), stream>>>(ma, mb, a);
+	}
 	return cudaGetLastError();
 }
 
-const void *tc_projection_kernel_ptr() { return (const void *) tc_projection_kernel; }
+const void *tc_projection_kernel_ptr(int slices) {
+	return slices == 3 ? (const void *) tc_projection_kernel<3> : (const void *) tc_projection_kernel<kSlicesFull>;
+}
 
 }  // namespace nlc

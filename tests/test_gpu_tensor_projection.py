@@ -77,3 +77,16 @@ def test_tensor_projection_reports_blowup(gpu, bad):
     assert e.value.code == gpu.EBLOWUP
     job.close()
     ctx.close()
+
+
+@pytest.mark.parametrize("n,copies", [(256, 512), (300, 33)])
+def test_bf16x3_projection_error_stated(gpu, n, copies):
+    # 3 BF16 slices (6 tensor products) instead of 7: mode energies within 1e-6 of the FP64 ones
+    # (the split keeps ~24 bits of every value), entropies within 1e-6
+    masses = ic.masses_uniform(n, seed=n)
+    state = np.random.default_rng(n).standard_normal((copies, n, 2))
+    l64, w64, i64 = lin_of(gpu, n, copies, state, masses, gpu.FLAG_FP64_PROJECTION)
+    l3, w3, i3 = lin_of(gpu, n, copies, state, masses, gpu.FLAG_BF16X3_PROJECTION)
+    err = np.abs(l3 - l64).max() / np.abs(l64).max()
+    assert 0 < err <= 1e-6
+    assert abs(w3 - w64) <= 1e-6 * max(1.0, abs(w64)) and abs(i3 - i64) <= 1e-6 * max(1.0, abs(i64))
