@@ -517,7 +517,8 @@ def run_reference(args):
 def run_profile_case(args):
     """Small cases of the headline kernels for ncu captures: 4 launches (10 steps; DNLS 2 steps),
     each followed by one diagnostics sample.  DNKG / Toda: 16384 of the 65536 copies (33.5 MB);
-    DNLS: the full 8192 copies of N = 1024 (134 MB, above the L2); dDNKG: the full 4096 x 256."""
+    DNLS: the full 8192 copies of N = 1024 (134 MB, above the L2); dDNKG: the full 4096 x 256;
+    long: 256 FPUT chains of 65535 sites (windowed tier, 268 MB)."""
     import torch
 
     import nlchains_gb300 as nlc
@@ -528,6 +529,9 @@ def run_profile_case(args):
         w, steps = dict(OTHERS[1]), 2
     if args.profile == "ddnkg":   # the full dDNKG workload: 4096 chains of 256 sites, tensor-core projection
         w = dict(OTHERS[2])
+    if args.profile == "long":    # chains beyond one block: the windowed tier (268 MB of state)
+        w = dict(name="FPUT-beta N=65535 copies=256 (windowed tier)", model="FPUT", n=65535, copies=256, dt=0.1,
+                 params=dict(alpha=0.0, beta=1.0), batching=10, eps=0.1, kmax=4, include_zero=False)
     state = initial_state(w, w["copies"], 0)
     plan = nlc.Plan(nlc.Model(w["model"], w["n"], w["copies"], w["dt"], masses=masses(w), flags=nlc.FLAG_NO_TUNE,
                               **w["params"]))
@@ -549,7 +553,7 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["engine", "reference"], default="engine")
-    ap.add_argument("--profile", choices=["dnkg", "toda", "dnls", "ddnkg"], default=None,
+    ap.add_argument("--profile", choices=["dnkg", "toda", "dnls", "ddnkg", "long"], default=None,
                     help="run only a small case of the integrator + diagnostics (for ncu captures)")
     args = ap.parse_args()
     if args.profile:

@@ -195,7 +195,57 @@ __global__ void __launch_bounds__(kFinishThreads) lin_finish_kernel(const Finish
 	}
 }
 
+// Long chains: the row sums of 256 modes per block (coalesced over the modes, rows in order), the
+// normalisation and the block's entropy sums {sum e, sum log e, sum e log e, count} in a fixed
+// tree; then one block adds the blocks' sums in order and forms the entropies.
+__global__ void __launch_bounds__(kFinishModesPerBlock) lin_finish_modes_kernel(const FinishArgs a) {
+	__shared__ double r_e[kFinishModesPerBlock], r_l[kFinishModesPerBlock], r_el[kFinishModesPerBlock];
+	__shared__ int r_c[kFinishModesPerBlock];
+	const int t = threadIdx.x, k = blockIdx.x * kFinishModesPerBlock + t;
+	double se = 0., sl = 0., sel = 0.;
+	int cnt = 0;
+	if (k < (int) a.n) {
+		double v = 0.;
+		for (int r = 0; r < a.nblocks; r++) v = dadd(v, a.partials[(size_t) r * a.n + k]);
+		finish_mode(a, k, v, se, sl, sel, cnt);
+	}
+	r_e[t] = se, r_l[t] = sl, r_el[t] = sel, r_c[t] = cnt;
+	__syncthreads();
+	for (int w = kFinishModesPerBlock / 2; w > 0; w >>= 1) {
+		if (t < w) {
+			r_e[t] = dadd(r_e[t], r_e[t + w]);
+			r_l[t] = dadd(r_l[t], r_l[t + w]);
+			r_el[t] = dadd(r_el[t], r_el[t + w]);
+			r_c[t] += r_c[t + w];
+		}
+		__syncthreads();
+	}
+	if (t == 0) {
+		double *o = a.block_sums + 4 * (size_t) blockIdx.x;
+		o[0] = r_e[0], o[1] = r_l[0], o[2] = r_el[0], o[3] = r_c[0];
+	}
+}
+
+__global__ void lin_finish_entropy_kernel(const FinishArgs a, int blocks) {
+	if (threadIdx.x != 0 || !a.entropies) return;
+	double se = 0., sl = 0., sel = 0., modes = 0.;
+	for (int b = 0; b < blocks; b++) {
+		const double *o = a.block_sums + 4 * (size_t) b;
+		se = dadd(se, o[0]), sl = dadd(sl, o[1]), sel = dadd(sel, o[2]), modes = dadd(modes, o[3]);
+	}
+	const double normalization = modes / se, lognorm = log(normalization);
+	a.entropies[0] = -(sl + modes * lognorm);
+	a.entropies[1] = normalization * (sel + lognorm * se);
+}
+
 cudaError_t launch_linenergies_finish(const FinishArgs &a, cudaStream_t stream) {
+	if (a.block_sums && a.n > (uint32_t) kFinishThreads) {
+		const int blocks = int((a.n + kFinishModesPerBlock - 1) / kFinishModesPerBlock);
+		count_launch(2);
+		lin_finish_modes_kernel<<<blocks, kFinishModesPerBlock, 0, stream>>>(a);
+		lin_finish_entropy_kernel<<<1, 32, 0, stream>>>(a, blocks);
+		return cudaGetLastError();
+	}
 	count_launch();
 	lin_finish_kernel<<<1, kFinishThreads, 0, stream>>>(a);
 	return cudaGetLastError();
