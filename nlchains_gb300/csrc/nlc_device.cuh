@@ -30,10 +30,10 @@ __device__ __forceinline__ double fadd(double a, double b, const FpOnes &k) { re
 __device__ __forceinline__ double fsub(double a, double b, const FpOnes &k) { return __fma_rn(b, k.mone, a); }
 __device__ __forceinline__ double fmul(double a, double b, const FpOnes &k) { return __fma_rn(a, b, k.mzero); }
 
-// Table-driven exp (Tang, ACM TOMS 15(2) 1989): x = (n/256) ln2 + r, |r| <= ln2/512,
-// scale*exp(x) = 2^(n>>8) * T[n&255] * (1 + r + r^2/2 + r^3/6 + r^4/24), T[j] = scale * 2^(j/256).
-// Nine FP64 operations (all issued as FMAs) on the fast path against ~22 DFMA-equivalents for the
-// library exp.  The
+// Table-driven exp (Tang, ACM TOMS 15(2) 1989): x = (n/2048) ln2 + r, |r| <= ln2/4096,
+// scale*exp(x) = 2^(n>>11) * T[n&2047] * (1 + r + r^2/2 + r^3/6), T[j] = scale * 2^(j/2048); the
+// dropped r^4/24 is below 2^-54.  Eight FP64 operations (all issued as FMAs) on the fast path
+// against ~22 DFMA-equivalents for the library exp; the 16 KB table sits in shared memory.  The
 // range checks use the integer high word of x, which costs no FP64 issue slot.
 __device__ __forceinline__ double exp_scaled(double x, const double *__restrict__ table, const FpOnes &k1,
                                              const ExpConsts &c) {
@@ -47,13 +47,12 @@ __device__ __forceinline__ double exp_scaled(double x, const double *__restrict_
 	const double nf = fsub(t, c.shifter, k1);
 	double r = dfma(-nf, c.l1, x);
 	r = dfma(-nf, c.l2, r);
-	double q = dfma(r, c.c4, c.c3);
-	q = dfma(q, r, c.c2);
+	double q = dfma(r, c.c3, c.c2);
 	q = dfma(q, r, k1.one);
 	const double p = fmul(q, r, k1);
-	const double tj = table[n & 255];
+	const double tj = table[n & (kExpTable - 1)];
 	double v = dfma(tj, p, tj);
-	const int k = n >> 8;
+	const int k = n >> 11;
 	long long vb = __double_as_longlong(v);
 	const int e = int((vb >> 52) & 0x7ff);
 	if (k > -1000 && k < 1000 && e + k > 0 && e + k < 0x7ff) {

@@ -18,8 +18,8 @@ int cuda_status(cudaError_t e, const char *what);
 extern const double kYoshidaC[8];
 extern const double kYoshidaD[8];
 
-// scale * 2^(j/256), j < 256, in double-double arithmetic (identical bits on every IEEE host)
-void exp_table(double scale, double table[256]);
+// scale * 2^(j/2048), j < 2048, in double-double arithmetic (identical bits on every IEEE host)
+void exp_table(double scale, double table[kExpTable]);
 
 // (cos, sin)(2 pi j / 256), j < 256, interleaved, in double-double arithmetic (identical bits on
 // every IEEE host): the table of the device's sincos_table

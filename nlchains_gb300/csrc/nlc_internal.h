@@ -17,12 +17,13 @@ struct FpOnes {
 	double one = 1., mone = -1., mzero = -0.;
 };
 // Constants of the table-driven exp (nlc_device.cuh exp_scaled).
+constexpr int kExpTable = 2048;   // entries of the table exp: 2^(j/2048), |r| <= ln 2 / 4096
 struct ExpConsts {
-	double shifter = 0x1.8p52;                    // 1.5 * 2^52: round-to-integer shifter
-	double inv_l = 256. / 0x1.62e42fefa39efp-1;   // 256 / ln 2
-	double l1 = 0x1.62e42fefa39efp-9;             // ln 2 / 256, leading part
-	double l2 = 0x1.abc9e3b39803fp-64;            // ln 2 / 256, trailing part
-	double c4 = 1. / 24, c3 = 1. / 6, c2 = 0.5;   // Taylor coefficients of exp(r) - 1 - r
+	double shifter = 0x1.8p52;                     // 1.5 * 2^52: round-to-integer shifter
+	double inv_l = 2048. / 0x1.62e42fefa39efp-1;   // 2048 / ln 2
+	double l1 = 0x1.62e42fefa39efp-12;             // ln 2 / 2048, leading part
+	double l2 = 0x1.abc9e3b39803fp-67;             // ln 2 / 2048, trailing part
+	double c3 = 1. / 6, c2 = 0.5;                  // Taylor coefficients of exp(r) - 1 - r (r^4/24 < 2^-54)
 };
 
 // Constants of the table-driven sincos (nlc_device.cuh sincos_table): Cody-Waite reduction by
@@ -66,7 +67,7 @@ struct RealArgs {
 	double alpha, beta;
 	double alpha2;         // Toda: 2 alpha
 	const double *mp2_site;  // dDNKG: m_x + 2 per site (device)
-	const double *exptab;    // Toda: alpha2_inv * 2^(j/256), 256 entries (device)
+	const double *exptab;    // Toda: alpha2_inv * 2^(j/2048), kExpTable entries (device)
 	unsigned long long *work_counter;  // [0] next unit, [1] finished blocks (device, self-resetting)
 	uint32_t n;
 	uint32_t copies;

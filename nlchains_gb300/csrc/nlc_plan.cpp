@@ -718,10 +718,10 @@ extern "C" int nlc_plan_create(const nlc_model *model, nlc_plan **out) {
 		}
 		if (mdl == NLC_TODA) {
 			if (!(model->alpha != 0.)) return set_error(NLC_EINVAL, "Toda needs --alpha != 0");
-			double tab[256];
+			double tab[kExpTable];
 			exp_table(1 / a.alpha2, tab);
 			double *d = nullptr;
-			if ((rc = P->upload(&d, tab, 256))) return rc;
+			if ((rc = P->upload(&d, tab, kExpTable))) return rc;
 			a.exptab = d;
 		}
 		switch (mdl) {

@@ -24,7 +24,7 @@
 //
 // FP64 operations per site and sub-step (GB300 is FP64-pipe bound, see nlc_device.cuh):
 //   DNKG / dDNKG 6 (5 with beta == 1), FPUT 7 (6 with alpha == 0 and beta == 1),
-//   Toda 14 (13 with 2 alpha == 1) including the 9-operation table exp.
+//   Toda 13 (12 with 2 alpha == 1) including the 8-operation table exp.
 #pragma once
 
 #include "nlc_device.cuh"
@@ -102,7 +102,7 @@ __device__ __forceinline__ double bond_force(double d, const RealArgs &a, const 
 template <int MODEL, int E, int VAR, bool WIN>
 __global__ void real_move_kernel_t(double2 *__restrict__ state, const RealArgs a) {
 	__shared__ double xbuf[4 * 32];
-	__shared__ double s_tab[MODEL == NLC_TODA ? 256 : 1];
+	__shared__ double s_tab[MODEL == NLC_TODA ? kExpTable : 1];
 	__shared__ unsigned long long s_unit;
 	__shared__ int s_job;
 
@@ -115,7 +115,7 @@ __global__ void real_move_kernel_t(double2 *__restrict__ state, const RealArgs a
 	Ring ring{G, lane, tid & 31, tid >> 5, G > 32 ? G >> 5 : 1, xbuf, 0};
 
 	if constexpr (MODEL == NLC_TODA) {
-		for (int i = tid; i < 256; i += blockDim.x) s_tab[i] = a.exptab[i];
+		for (int i = tid; i < kExpTable; i += blockDim.x) s_tab[i] = a.exptab[i];
 	}
 
 	// the ensemble of the current unit: the launch's own, or one entry of the batch table

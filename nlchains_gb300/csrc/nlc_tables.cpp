@@ -100,10 +100,10 @@ void sincos_table(double table[512]) {
 	}
 }
 
-void exp_table(double scale, double table[256]) {
+void exp_table(double scale, double table[kExpTable]) {
 	const DD ln2{0x1.62e42fefa39efp-1, 0x1.abc9e3b39803fp-56};
-	for (unsigned j = 0; j < 256; j++) {
-		DD v = dd_exp_small(dd_mul(ln2, DD{j / 256., 0.}));
+	for (unsigned j = 0; j < unsigned(kExpTable); j++) {
+		DD v = dd_exp_small(dd_mul(ln2, DD{double(j) / kExpTable, 0.}));
 		v = dd_mul(v, DD{scale, 0.});
 		table[j] = v.hi + v.lo;
 	}

@@ -166,7 +166,7 @@ def dispersion(model_id, n, m=0.0):
 
 
 def exp_table(scale):
-    t = np.zeros(256)
+    t = np.zeros(2048)
     _lib().nlo_exp_table(scale, _dp(t))
     return t
 

@@ -85,10 +85,10 @@ static dd dd_exp_small(dd y) {
 	return sum;
 }
 
-void nlo_exp_table(double scale, double table[256]) {
+void nlo_exp_table(double scale, double table[NLO_EXP_TABLE]) {
 	const dd ln2 = {0x1.62e42fefa39efp-1, 0x1.abc9e3b39803fp-56};
-	for (unsigned j = 0; j < 256; j++) {
-		dd frac = {j / 256., 0.};
+	for (unsigned j = 0; j < NLO_EXP_TABLE; j++) {
+		dd frac = {(double) j / NLO_EXP_TABLE, 0.};
 		dd v = dd_exp_small(dd_mul(ln2, frac));
 		dd s = {scale, 0.};
 		v = dd_mul(v, s);
@@ -97,9 +97,9 @@ void nlo_exp_table(double scale, double table[256]) {
 }
 
 /* The exact FP64 sequence of the device exp (nlchains_gb300/csrc/nlc_device.cuh, exp_scaled). */
-double nlo_exp_scaled(double x, const double table[256]) {
-	const double shifter = 0x1.8p52, inv_l = 256. / 0x1.62e42fefa39efp-1;
-	const double l1 = 0x1.62e42fefa39efp-9, l2 = 0x1.abc9e3b39803fp-64;
+double nlo_exp_scaled(double x, const double table[NLO_EXP_TABLE]) {
+	const double shifter = 0x1.8p52, inv_l = 2048. / 0x1.62e42fefa39efp-1;
+	const double l1 = 0x1.62e42fefa39efp-12, l2 = 0x1.abc9e3b39803fp-67;
 	int64_t xb;
 	memcpy(&xb, &x, 8);
 	const int32_t hi = (int32_t) (xb >> 32);
@@ -114,13 +114,12 @@ double nlo_exp_scaled(double x, const double table[256]) {
 	double nf = t - shifter;
 	double r = fma(-nf, l1, x);
 	r = fma(-nf, l2, r);
-	double q = fma(r, 1. / 24, 1. / 6);
-	q = fma(q, r, 0.5);
+	double q = fma(r, 1. / 6, 0.5);
 	q = fma(q, r, 1.);
 	double p = q * r;
-	double tj = table[n & 255];
+	double tj = table[n & (NLO_EXP_TABLE - 1)];
 	double v = fma(tj, p, tj);
-	int32_t k = n >> 8;   /* arithmetic shift: floor(n / 256) */
+	int32_t k = n >> 11;   /* arithmetic shift: floor(n / 2048) */
 	if (k > -1000 && k < 1000) {
 		int64_t vb;
 		memcpy(&vb, &v, 8);
@@ -143,7 +142,7 @@ typedef struct {
 	double dtc[8], dtd[8], dtc0x2;
 	double mp2;            /* DNKG: m + 2 */
 	double alpha2, alpha2_inv;
-	double exptab[256];    /* Toda device order: alpha2_inv * 2^(j/256) */
+	double exptab[NLO_EXP_TABLE];   /* Toda device order: alpha2_inv * 2^(j/2048) */
 } consts;
 
 static void make_consts(const nlo_model *M, consts *K) {

@@ -85,10 +85,11 @@ double nlo_energy(const nlo_model *mdl, const double *chain);
  * by cyclic Jacobi: ascending eigenvalues, omegas = sqrt(eigenvalues), column-major eigenvectors. */
 int nlo_eigensystem(uint32_t n, const double *mp2, double *omegas, double *eigvecs);
 
-/* Table-driven exp used by the device order (Tang's method, 256 entries); the table holds
- * scale * 2^(j/256) and the function returns scale * exp(x). */
-void nlo_exp_table(double scale, double table[256]);
-double nlo_exp_scaled(double x, const double table[256]);
+/* Table-driven exp used by the device order (Tang's method, 2048 entries, degree-3 polynomial);
+ * the table holds scale * 2^(j/2048) and the function returns scale * exp(x). */
+#define NLO_EXP_TABLE 2048
+void nlo_exp_table(double scale, double table[NLO_EXP_TABLE]);
+double nlo_exp_scaled(double x, const double table[NLO_EXP_TABLE]);
 
 #ifdef __cplusplus
 }
