@@ -62,13 +62,14 @@ __device__ __forceinline__ double exp_scaled(double x, const double *__restrict_
 	return ldexp(v, k);
 }
 
-// sin(th), cos(th) from a 256-entry table (S. Gal, "Computing elementary functions: a new approach
+// sin(th), cos(th) from a 1024-entry table (S. Gal, "Computing elementary functions: a new approach
 // for achieving high accuracy and good performance", LNCS 235, 1986; P. T. P. Tang's table-driven
-// method): th = j 2 pi/256 + r with j = round(th 256 / (2 pi)) by the shifter trick and r reduced in
-// two FMAs against pi/128 split into two doubles, |r| <= pi/256; sin r and cos r - 1 by their Taylor
-// series to r^7 / r^6 (next terms below 2^-64 relative), then
+// method): th = j 2 pi/1024 + r with j = round(th 1024 / (2 pi)) by the shifter trick and r reduced
+// in two FMAs against pi/512 split into two doubles, |r| <= pi/1024; sin r and cos r - 1 by their
+// Taylor series to r^5 / r^4 (next terms below 2^-59 relative), then
 //   cos th = C_j + C_j (cos r - 1) - S_j sin r,  sin th = S_j + S_j (cos r - 1) + C_j sin r.
-// 16 FP64 operations.  |th| >= 2^20, inf and NaN go to the library sincos.
+// 14 FP64 operations; the 16 KB table is read through the read-only cache.  |th| >= 2^20, inf and
+// NaN go to the library sincos.
 __device__ __forceinline__ void sincos_table(double th, const double2 *__restrict__ tab, const SinCosConsts &C,
                                              const FpOnes &k, double *s, double *c) {
 	if ((__double2hiint(th) & 0x7fffffff) >= 0x41300000) {
@@ -78,10 +79,10 @@ __device__ __forceinline__ void sincos_table(double th, const double2 *__restric
 	const double t = dfma(th, C.inv, C.shifter);
 	const double kd = fsub(t, C.shifter, k);
 	const double r = dfma(-kd, C.p2, dfma(-kd, C.p1, th));
-	const double2 e = __ldg(tab + (__double2loint(t) & 255));
+	const double2 e = __ldg(tab + (__double2loint(t) & (kSinCosTable - 1)));
 	const double r2 = fmul(r, r, k);
-	const double sr = dfma(fmul(r, r2, k), dfma(dfma(r2, C.s7, C.s5), r2, C.s3), r);
-	const double cm1 = fmul(r2, dfma(dfma(r2, C.c6, C.c4), r2, C.c2), k);
+	const double sr = dfma(fmul(r, r2, k), dfma(r2, C.s5, C.s3), r);
+	const double cm1 = fmul(r2, dfma(r2, C.c4, C.c2), k);
 	*c = dfma(e.x, cm1, dfma(-e.y, sr, e.x));
 	*s = dfma(e.y, cm1, dfma(e.x, sr, e.y));
 }

@@ -21,9 +21,9 @@ extern const double kYoshidaD[8];
 // scale * 2^(j/2048), j < 2048, in double-double arithmetic (identical bits on every IEEE host)
 void exp_table(double scale, double table[kExpTable]);
 
-// (cos, sin)(2 pi j / 256), j < 256, interleaved, in double-double arithmetic (identical bits on
+// (cos, sin)(2 pi j / 1024), j < 1024, interleaved, in double-double arithmetic (identical bits on
 // every IEEE host): the table of the device's sincos_table
-void sincos_table(double table[512]);
+void sincos_table(double table[2 * kSinCosTable]);
 
 // dispersion of the real models, sqrt(m + 4 sin^2(pi k / n)) (DNKG_FPUT_Toda/dispersion.cpp:9-16)
 std::vector<double> dispersion_real(uint32_t n, double m);

@@ -27,14 +27,15 @@ struct ExpConsts {
 };
 
 // Constants of the table-driven sincos (nlc_device.cuh sincos_table): Cody-Waite reduction by
-// 2 pi / 256 = pi / 128 (split as the double-double value of pi, scaled) and Taylor coefficients
+// 2 pi / 1024 = pi / 512 (split as the double-double value of pi, scaled) and Taylor coefficients
+constexpr int kSinCosTable = 1024;
 struct SinCosConsts {
 	double shifter = 0x1.8p52;                      // 1.5 * 2^52: round-to-integer shifter
-	double inv = 128. / 3.141592653589793116;       // 256 / (2 pi)
-	double p1 = 3.141592653589793116 / 128;         // pi / 128, leading part
-	double p2 = 1.2246467991473532072e-16 / 128;    // pi / 128, trailing part
-	double s3 = -1. / 6, s5 = 1. / 120, s7 = -1. / 5040;   // sin r = r + r^3 (s3 + r^2 (s5 + r^2 s7))
-	double c2 = -1. / 2, c4 = 1. / 24, c6 = -1. / 720;     // cos r - 1 = r^2 (c2 + r^2 (c4 + r^2 c6))
+	double inv = 512. / 3.141592653589793116;       // 1024 / (2 pi)
+	double p1 = 3.141592653589793116 / 512;         // pi / 512, leading part
+	double p2 = 1.2246467991473532072e-16 / 512;    // pi / 512, trailing part
+	double s3 = -1. / 6, s5 = 1. / 120;             // sin r = r + r^3 (s3 + r^2 s5)   (r^7/5040 < 2^-60 r)
+	double c2 = -1. / 2, c4 = 1. / 24;              // cos r - 1 = r^2 (c2 + r^2 c4)  (r^6/720 < 2^-59)
 };
 
 constexpr int kMaxSitesPerLane = 16;   // E: sites of a chain held in registers by one thread
@@ -173,7 +174,7 @@ struct DnlsArgs {
 	unsigned long long *work_counter;
 	int team;                  // lanes per chain of the warp-team variant (power of two, 4 .. 32)
 	uint32_t seg;              // NLC_SEG_*
-	const double2 *sctab;      // (cos, sin)(2 pi j / 256), j < 256 (device)
+	const double2 *sctab;      // (cos, sin)(2 pi j / 1024), j < 1024 (device)
 	SinCosConsts sc;
 	double2 *gscratch;         // block teams whose buffers exceed shared memory: [blocks][2][len]
 };

@@ -641,10 +641,10 @@ extern "C" int nlc_plan_create(const nlc_model *model, nlc_plan **out) {
 		if ((rc = P->upload(&d_tab, reinterpret_cast<const double2 *>(tab.data()), 7 * size_t(n)))) return rc;
 		d.lin_tables = d_tab;
 		{
-			double sct[512];
-			sincos_table(sct);
+			std::vector<double> sct(2 * kSinCosTable);
+			sincos_table(sct.data());
 			double2 *d_sct = nullptr;
-			if ((rc = P->upload(&d_sct, reinterpret_cast<const double2 *>(sct), 256))) return rc;
+			if ((rc = P->upload(&d_sct, reinterpret_cast<const double2 *>(sct.data()), kSinCosTable))) return rc;
 			d.sctab = d_sct;
 		}
 		if (d.fft.bluestein) {

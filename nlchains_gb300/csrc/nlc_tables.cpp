@@ -82,18 +82,19 @@ void dd_sincos_small(DD x, DD &s, DD &c) {
 
 }  // namespace
 
-void sincos_table(double table[512]) {
-	// octant values m pi/128, m = 0..32, then quarter-turn symmetries (exact sign and swap)
+void sincos_table(double table[2 * kSinCosTable]) {
+	// octant values m pi/512, m = 0..128, then quarter-turn symmetries (exact sign and swap)
+	constexpr unsigned Q = kSinCosTable / 4, O = kSinCosTable / 8;
 	const DD pi{3.141592653589793116, 1.2246467991473532072e-16};
-	double cs[33], sn[33];
-	for (unsigned m = 0; m <= 32; m++) {
+	double cs[O + 1], sn[O + 1];
+	for (unsigned m = 0; m <= O; m++) {
 		DD s, c;
-		dd_sincos_small(dd_div_u(dd_mul(pi, DD{double(m), 0.}), 128), s, c);
+		dd_sincos_small(dd_div_u(dd_mul(pi, DD{double(m), 0.}), kSinCosTable / 2), s, c);
 		sn[m] = s.hi + s.lo, cs[m] = c.hi + c.lo;
 	}
-	for (unsigned j = 0; j < 256; j++) {
-		const unsigned q = j / 64, jj = j % 64;
-		const double c0 = jj <= 32 ? cs[jj] : sn[64 - jj], s0 = jj <= 32 ? sn[jj] : cs[64 - jj];
+	for (unsigned j = 0; j < unsigned(kSinCosTable); j++) {
+		const unsigned q = j / Q, jj = j % Q;
+		const double c0 = jj <= O ? cs[jj] : sn[Q - jj], s0 = jj <= O ? sn[jj] : cs[Q - jj];
 		const double c = q == 0 ? c0 : q == 1 ? -s0 : q == 2 ? -c0 : s0;
 		const double s = q == 0 ? s0 : q == 1 ? c0 : q == 2 ? -s0 : -c0;
 		table[2 * j] = c, table[2 * j + 1] = s;
