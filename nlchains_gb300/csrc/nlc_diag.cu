@@ -239,7 +239,7 @@ __global__ void lin_finish_entropy_kernel(const FinishArgs a, int blocks) {
 }
 
 cudaError_t launch_linenergies_finish(const FinishArgs &a, cudaStream_t stream) {
-	if (a.block_sums && a.n > (uint32_t) kFinishThreads) {
+	if (a.block_sums && a.n > (uint32_t) kFinishModesPerBlock) {
 		const int blocks = int((a.n + kFinishModesPerBlock - 1) / kFinishModesPerBlock);
 		count_launch(2);
 		lin_finish_modes_kernel<<<blocks, kFinishModesPerBlock, 0, stream>>>(a);

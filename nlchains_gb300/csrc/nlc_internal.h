@@ -156,7 +156,7 @@ struct FinishArgs {
 	const uint8_t *mask;      // device, NULL = all modes
 	double *lin;              // out [n]
 	double *entropies;        // out [2] or NULL
-	double *block_sums;       // [ceil(n / 256)][4] scratch: with it, chains longer than 1024 sites
+	double *block_sums;       // [ceil(n / 256)][4] scratch: with it, chains longer than 256 sites
 	                          // are finished by a grid over the modes instead of one block
 };
 cudaError_t launch_linenergies_finish(const FinishArgs &a, cudaStream_t stream);

@@ -110,7 +110,7 @@ struct nlc_plan {
 	size_t device_bytes = 0;
 	unsigned long long *d_counter = nullptr;
 	double *d_partials = nullptr;
-	double *d_block_sums = nullptr;   // entropy sums of the mode blocks (chains above 1024 sites)
+	double *d_block_sums = nullptr;   // entropy sums of the mode blocks (chains above 256 sites)
 	uint8_t *d_mask = nullptr;
 
 	RealArgs ra{};
@@ -531,7 +531,8 @@ int setup_diagnostics(nlc_plan &P) {
 		return set_error(NLC_EUNSUPPORTED, "chain_length too large for the shared-memory diagnostics");
 	if ((rc = P.dalloc(&P.d_partials, size_t(P.diag_rows) * n))) return rc;
 	g.partials = P.d_partials;
-	if (n > 1024 && (rc = P.dalloc(&P.d_block_sums, 4 * size_t((n + kFinishModesPerBlock - 1) / kFinishModesPerBlock))))
+	if (n > uint32_t(kFinishModesPerBlock) &&
+	    (rc = P.dalloc(&P.d_block_sums, 4 * size_t((n + kFinishModesPerBlock - 1) / kFinishModesPerBlock))))
 		return rc;
 	if (!P.mask_host.empty()) {
 		if ((rc = P.upload(&P.d_mask, P.mask_host.data(), n))) return rc;
