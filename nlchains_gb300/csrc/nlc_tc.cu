@@ -13,8 +13,8 @@
 //   BF16).  P = 2^(e_r + f_k) sum_{t = 2..8} 2^(-8t) G_t,  G_t = sum_{i + j = t} A_i B_j^T.
 //
 // Every G_t is a sum of integer products below 2^16, accumulated in FP32 in tensor memory; it is
-// read out every 128 sites of K, while the partial sums are still exact (below 2^24), and the
-// groups are combined exactly in integers and added in FP64.  The slices beyond t = 8 and the residual of the 7-slice truncation are
+// read out every 256 sites of K, while the partial sums that matter are still exact (below 2^24),
+// and the groups are combined exactly in integers and added in FP64.  The slices beyond t = 8 and the residual of the 7-slice truncation are
 // below 2^-56 of the row and column maxima, so P carries FP64-level error.  The squares, the omega
 // weights and the sum over the tile's 128 rows are fused into the epilogue; a block's column sums
 // go to its row of partial sums, which the linenergies finish kernel adds in a fixed order.
@@ -24,8 +24,8 @@
 //
 // One CTA: 128 rows (64 chains) x 64 modes; 4 warps.  Thread 0 drives a two-stage TMA pipeline
 // (64-byte swizzle, 32 sites of K per stage: 7 A tiles of 128 x 32 and 7 B tiles of 64 x 32) and
-// issues 56 tcgen05.mma (M = 128, N = 64, K = 16, BF16 in, FP32 in TMEM) per stage into the seven
-// G_t accumulators (7 x 64 TMEM columns).  Every wait is bounded: on a timeout the block records a
+// issues 56 tcgen05.mma (M = 128, N = 64, K = 16, BF16 in, FP32 in TMEM) per stage into eight
+// accumulators: G_t, t = 2..8, with the (2,2) product of G_4 apart (8 x 64 = all 512 TMEM columns).  Every wait is bounded: on a timeout the block records a
 // status, writes NaN into its partial row (the host then sees a non-finite entropy) and returns
 // after freeing its tensor memory.
 #include <cuda.h>
@@ -39,10 +39,11 @@ namespace {
 
 constexpr int kSlicesFull = 7;   // FP64-accurate; 3: the BF16x3 option (~2^-24 of the maxima)
 constexpr int kBM = 128, kBN = 64, kBK = 32;
-// sites of K between two read-outs of the accumulators: 128 keeps every group sum G_t below 2^24
-// (G_2 <= 128 x 256 x 256; the later groups have more pairs of smaller digits), so the FP32
-// accumulation in tensor memory is exact
-constexpr int kChunkK = 128;
+// sites of K between two read-outs of the accumulators.  With 256, G_2 <= 256 x 256^2, G_3 <= 256 x
+// 2 x 256 x 128 and, the (2,2) product kept in an accumulator of its own, both parts of G_4 stay
+// within 2^24, so the FP32 accumulation in tensor memory is exact for every group the result
+// depends on above 2^-40; the groups t >= 5 may round in their last bit, 2^-40 below the maxima.
+constexpr int kChunkK = 256;
 constexpr uint32_t kTmemCols = 512;
 template <int S>
 __host__ __device__ constexpr uint32_t stage_a() { return S * kBM * kBK * 2; }
@@ -233,14 +234,16 @@ tc_projection_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_con
 				const uint32_t sa = smem_u32(stage_ptr(s)), sb = sa + kStageA;
 #pragma unroll 1
 				for (int t = 2; t <= S + 1; t++) {
-					const uint32_t d = tmem + (uint32_t) (t - 2) * kBN;
 					const int ilo = t - S > 1 ? t - S : 1, ihi = t - 1 < S ? t - 1 : S;
 					for (int i = ilo; i <= ihi; i++) {
 						const int j = t - i;
+						// accumulator t - 2; the (2,2) product of G_4 in accumulator S
+						const bool own = t == 4 && i == 2;
+						const uint32_t d = tmem + (uint32_t) (own ? S : t - 2) * kBN;
 						for (int kk = 0; kk < kBK / 16; kk++) {
 							const uint64_t ad = smem_desc(sa + (uint32_t) (i - 1) * kBM * kBK * 2 + kk * 32);
 							const uint64_t bd = smem_desc(sb + (uint32_t) (j - 1) * kBN * kBK * 2 + kk * 32);
-							const uint32_t accum = (it == c0 && i == ilo && kk == 0) ? 0u : 1u;
+							const uint32_t accum = (it == c0 && (own || i == ilo) && kk == 0) ? 0u : 1u;
 							asm volatile(
 							    "{ .reg .pred p; setp.ne.b32 p, %4, 0; tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p; }"
 							    ::"r"(d), "l"(ad), "l"(bd), "r"(kIdesc), "r"(accum));
@@ -278,14 +281,15 @@ tc_projection_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_con
 #pragma unroll
 			for (int j = 0; j < 8; j++) hi[j] = 0, lo[j] = 0;
 #pragma unroll
-			for (int t = 2; t <= S + 1; t++) {
+			for (int t = 2; t <= S + 2; t++) {   // t = S + 2: the (2,2) part of G_4 (accumulator S)
+				const int grp = t - 2, tt = t == S + 2 ? 4 : t;
 				float v[8];
-				tmem_ld8(tmem + lane_base + (uint32_t) (t - 2) * kBN + seg * 8, v);
+				tmem_ld8(tmem + lane_base + (uint32_t) grp * kBN + seg * 8, v);
 #pragma unroll
 				for (int j = 0; j < 8; j++) {
 					const long long g = __float2ll_rn(v[j]);
-					if (t <= 4) hi[j] += g << (8 * (4 - t));
-					else lo[j] += g << (8 * (8 - t));
+					if (tt <= 4) hi[j] += g << (8 * (4 - tt));
+					else lo[j] += g << (8 * (8 - tt));
 				}
 			}
 #pragma unroll
