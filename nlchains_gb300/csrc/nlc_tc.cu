@@ -90,6 +90,12 @@ __device__ __forceinline__ void tmem_ld8(uint32_t taddr, float (&v)[8]) {
 	for (int j = 0; j < 8; j++) v[j] = __uint_as_float(r[j]);
 }
 
+// an int64 of magnitude below 2^51 as a double, exactly: added to the bit pattern of 1.5 * 2^52 it
+// lands in the low mantissa bits, and one FP64 subtraction removes the offset
+__device__ __forceinline__ double i64_to_double(long long x) {
+	return __longlong_as_double(x + 0x4338000000000000ll) - 0x1.8p52;
+}
+
 // 2^k for a normal-range k, built from its bit pattern (an exact scaling, no library call)
 __device__ __forceinline__ double pow2i(int k) {
 	return k >= -1022 && k <= 1023 ? __longlong_as_double((long long) (k + 1023) << 52) : ldexp(1., k);
@@ -287,7 +293,7 @@ tc_projection_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_con
 				tmem_ld8(tmem + lane_base + (uint32_t) grp * kBN + seg * 8, v);
 #pragma unroll
 				for (int j = 0; j < 8; j++) {
-					const long long g = __float2ll_rn(v[j]);
+					const long long g = __float2int_rn(v[j]);   // an integer below 2^26: a 32-bit conversion
 					if (tt <= 4) hi[j] += g << (8 * (4 - tt));
 					else lo[j] += g << (8 * (8 - tt));
 				}
@@ -295,8 +301,8 @@ tc_projection_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_con
 #pragma unroll
 			for (int j = 0; j < 8; j++) {
 				double &x = acc[seg * 8 + j];
-				x = fma((double) hi[j], 0x1p-32, x);
-				if constexpr (S + 1 > 4) x = fma((double) lo[j], 0x1p-64, x);
+				x = fma(i64_to_double(hi[j]), 0x1p-32, x);
+				if constexpr (S + 1 > 4) x = fma(i64_to_double(lo[j]), 0x1p-64, x);
 			}
 		}
 		asm volatile("tcgen05.fence::before_thread_sync;");
