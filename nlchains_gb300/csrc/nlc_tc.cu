@@ -126,7 +126,8 @@ __device__ __forceinline__ void split7(double x, int e, uint16_t (&out)[7]) {
 		const int pos = 8 * (6 - i);
 		const long long sg = pos ? (F + (1ll << (pos - 1))) >> pos : F;
 		F -= sg << pos;
-		out[i] = uint16_t(__float_as_uint(float(sg)) >> 16);   // |sg| <= 256: exact in BF16
+		// |sg| <= 256: exact in BF16; converted from 32 bits (a 64-bit conversion uses the FP64 pipe)
+		out[i] = uint16_t(__float_as_uint(__int2float_rn(int(sg))) >> 16);
 	}
 }
 
