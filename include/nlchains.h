@@ -57,8 +57,9 @@ enum {
 	NLC_FLAG_SPLIT_KERNEL = 1,    /* --split_kernel (DNKG_FPUT_Toda.cpp:43): accepted; every length runs
 	                                 the resident (or, beyond one block, the windowed) integrator */
 	NLC_FLAG_NO_TUNE = 2,         /* skip the autotuner, use the heuristic launch shape */
-	NLC_FLAG_CANONICAL_SHAPE = 4, /* launch shape from the chain length alone (up to 8 sites per lane), so
-	                                 ensembles of equal length can share batched launches */
+	NLC_FLAG_CANONICAL_SHAPE = 4, /* launch shape from the chain length alone (up to 8 sites per lane, 16
+	                                 on a single warp), so ensembles of similar length can share batched
+	                                 launches */
 	NLC_FLAG_COMPACT_DIAG = 8,    /* fewer partial rows in the diagnostics (less device memory per plan) */
 	NLC_FLAG_SHARED_GPU = 16,     /* one work unit per block instead of a persistent grid: blocks retire as
 	                                 they finish, so launches on other streams interleave with this plan's */

@@ -208,7 +208,9 @@ bool finish_shape(const nlc_plan &P, int model, int variant, RealShape &s, int t
 // Canonical: the smallest group whose lanes hold at most 8 sites, from the chain length alone.
 RealShape canonical_shape(const nlc_plan &P, int model, int variant) {
 	for (auto c : shape_candidates(P.m.chain_length)) {
-		if (c.second > 8) continue;
+		// up to 8 sites per lane, or up to 16 on one warp rather than a block of more lanes (the
+		// block tier exchanges halos through shared memory with a barrier per sub-step)
+		if (c.second > (c.first == 32 ? 16 : 8)) continue;
 		RealShape s{};
 		s.lanes = c.first, s.sites = c.second;
 		if (finish_shape(P, model, variant, s, 128)) return s;
