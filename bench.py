@@ -219,23 +219,38 @@ def measure_e2e(w, steps, warmup, rank, local):
     host_in = torch.empty((copies, n, 2), dtype=torch.float64, pin_memory=True).numpy()
     host_out = torch.empty((copies, n, 2), dtype=torch.float64, pin_memory=True).numpy()
     host_in[...] = initial_state(w, copies, first_copy=rank * copies)
+    host_out2 = torch.empty((copies, n, 2), dtype=torch.float64, pin_memory=True).numpy()
     ctx = nlc.Context(local)
-    job = ctx.job(nlc.Model(w["model"], n, copies, w["dt"], **w["params"]), b)
+    # two jobs, each on its own stream: step i + 1's upload and integration run while step i's
+    # results are read back (every step still copies its input in and its state and energies out)
+    jobs = [ctx.job(nlc.Model(w["model"], n, copies, w["dt"], **w["params"]), b) for _ in range(2)]
+    outs = [host_out, host_out2]
 
-    def one_step():
-        job.upload(host_in)
+    def issue(i):
+        job = jobs[i % 2]
+        job.upload(host_in, wait=False)
         job.advance(b)
-        job.linenergies()
-        job.download(host_out)
+        job.sample_async(0)
 
-    for _ in range(warmup):
-        one_step()
+    def finish(i):
+        job = jobs[i % 2]
+        job.sample_wait(0)
+        job.download(outs[i % 2])
+
+    def run(count):
+        issue(0)
+        for i in range(count):
+            if i + 1 < count:
+                issue(i + 1)
+            finish(i)
+
+    run(max(warmup, 2))
     barrier()
     t0 = time.perf_counter()
-    for _ in range(steps):
-        one_step()
+    run(steps)
     t = float(allreduce([time.perf_counter() - t0], "max")[0])
-    job.close()
+    for job in jobs:
+        job.close()
     ctx.close()
     bi = host_in.nbytes
     bo = host_out.nbytes + (n + 2) * 8

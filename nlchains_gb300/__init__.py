@@ -286,11 +286,14 @@ class Job:
             lib().nlc_job_destroy(self.ctx._h, self.id)
             self.id = ctypes.c_uint64()
 
-    def upload(self, state):
+    def upload(self, state, wait=True):
+        """Copy the ensemble to the device.  wait=False returns at once (the copy is asynchronous
+        when `state` is pinned host memory, which must then stay alive until the job has used it)."""
         state = np.ascontiguousarray(state)
         assert state.nbytes == self.model.copies * self.model.chain_length * 16
         _check(lib().nlc_job_upload(self.ctx._h, self.id, state.ctypes.data_as(ctypes.c_void_p)))
-        _check(lib().nlc_job_wait(self.ctx._h, self.id, -1))
+        if wait:
+            _check(lib().nlc_job_wait(self.ctx._h, self.id, -1))
 
     def advance(self, steps):
         _check(lib().nlc_job_advance(self.ctx._h, self.id, int(steps)))
