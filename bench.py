@@ -431,7 +431,7 @@ def run_engine(args):
     peak = nlc.fp64_peak_tflops(ms=300.0)
     w = WORKLOAD
     r = measure_engine(w, args.steps, args.warmup, rank, world, local)
-    e2e = measure_e2e(w, max(2, args.steps // 2), 1, rank, local)
+    e2e = measure_e2e(w, max(4, args.steps), 2, rank, local)
     toda = measure_engine(TODA, max(2, args.steps // 2), 2, rank, world, local)
     others = {}
     for ow in OTHERS:

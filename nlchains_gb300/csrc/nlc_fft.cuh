@@ -1,12 +1,22 @@
 // Batched FP64 complex FFT in shared memory, one chain per team of threads (a warp or a block).
 //
-// Stockham autosort, decimation in frequency (C. Van Loan, "Computational Frameworks for the Fast
-// Fourier Transform", SIAM 1992, sec. 1.7): for each radix p of n = p_1 p_2 ... with the current
-// sub-length L (L = n before the first stage) and stride s (s = 1), every butterfly (q, t),
-// q < L/p, t < s, reads a_u = x[t + s (q + u L/p)], forms the p-point DFT, multiplies output v by
-// exp(-+2 pi i q v / L) and writes y[t + s (p q + v)]; then L /= p, s *= p.  The result lands in
-// natural order after the last stage, with no bit reversal.  Radices 4, 2, 3, 5 have dedicated
-// butterflies; any other prime radix uses a direct p-point DFT.
+// Stockham autosort, decimation in time (C. Van Loan, "Computational Frameworks for the Fast
+// Fourier Transform", SIAM 1992, sec. 1.7): for each radix p of len = p_1 p_2 ..., with Ns the
+// product of the radices already applied (1 before the first pass) and m = len / p, butterfly
+// b < m, q = b / Ns, k = b mod Ns, reads a_u = x[b + u m], forms the p-point DFT of a_u w^{uk},
+// w = exp(-+2 pi i / (Ns p)), and writes output v to y[q Ns p + k + v Ns]; then Ns *= p.  The
+// result lands in natural order after the last pass, with no bit reversal.
+//
+// Twiddled radix-4, -3 and -2 butterflies use the FMA factorisation of S. Goedecker ("Fast radix
+// 2, 3, 4, and 5 kernels for fast Fourier transformations on computers with overlapping
+// multiply-add instructions", SIAM J. Sci. Comput. 18(6), 1997): with w_u = c_u (1 + i t_u),
+// a_u w_u = c_u Z_u where Z_u = (x - t_u y, y + t_u x) takes two FMAs, and the c_u become the
+// multipliers of the FMAs that form the butterfly's sums.  A twiddled radix-4 butterfly takes 22
+// FP64 operations instead of 28 (three complex products and eight complex additions), radix 3 16
+// instead of 22, radix 2 6 instead of 8.  The per-pass tables of t_u, c_u and their ratios are
+// built on the host (fma_twiddle_entry).  Radix 5 multiplies its inputs by the twiddles and forms
+// the DFT with its own butterfly; any other prime radix forms the direct DFT with the twiddles
+// folded into the DFT's table index.
 //
 // Forward = exp(-2 pi i jk/n), unnormalised, as cuFFT / FFTW forward transforms in the reference.
 #pragma once
@@ -45,6 +55,16 @@ __device__ __forceinline__ double2 rot_mi(double2 a) {
 	return INV ? make_double2(-a.y, a.x) : make_double2(a.y, -a.x);
 }
 
+// a (1 + i t) (forward) or a (1 - i t) (inverse): two FMAs
+template <bool INV>
+__device__ __forceinline__ double2 ztan(double2 a, double t) {
+	return INV ? make_double2(dfma(a.y, t, a.x), dfma(-a.x, t, a.y)) : make_double2(dfma(-a.y, t, a.x), dfma(a.x, t, a.y));
+}
+// a + c z, a - c z
+__device__ __forceinline__ double2 fma2(double c, double2 z, double2 a) {
+	return make_double2(dfma(c, z.x, a.x), dfma(c, z.y, a.y));
+}
+
 // Stockham pass of length P.len on x (shared memory), y the ping-pong buffer.  t / T: this
 // thread's index / size of the team.  Returns the buffer holding the result.
 template <bool BLOCK, bool INV>
@@ -52,65 +72,103 @@ __device__ double2 *stockham_team(const FftPlanDev &P, double2 *x, double2 *y, i
 	const int n = P.len;
 	const double2 *__restrict__ tw = P.tw;
 	const FpOnes &k = P.k1;
-	int L = n, s = 1;
+	int Ns = 1;
 	for (int r = 0; r < P.nradix; r++) {
 		const int p = P.radix[r];
-		const int m = L / p;
-		const int tws = n / L;
-		const int nb = n / p;
+		const int m = n / p;
+		const double2 *__restrict__ g = P.gw + P.gw_off[r];
 		if (p == 4) {
-			for (int b = t; b < nb; b += T) {
-				const int q = b / s, tt = b - q * s;
-				const double2 a0 = x[tt + s * q], a1 = x[tt + s * (q + m)], a2 = x[tt + s * (q + 2 * m)],
-				              a3 = x[tt + s * (q + 3 * m)];
-				const double2 b0 = cadd(a0, a2, k), b1 = csub(a0, a2, k), b2 = cadd(a1, a3, k), b3 = rot_mi<INV>(csub(a1, a3, k));
-				double2 *o = y + tt + s * 4 * q;
-				o[0] = cadd(b0, b2, k);
-				if (q == 0) {
-					o[s] = cadd(b1, b3, k);
-					o[2 * s] = csub(b0, b2, k);
-					o[3 * s] = csub(b1, b3, k);
-				} else {
-					o[s] = cmul(cadd(b1, b3, k), twiddle<INV>(tw, q * tws), k);
-					o[2 * s] = cmul(csub(b0, b2, k), twiddle<INV>(tw, 2 * q * tws), k);
-					o[3 * s] = cmul(csub(b1, b3, k), twiddle<INV>(tw, 3 * q * tws), k);
+			if (Ns == 1) {
+				for (int b = t; b < m; b += T) {
+					const double2 a0 = x[b], a1 = x[b + m], a2 = x[b + 2 * m], a3 = x[b + 3 * m];
+					const double2 b0 = cadd(a0, a2, k), b1 = csub(a0, a2, k), b2 = cadd(a1, a3, k), b3 = rot_mi<INV>(csub(a1, a3, k));
+					double2 *o = y + 4 * b;
+					o[0] = cadd(b0, b2, k);
+					o[1] = cadd(b1, b3, k);
+					o[2] = csub(b0, b2, k);
+					o[3] = csub(b1, b3, k);
+				}
+			} else {
+				for (int b = t; b < m; b += T) {
+					const int q = b / Ns, kk = b - q * Ns;
+					const double2 a0 = x[b], a1 = x[b + m], a2 = x[b + 2 * m], a3 = x[b + 3 * m];
+					const double2 e0 = g[3 * kk], e1 = g[3 * kk + 1], e2 = g[3 * kk + 2];   // {t1,t2} {t3,c1} {c2,c3/c1}
+					const double2 z1 = ztan<INV>(a1, e0.x), z2 = ztan<INV>(a2, e0.y), z3 = ztan<INV>(a3, e1.x);
+					const double c1 = e1.y, c2 = e2.x, rho = e2.y;
+					// A_u = a_u w_u: A0 +- A2 = a0 +- c2 Z2, A1 +- A3 = c1 (Z1 +- (c3/c1) Z3)
+					const double2 b0 = fma2(c2, z2, a0), b1 = fma2(-c2, z2, a0);
+					const double2 p2 = fma2(rho, z3, z1), p3 = fma2(-rho, z3, z1);
+					// X1 = (A0 - A2) -+ i (A1 - A3), X3 = (A0 - A2) +- i (A1 - A3) (forward / inverse)
+					const double2 bm = make_double2(dfma(c1, p3.y, b1.x), dfma(-c1, p3.x, b1.y));   // b1 - i c1 p3
+					const double2 bp = make_double2(dfma(-c1, p3.y, b1.x), dfma(c1, p3.x, b1.y));   // b1 + i c1 p3
+					double2 *o = y + q * 4 * Ns + kk;
+					o[0] = fma2(c1, p2, b0);
+					o[Ns] = INV ? bp : bm;
+					o[2 * Ns] = fma2(-c1, p2, b0);
+					o[3 * Ns] = INV ? bm : bp;
 				}
 			}
 		} else if (p == 2) {
-			for (int b = t; b < nb; b += T) {
-				const int q = b / s, tt = b - q * s;
-				const double2 a0 = x[tt + s * q], a1 = x[tt + s * (q + m)];
-				double2 *o = y + tt + s * 2 * q;
-				o[0] = cadd(a0, a1, k);
-				o[s] = q == 0 ? csub(a0, a1, k) : cmul(csub(a0, a1, k), twiddle<INV>(tw, q * tws), k);
+			for (int b = t; b < m; b += T) {
+				const int q = b / Ns, kk = b - q * Ns;
+				const double2 a0 = x[b], a1 = x[b + m];
+				double2 *o = y + q * 2 * Ns + kk;
+				if (Ns == 1) {
+					o[0] = cadd(a0, a1, k);
+					o[Ns] = csub(a0, a1, k);
+				} else {
+					const double2 e = g[kk];   // {t1, c1}
+					const double2 z = ztan<INV>(a1, e.x);
+					o[0] = fma2(e.y, z, a0);
+					o[Ns] = fma2(-e.y, z, a0);
+				}
 			}
 		} else if (p == 3) {
-			const double sn = P.sin60;   // sin(2 pi / 3), a parameter-bank operand
-			for (int b = t; b < nb; b += T) {
-				const int q = b / s, tt = b - q * s;
-				const double2 a0 = x[tt + s * q], a1 = x[tt + s * (q + m)], a2 = x[tt + s * (q + 2 * m)];
-				const double2 t1 = cadd(a1, a2, k);
-				const double2 t2 = make_double2(dfma(t1.x, -P.half, a0.x), dfma(t1.y, -P.half, a0.y));
-				const double2 d = csub(a1, a2, k);
-				const double2 u = make_double2(fmul(sn, d.x, k), fmul(sn, d.y, k));
-				// forward: X1 = t2 - i u, X2 = t2 + i u
-				const double2 x1 = INV ? make_double2(fsub(t2.x, u.y, k), fadd(t2.y, u.x, k))
-				                       : make_double2(fadd(t2.x, u.y, k), fsub(t2.y, u.x, k));
-				const double2 x2 = INV ? make_double2(fadd(t2.x, u.y, k), fsub(t2.y, u.x, k))
-				                       : make_double2(fsub(t2.x, u.y, k), fadd(t2.y, u.x, k));
-				double2 *o = y + tt + s * 3 * q;
-				o[0] = cadd(a0, t1, k);
-				o[s] = q == 0 ? x1 : cmul(x1, twiddle<INV>(tw, q * tws), k);
-				o[2 * s] = q == 0 ? x2 : cmul(x2, twiddle<INV>(tw, 2 * q * tws), k);
+			for (int b = t; b < m; b += T) {
+				const int q = b / Ns, kk = b - q * Ns;
+				const double2 a0 = x[b], a1 = x[b + m], a2 = x[b + 2 * m];
+				double2 x0, xm, xp;   // X0, t2 - i u, t2 + i u
+				if (Ns == 1) {
+					const double sn = P.sin60;   // sin(2 pi / 3), a parameter-bank operand
+					const double2 t1 = cadd(a1, a2, k);
+					const double2 t2 = make_double2(dfma(t1.x, -P.half, a0.x), dfma(t1.y, -P.half, a0.y));
+					const double2 d = csub(a1, a2, k);
+					const double2 u = make_double2(fmul(sn, d.x, k), fmul(sn, d.y, k));
+					x0 = cadd(a0, t1, k);
+					xm = make_double2(fadd(t2.x, u.y, k), fsub(t2.y, u.x, k));
+					xp = make_double2(fsub(t2.x, u.y, k), fadd(t2.y, u.x, k));
+				} else {
+					const double2 e0 = g[3 * kk], e1 = g[3 * kk + 1], e2 = g[3 * kk + 2];   // {t1,t2} {c1,c2/c1} {c1/2, c1 sin60}
+					const double2 z1 = ztan<INV>(a1, e0.x), z2 = ztan<INV>(a2, e0.y);
+					// A1 +- A2 = c1 (Z1 +- (c2/c1) Z2)
+					const double2 ts = fma2(e1.y, z2, z1), d = fma2(-e1.y, z2, z1);
+					x0 = fma2(e1.x, ts, a0);
+					const double2 t2 = fma2(-e2.x, ts, a0);
+					xm = make_double2(dfma(e2.y, d.y, t2.x), dfma(-e2.y, d.x, t2.y));
+					xp = make_double2(dfma(-e2.y, d.y, t2.x), dfma(e2.y, d.x, t2.y));
+				}
+				// forward: X1 = t2 - i u, X2 = t2 + i u; the inverse the other way round
+				double2 *o = y + q * 3 * Ns + kk;
+				o[0] = x0;
+				o[Ns] = INV ? xp : xm;
+				o[2 * Ns] = INV ? xm : xp;
 			}
 		} else if (p == 5) {
 			// t1 = a1 + a4, t2 = a2 + a3, t3 = a1 - a4, t4 = a2 - a3;
 			// X1,4 = a0 + c1 t1 + c2 t2 -+ i (s1 t3 + s2 t4), X2,3 = a0 + c2 t1 + c1 t2 -+ i (s2 t3 - s1 t4)
-			// (forward; the inverse swaps the signs of i), c_j = cos(2 pi j/5), s_j = sin(2 pi j/5)
-			for (int b = t; b < nb; b += T) {
-				const int q = b / s, tt = b - q * s;
-				const double2 a0 = x[tt + s * q], a1 = x[tt + s * (q + m)], a2 = x[tt + s * (q + 2 * m)],
-				              a3 = x[tt + s * (q + 3 * m)], a4 = x[tt + s * (q + 4 * m)];
+			// (forward; the inverse swaps the signs of i), c_j = cos(2 pi j/5), s_j = sin(2 pi j/5),
+			// on the twiddled inputs a_u w^{uk}
+			const int stride = n / (Ns * 5);
+			for (int b = t; b < m; b += T) {
+				const int q = b / Ns, kk = b - q * Ns;
+				double2 a0 = x[b], a1 = x[b + m], a2 = x[b + 2 * m], a3 = x[b + 3 * m], a4 = x[b + 4 * m];
+				if (Ns > 1) {
+					const int e = kk * stride;
+					a1 = cmul(a1, twiddle<INV>(tw, e), k);
+					a2 = cmul(a2, twiddle<INV>(tw, 2 * e), k);
+					a3 = cmul(a3, twiddle<INV>(tw, 3 * e), k);
+					a4 = cmul(a4, twiddle<INV>(tw, 4 * e), k);
+				}
 				const double2 t1 = cadd(a1, a4, k), t2 = cadd(a2, a3, k), t3 = csub(a1, a4, k), t4 = csub(a2, a3, k);
 				const double2 b1 = make_double2(dfma(P.c52, t2.x, dfma(P.c51, t1.x, a0.x)),
 				                                dfma(P.c52, t2.y, dfma(P.c51, t1.y, a0.y)));
@@ -129,40 +187,36 @@ __device__ double2 *stockham_team(const FftPlanDev &P, double2 *x, double2 *y, i
 				                       : make_double2(fadd(b2.x, u2.y, k), fsub(b2.y, u2.x, k));
 				const double2 x3 = INV ? make_double2(fadd(b2.x, u2.y, k), fsub(b2.y, u2.x, k))
 				                       : make_double2(fsub(b2.x, u2.y, k), fadd(b2.y, u2.x, k));
-				double2 *o = y + tt + s * 5 * q;
+				double2 *o = y + q * 5 * Ns + kk;
 				o[0] = cadd(a0, cadd(t1, t2, k), k);
-				if (q == 0) {
-					o[s] = x1, o[2 * s] = x2, o[3 * s] = x3, o[4 * s] = x4;
-				} else {
-					o[s] = cmul(x1, twiddle<INV>(tw, q * tws), k);
-					o[2 * s] = cmul(x2, twiddle<INV>(tw, 2 * q * tws), k);
-					o[3 * s] = cmul(x3, twiddle<INV>(tw, 3 * q * tws), k);
-					o[4 * s] = cmul(x4, twiddle<INV>(tw, 4 * q * tws), k);
-				}
+				o[Ns] = x1, o[2 * Ns] = x2, o[3 * Ns] = x3, o[4 * Ns] = x4;
 			}
 		} else {
-			// direct p-point DFT: X_v = sum_u a_u W_p^{uv}, W_p^e = tw[(e mod p) n/p]
-			const int np = n / p;
-			for (int b = t; b < nb; b += T) {
-				const int q = b / s, tt = b - q * s;
+			// direct p-point DFT of the twiddled inputs: X_v = sum_u a_u w^{uk} W_p^{uv}
+			// = sum_u a_u tw[u (k + v Ns) n / (Ns p) mod n]
+			const int stride = n / (Ns * p);
+			for (int b = t; b < m; b += T) {
+				const int q = b / Ns, kk = b - q * Ns;
 				for (int v = 0; v < p; v++) {
+					const int step = int((long long) (kk + v * Ns) * stride % n);
 					double re = 0., im = 0.;
+					int e = 0;
 					for (int u = 0; u < p; u++) {
-						const double2 a = x[tt + s * (q + u * m)];
-						const double2 w = twiddle<INV>(tw, (u * v) % p * np);
+						const double2 a = x[b + u * m];
+						const double2 w = twiddle<INV>(tw, e);
 						re = dfma(a.x, w.x, dfma(-a.y, w.y, re));
 						im = dfma(a.x, w.y, dfma(a.y, w.x, im));
+						e += step;
+						if (e >= n) e -= n;
 					}
-					double2 out = make_double2(re, im);
-					if (q != 0 && v != 0) out = cmul(out, twiddle<INV>(tw, q * v * tws), k);
-					y[tt + s * (p * q + v)] = out;
+					y[q * p * Ns + kk + v * Ns] = make_double2(re, im);
 				}
 			}
 		}
 		team_sync<BLOCK>();
 		double2 *sw = x;
 		x = y, y = sw;
-		L = m, s *= p;
+		Ns *= p;
 	}
 	return x;
 }

@@ -45,7 +45,11 @@ struct FftTables {
 	bool bluestein = false;
 	std::vector<int> radices;
 	std::vector<double> tw, chirp, bf, bi;   // interleaved re/im
+	std::vector<double> gw;    // FMA-form twiddle entries of the radix-2/3/4 passes (fma_twiddle_entry)
+	std::vector<int> gw_off;   // per pass: offset of its entries in gw, in double2 units
 };
+// FMA-form twiddle entries of the decimation-in-time passes of `radices`.
+void fft_fma_twiddles(const std::vector<int> &radices, std::vector<double> &gw, std::vector<int> &off);
 FftTables fft_tables(uint32_t n, uint32_t smem_len, uint32_t max_len, bool convolution);
 // the longest padded length of the FFT tables (2^18 >= 2 x 65535 - 1: any chain length of the
 // reference's 16-bit --chain_length)

@@ -119,6 +119,8 @@ struct FftPlanDev {
 	int nradix;
 	int radix[kMaxRadices];  // radices of len
 	const double2 *tw;     // tw[e] = exp(-2 pi i e / len), device
+	const double2 *gw;     // FMA-form twiddle entries of the radix-2/3/4 passes (fma_twiddle_entry), device
+	int gw_off[kMaxRadices];  // offset of pass r's entries in gw, in double2 units
 	int bluestein;         // 1: chirp-z transform through a length-m cyclic convolution
 	const double2 *chirp;  // exp(-i pi j^2 / n), j < n
 	const double2 *bf;     // FFT_m(b) / m, b_j = exp(+i pi j^2 / n) wrapped (forward transforms)
@@ -142,6 +144,31 @@ struct DiagArgs {
 	double2 *gscratch;       // block teams whose buffers exceed shared memory: [blocks][2][len]
 	int proj_chunk;          // dDNKG: sites per shared-memory chunk of the projection
 };
+
+// FMA-form twiddles of a decimation-in-time pass (nlc_fft.cuh): pass radix p in {2, 3, 4} after Ns
+// points, entry k < Ns.  With theta_u = 2 pi u k / (Ns p), c_u = cos theta_u and the forward
+// twiddle w_u = exp(-i theta_u) = c_u (1 + i t_u), t_u = -tan theta_u, the entry holds
+//   p = 4: {t1, t2}, {t3, c1}, {c2, c3 / c1}
+//   p = 3: {t1, t2}, {c1, c2 / c1}, {c1 / 2, c1 sin(2 pi / 3)}
+//   p = 2: {t1, c1}
+// (fma_twiddle_double2s(p) double2s each), from cu[u] = cos theta_u and s[u] = sin theta_u,
+// u = 1 .. p - 1.  A cosine near zero makes t_u large and c_u small; their product still reproduces s_u to rounding,
+// so the butterfly's error stays relative to its inputs.  An exactly zero cosine (theta = pi/2) is
+// replaced by 2^-60: c t = -s stays exact and the real part left behind, 2^-60, is below rounding.
+__host__ __device__ inline int fma_twiddle_double2s(int p) { return p == 2 ? 1 : (p == 3 || p == 4) ? 3 : 0; }
+__host__ __device__ inline void fma_twiddle_entry(int p, const double *cu, const double *s, double *out) {
+	double c[4];
+	for (int u = 0; u < 4; u++) c[u] = (cu[u] < 0x1p-60 && cu[u] > -0x1p-60) ? (cu[u] < 0 ? -0x1p-60 : 0x1p-60) : cu[u];
+	if (p == 4) {
+		out[0] = -s[1] / c[1], out[1] = -s[2] / c[2], out[2] = -s[3] / c[3], out[3] = c[1];
+		out[4] = c[2], out[5] = c[3] / c[1];
+	} else if (p == 3) {
+		out[0] = -s[1] / c[1], out[1] = -s[2] / c[2], out[2] = c[1], out[3] = c[2] / c[1];
+		out[4] = 0.5 * c[1], out[5] = c[1] * 0.86602540378443864676;
+	} else if (p == 2) {
+		out[0] = -s[1] / c[1], out[1] = c[1];
+	}
+}
 
 cudaError_t launch_linenergies_partials(const DiagArgs &a, const void *state, int blocks, int threads,
                                         size_t smem, int team_block, cudaStream_t stream);

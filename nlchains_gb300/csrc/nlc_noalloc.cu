@@ -41,14 +41,31 @@ struct DeviceSetup {
 std::mutex g_setup_mutex;
 DeviceSetup g_setup[kMaxDevices];
 
-// twiddles exp(-2 pi i e/n) and the per-mode coefficients: (omega+1)/2, (omega-1)/2 for the real
-// models, omega for DNLS (omega as in DNKG_FPUT_Toda/dispersion.cpp:9-16, DNLS/dispersion.cpp:10-17)
-__global__ void noalloc_tables_kernel(uint32_t n, int model, double m, double2 *tw, double *ca, double *cb) {
+// twiddles exp(-2 pi i e/n), the FMA-form twiddle entries of the radix-2/3/4 passes (entry e of
+// every pass after more than e points) and the per-mode coefficients: (omega+1)/2, (omega-1)/2 for
+// the real models, omega for DNLS (omega as in DNKG_FPUT_Toda/dispersion.cpp:9-16,
+// DNLS/dispersion.cpp:10-17)
+__global__ void noalloc_tables_kernel(uint32_t n, int model, double m, const FftPlanDev f, double2 *tw, double2 *gw,
+                                      double *ca, double *cb) {
 	const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
 	if (e >= n) return;
 	double s, c;
 	sincospi(2. * e / n, &s, &c);
 	tw[e] = make_double2(c, -s);
+	unsigned long long ns = 1;
+	for (int r = 0; r < f.nradix; r++) {
+		const int p = f.radix[r];
+		const int per = fma_twiddle_double2s(p);
+		if (ns > 1 && per && e < ns) {
+			const unsigned long long span = ns * (unsigned long long) p;
+			double cu[4] = {1., 1., 1., 1.}, su[4] = {0., 0., 0., 0.}, v[6];
+			for (int u = 1; u < p; u++) sincospi(2. * double((u * (unsigned long long) e) % span) / double(span), &su[u], &cu[u]);
+			fma_twiddle_entry(p, cu, su, v);
+			double2 *o = gw + f.gw_off[r] + (size_t) per * e;
+			for (int i = 0; i < per; i++) o[i] = make_double2(v[2 * i], v[2 * i + 1]);
+		}
+		ns *= (unsigned long long) p;
+	}
 	const double s2 = 2. * sinpi(double(e) / n);
 	if (model == NLC_DNLS) {
 		ca[e] = s2 * s2;
@@ -136,12 +153,24 @@ extern "C" int nlc_linenergies_noalloc(int32_t model, uint32_t chain_length, uin
 	g.fft.n = int(n);
 	g.fft.len = int(n);   // direct passes only: the static scratch holds no Bluestein tables
 	if (fill_radices(n, g.fft)) return set_error(NLC_EINVAL, "nlc_linenergies_noalloc: too many prime factors");
-	// scratch layout: [twiddles 2n][coef a n][coef b n][partial rows rows x n]
+	// offsets of the FMA-form twiddle entries: Ns entries for each radix-2/3/4 pass after Ns > 1
+	// points, at most 3 n double2s in all (the Ns of the passes sum to less than n)
+	{
+		int off = 0;
+		unsigned long long ns = 1;
+		for (int r = 0; r < g.fft.nradix; r++) {
+			g.fft.gw_off[r] = off;
+			if (ns > 1) off += fma_twiddle_double2s(g.fft.radix[r]) * int(ns);
+			ns *= (unsigned long long) g.fft.radix[r];
+		}
+	}
+	// scratch layout: [twiddles 2n][FMA-form twiddles 6n][coef a n][coef b n][partial rows rows x n]
 	double *base = S->scratch;
 	double2 *tw = reinterpret_cast<double2 *>(base);
-	double *ca = base + 2 * size_t(n), *cb = ca + n;
+	double2 *gw = tw + n;
+	double *ca = base + 8 * size_t(n), *cb = ca + n;
 	double *rows_base = cb + n;
-	const size_t rows_cap = (kNoAllocScratchDoubles - 4 * size_t(n)) / n;
+	const size_t rows_cap = (kNoAllocScratchDoubles - 10 * size_t(n)) / n;
 	const int team_block = n > 1024;
 	const int teams = team_block ? 1 : 4;
 	const int threads = team_block ? 256 : 128;
@@ -151,13 +180,14 @@ extern "C" int nlc_linenergies_noalloc(int32_t model, uint32_t chain_length, uin
 	blocks = std::min<unsigned long long>(blocks, rows_cap / teams);
 	if (!blocks) return set_error(NLC_EINVAL, "nlc_linenergies_noalloc: scratch too small for this chain_length");
 	g.fft.tw = tw;
+	g.fft.gw = gw;
 	if (model == NLC_DNLS) g.omega = ca;
 	else g.coef_a = ca, g.coef_b = cb;
 	g.partials = rows_base;
 
 	cudaStream_t st = static_cast<cudaStream_t>(stream);
 	count_launch();
-	noalloc_tables_kernel<<<(n + 127) / 128, 128, 0, st>>>(n, model, model == NLC_DNKG ? m : 0., tw, ca, cb);
+	noalloc_tables_kernel<<<(n + 127) / 128, 128, 0, st>>>(n, model, model == NLC_DNKG ? m : 0., g.fft, tw, gw, ca, cb);
 	if ((rc = cuda_status(cudaGetLastError(), "nlc_linenergies_noalloc tables launch"))) return rc;
 	if ((rc = cuda_status(launch_linenergies_partials(g, state_dev, int(blocks), threads, smem, team_block, st),
 	                      "nlc_linenergies_noalloc launch")))

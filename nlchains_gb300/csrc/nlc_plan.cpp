@@ -368,6 +368,12 @@ int setup_fft(nlc_plan &P, FftPlanDev &f, bool convolution) {
 	int rc = P.upload(&d, reinterpret_cast<const double2 *>(T.tw.data()), T.len);
 	if (rc) return rc;
 	f.tw = d;
+	double2 *g = nullptr;
+	if (!T.gw.empty()) {
+		if ((rc = P.upload(&g, reinterpret_cast<const double2 *>(T.gw.data()), T.gw.size() / 2))) return rc;
+	}
+	f.gw = g;
+	for (size_t i = 0; i < T.gw_off.size(); i++) f.gw_off[i] = T.gw_off[i];
 	if (T.bluestein) {
 		double2 *c = nullptr, *bf = nullptr, *bi = nullptr;
 		if ((rc = P.upload(&c, reinterpret_cast<const double2 *>(T.chirp.data()), n))) return rc;

@@ -149,6 +149,31 @@ std::vector<double> fft_twiddles(uint32_t n) {
 	return tw;
 }
 
+void fft_fma_twiddles(const std::vector<int> &radices, std::vector<double> &gw, std::vector<int> &off) {
+	gw.clear();
+	off.assign(radices.size(), 0);
+	uint64_t ns = 1;
+	for (size_t r = 0; r < radices.size(); r++) {
+		const int p = radices[r];
+		off[r] = int(gw.size() / 2);
+		const int per = fma_twiddle_double2s(p);
+		if (ns > 1 && per) {
+			const uint64_t span = ns * uint64_t(p);
+			for (uint64_t k = 0; k < ns; k++) {
+				double c[4] = {1., 1., 1., 1.}, s[4] = {0., 0., 0., 0.}, e[6];
+				for (int u = 1; u < p; u++) {
+					// theta_u = 2 pi (u k mod span) / span, the argument reduced exactly
+					const double a = 2 * M_PI * double((uint64_t(u) * k) % span) / double(span);
+					c[u] = std::cos(a), s[u] = std::sin(a);
+				}
+				fma_twiddle_entry(p, c, s, e);
+				gw.insert(gw.end(), e, e + 2 * per);
+			}
+		}
+		ns *= uint64_t(p);
+	}
+}
+
 namespace {
 
 // Fork-join pool for the O(n^3) loops of the eigensolver: the calling thread plus helpers, each
@@ -233,11 +258,11 @@ uint32_t largest_prime_factor(uint32_t n) {
 // direct p-point DFT of any other radix (4p for the sums plus a twiddle product)
 double pass_cost(int r) {
 	switch (r) {
-		case 4: return 7.;
-		case 2: return 4.;
-		case 3: return 26. / 3;
+		case 4: return 22. / 4;
+		case 2: return 6. / 2;
+		case 3: return 16. / 3;
 		case 5: return 52. / 5;
-		default: return 4. * r + 4;
+		default: return 4. * r;
 	}
 }
 
@@ -359,6 +384,7 @@ FftTables fft_tables(uint32_t n, uint32_t smem_len, uint32_t max_len, bool convo
 	}
 	T.radices = fft_radices(T.len);
 	T.tw = fft_twiddles(T.len);
+	fft_fma_twiddles(T.radices, T.gw, T.gw_off);
 	if (!T.bluestein) return T;
 	const uint32_t m = T.len;
 	T.chirp.resize(2 * size_t(n));
