@@ -221,14 +221,18 @@ def measure_e2e(w, steps, warmup, rank, local):
     host_in[...] = initial_state(w, copies, first_copy=rank * copies)
     host_out2 = torch.empty((copies, n, 2), dtype=torch.float64, pin_memory=True).numpy()
     ctx = nlc.Context(local)
-    # two jobs, each on its own stream: step i + 1's upload and integration run while step i's
-    # results are read back (every step still copies its input in and its state and energies out)
+    # two jobs, each on its own stream: step i + 1's upload runs during step i's integration and
+    # step i's read-back during step i + 1's (every step still copies its input in and its state
+    # and energies out); the integrations stay in sequence (Job.after), so that step i + 1's
+    # persistent launch does not hold the SMs that step i's diagnostics wait for
     jobs = [ctx.job(nlc.Model(w["model"], n, copies, w["dt"], **w["params"]), b) for _ in range(2)]
     outs = [host_out, host_out2]
 
     def issue(i):
         job = jobs[i % 2]
         job.upload(host_in, wait=False)
+        if i:
+            job.after(jobs[(i - 1) % 2])
         job.advance(b)
         job.sample_async(0)
 

@@ -213,6 +213,12 @@ int nlc_job_sample_wait(nlc_ctx *ctx, uint64_t job, int32_t slot, double *lin, d
                         void *host_state, int32_t timeout_ms);
 /* wait for the job's queued work, at most timeout_ms (< 0: no limit); NLC_ETIMEDOUT if not done */
 int nlc_job_wait(nlc_ctx *ctx, uint64_t job, int32_t timeout_ms);
+/* order two jobs of one context on the device, without blocking the host: work enqueued on `job`
+ * after this call starts only once everything enqueued on `after_job` so far has completed.  Two
+ * jobs that take turns on one GPU (one uploading or reading back while the other integrates) keep
+ * their integrations in sequence this way, so that one job's persistent launch does not take the
+ * SMs that the other job's diagnostics are waiting for. */
+int nlc_job_after(nlc_ctx *ctx, uint64_t job, uint64_t after_job);
 /* device pointer of the job's state, for callers that mix levels 1 and 2 */
 int nlc_job_state_ptr(nlc_ctx *ctx, uint64_t job, void **state_dev);
 

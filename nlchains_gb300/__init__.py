@@ -39,7 +39,7 @@ EXPORTS = (
     "nlc_version", "nlc_kernel_launches", "nlc_fp64_peak", "nlc_linenergies_noalloc",
     "nlc_server_create", "nlc_server_destroy", "nlc_server_submit", "nlc_server_poll", "nlc_server_wait",
     "nlc_server_result", "nlc_entropies", "nlc_job_sample_async", "nlc_job_sample_wait", "nlc_energies",
-    "nlc_job_energies", "nlc_job_step_async",
+    "nlc_job_energies", "nlc_job_step_async", "nlc_job_after",
 )
 
 
@@ -104,6 +104,7 @@ def lib():
         "nlc_job_linenergies": ([vp, u64, dp, dp, dp], i32),
         "nlc_job_download": ([vp, u64, vp], i32),
         "nlc_job_wait": ([vp, u64, i32], i32),
+        "nlc_job_after": ([vp, u64, u64], i32),
         "nlc_job_state_ptr": ([vp, u64, P(vp)], i32),
         "nlc_program_run": ([ctypes.c_int, P(ctypes.c_char_p)], ctypes.c_int),
         "nlc_last_error": ([], ctypes.c_char_p),
@@ -300,6 +301,10 @@ class Job:
 
     def wait(self, timeout_ms=-1):
         _check(lib().nlc_job_wait(self.ctx._h, self.id, int(timeout_ms)))
+
+    def after(self, other):
+        """Work enqueued on this job from now on starts after everything queued on `other` so far."""
+        _check(lib().nlc_job_after(self.ctx._h, self.id, other.id))
 
     def linenergies(self):
         """(linenergies[n], WT entropy, information entropy); raises NlcError(EBLOWUP) on blow-up."""

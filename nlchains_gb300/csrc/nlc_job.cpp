@@ -33,6 +33,7 @@ struct Job {
 	double2 *h_state_slot[2] = {nullptr, nullptr};
 	cudaEvent_t ev_slot[2] = {nullptr, nullptr};
 	bool slot_state[2] = {false, false};
+	cudaEvent_t ev_order = nullptr;   // marks the end of the queued work for jobs ordered after this one
 	// one batch + its sample as a CUDA graph, per [slot][copy_state], captured on first use
 	cudaGraphExec_t step_exec[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
 	uint64_t step_kernels[2][2] = {{0, 0}, {0, 0}};
@@ -52,6 +53,7 @@ struct Job {
 			cudaFreeHost(h_state_slot[i]);
 			if (ev_slot[i]) cudaEventDestroy(ev_slot[i]);
 		}
+		if (ev_order) cudaEventDestroy(ev_order);
 		if (stream) cudaStreamDestroy(stream);
 	}
 };
@@ -284,6 +286,19 @@ extern "C" int nlc_job_sample_wait(nlc_ctx *ctx, uint64_t id, int32_t slot, doub
 	if (!std::isfinite(h[n]) || !std::isfinite(h[n + 1]))
 		return set_error(NLC_EBLOWUP, "non-finite entropy (blow-up or vanishing mode energy)");
 	return NLC_OK;
+}
+
+extern "C" int nlc_job_after(nlc_ctx *ctx, uint64_t id, uint64_t after_id) {
+	Job *J = find_job(ctx, id);
+	Job *A = find_job(ctx, after_id);
+	if (!J || !A) return set_error(NLC_ENOTFOUND, "no such job");
+	if (J == A) return NLC_OK;   // a job's own work is in order already
+	int rc;
+	if (!A->ev_order &&
+	    (rc = cuda_status(cudaEventCreateWithFlags(&A->ev_order, cudaEventDisableTiming), "cudaEventCreate")))
+		return rc;
+	if ((rc = cuda_status(cudaEventRecord(A->ev_order, A->stream), "cudaEventRecord"))) return rc;
+	return cuda_status(cudaStreamWaitEvent(J->stream, A->ev_order, 0), "cudaStreamWaitEvent");
 }
 
 extern "C" int nlc_job_wait(nlc_ctx *ctx, uint64_t id, int32_t timeout_ms) {

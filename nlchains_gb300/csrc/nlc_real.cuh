@@ -27,12 +27,17 @@
 //   Toda 13 (12 with 2 alpha == 1) including the 8-operation table exp.
 #pragma once
 
+#include <type_traits>
+
 #include "nlc_device.cuh"
 #include "nlc_internal.h"
 
 namespace nlc {
 
-// Halo exchange around the ring of G lanes that hold one chain.
+// Halo exchange around the ring of G lanes that hold one chain.  SHFL: G <= 32, the whole ring in
+// one warp (width-G shuffles); otherwise warp-boundary halos go through shared memory.  The kernel
+// picks the form once per launch, outside the step loop, so that for SHFL the seven sub-steps of a
+// step are one straight-line block the compiler can schedule across.
 struct Ring {
 	int G;          // lanes per chain
 	int lane;       // lane index within the chain
@@ -43,8 +48,9 @@ struct Ring {
 	int parity;
 
 	// value of lane (lane - 1) mod G
+	template <bool SHFL>
 	__device__ __forceinline__ double from_left(double v) {
-		if (G <= 32) return __shfl_sync(0xffffffffu, v, (lane + G - 1) & (G - 1), G);
+		if constexpr (SHFL) return __shfl_sync(0xffffffffu, v, (lane + G - 1) & (G - 1), G);
 		double a = __shfl_sync(0xffffffffu, v, (wl + 31) & 31);
 		double *buf = xbuf + parity * 2 * W;
 		if (wl == 31) buf[warp] = v;
@@ -55,8 +61,9 @@ struct Ring {
 	}
 
 	// value of lane (lane + 1) mod G
+	template <bool SHFL>
 	__device__ __forceinline__ double from_right(double v) {
-		if (G <= 32) return __shfl_sync(0xffffffffu, v, (lane + 1) & (G - 1), G);
+		if constexpr (SHFL) return __shfl_sync(0xffffffffu, v, (lane + 1) & (G - 1), G);
 		double a = __shfl_sync(0xffffffffu, v, (wl + 1) & 31);
 		double *buf = xbuf + parity * 2 * W + W;
 		if (wl == 0) buf[warp] = v;
@@ -67,8 +74,9 @@ struct Ring {
 	}
 
 	// both directions with a single barrier: left <- lane-1's `to_right`, right <- lane+1's `to_left`
+	template <bool SHFL>
 	__device__ __forceinline__ void both(double to_right, double to_left, double &left, double &right) {
-		if (G <= 32) {
+		if constexpr (SHFL) {
 			left = __shfl_sync(0xffffffffu, to_right, (lane + G - 1) & (G - 1), G);
 			right = __shfl_sync(0xffffffffu, to_left, (lane + 1) & (G - 1), G);
 			return;
@@ -204,6 +212,8 @@ __global__ void real_move_kernel_t(double2 *__restrict__ state, const RealArgs a
 		}
 
 		const double cd_lead = (seg & NLC_SEG_CONTINUE) ? a.cd0_merged : a.cd[0];
+		auto integrate = [&](auto shfl_tag) {
+		constexpr bool SHFL = decltype(shfl_tag)::value;
 		for (uint32_t i = 0; i < steps; i++) {
 #pragma unroll
 			for (int k = 0; k < 7; k++) {
@@ -214,7 +224,7 @@ __global__ void real_move_kernel_t(double2 *__restrict__ state, const RealArgs a
 
 				if constexpr (MODEL == NLC_DNKG || MODEL == NLC_DDNKG) {
 					double l, r;
-					ring.both(fl ? x[E] : x[E - 1], x[1], l, r);
+					ring.template both<SHFL>(fl ? x[E] : x[E - 1], x[1], l, r);
 					x[0] = l, x[E + 1] = r;
 					if (!fl) x[E] = r;
 #pragma unroll
@@ -230,19 +240,22 @@ __global__ void real_move_kernel_t(double2 *__restrict__ state, const RealArgs a
 						p[j - 1] = dfma(a.nck[k], v, p[j - 1]);
 					}
 				} else {
-					const double r = ring.from_right(x[1]);
+					const double r = ring.template from_right<SHFL>(x[1]);
 					x[E + 1] = r;
 					if (!fl) x[E] = r;
 					double g[E + 1];
 #pragma unroll
 					for (int j = 1; j <= E; j++) g[j] = bond_force<MODEL, VAR>(fsub(x[j + 1], x[j], a.k1), a, s_tab);
-					g[0] = ring.from_left(fl ? g[E] : g[E - 1]);
+					g[0] = ring.template from_left<SHFL>(fl ? g[E] : g[E - 1]);
 #pragma unroll
 					for (int j = 1; j <= E; j++) p[j - 1] = dfma(a.ck[k], fsub(g[j], g[j - 1], a.k1), p[j - 1]);
 				}
 				if (!fl) p[E - 1] = 0.;   // the slot past a short lane's last site stays inert
 			}
 		}
+		};
+		if (G <= 32) integrate(std::true_type{});
+		else integrate(std::false_type{});
 
 		if (active) {
 			const bool open = seg & NLC_SEG_OPEN;

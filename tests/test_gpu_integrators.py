@@ -168,6 +168,49 @@ def test_pipelined_sampling_equals_synchronous(gpu):
     ctx.close()
 
 
+def test_two_jobs_taking_turns(gpu):
+    """Two jobs alternating as a double-buffered end-to-end loop does (upload without waiting, the
+    integration ordered after the other job's by nlc_job_after, sample, read back): every step's
+    state and sample equal the synchronous single-job results; unknown job ids are rejected."""
+    n, copies, b, rounds = 64, 4096, 20, 5
+    model = gpu.Model("DNKG", n, copies, 0.05, m=1.0, beta=1.0)
+    inputs = [0.3 * np.random.default_rng(10 + r).standard_normal((copies, n, 2)) for r in range(rounds)]
+    ctx = gpu.Context(0)
+    ref = ctx.job(model, b)
+    exp = []
+    for st in inputs:
+        ref.upload(st)
+        ref.advance(b)
+        lin, wt, inf = ref.linenergies()
+        exp.append((lin, wt, inf, ref.download()))
+    jobs = [ctx.job(model, b) for _ in range(2)]
+    ins = [np.ascontiguousarray(st) for st in inputs]
+    got = []
+
+    def issue(i):
+        job = jobs[i % 2]
+        job.upload(ins[i], wait=False)
+        if i:
+            job.after(jobs[(i - 1) % 2])
+        job.advance(b)
+        job.sample_async(0)
+
+    issue(0)
+    for i in range(rounds):
+        if i + 1 < rounds:
+            issue(i + 1)
+        lin, wt, inf, _ = jobs[i % 2].sample_wait(0)
+        got.append((lin, wt, inf, jobs[i % 2].download()))
+    for (el, ew, ei, es), (gl, gw, gi, gs) in zip(exp, got):
+        assert np.array_equal(el, gl) and ew == gw and ei == gi and np.array_equal(es, gs)
+    with pytest.raises(gpu.NlcError) as e:
+        gpu._check(gpu.lib().nlc_job_after(ctx._h, jobs[0].id, 987654321))
+    assert e.value.code == gpu.ENOTFOUND
+    for job in jobs + [ref]:
+        job.close()
+    ctx.close()
+
+
 @pytest.mark.parametrize("name,n,params,window", [
     ("FPUT", 64, dict(alpha=0.0, beta=1.0), None),
     ("DNLS", 97, dict(beta=1.0), None),
