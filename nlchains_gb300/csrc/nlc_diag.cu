@@ -14,6 +14,8 @@
 // partial row, and a single-block finish kernel sums the rows in row order, normalises, and
 // computes the WT / information entropies (results_entropy.cpp:21-46).  Results are therefore
 // identical from run to run on a given GPU.
+#include <algorithm>
+
 #include "nlc_fft.cuh"
 
 namespace nlc {
@@ -238,7 +240,41 @@ __global__ void lin_finish_entropy_kernel(const FinishArgs a, int blocks) {
 	a.entropies[1] = normalization * (sel + lognorm * se);
 }
 
-cudaError_t launch_linenergies_finish(const FinishArgs &a, cudaStream_t stream) {
+// Pre-reduction of many partial rows: block (x, y) adds rows [y per_slice, (y + 1) per_slice) of
+// the modes of tile x in row order, so that the finish reads one row per slice.  Every sum keeps a
+// fixed order: the result is identical on every run.
+__global__ void lin_rows_kernel(const double *__restrict__ partials, int rows, uint32_t n, int per_slice,
+                                double *__restrict__ out) {
+	const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+	if (k >= n) return;
+	const int r0 = int(blockIdx.y) * per_slice, r1 = min(rows, r0 + per_slice);
+	double v = 0.;
+	for (int r = r0; r < r1; r++) v = dadd(v, partials[(size_t) r * n + k]);
+	out[(size_t) blockIdx.y * n + k] = v;
+}
+
+constexpr int kRowsPerSliceMin = 8;
+
+int finish_row_slices(uint32_t n, int rows, int sms) {
+	if (rows < 8 * kRowsPerSliceMin) return 0;
+	const int tiles = int((n + kFinishModesPerBlock - 1) / kFinishModesPerBlock);
+	const int want = (2 * sms + tiles - 1) / tiles;   // about two blocks per SM
+	const int slices = std::min(want, (rows + kRowsPerSliceMin - 1) / kRowsPerSliceMin);
+	return slices >= 2 ? slices : 0;
+}
+
+cudaError_t launch_linenergies_finish(const FinishArgs &in, cudaStream_t stream) {
+	FinishArgs a = in;
+	if (a.row_slices && a.row_slice_cap >= 2 && a.nblocks >= 8 * kRowsPerSliceMin) {
+		const int per_slice = (a.nblocks + a.row_slice_cap - 1) / a.row_slice_cap;
+		const int slices = (a.nblocks + per_slice - 1) / per_slice;
+		const int threads = int(std::min<uint32_t>(kFinishModesPerBlock, (a.n + 31) / 32 * 32));
+		count_launch();
+		lin_rows_kernel<<<dim3((a.n + threads - 1) / threads, slices), threads, 0, stream>>>(a.partials, a.nblocks, a.n,
+		                                                                                   per_slice, a.row_slices);
+		a.partials = a.row_slices;
+		a.nblocks = slices;
+	}
 	if (a.block_sums && a.n > (uint32_t) kFinishModesPerBlock) {
 		const int blocks = int((a.n + kFinishModesPerBlock - 1) / kFinishModesPerBlock);
 		count_launch(2);

@@ -185,7 +185,12 @@ struct FinishArgs {
 	double *entropies;        // out [2] or NULL
 	double *block_sums;       // [ceil(n / 256)][4] scratch: with it, chains longer than 256 sites
 	                          // are finished by a grid over the modes instead of one block
+	double *row_slices;       // [row_slice_cap][n] scratch: with it, many partial rows are first
+	int row_slice_cap;        // added in slices by a grid over (mode tiles x slices)
 };
+// slices of the partial rows for a finish of n modes over `rows` rows on `sms` SMs: 0 when the
+// rows go to the finish directly
+int finish_row_slices(uint32_t n, int rows, int sms);
 cudaError_t launch_linenergies_finish(const FinishArgs &a, cudaStream_t stream);
 constexpr int kFinishModesPerBlock = 256;
 

@@ -110,6 +110,8 @@ struct nlc_plan {
 	size_t device_bytes = 0;
 	unsigned long long *d_counter = nullptr;
 	double *d_partials = nullptr;
+	double *d_row_slices = nullptr;   // pre-reduced partial rows (finish_row_slices)
+	int row_slice_cap = 0;
 	double *d_block_sums = nullptr;   // entropy sums of the mode blocks (chains above 256 sites)
 	uint8_t *d_mask = nullptr;
 
@@ -250,7 +252,8 @@ struct TuneKey {
 std::mutex g_tune_mutex;
 std::map<TuneKey, RealShape> g_tune_cache;
 
-// Time every launchable (G, threads) shape on a zero ensemble for a few steps; keep the fastest.
+// Time every launchable (G, threads) shape on a zero ensemble for a few steps (best of three
+// launches after a warm-up one); keep the fastest.
 // Results are cached per (device, model, variant, n, copies) for the life of the process.
 RealShape autotune_shape(nlc_plan &P, int model, int variant) {
 	const TuneKey key{P.device, model, variant, P.m.chain_length, P.m.copies};
@@ -273,7 +276,10 @@ RealShape autotune_shape(nlc_plan &P, int model, int variant) {
 	cudaEventCreate(&e0);
 	cudaEventCreate(&e1);
 	RealArgs a = P.ra;
-	a.steps = 2;
+	// about 2e7 site-steps per timed launch (2 .. 100 steps): small ensembles would otherwise time
+	// launches of a few microseconds, where the launch itself decides the ranking
+	const double sites = double(P.m.chain_length) * double(P.m.copies);
+	a.steps = uint32_t(std::max(2., std::min(100., std::ceil(2e7 / sites))));
 	RealShape best = fallback;
 	float best_ms = 1e30f;
 	for (auto c : shape_candidates(P.m.chain_length)) {
@@ -285,7 +291,7 @@ RealShape autotune_shape(nlc_plan &P, int model, int variant) {
 			if (c.first <= 32 && s.threads != std::max(tpb, s.lanes)) continue;
 			float ms = 1e30f;
 			bool ok = true;
-			for (int rep = 0; rep < 3 && ok; rep++) {
+			for (int rep = 0; rep < 4 && ok; rep++) {
 				cudaEventRecord(e0, st);
 				ok = launch_real_move(model, variant, s, scratch, a, st) == cudaSuccess;
 				cudaEventRecord(e1, st);
@@ -539,6 +545,8 @@ int setup_diagnostics(nlc_plan &P) {
 		return set_error(NLC_EUNSUPPORTED, "chain_length too large for the shared-memory diagnostics");
 	if ((rc = P.dalloc(&P.d_partials, size_t(P.diag_rows) * n))) return rc;
 	g.partials = P.d_partials;
+	P.row_slice_cap = finish_row_slices(n, P.diag_rows, sms);
+	if (P.row_slice_cap && (rc = P.dalloc(&P.d_row_slices, size_t(P.row_slice_cap) * n))) return rc;
 	if (n > uint32_t(kFinishModesPerBlock) &&
 	    (rc = P.dalloc(&P.d_block_sums, 4 * size_t((n + kFinishModesPerBlock - 1) / kFinishModesPerBlock))))
 		return rc;
@@ -933,6 +941,8 @@ extern "C" int nlc_linenergies(nlc_plan *P, const void *state, double *lin, doub
 	f.lin = lin;
 	f.entropies = ent;
 	f.block_sums = P->d_block_sums;
+	f.row_slices = P->d_row_slices;
+	f.row_slice_cap = P->row_slice_cap;
 	return cuda_status(launch_linenergies_finish(f, st), "linenergies finish launch");
 }
 
