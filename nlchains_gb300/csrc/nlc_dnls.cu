@@ -30,8 +30,10 @@ __device__ __forceinline__ double2 nonlinear_rotate(double2 v, double neg_coef, 
 // warp, 32 / a.team chains per warp: short chains keep every lane busy.  A warp takes its chains as
 // one unit from the self-resetting counter, so all its teams run the same control flow (a team
 // past the last chain repeats the last one and does not store).
+// 64 registers a thread: four 256-thread chains (or eight 128-thread team blocks) per SM; the block
+// variant also runs with 512 threads when the chain's buffers live in global memory
 template <bool BLOCK>
-__global__ void dnls_move_kernel(double2 *__restrict__ psi, const DnlsArgs a) {
+__global__ void __launch_bounds__(BLOCK ? 512 : 128, BLOCK ? 2 : 8) dnls_move_kernel(double2 *__restrict__ psi, const DnlsArgs a) {
 	extern __shared__ double2 sm[];
 	__shared__ unsigned long long s_chain[32];
 	const int n = int(a.n);
@@ -70,27 +72,17 @@ __global__ void dnls_move_kernel(double2 *__restrict__ psi, const DnlsArgs a) {
 		for (uint32_t i = 0; i < a.steps; i++) {
 			for (int k = 0; k < 7; k++) {
 				const double coef = (k == 0 && (i != 0 || (a.seg & NLC_SEG_CONTINUE))) ? a.nl[7] : a.nl[k];
-				if (a.conv_tables) {
-					// rotation, zero padding to len, then FFT_len, product with G_k, IFFT_len
-					for (int j = t; j < len; j += T) x[j] = j < n ? nonlinear_rotate(x[j], -coef, a.sctab, a.sc, a.fft.k1) : make_double2(0., 0.);
-					team_sync<BLOCK>();
-					double2 *r = stockham_team<BLOCK, false>(a.fft, x, y, t, T);
-					double2 *o = r == x ? y : x;
-					const double2 *tab = a.conv_tables + (size_t) k * len;
-					for (int j = t; j < len; j += T) r[j] = cmul(r[j], tab[j], a.fft.k1);
-					team_sync<BLOCK>();
-					x = stockham_team<BLOCK, true>(a.fft, r, o, t, T);
-					y = x == buf0 ? buf1 : buf0;
-					continue;
-				}
-				for (int j = t; j < n; j += T) x[j] = nonlinear_rotate(x[j], -coef, a.sctab, a.sc, a.fft.k1);
-				team_sync<BLOCK>();
-				double2 *r = fft_team<BLOCK, false>(a.fft, x, y, t, T);
+				// the phase rotation is applied as the forward transform's first pass reads each
+				// element (beyond n: the zero padding of the convolution form), the propagator (or
+				// the convolution kernel's spectrum) as its last pass writes each element
+				auto rotate = [&](int j, double2 v) {
+					return j < n ? nonlinear_rotate(v, -coef, a.sctab, a.sc, a.fft.k1) : make_double2(0., 0.);
+				};
+				const double2 *tab = a.conv_tables ? a.conv_tables + (size_t) k * len : a.lin_tables + (size_t) k * n;
+				auto propagate = [&](int j, double2 v) { return cmul(v, tab[j], a.fft.k1); };
+				double2 *r = stockham_team<BLOCK, false>(a.fft, x, y, t, T, rotate, propagate);
 				double2 *o = r == x ? y : x;
-				const double2 *tab = a.lin_tables + (size_t) k * n;
-				for (int j = t; j < n; j += T) r[j] = cmul(r[j], tab[j], a.fft.k1);
-				team_sync<BLOCK>();
-				x = fft_team<BLOCK, true>(a.fft, r, o, t, T);
+				x = stockham_team<BLOCK, true>(a.fft, r, o, t, T);
 				y = x == buf0 ? buf1 : buf0;
 			}
 		}

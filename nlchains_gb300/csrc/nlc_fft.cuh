@@ -21,6 +21,8 @@
 // Forward = exp(-2 pi i jk/n), unnormalised, as cuFFT / FFTW forward transforms in the reference.
 #pragma once
 
+#include <type_traits>
+
 #include "nlc_device.cuh"
 #include "nlc_internal.h"
 
@@ -65,158 +67,194 @@ __device__ __forceinline__ double2 fma2(double c, double2 z, double2 a) {
 	return make_double2(dfma(c, z.x, a.x), dfma(c, z.y, a.y));
 }
 
-// Stockham pass of length P.len on x (shared memory), y the ping-pong buffer.  t / T: this
-// thread's index / size of the team.  Returns the buffer holding the result.
-template <bool BLOCK, bool INV>
-__device__ double2 *stockham_team(const FftPlanDev &P, double2 *x, double2 *y, int t, int T) {
+// Elementwise maps fused into a transform: `Pre` is applied to every element as the first pass
+// reads it, `Post` to every element as the last pass writes it (index in [0, len)); each element
+// passes through each exactly once, so the result equals a separate pass over the buffer.
+struct NoMap {
+	__device__ __forceinline__ double2 operator()(int, double2 v) const { return v; }
+};
+
+// One Stockham pass r (radix P.radix[r], Ns points already combined) from x to y.  PRE / POST: the
+// pass applies `pre` to its inputs (the first pass) / `post` to its outputs (the last pass); they
+// are template flags so that the other passes carry no trace of the maps.
+template <bool BLOCK, bool INV, bool PRE, bool POST, class Pre, class Post>
+__device__ __forceinline__ void stockham_pass(const FftPlanDev &P, int r, int Ns, double2 *x, double2 *y, int t, int T,
+                                              const Pre &pre, const Post &post) {
 	const int n = P.len;
 	const double2 *__restrict__ tw = P.tw;
 	const FpOnes &k = P.k1;
-	int Ns = 1;
-	for (int r = 0; r < P.nradix; r++) {
-		const int p = P.radix[r];
-		const int m = n / p;
-		const double2 *__restrict__ g = P.gw + P.gw_off[r];
-		if (p == 4) {
-			if (Ns == 1) {
-				for (int b = t; b < m; b += T) {
-					const double2 a0 = x[b], a1 = x[b + m], a2 = x[b + 2 * m], a3 = x[b + 3 * m];
-					const double2 b0 = cadd(a0, a2, k), b1 = csub(a0, a2, k), b2 = cadd(a1, a3, k), b3 = rot_mi<INV>(csub(a1, a3, k));
-					double2 *o = y + 4 * b;
-					o[0] = cadd(b0, b2, k);
-					o[1] = cadd(b1, b3, k);
-					o[2] = csub(b0, b2, k);
-					o[3] = csub(b1, b3, k);
-				}
-			} else {
-				for (int b = t; b < m; b += T) {
-					const int q = b / Ns, kk = b - q * Ns;
-					const double2 a0 = x[b], a1 = x[b + m], a2 = x[b + 2 * m], a3 = x[b + 3 * m];
-					const double2 e0 = g[3 * kk], e1 = g[3 * kk + 1], e2 = g[3 * kk + 2];   // {t1,t2} {t3,c1} {c2,c3/c1}
-					const double2 z1 = ztan<INV>(a1, e0.x), z2 = ztan<INV>(a2, e0.y), z3 = ztan<INV>(a3, e1.x);
-					const double c1 = e1.y, c2 = e2.x, rho = e2.y;
-					// A_u = a_u w_u: A0 +- A2 = a0 +- c2 Z2, A1 +- A3 = c1 (Z1 +- (c3/c1) Z3)
-					const double2 b0 = fma2(c2, z2, a0), b1 = fma2(-c2, z2, a0);
-					const double2 p2 = fma2(rho, z3, z1), p3 = fma2(-rho, z3, z1);
-					// X1 = (A0 - A2) -+ i (A1 - A3), X3 = (A0 - A2) +- i (A1 - A3) (forward / inverse)
-					const double2 bm = make_double2(dfma(c1, p3.y, b1.x), dfma(-c1, p3.x, b1.y));   // b1 - i c1 p3
-					const double2 bp = make_double2(dfma(-c1, p3.y, b1.x), dfma(c1, p3.x, b1.y));   // b1 + i c1 p3
-					double2 *o = y + q * 4 * Ns + kk;
-					o[0] = fma2(c1, p2, b0);
-					o[Ns] = INV ? bp : bm;
-					o[2 * Ns] = fma2(-c1, p2, b0);
-					o[3 * Ns] = INV ? bm : bp;
-				}
-			}
-		} else if (p == 2) {
+	const int p = P.radix[r];
+	const int m = n / p;
+	const double2 *__restrict__ g = P.gw + P.gw_off[r];
+	// input u of butterfly b, and output v of the butterfly at base o (stride Ns)
+	auto in = [&](int b, int u) {
+		if constexpr (PRE) return pre(b + u * m, x[b + u * m]);
+		else return x[b + u * m];
+	};
+	auto out = [&](int o, int v, double2 val) {
+		if constexpr (POST) y[o + v * Ns] = post(o + v * Ns, val);
+		else y[o + v * Ns] = val;
+	};
+	if (PRE && p != 4 && p != 2 && p != 3 && p != 5) {
+		// a direct DFT reads each input p times: map the inputs once, in place, first
+		for (int j = t; j < n; j += T) x[j] = pre(j, x[j]);
+		team_sync<BLOCK>();
+	}
+	if (p == 4) {
+		if (Ns == 1) {
 			for (int b = t; b < m; b += T) {
-				const int q = b / Ns, kk = b - q * Ns;
-				const double2 a0 = x[b], a1 = x[b + m];
-				double2 *o = y + q * 2 * Ns + kk;
-				if (Ns == 1) {
-					o[0] = cadd(a0, a1, k);
-					o[Ns] = csub(a0, a1, k);
-				} else {
-					const double2 e = g[kk];   // {t1, c1}
-					const double2 z = ztan<INV>(a1, e.x);
-					o[0] = fma2(e.y, z, a0);
-					o[Ns] = fma2(-e.y, z, a0);
-				}
-			}
-		} else if (p == 3) {
-			for (int b = t; b < m; b += T) {
-				const int q = b / Ns, kk = b - q * Ns;
-				const double2 a0 = x[b], a1 = x[b + m], a2 = x[b + 2 * m];
-				double2 x0, xm, xp;   // X0, t2 - i u, t2 + i u
-				if (Ns == 1) {
-					const double sn = P.sin60;   // sin(2 pi / 3), a parameter-bank operand
-					const double2 t1 = cadd(a1, a2, k);
-					const double2 t2 = make_double2(dfma(t1.x, -P.half, a0.x), dfma(t1.y, -P.half, a0.y));
-					const double2 d = csub(a1, a2, k);
-					const double2 u = make_double2(fmul(sn, d.x, k), fmul(sn, d.y, k));
-					x0 = cadd(a0, t1, k);
-					xm = make_double2(fadd(t2.x, u.y, k), fsub(t2.y, u.x, k));
-					xp = make_double2(fsub(t2.x, u.y, k), fadd(t2.y, u.x, k));
-				} else {
-					const double2 e0 = g[3 * kk], e1 = g[3 * kk + 1], e2 = g[3 * kk + 2];   // {t1,t2} {c1,c2/c1} {c1/2, c1 sin60}
-					const double2 z1 = ztan<INV>(a1, e0.x), z2 = ztan<INV>(a2, e0.y);
-					// A1 +- A2 = c1 (Z1 +- (c2/c1) Z2)
-					const double2 ts = fma2(e1.y, z2, z1), d = fma2(-e1.y, z2, z1);
-					x0 = fma2(e1.x, ts, a0);
-					const double2 t2 = fma2(-e2.x, ts, a0);
-					xm = make_double2(dfma(e2.y, d.y, t2.x), dfma(-e2.y, d.x, t2.y));
-					xp = make_double2(dfma(-e2.y, d.y, t2.x), dfma(e2.y, d.x, t2.y));
-				}
-				// forward: X1 = t2 - i u, X2 = t2 + i u; the inverse the other way round
-				double2 *o = y + q * 3 * Ns + kk;
-				o[0] = x0;
-				o[Ns] = INV ? xp : xm;
-				o[2 * Ns] = INV ? xm : xp;
-			}
-		} else if (p == 5) {
-			// t1 = a1 + a4, t2 = a2 + a3, t3 = a1 - a4, t4 = a2 - a3;
-			// X1,4 = a0 + c1 t1 + c2 t2 -+ i (s1 t3 + s2 t4), X2,3 = a0 + c2 t1 + c1 t2 -+ i (s2 t3 - s1 t4)
-			// (forward; the inverse swaps the signs of i), c_j = cos(2 pi j/5), s_j = sin(2 pi j/5),
-			// on the twiddled inputs a_u w^{uk}
-			const int stride = n / (Ns * 5);
-			for (int b = t; b < m; b += T) {
-				const int q = b / Ns, kk = b - q * Ns;
-				double2 a0 = x[b], a1 = x[b + m], a2 = x[b + 2 * m], a3 = x[b + 3 * m], a4 = x[b + 4 * m];
-				if (Ns > 1) {
-					const int e = kk * stride;
-					a1 = cmul(a1, twiddle<INV>(tw, e), k);
-					a2 = cmul(a2, twiddle<INV>(tw, 2 * e), k);
-					a3 = cmul(a3, twiddle<INV>(tw, 3 * e), k);
-					a4 = cmul(a4, twiddle<INV>(tw, 4 * e), k);
-				}
-				const double2 t1 = cadd(a1, a4, k), t2 = cadd(a2, a3, k), t3 = csub(a1, a4, k), t4 = csub(a2, a3, k);
-				const double2 b1 = make_double2(dfma(P.c52, t2.x, dfma(P.c51, t1.x, a0.x)),
-				                                dfma(P.c52, t2.y, dfma(P.c51, t1.y, a0.y)));
-				const double2 b2 = make_double2(dfma(P.c51, t2.x, dfma(P.c52, t1.x, a0.x)),
-				                                dfma(P.c51, t2.y, dfma(P.c52, t1.y, a0.y)));
-				const double2 u1 = make_double2(dfma(P.s52, t4.x, fmul(P.s51, t3.x, k)),
-				                                dfma(P.s52, t4.y, fmul(P.s51, t3.y, k)));
-				const double2 u2 = make_double2(dfma(-P.s51, t4.x, fmul(P.s52, t3.x, k)),
-				                                dfma(-P.s51, t4.y, fmul(P.s52, t3.y, k)));
-				// b -+ i u: forward X1 = b1 - i u1 = (b1.x + u1.y, b1.y - u1.x)
-				const double2 x1 = INV ? make_double2(fsub(b1.x, u1.y, k), fadd(b1.y, u1.x, k))
-				                       : make_double2(fadd(b1.x, u1.y, k), fsub(b1.y, u1.x, k));
-				const double2 x4 = INV ? make_double2(fadd(b1.x, u1.y, k), fsub(b1.y, u1.x, k))
-				                       : make_double2(fsub(b1.x, u1.y, k), fadd(b1.y, u1.x, k));
-				const double2 x2 = INV ? make_double2(fsub(b2.x, u2.y, k), fadd(b2.y, u2.x, k))
-				                       : make_double2(fadd(b2.x, u2.y, k), fsub(b2.y, u2.x, k));
-				const double2 x3 = INV ? make_double2(fadd(b2.x, u2.y, k), fsub(b2.y, u2.x, k))
-				                       : make_double2(fsub(b2.x, u2.y, k), fadd(b2.y, u2.x, k));
-				double2 *o = y + q * 5 * Ns + kk;
-				o[0] = cadd(a0, cadd(t1, t2, k), k);
-				o[Ns] = x1, o[2 * Ns] = x2, o[3 * Ns] = x3, o[4 * Ns] = x4;
+				const double2 a0 = in(b, 0), a1 = in(b, 1), a2 = in(b, 2), a3 = in(b, 3);
+				const double2 b0 = cadd(a0, a2, k), b1 = csub(a0, a2, k), b2 = cadd(a1, a3, k), b3 = rot_mi<INV>(csub(a1, a3, k));
+				const int o = 4 * b;
+				out(o, 0, cadd(b0, b2, k));
+				out(o, 1, cadd(b1, b3, k));
+				out(o, 2, csub(b0, b2, k));
+				out(o, 3, csub(b1, b3, k));
 			}
 		} else {
-			// direct p-point DFT of the twiddled inputs: X_v = sum_u a_u w^{uk} W_p^{uv}
-			// = sum_u a_u tw[u (k + v Ns) n / (Ns p) mod n]
-			const int stride = n / (Ns * p);
 			for (int b = t; b < m; b += T) {
 				const int q = b / Ns, kk = b - q * Ns;
-				for (int v = 0; v < p; v++) {
-					const int step = int((long long) (kk + v * Ns) * stride % n);
-					double re = 0., im = 0.;
-					int e = 0;
-					for (int u = 0; u < p; u++) {
-						const double2 a = x[b + u * m];
-						const double2 w = twiddle<INV>(tw, e);
-						re = dfma(a.x, w.x, dfma(-a.y, w.y, re));
-						im = dfma(a.x, w.y, dfma(a.y, w.x, im));
-						e += step;
-						if (e >= n) e -= n;
-					}
-					y[q * p * Ns + kk + v * Ns] = make_double2(re, im);
-				}
+				const double2 a0 = x[b], a1 = x[b + m], a2 = x[b + 2 * m], a3 = x[b + 3 * m];
+				const double2 e0 = g[3 * kk], e1 = g[3 * kk + 1], e2 = g[3 * kk + 2];   // {t1,t2} {t3,c1} {c2,c3/c1}
+				const double2 z1 = ztan<INV>(a1, e0.x), z2 = ztan<INV>(a2, e0.y), z3 = ztan<INV>(a3, e1.x);
+				const double c1 = e1.y, c2 = e2.x, rho = e2.y;
+				// A_u = a_u w_u: A0 +- A2 = a0 +- c2 Z2, A1 +- A3 = c1 (Z1 +- (c3/c1) Z3)
+				const double2 b0 = fma2(c2, z2, a0), b1 = fma2(-c2, z2, a0);
+				const double2 p2 = fma2(rho, z3, z1), p3 = fma2(-rho, z3, z1);
+				// X1 = (A0 - A2) -+ i (A1 - A3), X3 = (A0 - A2) +- i (A1 - A3) (forward / inverse)
+				const double2 bm = make_double2(dfma(c1, p3.y, b1.x), dfma(-c1, p3.x, b1.y));   // b1 - i c1 p3
+				const double2 bp = make_double2(dfma(-c1, p3.y, b1.x), dfma(c1, p3.x, b1.y));   // b1 + i c1 p3
+				const int o = q * 4 * Ns + kk;
+				out(o, 0, fma2(c1, p2, b0));
+				out(o, 1, INV ? bp : bm);
+				out(o, 2, fma2(-c1, p2, b0));
+				out(o, 3, INV ? bm : bp);
 			}
 		}
+	} else if (p == 2) {
+		for (int b = t; b < m; b += T) {
+			const int q = b / Ns, kk = b - q * Ns;
+			const double2 a0 = in(b, 0), a1 = in(b, 1);
+			const int o = q * 2 * Ns + kk;
+			if (Ns == 1) {
+				out(o, 0, cadd(a0, a1, k));
+				out(o, 1, csub(a0, a1, k));
+			} else {
+				const double2 e = g[kk];   // {t1, c1}
+				const double2 z = ztan<INV>(a1, e.x);
+				out(o, 0, fma2(e.y, z, a0));
+				out(o, 1, fma2(-e.y, z, a0));
+			}
+		}
+	} else if (p == 3) {
+		for (int b = t; b < m; b += T) {
+			const int q = b / Ns, kk = b - q * Ns;
+			const double2 a0 = in(b, 0), a1 = in(b, 1), a2 = in(b, 2);
+			double2 x0, xm, xp;   // X0, t2 - i u, t2 + i u
+			if (Ns == 1) {
+				const double sn = P.sin60;   // sin(2 pi / 3), a parameter-bank operand
+				const double2 t1 = cadd(a1, a2, k);
+				const double2 t2 = make_double2(dfma(t1.x, -P.half, a0.x), dfma(t1.y, -P.half, a0.y));
+				const double2 d = csub(a1, a2, k);
+				const double2 u = make_double2(fmul(sn, d.x, k), fmul(sn, d.y, k));
+				x0 = cadd(a0, t1, k);
+				xm = make_double2(fadd(t2.x, u.y, k), fsub(t2.y, u.x, k));
+				xp = make_double2(fsub(t2.x, u.y, k), fadd(t2.y, u.x, k));
+			} else {
+				const double2 e0 = g[3 * kk], e1 = g[3 * kk + 1], e2 = g[3 * kk + 2];   // {t1,t2} {c1,c2/c1} {c1/2, c1 sin60}
+				const double2 z1 = ztan<INV>(a1, e0.x), z2 = ztan<INV>(a2, e0.y);
+				// A1 +- A2 = c1 (Z1 +- (c2/c1) Z2)
+				const double2 ts = fma2(e1.y, z2, z1), d = fma2(-e1.y, z2, z1);
+				x0 = fma2(e1.x, ts, a0);
+				const double2 t2 = fma2(-e2.x, ts, a0);
+				xm = make_double2(dfma(e2.y, d.y, t2.x), dfma(-e2.y, d.x, t2.y));
+				xp = make_double2(dfma(-e2.y, d.y, t2.x), dfma(e2.y, d.x, t2.y));
+			}
+			// forward: X1 = t2 - i u, X2 = t2 + i u; the inverse the other way round
+			const int o = q * 3 * Ns + kk;
+			out(o, 0, x0);
+			out(o, 1, INV ? xp : xm);
+			out(o, 2, INV ? xm : xp);
+		}
+	} else if (p == 5) {
+		// t1 = a1 + a4, t2 = a2 + a3, t3 = a1 - a4, t4 = a2 - a3;
+		// X1,4 = a0 + c1 t1 + c2 t2 -+ i (s1 t3 + s2 t4), X2,3 = a0 + c2 t1 + c1 t2 -+ i (s2 t3 - s1 t4)
+		// (forward; the inverse swaps the signs of i), c_j = cos(2 pi j/5), s_j = sin(2 pi j/5),
+		// on the twiddled inputs a_u w^{uk}
+		const int stride = n / (Ns * 5);
+		for (int b = t; b < m; b += T) {
+			const int q = b / Ns, kk = b - q * Ns;
+			double2 a0 = in(b, 0), a1 = in(b, 1), a2 = in(b, 2), a3 = in(b, 3), a4 = in(b, 4);
+			if (Ns > 1) {
+				const int e = kk * stride;
+				a1 = cmul(a1, twiddle<INV>(tw, e), k);
+				a2 = cmul(a2, twiddle<INV>(tw, 2 * e), k);
+				a3 = cmul(a3, twiddle<INV>(tw, 3 * e), k);
+				a4 = cmul(a4, twiddle<INV>(tw, 4 * e), k);
+			}
+			const double2 t1 = cadd(a1, a4, k), t2 = cadd(a2, a3, k), t3 = csub(a1, a4, k), t4 = csub(a2, a3, k);
+			const double2 b1 = make_double2(dfma(P.c52, t2.x, dfma(P.c51, t1.x, a0.x)),
+			                                dfma(P.c52, t2.y, dfma(P.c51, t1.y, a0.y)));
+			const double2 b2 = make_double2(dfma(P.c51, t2.x, dfma(P.c52, t1.x, a0.x)),
+			                                dfma(P.c51, t2.y, dfma(P.c52, t1.y, a0.y)));
+			const double2 u1 = make_double2(dfma(P.s52, t4.x, fmul(P.s51, t3.x, k)),
+			                                dfma(P.s52, t4.y, fmul(P.s51, t3.y, k)));
+			const double2 u2 = make_double2(dfma(-P.s51, t4.x, fmul(P.s52, t3.x, k)),
+			                                dfma(-P.s51, t4.y, fmul(P.s52, t3.y, k)));
+			// b -+ i u: forward X1 = b1 - i u1 = (b1.x + u1.y, b1.y - u1.x)
+			const double2 x1 = INV ? make_double2(fsub(b1.x, u1.y, k), fadd(b1.y, u1.x, k))
+			                       : make_double2(fadd(b1.x, u1.y, k), fsub(b1.y, u1.x, k));
+			const double2 x4 = INV ? make_double2(fadd(b1.x, u1.y, k), fsub(b1.y, u1.x, k))
+			                       : make_double2(fsub(b1.x, u1.y, k), fadd(b1.y, u1.x, k));
+			const double2 x2 = INV ? make_double2(fsub(b2.x, u2.y, k), fadd(b2.y, u2.x, k))
+			                       : make_double2(fadd(b2.x, u2.y, k), fsub(b2.y, u2.x, k));
+			const double2 x3 = INV ? make_double2(fadd(b2.x, u2.y, k), fsub(b2.y, u2.x, k))
+			                       : make_double2(fsub(b2.x, u2.y, k), fadd(b2.y, u2.x, k));
+			const int o = q * 5 * Ns + kk;
+			out(o, 0, cadd(a0, cadd(t1, t2, k), k));
+			out(o, 1, x1), out(o, 2, x2), out(o, 3, x3), out(o, 4, x4);
+		}
+	} else {
+		// direct p-point DFT of the twiddled inputs: X_v = sum_u a_u w^{uk} W_p^{uv}
+		// = sum_u a_u tw[u (k + v Ns) n / (Ns p) mod n]
+		const int stride = n / (Ns * p);
+		for (int b = t; b < m; b += T) {
+			const int q = b / Ns, kk = b - q * Ns;
+			for (int v = 0; v < p; v++) {
+				const int step = int((long long) (kk + v * Ns) * stride % n);
+				double re = 0., im = 0.;
+				int e = 0;
+				for (int u = 0; u < p; u++) {
+					const double2 a = x[b + u * m];
+					const double2 w = twiddle<INV>(tw, e);
+					re = dfma(a.x, w.x, dfma(-a.y, w.y, re));
+					im = dfma(a.x, w.y, dfma(a.y, w.x, im));
+					e += step;
+					if (e >= n) e -= n;
+				}
+				out(q * p * Ns + kk, v, make_double2(re, im));
+			}
+		}
+	}
+}
+
+// Stockham transform of length P.len on x (shared memory), y the ping-pong buffer.  t / T: this
+// thread's index / size of the team.  Returns the buffer holding the result.
+template <bool BLOCK, bool INV, class Pre = NoMap, class Post = NoMap>
+__device__ double2 *stockham_team(const FftPlanDev &P, double2 *x, double2 *y, int t, int T, Pre pre = Pre(),
+                                  Post post = Post()) {
+	constexpr bool kPre = !std::is_same<Pre, NoMap>::value, kPost = !std::is_same<Post, NoMap>::value;
+	int Ns = 1;
+	for (int r = 0; r < P.nradix; r++) {
+		const bool first = r == 0, last = r == P.nradix - 1;
+		if (kPre && kPost && first && last) stockham_pass<BLOCK, INV, kPre, kPost>(P, r, Ns, x, y, t, T, pre, post);
+		else if (kPre && first) stockham_pass<BLOCK, INV, kPre, false>(P, r, Ns, x, y, t, T, pre, post);
+		else if (kPost && last) stockham_pass<BLOCK, INV, false, kPost>(P, r, Ns, x, y, t, T, pre, post);
+		else stockham_pass<BLOCK, INV, false, false>(P, r, Ns, x, y, t, T, pre, post);
 		team_sync<BLOCK>();
 		double2 *sw = x;
 		x = y, y = sw;
-		Ns *= p;
+		Ns *= P.radix[r];
 	}
 	return x;
 }
