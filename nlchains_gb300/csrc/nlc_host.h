@@ -9,6 +9,28 @@
 #include "nlc_internal.h"
 
 namespace nlc {
+// Makes `device` current for the life of the object (one entry point of the C ABI) and restores
+// the caller's current device afterwards, so that a process driving several GPUs from one thread
+// can call any context or plan whatever device it left current; device < 0: no change.
+class DeviceScope {
+public:
+	explicit DeviceScope(int device) {
+		int cur = -1;
+		if (device >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != device && cudaSetDevice(device) == cudaSuccess)
+			prev_ = cur;
+	}
+	~DeviceScope() {
+		if (prev_ >= 0) cudaSetDevice(prev_);
+	}
+	DeviceScope(const DeviceScope &) = delete;
+	DeviceScope &operator=(const DeviceScope &) = delete;
+
+private:
+	int prev_ = -1;
+};
+}  // namespace nlc
+
+namespace nlc {
 
 // thread-local error message + status helpers
 int set_error(int code, const std::string &msg);

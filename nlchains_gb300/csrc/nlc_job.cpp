@@ -76,7 +76,6 @@ extern "C" int nlc_create(nlc_ctx **out, int device) {
 	int rc = cuda_status(cudaGetDeviceCount(&count), "cudaGetDeviceCount");
 	if (rc) return rc;
 	if (device < 0 || device >= count) return set_error(NLC_EINVAL, "no such CUDA device");
-	if ((rc = cuda_status(cudaSetDevice(device), "cudaSetDevice"))) return rc;
 	auto *c = new nlc_ctx;
 	c->device = device;
 	*out = c;
@@ -85,8 +84,10 @@ extern "C" int nlc_create(nlc_ctx **out, int device) {
 
 extern "C" int nlc_destroy(nlc_ctx *ctx) {
 	if (!ctx) return NLC_OK;
-	cudaSetDevice(ctx->device);
-	ctx->jobs.clear();
+	{
+		DeviceScope ds(ctx->device);
+		ctx->jobs.clear();
+	}
 	delete ctx;
 	return NLC_OK;
 }
@@ -94,8 +95,8 @@ extern "C" int nlc_destroy(nlc_ctx *ctx) {
 extern "C" int nlc_job_create(nlc_ctx *ctx, const nlc_model *model, uint32_t batching, uint64_t *id) {
 	if (!ctx || !model || !id) return set_error(NLC_EINVAL, "NULL argument");
 	if (!batching) return set_error(NLC_EINVAL, "--kernel_batching must be a positive number");
-	int rc = cuda_status(cudaSetDevice(ctx->device), "cudaSetDevice");
-	if (rc) return rc;
+	DeviceScope ds(ctx->device);
+	int rc;
 	std::unique_ptr<Job> J(new Job);
 	J->model = *model;
 	J->batching = batching;
@@ -114,12 +115,14 @@ extern "C" int nlc_job_create(nlc_ctx *ctx, const nlc_model *model, uint32_t bat
 }
 
 extern "C" int nlc_job_destroy(nlc_ctx *ctx, uint64_t id) {
+	DeviceScope ds(ctx ? ctx->device : -1);
 	if (!find_job(ctx, id)) return set_error(NLC_ENOTFOUND, "no such job");
 	ctx->jobs.erase(id);
 	return NLC_OK;
 }
 
 extern "C" int nlc_job_upload(nlc_ctx *ctx, uint64_t id, const void *host) {
+	DeviceScope ds(ctx ? ctx->device : -1);
 	Job *J = find_job(ctx, id);
 	if (!J) return set_error(NLC_ENOTFOUND, "no such job");
 	if (!host) return set_error(NLC_EINVAL, "host state is NULL");
@@ -127,6 +130,7 @@ extern "C" int nlc_job_upload(nlc_ctx *ctx, uint64_t id, const void *host) {
 }
 
 extern "C" int nlc_job_download(nlc_ctx *ctx, uint64_t id, void *host) {
+	DeviceScope ds(ctx ? ctx->device : -1);
 	Job *J = find_job(ctx, id);
 	if (!J) return set_error(NLC_ENOTFOUND, "no such job");
 	if (!host) return set_error(NLC_EINVAL, "host state is NULL");
@@ -136,6 +140,7 @@ extern "C" int nlc_job_download(nlc_ctx *ctx, uint64_t id, void *host) {
 }
 
 extern "C" int nlc_job_advance(nlc_ctx *ctx, uint64_t id, uint64_t steps) {
+	DeviceScope ds(ctx ? ctx->device : -1);
 	Job *J = find_job(ctx, id);
 	if (!J) return set_error(NLC_ENOTFOUND, "no such job");
 	if (steps % J->batching) return set_error(NLC_EINVAL, "--steps must be a multiple of --kernel_batching");
@@ -147,6 +152,7 @@ extern "C" int nlc_job_advance(nlc_ctx *ctx, uint64_t id, uint64_t steps) {
 }
 
 extern "C" int nlc_job_linenergies(nlc_ctx *ctx, uint64_t id, double *lin, double *wt, double *inf) {
+	DeviceScope ds(ctx ? ctx->device : -1);
 	Job *J = find_job(ctx, id);
 	if (!J) return set_error(NLC_ENOTFOUND, "no such job");
 	const size_t n = J->model.chain_length;
@@ -166,6 +172,7 @@ extern "C" int nlc_job_linenergies(nlc_ctx *ctx, uint64_t id, double *lin, doubl
 }
 
 extern "C" int nlc_job_energies(nlc_ctx *ctx, uint64_t id, double *host_energies) {
+	DeviceScope ds(ctx ? ctx->device : -1);
 	Job *J = find_job(ctx, id);
 	if (!J) return set_error(NLC_ENOTFOUND, "no such job");
 	if (!host_energies) return set_error(NLC_EINVAL, "NULL argument");
@@ -220,6 +227,7 @@ int enqueue_sample(Job *J, int slot, int copy_state, bool external) {
 }  // namespace
 
 extern "C" int nlc_job_sample_async(nlc_ctx *ctx, uint64_t id, int32_t slot, int32_t copy_state) {
+	DeviceScope ds(ctx ? ctx->device : -1);
 	Job *J = find_job(ctx, id);
 	if (!J) return set_error(NLC_ENOTFOUND, "no such job");
 	if (slot < 0 || slot > 1) return set_error(NLC_EINVAL, "slot must be 0 or 1");
@@ -231,6 +239,7 @@ extern "C" int nlc_job_sample_async(nlc_ctx *ctx, uint64_t id, int32_t slot, int
 }
 
 extern "C" int nlc_job_step_async(nlc_ctx *ctx, uint64_t id, int32_t slot, int32_t copy_state) {
+	DeviceScope ds(ctx ? ctx->device : -1);
 	Job *J = find_job(ctx, id);
 	if (!J) return set_error(NLC_ENOTFOUND, "no such job");
 	if (slot < 0 || slot > 1) return set_error(NLC_EINVAL, "slot must be 0 or 1");
@@ -262,6 +271,7 @@ extern "C" int nlc_job_step_async(nlc_ctx *ctx, uint64_t id, int32_t slot, int32
 
 extern "C" int nlc_job_sample_wait(nlc_ctx *ctx, uint64_t id, int32_t slot, double *lin, double *wt, double *inf,
                                    void *host_state, int32_t timeout_ms) {
+	DeviceScope ds(ctx ? ctx->device : -1);
 	Job *J = find_job(ctx, id);
 	if (!J) return set_error(NLC_ENOTFOUND, "no such job");
 	if (slot < 0 || slot > 1 || !J->ev_slot[slot]) return set_error(NLC_EINVAL, "slot was never filled");
@@ -289,6 +299,7 @@ extern "C" int nlc_job_sample_wait(nlc_ctx *ctx, uint64_t id, int32_t slot, doub
 }
 
 extern "C" int nlc_job_after(nlc_ctx *ctx, uint64_t id, uint64_t after_id) {
+	DeviceScope ds(ctx ? ctx->device : -1);
 	Job *J = find_job(ctx, id);
 	Job *A = find_job(ctx, after_id);
 	if (!J || !A) return set_error(NLC_ENOTFOUND, "no such job");
@@ -302,6 +313,7 @@ extern "C" int nlc_job_after(nlc_ctx *ctx, uint64_t id, uint64_t after_id) {
 }
 
 extern "C" int nlc_job_wait(nlc_ctx *ctx, uint64_t id, int32_t timeout_ms) {
+	DeviceScope ds(ctx ? ctx->device : -1);
 	Job *J = find_job(ctx, id);
 	if (!J) return set_error(NLC_ENOTFOUND, "no such job");
 	const auto t0 = std::chrono::steady_clock::now();
@@ -317,6 +329,7 @@ extern "C" int nlc_job_wait(nlc_ctx *ctx, uint64_t id, int32_t timeout_ms) {
 }
 
 extern "C" int nlc_job_state_ptr(nlc_ctx *ctx, uint64_t id, void **ptr) {
+	DeviceScope ds(ctx ? ctx->device : -1);
 	Job *J = find_job(ctx, id);
 	if (!J) return set_error(NLC_ENOTFOUND, "no such job");
 	if (!ptr) return set_error(NLC_EINVAL, "NULL argument");
@@ -570,7 +583,7 @@ int run_program(int argc, char **argv) {
 		int32_t lanes, sites, threads, tier;
 		nlc_plan_shape(find_job(ctx, job)->plan, &lanes, &sites, &threads, &tier);
 		cudaDeviceProp p{};
-		cudaGetDeviceProperties(&p, 0);
+		cudaGetDeviceProperties(&p, ctx->device);
 		std::cout << "nlchains-gb300: GPU " << p.name << ", integrator tier " << tier << ", " << lanes
 		          << " lanes/chain, " << sites << " sites/lane, " << threads << " threads/block" << std::endl;
 	}

@@ -822,6 +822,7 @@ bool nlc::plan_info(const nlc_plan *P, PlanInfo *info) {
 
 extern "C" int nlc_plan_destroy(nlc_plan *plan) {
 	if (!plan) return NLC_OK;
+	DeviceScope ds(plan->device);
 	// the caller may still have work using the plan on any stream: wait for the device, as cudaFree did
 	cudaDeviceSynchronize();
 	delete plan;
@@ -850,6 +851,7 @@ extern "C" int nlc_plan_omegas(const nlc_plan *P, double *omegas) {
 }
 
 extern "C" int nlc_move(nlc_plan *P, void *state, uint32_t steps, void *stream) {
+	DeviceScope ds(P ? P->device : -1);
 	return nlc::move_segment(P, state, steps, 0, static_cast<cudaStream_t>(stream));
 }
 
@@ -905,6 +907,7 @@ int nlc::move_segment(nlc_plan *P, void *state, uint32_t steps, uint32_t seg, cu
 
 extern "C" int nlc_energies(nlc_plan *P, const void *state, double *energies, void *stream) {
 	if (!P || !state || !energies) return set_error(NLC_EINVAL, "NULL argument");
+	DeviceScope ds(P->device);
 	EnergyArgs e{};
 	e.model = P->m.model;
 	e.n = P->m.chain_length, e.copies = P->m.copies;
@@ -916,6 +919,7 @@ extern "C" int nlc_energies(nlc_plan *P, const void *state, double *energies, vo
 
 extern "C" int nlc_linenergies(nlc_plan *P, const void *state, double *lin, double *ent, void *stream) {
 	if (!P || !state || !lin) return set_error(NLC_EINVAL, "NULL argument");
+	DeviceScope ds(P->device);
 	cudaStream_t st = static_cast<cudaStream_t>(stream);
 	int rc;
 	if (P->tc) {
@@ -949,6 +953,7 @@ extern "C" int nlc_linenergies(nlc_plan *P, const void *state, double *lin, doub
 extern "C" int nlc_dnls_evolve_nonlinear(nlc_plan *P, void *psi, double coef, void *stream) {
 	if (!P || !psi) return set_error(NLC_EINVAL, "NULL argument");
 	if (P->m.model != NLC_DNLS) return set_error(NLC_EINVAL, "not a DNLS plan");
+	DeviceScope ds(P->device);
 	return cuda_status(launch_dnls_nonlinear(static_cast<double2 *>(psi), uint64_t(P->m.copies) * P->m.chain_length, coef,
 	                                         P->da.sctab, static_cast<cudaStream_t>(stream)),
 	                   "evolve_nonlinear launch");
@@ -957,6 +962,7 @@ extern "C" int nlc_dnls_evolve_nonlinear(nlc_plan *P, void *psi, double coef, vo
 extern "C" int nlc_dnls_evolve_linear(nlc_plan *P, void *psi, const void *table, void *stream) {
 	if (!P || !psi) return set_error(NLC_EINVAL, "NULL argument");
 	if (P->m.model != NLC_DNLS) return set_error(NLC_EINVAL, "not a DNLS plan");
+	DeviceScope ds(P->device);
 	const double2 *tab = table ? static_cast<const double2 *>(table) : P->da.lin_tables;
 	return cuda_status(launch_dnls_linear(static_cast<double2 *>(psi), uint64_t(P->m.copies) * P->m.chain_length,
 	                                      P->m.chain_length, tab, static_cast<cudaStream_t>(stream)),
