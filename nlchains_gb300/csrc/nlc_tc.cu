@@ -207,7 +207,10 @@ tc_projection_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_con
 	const int per_chunk = kChunkK / kBK;
 	constexpr uint32_t kStageA = stage_a<S>(), kStageBytes = stage_bytes<S>();
 	auto stage_ptr = [&](int s) { return smem + (size_t) s * kStageBytes; };
+	int issued = 0, consumed = 0;    // thread 0: stages loaded / stages whose load has landed
+	bool committed = false;          // thread 0: the current chunk's MMAs are committed to accb
 	auto load_stage = [&](int it, int s) {
+		issued = it + 1;
 		const uint32_t full = full0 + 8 * s;
 		asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(full), "r"(kStageBytes) : "memory");
 		unsigned char *base = stage_ptr(s);
@@ -226,6 +229,7 @@ tc_projection_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_con
 		const int c1 = min(nk, c0 + per_chunk);
 		if (tid == 0 && !s_fail) {
 			bool ok = true;
+			committed = false;
 			if (c0 == 0) {
 				load_stage(0, 0);
 				if (nk > 1) load_stage(1, 1);
@@ -237,6 +241,7 @@ tc_projection_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_con
 					ok = false;
 					break;
 				}
+				consumed = it + 1;
 				asm volatile("tcgen05.fence::after_thread_sync;");
 				const uint32_t sa = smem_u32(stage_ptr(s)), sb = sa + kStageA;
 #pragma unroll 1
@@ -268,11 +273,13 @@ tc_projection_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_con
 					load_stage(it + 2, s);
 				}
 			}
-			if (ok)
+			if (ok) {
 				asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(accb)
 				             : "memory");
-			else
+				committed = true;
+			} else {
 				s_fail = 1;
+			}
 		}
 		// every thread: wait for the chunk's MMAs, then add its groups into the FP64 row sums
 		if (!s_fail && !mbar_wait(accb, chunks & 1)) s_fail = 1;
@@ -336,7 +343,17 @@ tc_projection_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_con
 			a.partials[(size_t) blockIdx.x * a.n + k] = s_fail ? __longlong_as_double(0x7ff8000000000000ll) : s;
 		}
 	}
-	if (tid == 0 && s_fail) atomicOr(a.status, 1);
+	if (tid == 0 && s_fail) {
+		// after a timeout: wait (each wait bounded again) for the loads this block issued and has not
+		// consumed, then for every MMA it issued, so that nothing lands in shared memory or TMEM after
+		// the block has released them
+		for (int it = consumed; it < issued; it++) mbar_wait(full0 + 8 * (it & 1), (it >> 1) & 1);
+		if (!committed)
+			asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(accb)
+			             : "memory");
+		mbar_wait(accb, chunks & 1);
+		atomicOr(a.status, 1);
+	}
 	asm volatile("tcgen05.fence::before_thread_sync;");
 	__syncthreads();
 	if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols));
