@@ -111,6 +111,9 @@ bool plan_info(const nlc_plan *plan, PlanInfo *info);
 void plan_destroy_ordered(nlc_plan *plan, cudaStream_t stream);
 // nlc_move of one segment of a round (seg: NLC_SEG_* flags)
 int move_segment(nlc_plan *plan, void *state, uint32_t steps, uint32_t seg, cudaStream_t stream);
+// NLC_ETIMEDOUT (and the flag cleared) when a bounded wait of the plan's tensor-core projection ran
+// out since the last call, else NLC_OK; synchronous.  Asked only when a sample is not finite.
+int plan_device_status(nlc_plan *plan);
 // a batched launch of the resident integrator (args.batch / nbatch / batch_units set)
 cudaError_t launch_real_move_batch(int model, int variant, const RealShape &shape, const RealArgs &args,
                                    cudaStream_t stream);

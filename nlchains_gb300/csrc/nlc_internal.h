@@ -238,6 +238,8 @@ struct TcArgs {
 	const double *omega;       // [n]
 	double *partials;          // [mp / 128][n] weighted squared sums per row tile
 	int *status;               // set on a bounded-wait timeout
+	unsigned long long wait_ns;  // limit of every mbarrier wait (wall clock)
+	int wait_test;             // tests only: thread 0 first waits on a barrier nothing arrives at
 };
 cudaError_t launch_tc_projection(const TcArgs &a, const void *map_a, const void *map_b, const double2 *state,
                                  cudaStream_t stream);

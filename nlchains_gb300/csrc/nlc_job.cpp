@@ -166,8 +166,10 @@ extern "C" int nlc_job_linenergies(nlc_ctx *ctx, uint64_t id, double *lin, doubl
 	if (lin) std::memcpy(lin, J->h_diag, n * sizeof(double));
 	if (wt) *wt = J->h_diag[n];
 	if (inf) *inf = J->h_diag[n + 1];
-	if (!std::isfinite(J->h_diag[n]) || !std::isfinite(J->h_diag[n + 1]))
+	if (!std::isfinite(J->h_diag[n]) || !std::isfinite(J->h_diag[n + 1])) {
+		if ((rc = plan_device_status(J->plan))) return rc;
 		return set_error(NLC_EBLOWUP, "non-finite entropy (blow-up or vanishing mode energy)");
+	}
 	return NLC_OK;
 }
 
@@ -293,8 +295,10 @@ extern "C" int nlc_job_sample_wait(nlc_ctx *ctx, uint64_t id, int32_t slot, doub
 	if (wt) *wt = h[n];
 	if (inf) *inf = h[n + 1];
 	if (host_state) std::memcpy(host_state, J->h_state_slot[slot], J->state_bytes);
-	if (!std::isfinite(h[n]) || !std::isfinite(h[n + 1]))
+	if (!std::isfinite(h[n]) || !std::isfinite(h[n + 1])) {
+		if (const int rc = plan_device_status(J->plan)) return rc;
 		return set_error(NLC_EBLOWUP, "non-finite entropy (blow-up or vanishing mode energy)");
+	}
 	return NLC_OK;
 }
 

@@ -464,6 +464,10 @@ int setup_tc_projection(nlc_plan &P, const double *d_omega, int slices) {
 	const int zero = 0;
 	if ((rc = P.upload(&d_status, &zero, 1))) return rc;
 	t.a_slices = d_a, t.row_exp = d_rexp, t.col_exp = d_fexp, t.omega = d_omega, t.status = d_status;
+	// every mbarrier wait of the projection gives up after 2 s; NLC_TEST_TC_WAIT (tests only) makes
+	// each block first wait 1 ms on a barrier nothing arrives at, to exercise the failure path
+	t.wait_ns = 2000000000ull;
+	if (const char *e = std::getenv("NLC_TEST_TC_WAIT"); e && *e && *e != '0') t.wait_test = 1, t.wait_ns = 1000000ull;
 	if ((rc = bf16_map(&P.tc_map_a, d_a, uint64_t(t.kp), uint64_t(slices) * t.mp, 128))) return rc;
 	if ((rc = bf16_map(&P.tc_map_b, d_b, uint64_t(t.kp), uint64_t(slices) * t.np, 64))) return rc;
 	if ((rc = set_smem_attr(tc_projection_kernel_ptr(slices), tc_projection_smem(slices), P.prop))) return rc;
@@ -848,6 +852,15 @@ extern "C" int nlc_plan_omegas(const nlc_plan *P, double *omegas) {
 	if (!P || !omegas) return set_error(NLC_EINVAL, "NULL argument");
 	std::memcpy(omegas, P->omega_host.data(), P->omega_host.size() * sizeof(double));
 	return NLC_OK;
+}
+
+int nlc::plan_device_status(nlc_plan *P) {
+	if (!P || !P->tc || !P->tca.status) return NLC_OK;
+	int st = 0;
+	int rc = cuda_status(cudaMemcpy(&st, P->tca.status, sizeof st, cudaMemcpyDeviceToHost), "projection status");
+	if (rc || !st) return rc;
+	cudaMemset(P->tca.status, 0, sizeof st);
+	return set_error(NLC_ETIMEDOUT, "tensor-core projection: a bounded wait ran out (the sample is NaN)");
 }
 
 extern "C" int nlc_move(nlc_plan *P, void *state, uint32_t steps, void *stream) {

@@ -407,7 +407,10 @@ void worker_loop(nlc_server *S) {
 					R->round_pos = 0;
 				}
 				R->entropies.push_back(R->h_diag[n]), R->entropies.push_back(R->h_diag[n + 1]);
-				if (!std::isfinite(R->h_diag[n]) || !std::isfinite(R->h_diag[n + 1])) R->error = NLC_EBLOWUP;
+				if (!std::isfinite(R->h_diag[n]) || !std::isfinite(R->h_diag[n + 1])) {
+					const int st = plan_device_status(R->plan);   // a timed-out projection, else a blow-up
+					R->error = st ? st : NLC_EBLOWUP;
+				}
 			}
 			g.clear();
 			progressed = true;
@@ -665,5 +668,8 @@ extern "C" int nlc_server_result(nlc_server *S, uint64_t id, void *host_state, d
 	const int err = R.error;
 	S->finished.erase(it);
 	S->where.erase(id);
-	return err ? set_error(err, err == NLC_EBLOWUP ? "non-finite entropy" : "request failed") : NLC_OK;
+	return err ? set_error(err, err == NLC_EBLOWUP    ? "non-finite entropy"
+	                            : err == NLC_ETIMEDOUT ? "a bounded wait of the tensor-core projection ran out"
+	                                                   : "request failed")
+	           : NLC_OK;
 }

@@ -49,17 +49,28 @@ template <int S>
 __host__ __device__ constexpr uint32_t stage_a() { return S * kBM * kBK * 2; }
 template <int S>
 __host__ __device__ constexpr uint32_t stage_bytes() { return S * (kBM + kBN) * kBK * 2; }
-constexpr long long kWaitTries = 1ll << 24;
 constexpr int kNonFiniteRow = 0x7fff;   // row exponent of a row holding inf or NaN
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t) __cvta_generic_to_shared(p); }
 
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
-	for (long long i = 0; i < kWaitTries; i++) {
+// Every mbarrier wait gives up after limit_ns of wall clock (%globaltimer), with an iteration cap
+// as a second bound.
+constexpr long long kWaitTriesMax = 1ll << 30;
+
+__device__ __forceinline__ unsigned long long global_ns() {
+	unsigned long long t;
+	asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+	return t;
+}
+
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, unsigned long long limit_ns) {
+	const unsigned long long t0 = global_ns();
+	for (long long i = 0; i < kWaitTriesMax; i++) {
 		uint32_t ok;
 		asm volatile("{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
 		             : "=r"(ok) : "r"(bar), "r"(parity) : "memory");
 		if (ok) return true;
+		if (global_ns() - t0 > limit_ns) return false;
 	}
 	return false;
 }
@@ -182,14 +193,14 @@ __global__ void __launch_bounds__(128, 1)
 tc_projection_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b, const TcArgs a) {
 	extern __shared__ __align__(1024) unsigned char smem_raw[];
 	unsigned char *smem = (unsigned char *) (((uintptr_t) smem_raw + 1023) & ~(uintptr_t) 1023);
-	__shared__ __align__(8) unsigned long long bars[5];   // full[2], empty[2], acc
+	__shared__ __align__(8) unsigned long long bars[6];   // full[2], empty[2], acc, test
 	__shared__ uint32_t tmem_slot;
 	__shared__ int s_fail;
 	const int tid = threadIdx.x, warp = tid >> 5;
 	const int row0 = blockIdx.x * kBM, col0 = blockIdx.y * kBN;
 	const uint32_t full0 = smem_u32(&bars[0]), empty0 = smem_u32(&bars[2]), accb = smem_u32(&bars[4]);
 	if (tid == 0) {
-		for (int i = 0; i < 5; i++) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&bars[i])));
+		for (int i = 0; i < 6; i++) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&bars[i])));
 		asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 		s_fail = 0;
 	}
@@ -198,6 +209,8 @@ tc_projection_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_con
 		             "r"(kTmemCols));
 		asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
 	}
+	// tests only: a wait that runs out (nothing arrives at the test barrier) takes the failure path
+	if (a.wait_test && tid == 0 && !mbar_wait(smem_u32(&bars[5]), 0, a.wait_ns)) s_fail = 1;
 	asm volatile("tcgen05.fence::before_thread_sync;");
 	__syncthreads();
 	asm volatile("tcgen05.fence::after_thread_sync;");
@@ -237,7 +250,7 @@ tc_projection_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_con
 			for (int it = c0; it < c1 && ok; it++) {
 				const int s = it & 1;
 				const uint32_t ph = (it >> 1) & 1;
-				if (!mbar_wait(full0 + 8 * s, ph)) {
+				if (!mbar_wait(full0 + 8 * s, ph, a.wait_ns)) {
 					ok = false;
 					break;
 				}
@@ -266,7 +279,7 @@ tc_projection_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_con
 				             : "memory");
 				if (it + 2 < nk) {
 					// the stage is free once its MMAs are done; then prefetch two stages ahead
-					if (!mbar_wait(empty0 + 8 * s, ph)) {
+					if (!mbar_wait(empty0 + 8 * s, ph, a.wait_ns)) {
 						ok = false;
 						break;
 					}
@@ -282,7 +295,7 @@ tc_projection_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_con
 			}
 		}
 		// every thread: wait for the chunk's MMAs, then add its groups into the FP64 row sums
-		if (!s_fail && !mbar_wait(accb, chunks & 1)) s_fail = 1;
+		if (!s_fail && !mbar_wait(accb, chunks & 1, a.wait_ns)) s_fail = 1;
 		__syncthreads();
 		if (s_fail) break;
 		asm volatile("tcgen05.fence::after_thread_sync;");
@@ -347,11 +360,11 @@ tc_projection_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_con
 		// after a timeout: wait (each wait bounded again) for the loads this block issued and has not
 		// consumed, then for every MMA it issued, so that nothing lands in shared memory or TMEM after
 		// the block has released them
-		for (int it = consumed; it < issued; it++) mbar_wait(full0 + 8 * (it & 1), (it >> 1) & 1);
+		for (int it = consumed; it < issued; it++) mbar_wait(full0 + 8 * (it & 1), (it >> 1) & 1, a.wait_ns);
 		if (!committed)
 			asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(accb)
 			             : "memory");
-		mbar_wait(accb, chunks & 1);
+		mbar_wait(accb, chunks & 1, a.wait_ns);
 		atomicOr(a.status, 1);
 	}
 	asm volatile("tcgen05.fence::before_thread_sync;");

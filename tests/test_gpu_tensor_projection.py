@@ -90,3 +90,29 @@ def test_bf16x3_projection_error_stated(gpu, n, copies):
     err = np.abs(l3 - l64).max() / np.abs(l64).max()
     assert 0 < err <= 1e-6
     assert abs(w3 - w64) <= 1e-6 * max(1.0, abs(w64)) and abs(i3 - i64) <= 1e-6 * max(1.0, abs(i64))
+
+
+def test_projection_wait_timeout_reported(gpu, monkeypatch):
+    """A projection whose bounded wait runs out (tests only: each block first waits 1 ms on a barrier
+    nothing arrives at) reports NLC_ETIMEDOUT, not a blow-up, and leaves the context usable: a plan
+    made afterwards without the test wait gives the normal result."""
+    n, copies = 256, 64
+    masses = ic.masses_uniform(n, seed=9)
+    state = ic.ddnkg_ensemble(masses, copies, 0.5, 8, seed=9)
+    model = gpu.Model("dDNKG", n, copies, 0.05, masses=masses, beta=1.0)
+    ctx = gpu.Context(0)
+    monkeypatch.setenv("NLC_TEST_TC_WAIT", "1")
+    bad = ctx.job(model, 10)
+    monkeypatch.delenv("NLC_TEST_TC_WAIT")
+    bad.upload(state)
+    for _ in range(2):
+        with pytest.raises(gpu.NlcError) as e:
+            bad.linenergies()
+        assert e.value.code == gpu.ETIMEDOUT
+    good = ctx.job(model, 10)
+    good.upload(state)
+    lin, wt, inf = good.linenergies()
+    assert np.all(np.isfinite(lin)) and np.isfinite(wt) and np.isfinite(inf)
+    bad.close()
+    good.close()
+    ctx.close()
