@@ -75,6 +75,21 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, unsigne
 	return false;
 }
 
+// The same wait with a suspend-time hint (1 us): the thread sleeps in the barrier until it completes
+// or the hint elapses, leaving the issue slots to the thread that issues the loads and MMAs.
+constexpr uint32_t kSleepHintNs = 1000;
+__device__ __forceinline__ bool mbar_wait_sleep(uint32_t bar, uint32_t parity, unsigned long long limit_ns) {
+	const unsigned long long t0 = global_ns();
+	for (long long i = 0; i < kWaitTriesMax; i++) {
+		uint32_t ok;
+		asm volatile("{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3; selp.u32 %0, 1, 0, p; }"
+		             : "=r"(ok) : "r"(bar), "r"(parity), "r"(kSleepHintNs) : "memory");
+		if (ok) return true;
+		if (global_ns() - t0 > limit_ns) return false;
+	}
+	return false;
+}
+
 // Shared-memory matrix descriptor of a K-major tile written by TMA with the 64-byte swizzle:
 // 8-row atoms of 512 bytes (stride byte offset), descriptor version 1, layout type 4.
 __device__ __forceinline__ uint64_t smem_desc(uint32_t saddr) {
@@ -295,7 +310,7 @@ tc_projection_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_con
 			}
 		}
 		// every thread: wait for the chunk's MMAs, then add its groups into the FP64 row sums
-		if (!s_fail && !mbar_wait(accb, chunks & 1, a.wait_ns)) s_fail = 1;
+		if (!s_fail && !mbar_wait_sleep(accb, chunks & 1, a.wait_ns)) s_fail = 1;
 		__syncthreads();
 		if (s_fail) break;
 		asm volatile("tcgen05.fence::after_thread_sync;");
