@@ -211,6 +211,8 @@ tc_projection_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_con
 	__shared__ __align__(8) unsigned long long bars[6];   // full[2], empty[2], acc, test
 	__shared__ uint32_t tmem_slot;
 	__shared__ int s_fail;
+	__shared__ double s_w[kBN];   // per column of the tile: omega_k^2 (weight of the phi rows)
+	__shared__ int s_cexp[kBN];   // per column: the eigenvector's power-of-two exponent
 	const int tid = threadIdx.x, warp = tid >> 5;
 	const int row0 = blockIdx.x * kBM, col0 = blockIdx.y * kBN;
 	const uint32_t full0 = smem_u32(&bars[0]), empty0 = smem_u32(&bars[2]), accb = smem_u32(&bars[4]);
@@ -223,6 +225,11 @@ tc_projection_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_con
 		asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_slot)),
 		             "r"(kTmemCols));
 		asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+	}
+	if (tid < kBN) {
+		const int k = col0 + tid;
+		s_w[tid] = k < (int) a.n ? a.omega[k] * a.omega[k] : 0.;
+		s_cexp[tid] = k < (int) a.n ? a.col_exp[k] : 0;
 	}
 	// tests only: a wait that runs out (nothing arrives at the test barrier) takes the failure path
 	if (a.wait_test && tid == 0 && !mbar_wait(smem_u32(&bars[5]), 0, a.wait_ns)) s_fail = 1;
@@ -345,29 +352,34 @@ tc_projection_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_con
 		__syncthreads();
 	}
 
-	// epilogue: this thread's row r of P, squared and weighted, summed over the tile's rows
-	double *red = reinterpret_cast<double *>(smem);   // [128][64], over the (finished) stages
+	// epilogue: this thread's row r of P, squared and weighted, summed over the tile's rows.  The
+	// buffer (over the finished stages) is column-major with a padded stride: the rows' stores and
+	// the column sums' loads are both free of bank conflicts.
+	constexpr int kRedStride = kBM + 1;
+	double *red = reinterpret_cast<double *>(smem);   // [64][129]
 	const int r = row0 + tid;
 	const bool phi = (r & 1) == 0;
 	const int er = r < 2 * (int) a.copies ? a.row_exp[r] : 0;
 	if (!s_fail) {
 #pragma unroll
 		for (int c = 0; c < kBN; c++) {
-			const int k = col0 + c;
 			double p = 0., w = 1.;
-			if (k < (int) a.n) {
-				p = er == kNonFiniteRow ? __longlong_as_double(0x7ff8000000000000ll) : acc[c] * pow2i(er + a.col_exp[k]);
-				if (phi) w = a.omega[k] * a.omega[k];
+			if (col0 + c < (int) a.n) {
+				p = er == kNonFiniteRow ? __longlong_as_double(0x7ff8000000000000ll) : acc[c] * pow2i(er + s_cexp[c]);
+				if (phi) w = s_w[c];
 			}
-			red[tid * kBN + c] = w * p * p;
+			red[c * kRedStride + tid] = w * p * p;
 		}
 	}
 	__syncthreads();
 	if (tid < kBN) {
 		const int k = col0 + tid;
 		if (k < (int) a.n) {
-			double s = 0.;
-			for (int rr = 0; rr < kBM; rr++) s += red[rr * kBN + tid];
+			// four interleaved partial sums in a fixed order, then added pairwise
+			const double *col = red + tid * kRedStride;
+			double s0 = 0., s1 = 0., s2 = 0., s3 = 0.;
+			for (int rr = 0; rr < kBM; rr += 4) s0 += col[rr], s1 += col[rr + 1], s2 += col[rr + 2], s3 += col[rr + 3];
+			const double s = (s0 + s1) + (s2 + s3);
 			a.partials[(size_t) blockIdx.x * a.n + k] = s_fail ? __longlong_as_double(0x7ff8000000000000ll) : s;
 		}
 	}
