@@ -22,7 +22,7 @@
 // With 3 slices instead of 7 (NLC_FLAG_BF16X3_PROJECTION: 6 slice products, t = 2..4) the same
 // kernels give P to ~2^-24 of the maxima: the north star's "split BF16x3" precision, faster.
 //
-// One CTA: 128 rows (64 chains) x 64 modes; 4 warps.  Thread 0 drives a two-stage TMA pipeline
+// One CTA: 128 rows (64 chains) x 64 modes; 8 warps.  Thread 0 drives a two-stage TMA pipeline
 // (64-byte swizzle, 32 sites of K per stage: 7 A tiles of 128 x 32 and 7 B tiles of 64 x 32) and
 // issues 56 tcgen05.mma (M = 128, N = 64, K = 16, BF16 in, FP32 in TMEM) per stage into eight
 // accumulators: G_t, t = 2..8, with the (2,2) product of G_4 apart (8 x 64 = all 512 TMEM columns).  Every wait is bounded: on a timeout the block records a
@@ -203,8 +203,13 @@ __global__ void tc_split_rows_kernel(const double2 *__restrict__ state, TcArgs a
 	}
 }
 
+// 8 warps: warps w and w + 4 read the same 32 rows of the tile (TMEM lane quarter w mod 4), each
+// one half of the 64 columns, so the FP64 read-out and epilogue work of a thread is halved and
+// every scheduler has two warps to interleave
+constexpr int kThreads = 256, kCols = kBN / 2;
+
 template <int S>
-__global__ void __launch_bounds__(128, 1)
+__global__ void __launch_bounds__(kThreads, 1)
 tc_projection_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b, const TcArgs a) {
 	extern __shared__ __align__(1024) unsigned char smem_raw[];
 	unsigned char *smem = (unsigned char *) (((uintptr_t) smem_raw + 1023) & ~(uintptr_t) 1023);
@@ -214,6 +219,8 @@ tc_projection_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_con
 	__shared__ double s_w[kBN];   // per column of the tile: omega_k^2 (weight of the phi rows)
 	__shared__ int s_cexp[kBN];   // per column: the eigenvector's power-of-two exponent
 	const int tid = threadIdx.x, warp = tid >> 5;
+	const int rl = (warp & 3) * 32 + (tid & 31);   // this thread's row of the tile (its TMEM lane)
+	const int half = warp >> 2;                    // its columns: [kCols half, kCols (half + 1))
 	const int row0 = blockIdx.x * kBM, col0 = blockIdx.y * kBN;
 	const uint32_t full0 = smem_u32(&bars[0]), empty0 = smem_u32(&bars[2]), accb = smem_u32(&bars[4]);
 	if (tid == 0) {
@@ -255,10 +262,10 @@ tc_projection_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_con
 		}
 	};
 
-	double acc[kBN];
+	double acc[kCols];
 #pragma unroll
-	for (int c = 0; c < kBN; c++) acc[c] = 0.;
-	const uint32_t lane_base = (uint32_t) (warp * 32) << 16;
+	for (int c = 0; c < kCols; c++) acc[c] = 0.;
+	const uint32_t lane_base = (uint32_t) ((warp & 3) * 32) << 16;
 	int chunks = 0;
 	for (int c0 = 0; c0 < nk; c0 += per_chunk, chunks++) {
 		const int c1 = min(nk, c0 + per_chunk);
@@ -325,7 +332,8 @@ tc_projection_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_con
 		// of 2^-32, below 2^41; lo: t = 5..8 in units of 2^-64, below 2^49: both exact in FP64), then
 		// two FMAs per column into the FP64 row sums
 #pragma unroll
-		for (int seg = 0; seg < kBN / 8; seg++) {
+		for (int sg = 0; sg < kCols / 8; sg++) {
+			const int seg = half * (kCols / 8) + sg;   // 8-column segment of the tile
 			long long hi[8], lo[8];
 #pragma unroll
 			for (int j = 0; j < 8; j++) hi[j] = 0, lo[j] = 0;
@@ -343,7 +351,7 @@ tc_projection_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_con
 			}
 #pragma unroll
 			for (int j = 0; j < 8; j++) {
-				double &x = acc[seg * 8 + j];
+				double &x = acc[sg * 8 + j];
 				x = fma(i64_to_double(hi[j]), 0x1p-32, x);
 				if constexpr (S + 1 > 4) x = fma(i64_to_double(lo[j]), 0x1p-64, x);
 			}
@@ -357,18 +365,19 @@ tc_projection_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_con
 	// the column sums' loads are both free of bank conflicts.
 	constexpr int kRedStride = kBM + 1;
 	double *red = reinterpret_cast<double *>(smem);   // [64][129]
-	const int r = row0 + tid;
+	const int r = row0 + rl;
 	const bool phi = (r & 1) == 0;
 	const int er = r < 2 * (int) a.copies ? a.row_exp[r] : 0;
 	if (!s_fail) {
 #pragma unroll
-		for (int c = 0; c < kBN; c++) {
+		for (int c = 0; c < kCols; c++) {
+			const int col = half * kCols + c;
 			double p = 0., w = 1.;
-			if (col0 + c < (int) a.n) {
-				p = er == kNonFiniteRow ? __longlong_as_double(0x7ff8000000000000ll) : acc[c] * pow2i(er + s_cexp[c]);
-				if (phi) w = s_w[c];
+			if (col0 + col < (int) a.n) {
+				p = er == kNonFiniteRow ? __longlong_as_double(0x7ff8000000000000ll) : acc[c] * pow2i(er + s_cexp[col]);
+				if (phi) w = s_w[col];
 			}
-			red[c * kRedStride + tid] = w * p * p;
+			red[col * kRedStride + rl] = w * p * p;
 		}
 	}
 	__syncthreads();
@@ -411,10 +420,10 @@ cudaError_t launch_tc_projection(const TcArgs &a, const void *map_a, const void 
 	const unsigned split_blocks = (unsigned) ((a.copies + 7) / 8);
 	if (a.slices == 3) {
 		tc_split_rows_kernel<3><<<split_blocks, 256, 0, stream>>>(state, a);
-		tc_projection_kernel<3><<<grid, 128, tc_projection_smem(3), stream>>>(ma, mb, a);
+		tc_projection_kernel<3><<<grid, kThreads, tc_projection_smem(3), stream>>>(ma, mb, a);
 	} else {
 		tc_split_rows_kernel<kSlicesFull><<<split_blocks, 256, 0, stream>>>(state, a);
-		tc_projection_kernel<kSlicesFull><<<grid, 128, tc_projection_smem(kSlicesFull), stream>>>(ma, mb, a);
+		tc_projection_kernel<kSlicesFull><<<grid, kThreads, tc_projection_smem(kSlicesFull), stream>>>(ma, mb, a);
 	}
 	return cudaGetLastError();
 }
