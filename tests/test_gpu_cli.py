@@ -76,3 +76,47 @@ def test_entropy_limit_stops_early(gpu, tmp_path):
     assert 1 <= ent.shape[0] <= 3
     assert os.path.exists(tmp_path / "o-0")
     assert os.path.exists(tmp_path / f"o-{10 * (ent.shape[0] - 1)}")
+
+
+CLI_MODELS = [
+    ("DNKG", ["-m", "0.5", "--beta", "0.7"], dict(m=0.5, beta=0.7), 0.05),
+    ("FPUT", ["--alpha", "0.3", "--beta", "0.8"], dict(alpha=0.3, beta=0.8), 0.05),
+    ("Toda", ["--alpha", "0.5"], dict(alpha=0.5), 0.05),
+    ("dDNKG", ["-m", "masses", "--beta", "1"], dict(beta=1.0), 0.05),
+    ("DNLS", ["--beta", "1"], dict(beta=1.0), 0.01),
+]
+
+
+@pytest.mark.parametrize("name,flags,params,dt", CLI_MODELS, ids=[c[0] for c in CLI_MODELS])
+@pytest.mark.parametrize("offset", [0, 20])
+def test_every_model_matches_job_api(gpu, tmp_path, name, flags, params, dt, offset):
+    """`nlchains <model>` against the job API on the same input: the entropy rows (times offset,
+    offset + b, ..., steps), the linear energies of every dump and the final dump, identical (the
+    same kernels run in both)."""
+    n, copies, b, steps = 48, 24, 10, 60
+    rng = np.random.default_rng(hash(name) % 1000)
+    state = 0.3 * rng.standard_normal((copies, n, 2))
+    masses = ic.masses_uniform(n, seed=7) if name == "dDNKG" else None
+    if masses is not None:
+        masses.tofile(tmp_path / "masses")
+    ic.write_state(tmp_path / "init", state)
+    r = run_cli(gpu, [name, "-i", "init", "-n", str(n), "-c", str(copies), "--dt", str(dt), "-b", str(b), "-s", str(steps),
+                      "-o", str(offset), "-p", "out", "--dump_interval", "20", *flags], tmp_path)
+    assert r.returncode == 0, r.stderr
+    ent = np.fromfile(tmp_path / "out-entropy").reshape(-1, 3)
+    times = list(range(offset, steps + 1, b))
+    assert ent.shape == (len(times), 3)
+    ctx = gpu.Context(0)
+    job = ctx.job(gpu.Model(name, n, copies, dt, masses=masses, **params), b)
+    job.upload(state)
+    for i, t in enumerate(times):
+        if i:
+            job.advance(b)
+        lin, wt, inf = job.linenergies()
+        assert ent[i, 0] == t * dt and ent[i, 1] == wt and ent[i, 2] == inf, (t, ent[i], wt, inf)
+        if t % 20 == 0:
+            assert np.array_equal(np.fromfile(tmp_path / f"out-linenergies-{t}"), lin)
+            assert np.array_equal(np.fromfile(tmp_path / f"out-{t}").reshape(copies, n, 2),
+                                  job.download().reshape(copies, n, 2))
+    job.close()
+    ctx.close()
