@@ -94,7 +94,7 @@ def test_every_model_matches_job_api(gpu, tmp_path, name, flags, params, dt, off
     offset + b, ..., steps), the linear energies of every dump and the final dump, identical (the
     same kernels run in both)."""
     n, copies, b, steps = 48, 24, 10, 60
-    rng = np.random.default_rng(hash(name) % 1000)
+    rng = np.random.default_rng(sum(map(ord, name)))
     state = 0.3 * rng.standard_normal((copies, n, 2))
     masses = ic.masses_uniform(n, seed=7) if name == "dDNKG" else None
     if masses is not None:
@@ -120,3 +120,38 @@ def test_every_model_matches_job_api(gpu, tmp_path, name, flags, params, dt, off
                                   job.download().reshape(copies, n, 2))
     job.close()
     ctx.close()
+
+
+def test_sigint_stops_an_endless_run(gpu, tmp_path):
+    """`-s 0` runs until stopped (main.cpp:63); SIGINT stops it gracefully after the sample in flight
+    (main.cpp:144, loop_control.hpp:22-25): exit status 0, one entropy row per sample at 0, b, 2b,
+    ..., and a final dump at the last sample's step."""
+    import signal
+    import time
+    n, copies, b, dt = 64, 256, 100, 0.05
+    state = 0.3 * np.random.default_rng(6).standard_normal((copies, n, 2))
+    ic.write_state(tmp_path / "init", state)
+    gpu.build()
+    p = subprocess.Popen([gpu.EXECUTABLE_PATH, "FPUT", "-i", "init", "-n", str(n), "-c", str(copies), "--dt", str(dt),
+                          "-b", str(b), "-s", "0", "-p", "o", "--alpha", "0", "--beta", "1", "--dump_interval", "1000000"],
+                         cwd=tmp_path, stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True)
+    ent = tmp_path / "o-entropy"
+    try:
+        deadline = time.time() + 120
+        while time.time() < deadline and not (ent.exists() and ent.stat().st_size >= 5 * 24):
+            time.sleep(0.05)
+        p.send_signal(signal.SIGINT)
+        _, err = p.communicate(timeout=120)
+    finally:
+        if p.poll() is None:
+            p.kill()
+            p.wait()
+    assert p.returncode == 0, err
+    rows = np.fromfile(ent).reshape(-1, 3)
+    assert rows.shape[0] >= 5
+    steps = np.rint(rows[:, 0] / dt).astype(np.int64)
+    assert np.array_equal(steps, b * np.arange(rows.shape[0]))
+    assert np.all(np.isfinite(rows[:, 1:]))
+    assert os.path.exists(tmp_path / "o-0")
+    last = np.fromfile(tmp_path / f"o-{steps[-1]}").reshape(copies, n, 2)
+    assert np.all(np.isfinite(last))
