@@ -41,6 +41,13 @@ WORKLOAD = dict(name="DNKG N=128 copies=65536 (register-resident tier)", model="
 TODA = dict(name="Toda N=128 copies=65536", model="Toda", n=128, copies=65536, dt=0.05,
             params=dict(alpha=0.5), batching=100, eps=0.5, fraction=0.08, include_zero=False)
 FLOPS_PER_SITE_STEP = {"DNKG": 70, "dDNKG": 70, "FPUT": 91, "Toda": 56, "DNLS": 812}
+# FP64 instructions the engine issues per site-step for these workloads (7 sub-steps, the drift
+# merged across steps): DNKG / dDNKG with beta = 1: 5 per sub-step; FPUT with alpha = 0, beta = 1: 6;
+# Toda with 2 alpha = 1: 12 (8 of them the table exp); DNLS at n = 1024: 77 per sub-step (two
+# 26-operation transforms, the 21-operation phase rotation, the 4-operation propagator) plus the
+# closing rotation of a 10-step launch.  Against the measured FMA issue rate they give the
+# fraction of the FP64 pipe's issue rate the integrator sustains, whatever the operation mix.
+FP64_OPS_PER_SITE_STEP = {"DNKG": 35, "dDNKG": 35, "FPUT": 42, "Toda": 84, "DNLS": 7 * 77 + 21 / 10}
 # the other workloads of the reference's benchmark list, measured as secondary line items
 OTHERS = [
     dict(name="FPUT-beta N=64 copies=1024 (small ensemble)", model="FPUT", n=64, copies=1024, dt=0.1,
@@ -444,7 +451,9 @@ def run_engine(args):
                                "ms_per_step": o["step_ms"], "kernel_ms": o["move_ms"],
                                "steps_per_launch": ow["batching"], "shape": o["shape"],
                                "fp64_frac_of_peak": FLOPS_PER_SITE_STEP[ow["model"]] * ow["n"] * ow["copies"] *
-                               ow["batching"] / (o["move_ms"] * 1e-3) / 1e12 / peak}
+                               ow["batching"] / (o["move_ms"] * 1e-3) / 1e12 / peak,
+                               "fp64_issue_frac": FP64_OPS_PER_SITE_STEP[ow["model"]] * ow["n"] * ow["copies"] *
+                               ow["batching"] / (o["move_ms"] * 1e-3) / (peak * 1e12 / 2)}
         if ow["model"] == "dDNKG" and rank == 0:
             others["dDNKG"]["projection"] = measure_projection(ow, local)
     flops = FLOPS_PER_SITE_STEP[w["model"]] * w["n"] * w["copies"] * w["batching"]
@@ -480,7 +489,9 @@ def run_engine(args):
         "energy_drift": r["energy_drift"] if rank == 0 else None,
         "toda": {"value": toda["value"], "unit": "site-steps/s", "workload": TODA["name"],
                  "roofline_frac": FLOPS_PER_SITE_STEP["Toda"] * TODA["n"] * TODA["copies"] * TODA["batching"] /
-                 (toda["move_ms"] * 1e-3) / 1e12 / peak, "kernel_ms": toda["move_ms"],
+                 (toda["move_ms"] * 1e-3) / 1e12 / peak,
+                 "fp64_issue_frac": FP64_OPS_PER_SITE_STEP["Toda"] * TODA["n"] * TODA["copies"] * TODA["batching"] /
+                 (toda["move_ms"] * 1e-3) / (peak * 1e12 / 2), "kernel_ms": toda["move_ms"],
                  "shape": toda["shape"]},
         "other_workloads": others,
     }
