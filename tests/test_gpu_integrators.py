@@ -253,3 +253,28 @@ def test_graph_steps_equal_plain(gpu, name, n, params, window):
                 os.environ["NLC_FORCE_WINDOW"] = old
     for (pl, pw, pi, ps), (gl, gw, gi, gs) in zip(*runs):
         assert np.array_equal(pl, gl) and pw == gw and pi == gi and np.array_equal(ps, gs)
+
+
+def test_long_run_bit_exact_and_drift(gpu):
+    """10^5 steps of the DNKG benchmark configuration (N = 128, dt = 0.05, m = beta = 1, a low-mode
+    state at energy density 0.5) on 64 copies: the state stays bit-identical to the oracle's device
+    operation order through the whole run (the dynamics is chaotic, so a single differing bit would
+    grow), and the energy drift is no larger than that of the reference's arithmetic order."""
+    n, copies, b, steps = 128, 64, 100, 100000
+    state = ic.real_ensemble(n, copies, 0.5, ic.low_modes(n, 0.08), m=1.0, seed=11)
+    ctx = gpu.Context(0)
+    job = ctx.job(gpu.Model("DNKG", n, copies, 0.05, m=1.0, beta=1.0), b)
+    job.upload(state)
+    job.advance(steps)
+    out = job.download().reshape(copies, n, 2)
+    e_gpu = job.energies()
+    job.close()
+    ctx.close()
+    mdl = O.Model("DNKG", n, copies, 0.05, m=1.0, beta=1.0)
+    dev = O.advance(mdl, state, steps, b, order=O.ORDER_DEVICE).reshape(copies, n, 2)
+    assert np.array_equal(out, dev)
+    ref = O.advance(mdl, state, steps, b, order=O.ORDER_REFERENCE).reshape(copies, n, 2)
+    e0 = O.energies(mdl, state)
+    drift_gpu = np.abs(e_gpu / e0 - 1).max()
+    drift_ref = np.abs(O.energies(mdl, ref) / e0 - 1).max()
+    assert drift_gpu <= 2 * drift_ref + 1e-12, (drift_gpu, drift_ref)
