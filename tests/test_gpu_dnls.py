@@ -94,3 +94,19 @@ def test_phase_rotation_accuracy(gpu):
         theta = -coef * (x * x)
         err = max(np.abs(out[:, 0] - x * np.cos(theta)).max(), np.abs(out[:, 1] - x * np.sin(theta)).max())
         assert err <= 4 * 2.0 ** -52, (coef, err)
+
+
+def test_long_run_conservation(gpu):
+    """10^4 steps of the DNLS benchmark configuration (N = 1024, beta = 1, dt = 0.01, norm density 1
+    over the lowest 10% of modes) on 32 copies: the norm of every chain, exact in exact arithmetic
+    (the phase rotation and the unitary propagator both keep it), holds to rounding, and the
+    energy drift stays bounded."""
+    n, copies, steps = 1024, 32, 10000
+    psi = ic.dnls_ensemble(n, copies, 1.0, ic.low_modes(n, 0.1), seed=9)
+    out = run(gpu, n, copies, 0.01, 1.0, psi, steps, 100)
+    norm0, norm1 = (np.abs(psi) ** 2).sum(1), (np.abs(out) ** 2).sum(1)
+    assert np.abs(norm1 / norm0 - 1).max() < 1e-11
+    mdl = O.Model("DNLS", n, copies, 0.01, beta=1.0)
+    e0 = O.energies(mdl, psi.view(np.float64))
+    e1 = O.energies(mdl, out.view(np.float64))
+    assert np.abs(e1 / e0 - 1).max() < 1e-7
