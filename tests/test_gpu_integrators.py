@@ -278,3 +278,30 @@ def test_long_run_bit_exact_and_drift(gpu):
     drift_gpu = np.abs(e_gpu / e0 - 1).max()
     drift_ref = np.abs(O.energies(mdl, ref) / e0 - 1).max()
     assert drift_gpu <= 2 * drift_ref + 1e-12, (drift_gpu, drift_ref)
+
+
+def test_fput_benchmark_configuration_full_run(gpu):
+    """The FPUT-beta benchmark configuration in full (N = 64, 1024 copies, alpha = 0, beta = 1,
+    dt = 0.1, 10^4 steps sampled every 100: 101 samples; energy density 0.1 in modes +-1..+-4)
+    against the oracle: the final state bit-identical, the linear energies of every sample within
+    1e-10 of the largest and the information entropy within 1e-10.  (The WT entropy, a sum of logs
+    of mode energies, is ill-conditioned while modes hold rounding-level energy, as here.)"""
+    n, copies, b, steps, dt = 64, 1024, 100, 10000, 0.1
+    state = ic.real_ensemble(n, copies, 0.1, ic.low_modes(n, kmax=4, include_zero=False), seed=21)
+    ctx = gpu.Context(0)
+    job = ctx.job(gpu.Model("FPUT", n, copies, dt, alpha=0.0, beta=1.0), b)
+    job.upload(state)
+    mdl = O.Model("FPUT", n, copies, dt, alpha=0.0, beta=1.0)
+    cur = state
+    for t in range(0, steps + 1, b):
+        if t:
+            job.advance(b)
+            cur = O.advance(mdl, cur, b, b, order=O.ORDER_DEVICE)
+        lin, wt, inf = job.linenergies()
+        elin = O.linenergies(mdl, cur)
+        _, einf = O.entropies(elin, True)
+        assert np.abs(lin - elin).max() <= 1e-10 * elin.max(), t
+        assert abs(inf - einf) <= 1e-10 * max(1.0, abs(einf)), t
+    assert np.array_equal(job.download().reshape(copies, n, 2), cur.reshape(copies, n, 2))
+    job.close()
+    ctx.close()
