@@ -255,22 +255,27 @@ def test_graph_steps_equal_plain(gpu, name, n, params, window):
         assert np.array_equal(pl, gl) and pw == gw and pi == gi and np.array_equal(ps, gs)
 
 
-def test_long_run_bit_exact_and_drift(gpu):
-    """10^5 steps of the DNKG benchmark configuration (N = 128, dt = 0.05, m = beta = 1, a low-mode
-    state at energy density 0.5) on 64 copies: the state stays bit-identical to the oracle's device
-    operation order through the whole run (the dynamics is chaotic, so a single differing bit would
-    grow), and the energy drift is no larger than that of the reference's arithmetic order."""
-    n, copies, b, steps = 128, 64, 100, 100000
-    state = ic.real_ensemble(n, copies, 0.5, ic.low_modes(n, 0.08), m=1.0, seed=11)
+@pytest.mark.parametrize("name,params,m,steps,copies", [
+    ("DNKG", dict(m=1.0, beta=1.0), 1.0, 100000, 64),
+    ("Toda", dict(alpha=0.5), 0.0, 20000, 32),
+], ids=["DNKG", "Toda"])
+def test_long_run_bit_exact_and_drift(gpu, name, params, m, steps, copies):
+    """A long run of the benchmark configuration (N = 128, dt = 0.05; DNKG m = beta = 1 for 10^5
+    steps, Toda alpha = 0.5 for 2 10^4; a low-mode state at energy density 0.5): the state stays
+    bit-identical to the oracle's device operation order through the whole run (the dynamics is
+    chaotic, so a single differing bit would grow), and the energy drift is no larger than that of
+    the reference's arithmetic order."""
+    n, b = 128, 100
+    state = ic.real_ensemble(n, copies, 0.5, ic.low_modes(n, 0.08, include_zero=m > 0), m=m, seed=11)
     ctx = gpu.Context(0)
-    job = ctx.job(gpu.Model("DNKG", n, copies, 0.05, m=1.0, beta=1.0), b)
+    job = ctx.job(gpu.Model(name, n, copies, 0.05, **params), b)
     job.upload(state)
     job.advance(steps)
     out = job.download().reshape(copies, n, 2)
     e_gpu = job.energies()
     job.close()
     ctx.close()
-    mdl = O.Model("DNKG", n, copies, 0.05, m=1.0, beta=1.0)
+    mdl = O.Model(name, n, copies, 0.05, **params)
     dev = O.advance(mdl, state, steps, b, order=O.ORDER_DEVICE).reshape(copies, n, 2)
     assert np.array_equal(out, dev)
     ref = O.advance(mdl, state, steps, b, order=O.ORDER_REFERENCE).reshape(copies, n, 2)
