@@ -63,7 +63,7 @@ def build(verbose=False):
         raise RuntimeError("compilation failed: " + ", ".join(failed))
     if _newer(LIB, objs):
         tmp = LIB + ".tmp"
-        cmd = [NVCC, "-shared", *ARCH, "-Xcompiler", "-fPIC", "-o", tmp, *objs, "-lpthread"]
+        cmd = [NVCC, "-shared", *ARCH, "-Xcompiler", "-fPIC", "-o", tmp, *objs, "-lpthread", "-ldl"]
         if verbose:
             print(" ".join(cmd), flush=True)
         subprocess.check_call(cmd)

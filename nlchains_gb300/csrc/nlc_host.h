@@ -8,7 +8,18 @@
 
 #include "nlc_internal.h"
 
+#include <nvtx3/nvToolsExt.h>
+
 namespace nlc {
+// An NVTX range for the life of the object (a stage of an entry point), so that a timeline taken
+// with a profiler shows the engine's stages; without a tool attached the calls return at once.
+struct NvtxRange {
+	explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+	~NvtxRange() { nvtxRangePop(); }
+	NvtxRange(const NvtxRange &) = delete;
+	NvtxRange &operator=(const NvtxRange &) = delete;
+};
+
 // Makes `device` current for the life of the object (one entry point of the C ABI) and restores
 // the caller's current device afterwards, so that a process driving several GPUs from one thread
 // can call any context or plan whatever device it left current; device < 0: no change.

@@ -242,6 +242,7 @@ extern "C" int nlc_job_sample_async(nlc_ctx *ctx, uint64_t id, int32_t slot, int
 
 extern "C" int nlc_job_step_async(nlc_ctx *ctx, uint64_t id, int32_t slot, int32_t copy_state) {
 	DeviceScope ds(ctx ? ctx->device : -1);
+	NvtxRange r("nlc_job_step");
 	Job *J = find_job(ctx, id);
 	if (!J) return set_error(NLC_ENOTFOUND, "no such job");
 	if (slot < 0 || slot > 1) return set_error(NLC_EINVAL, "slot must be 0 or 1");

@@ -596,6 +596,7 @@ extern "C" int nlc_plan_create(const nlc_model *model, nlc_plan **out) {
 	*out = nullptr;
 	int rc = validate(model);
 	if (rc) return rc;
+	NvtxRange r("nlc_plan_create");
 	std::unique_ptr<nlc_plan> P(new nlc_plan);
 	P->m = *model;
 	P->m.masses = nullptr;
@@ -865,6 +866,7 @@ int nlc::plan_device_status(nlc_plan *P) {
 
 extern "C" int nlc_move(nlc_plan *P, void *state, uint32_t steps, void *stream) {
 	DeviceScope ds(P ? P->device : -1);
+	NvtxRange r("nlc_move");
 	return nlc::move_segment(P, state, steps, 0, static_cast<cudaStream_t>(stream));
 }
 
@@ -933,6 +935,7 @@ extern "C" int nlc_energies(nlc_plan *P, const void *state, double *energies, vo
 extern "C" int nlc_linenergies(nlc_plan *P, const void *state, double *lin, double *ent, void *stream) {
 	if (!P || !state || !lin) return set_error(NLC_EINVAL, "NULL argument");
 	DeviceScope ds(P->device);
+	NvtxRange r("nlc_linenergies");
 	cudaStream_t st = static_cast<cudaStream_t>(stream);
 	int rc;
 	if (P->tc) {

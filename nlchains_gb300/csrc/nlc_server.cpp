@@ -269,6 +269,7 @@ uint32_t segment_steps(const nlc_server *S, const Request &R, unsigned long long
 // packed launch; one: its own plan's launch) on stream slot `slot`, plus the sample of each request
 // whose round the segment closes.
 int launch_group(nlc_server *S, size_t slot, const std::vector<Request *> &reqs) {
+	NvtxRange r("server group");
 	cudaStream_t st = S->streams[slot];
 	int rc = NLC_OK;
 	unsigned long long group_blocks = 0;
