@@ -185,7 +185,7 @@ int admit(nlc_server *S, Request &R, cudaStream_t st) {
 	return NLC_OK;
 }
 
-int sample(nlc_server *S, Request &R, cudaStream_t st) {
+int sample(Request &R, cudaStream_t st) {
 	const size_t n = R.model.chain_length;
 	int rc = nlc_linenergies(R.plan, R.d_state, R.d_diag, R.d_diag + n, st);
 	if (rc) return rc;
@@ -322,7 +322,7 @@ int launch_group(nlc_server *S, size_t slot, const std::vector<Request *> &reqs)
 			return rc;
 	}
 	for (Request *R : reqs)
-		if (!rc && R->seg_samples) rc = sample(S, *R, st);
+		if (!rc && R->seg_samples) rc = sample(*R, st);
 	if (!rc) rc = cuda_status(cudaEventRecord(S->events[slot], st), "cudaEventRecord");
 	return rc;
 }
@@ -478,7 +478,7 @@ void worker_loop(nlc_server *S) {
 			if (sample_only) {
 				g.swap(first_samples);
 				for (Request *R : g)
-					if (!rc) rc = sample(S, *R, S->streams[slot]);
+					if (!rc) rc = sample(*R, S->streams[slot]);
 				if (!rc) rc = cuda_status(cudaEventRecord(S->events[slot], S->streams[slot]), "cudaEventRecord");
 			} else {
 				g = groups[next++];
