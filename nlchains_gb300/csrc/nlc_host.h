@@ -95,6 +95,12 @@ constexpr uint32_t kMaxFftLen = 1u << 18;
 // spectra FFT_m(g_k) / m (interleaved), so that x (*) h_k = IFFT_m(FFT_m(x) G_k) on [0, n).
 std::vector<double> dnls_conv_tables(const std::vector<double> &lin, uint32_t n, uint32_t m);
 
+// Host threads of the set-up work (the dDNKG eigensolver): one per core (at most 32, or
+// NLC_HOST_THREADS), or what set_host_setup_threads chose for the calling thread (the request
+// server's preparers share the cores with each other and with its scheduler).
+unsigned host_setup_threads();
+void set_host_setup_threads(unsigned threads);
+
 // Symmetric eigensystem of the periodic dDNKG operator diag(mp2) - shift(+-1) (eigensystem.cpp:
 // 15-18): ascending eigenvalues, omegas = sqrt(eigenvalues), eigenvectors column-major
 // (eigvec[k*n + s] = component s of eigenvector k), as Armadillo's eig_sym would return them.

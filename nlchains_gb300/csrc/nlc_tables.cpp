@@ -5,6 +5,7 @@
 #include <cmath>
 #include <complex>
 #include <condition_variable>
+#include <cstdlib>
 #include <cstring>
 #include <functional>
 #include <mutex>
@@ -408,11 +409,23 @@ FftTables fft_tables(uint32_t n, uint32_t smem_len, uint32_t max_len, bool convo
 	return T;
 }
 
+namespace {
+thread_local unsigned t_host_threads = 0;
+}
+
+void set_host_setup_threads(unsigned threads) { t_host_threads = threads; }
+
+unsigned host_setup_threads() {
+	if (t_host_threads) return t_host_threads;
+	unsigned hw = std::max(1u, std::min(32u, std::thread::hardware_concurrency()));
+	if (const char *e = std::getenv("NLC_HOST_THREADS"); e && std::atoi(e) > 0) hw = unsigned(std::atoi(e));
+	return hw;
+}
+
 bool eigensystem_periodic(const std::vector<double> &mp2, std::vector<double> &omegas, std::vector<double> &eigvec) {
 	const size_t n = mp2.size();
 	if (n < 2) return false;
-	const unsigned hw = std::max(1u, std::min(32u, std::thread::hardware_concurrency()));
-	Pool pool(n >= 512 ? hw : 1);
+	Pool pool(n >= 512 ? host_setup_threads() : 1);
 	// dense symmetric matrix, column-major A[j*n + i]
 	std::vector<double> A(n * n, 0.), Q(n * n, 0.);
 	auto a = [&](size_t i, size_t j) -> double & { return A[j * n + i]; };
