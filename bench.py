@@ -419,6 +419,42 @@ def measure_projection(w, local):
                       "FP64 recombination, energy epilogue fused"}
 
 
+def measure_fp32_diagnostics(w, local, evolve_steps=1000):
+    """One diagnostics sample of the DNLS workload (its initial state advanced by 1000 steps, so that
+    energy has spread beyond the initial modes) with the FP64 transform and with
+    NLC_FLAG_FP32_DIAGNOSTICS: times, and the FP32 path's error against FP64 for the mode energies
+    (largest difference over the largest energy) and both entropies."""
+    import torch
+
+    import nlchains_gb300 as nlc
+    n, copies = w["n"], w["copies"]
+    dev = torch.from_numpy(initial_state(w, copies, 0)).cuda()
+    sp = torch.cuda.current_stream().cuda_stream
+    plans = {name: nlc.Plan(nlc.Model(w["model"], n, copies, w["dt"], flags=flag, **w["params"]))
+             for name, flag in (("fp64", 0), ("fp32", nlc.FLAG_FP32_DIAGNOSTICS))}
+    plans["fp64"].move(dev.data_ptr(), evolve_steps, sp)
+    res = {}
+    for name, plan in plans.items():
+        lin = torch.zeros(n, dtype=torch.float64, device="cuda")
+        ent = torch.zeros(2, dtype=torch.float64, device="cuda")
+        for _ in range(3):
+            plan.linenergies(dev.data_ptr(), lin.data_ptr(), ent.data_ptr(), sp)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(20):
+            plan.linenergies(dev.data_ptr(), lin.data_ptr(), ent.data_ptr(), sp)
+        e1.record()
+        torch.cuda.synchronize()
+        res[name] = (e0.elapsed_time(e1) / 20, lin.cpu().numpy(), ent.cpu().numpy())
+        plan.close()
+    (t64, l64, s64), (t32, l32, s32) = res["fp64"], res["fp32"]
+    return {"state": f"the workload's initial state after {evolve_steps} steps", "fp64_ms": t64, "fp32_ms": t32,
+            "speedup": t64 / t32, "energies_max_diff_over_max": float(np.abs(l32 - l64).max() / np.abs(l64).max()),
+            "wt_abs_diff": float(abs(s32[0] - s64[0])), "inf_rel_diff": float(abs(s32[1] - s64[1]) / abs(s64[1])),
+            "method": "per-chain FFT and mode energies in FP32, sum over chains in FP64"}
+
+
 def read_traffic(kernel_key):
     """DRAM bytes per launch from the committed ncu summary (profiles/traffic.tsv), or None."""
     path = os.path.join(ROOT, "profiles", "traffic.tsv")
@@ -456,6 +492,8 @@ def run_engine(args):
                                ow["batching"] / (o["move_ms"] * 1e-3) / (peak * 1e12 / 2)}
         if ow["model"] == "dDNKG" and rank == 0:
             others["dDNKG"]["projection"] = measure_projection(ow, local)
+        if ow["model"] == "DNLS" and rank == 0:
+            others["DNLS"]["fp32_diagnostics"] = measure_fp32_diagnostics(ow, local)
     flops = FLOPS_PER_SITE_STEP[w["model"]] * w["n"] * w["copies"] * w["batching"]
     achieved = flops / (r["move_ms"] * 1e-3) / 1e12
     out = {

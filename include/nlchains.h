@@ -67,8 +67,12 @@ enum {
 	                                    split, FP32 accumulation, FP64 recombination: FP64-level error);
 	                                    chosen by default from 128 sites */
 	NLC_FLAG_FP64_PROJECTION = 64,   /* dDNKG: the mode projection on the FP64 CUDA cores at any length */
-	NLC_FLAG_BF16X3_PROJECTION = 128 /* dDNKG: the tensor-core projection with 3 BF16 slices: faster, with
+	NLC_FLAG_BF16X3_PROJECTION = 128, /* dDNKG: the tensor-core projection with 3 BF16 slices: faster, with
 	                                    mode energies to ~1e-7 relative instead of FP64 level */
+	NLC_FLAG_FP32_DIAGNOSTICS = 256  /* DNKG, FPUT, Toda, DNLS: the per-chain transform and mode energies
+	                                    in FP32 (the sum over chains in FP64): mode energies to ~1e-7 of
+	                                    the largest; lengths that need the padded transform or
+	                                    global-memory passes keep the FP64 diagnostics */
 };
 
 /*

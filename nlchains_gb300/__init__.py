@@ -28,6 +28,7 @@ MODEL_NAMES = {v: k for k, v in MODELS.items()}
 OK, EINVAL, ECUDA, ENOMEM, EIO, ETIMEDOUT, ENOTFOUND, EBLOWUP, EUNSUPPORTED = 0, -1, -2, -3, -4, -5, -6, -7, -8
 FLAG_SPLIT_KERNEL, FLAG_NO_TUNE, FLAG_CANONICAL_SHAPE, FLAG_COMPACT_DIAG = 1, 2, 4, 8
 FLAG_SHARED_GPU, FLAG_TENSOR_PROJECTION, FLAG_FP64_PROJECTION, FLAG_BF16X3_PROJECTION = 16, 32, 64, 128
+FLAG_FP32_DIAGNOSTICS = 256
 REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_FAILED = 0, 1, 2, 3
 
 # the exported symbols, as declared in include/nlchains.h

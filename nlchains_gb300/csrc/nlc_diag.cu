@@ -63,6 +63,50 @@ __global__ void lin_fft_kernel(const double2 *__restrict__ state, const DiagArgs
 	}
 }
 
+// The FP32 diagnostics (NLC_FLAG_FP32_DIAGNOSTICS): the same teams and partial rows, each chain
+// transformed in FP32 in shared memory (half the bytes of the FP64 buffers) and its mode energies
+// formed in FP32; the sum over chains stays in the FP64 partial rows.  The error against the FP64
+// path is that of an FP32 transform, ~1e-7 of the largest mode energies.
+template <bool BLOCK>
+__global__ void lin_fft32_kernel(const double2 *__restrict__ state, const DiagArgs a) {
+	extern __shared__ float2 smf[];
+	const int n = int(a.n);
+	const int T = BLOCK ? blockDim.x : 32;
+	const int t = BLOCK ? threadIdx.x : (threadIdx.x & 31);
+	const int team = BLOCK ? 0 : (threadIdx.x >> 5);
+	const int teams = BLOCK ? 1 : (blockDim.x >> 5);
+	const int len = a.fft.len;
+	float2 *x = smf + (size_t) team * 2 * len;
+	float2 *y = x + len;
+	double *acc = a.partials + ((size_t) blockIdx.x * teams + team) * n;
+	for (int k = t; k < n; k += T) acc[k] = 0.;
+	const bool dnls = a.model == NLC_DNLS;
+	for (unsigned long long chain = (unsigned long long) blockIdx.x * teams + team; chain < a.copies;
+	     chain += (unsigned long long) gridDim.x * teams) {
+		const double2 *src = state + chain * (unsigned long long) n;
+		for (int k = t; k < n; k += T) {
+			const double2 v = src[k];
+			x[k] = make_float2(__double2float_rn(v.x), __double2float_rn(v.y));
+		}
+		team_sync<BLOCK>();
+		const float2 *Z = stockham32_team<BLOCK>(a.fft, a.tw32, x, y, t, T);
+		for (int k = t; k < n; k += T) {
+			const float2 zk = Z[k];
+			float e;
+			if (dnls) {
+				e = fmaf(zk.x, zk.x, zk.y * zk.y);
+			} else {
+				const float2 zm = Z[k ? n - k : 0];
+				const float ak = a.coef32[k], bk = a.coef32[n + k];
+				const float re = fmaf(ak, zk.x, bk * zm.x), im = fmaf(ak, zk.y, -(bk * zm.y));
+				e = fmaf(re, re, im * im);
+			}
+			acc[k] += (double) e;
+		}
+		team_sync<BLOCK>();
+	}
+}
+
 // dDNKG projection: a block takes CH chains at a time; thread k of a block of modes accumulates
 // sum_c (omega_k e_k.phi_c)^2 + (e_k.pi_c)^2 over its chains.  The chains' sites pass through shared
 // memory in chunks of a.proj_chunk (whole chains when they fit), the eigenvector matrix is read
@@ -124,6 +168,9 @@ cudaError_t launch_linenergies_partials(const DiagArgs &a, const void *state, in
 	count_launch();
 	if (a.model == NLC_DDNKG) {
 		lin_ddnkg_kernel<<<blocks, threads, smem, stream>>>(st, a);
+	} else if (a.tw32) {
+		if (team_block) lin_fft32_kernel<true><<<blocks, threads, smem / 2, stream>>>(st, a);
+		else lin_fft32_kernel<false><<<blocks, threads, smem / 2, stream>>>(st, a);
 	} else if (team_block) {
 		lin_fft_kernel<true><<<blocks, threads, smem, stream>>>(st, a);
 	} else {
@@ -312,6 +359,9 @@ cudaError_t launch_fp64_probe(double *out, int blocks, int threads, int iters, c
 }  // namespace nlc
 
 namespace nlc {
+const void *lin32_kernel_ptr(int team_block) {
+	return team_block ? (const void *) lin_fft32_kernel<true> : (const void *) lin_fft32_kernel<false>;
+}
 const void *lin_kernel_ptr(int model, int team_block) {
 	if (model == NLC_DDNKG) return (const void *) lin_ddnkg_kernel;
 	return team_block ? (const void *) lin_fft_kernel<true> : (const void *) lin_fft_kernel<false>;

@@ -259,6 +259,75 @@ __device__ double2 *stockham_team(const FftPlanDev &P, double2 *x, double2 *y, i
 	return x;
 }
 
+// FP32 forward transform for the FP32 diagnostics: the same decimation-in-time passes, with plain
+// complex products by the twiddles of a float table tw[e] = exp(-2 pi i e / len) and FP32 sums.
+// Only for direct passes (the plan keeps FP64 diagnostics for padded lengths).
+__device__ __forceinline__ float2 cmulf(float2 a, float2 w) {
+	return make_float2(fmaf(a.x, w.x, -(a.y * w.y)), fmaf(a.x, w.y, a.y * w.x));
+}
+
+template <bool BLOCK>
+__device__ float2 *stockham32_team(const FftPlanDev &P, const float2 *__restrict__ tw, float2 *x, float2 *y, int t,
+                                   int T) {
+	const int n = P.len;
+	int Ns = 1;
+	for (int r = 0; r < P.nradix; r++) {
+		const int p = P.radix[r];
+		const int m = n / p;
+		const int stride = n / (Ns * p);   // twiddle w^{uk} = tw[u k stride]
+		if (p == 4) {
+			for (int b = t; b < m; b += T) {
+				const int q = b / Ns, kk = b - q * Ns;
+				float2 a0 = x[b], a1 = x[b + m], a2 = x[b + 2 * m], a3 = x[b + 3 * m];
+				if (Ns > 1) {
+					const int e = kk * stride;
+					a1 = cmulf(a1, tw[e]), a2 = cmulf(a2, tw[2 * e]), a3 = cmulf(a3, tw[3 * e]);
+				}
+				const float2 b0 = make_float2(a0.x + a2.x, a0.y + a2.y), b1 = make_float2(a0.x - a2.x, a0.y - a2.y);
+				const float2 b2 = make_float2(a1.x + a3.x, a1.y + a3.y);
+				const float2 b3 = make_float2(a1.y - a3.y, a3.x - a1.x);   // -i (a1 - a3)
+				float2 *o = y + q * 4 * Ns + kk;
+				o[0] = make_float2(b0.x + b2.x, b0.y + b2.y);
+				o[Ns] = make_float2(b1.x + b3.x, b1.y + b3.y);
+				o[2 * Ns] = make_float2(b0.x - b2.x, b0.y - b2.y);
+				o[3 * Ns] = make_float2(b1.x - b3.x, b1.y - b3.y);
+			}
+		} else if (p == 2) {
+			for (int b = t; b < m; b += T) {
+				const int q = b / Ns, kk = b - q * Ns;
+				float2 a0 = x[b], a1 = x[b + m];
+				if (Ns > 1) a1 = cmulf(a1, tw[kk * stride]);
+				float2 *o = y + q * 2 * Ns + kk;
+				o[0] = make_float2(a0.x + a1.x, a0.y + a1.y);
+				o[Ns] = make_float2(a0.x - a1.x, a0.y - a1.y);
+			}
+		} else {
+			// direct p-point DFT of the twiddled inputs: X_v = sum_u a_u tw[u (k + v Ns) stride mod n]
+			for (int b = t; b < m; b += T) {
+				const int q = b / Ns, kk = b - q * Ns;
+				for (int v = 0; v < p; v++) {
+					const int step = int((long long) (kk + v * Ns) * stride % n);
+					float re = 0.f, im = 0.f;
+					int e = 0;
+					for (int u = 0; u < p; u++) {
+						const float2 a = x[b + u * m], w = tw[e];
+						re = fmaf(a.x, w.x, fmaf(-a.y, w.y, re));
+						im = fmaf(a.x, w.y, fmaf(a.y, w.x, im));
+						e += step;
+						if (e >= n) e -= n;
+					}
+					y[q * p * Ns + kk + v * Ns] = make_float2(re, im);
+				}
+			}
+		}
+		team_sync<BLOCK>();
+		float2 *sw = x;
+		x = y, y = sw;
+		Ns *= p;
+	}
+	return x;
+}
+
 __device__ __forceinline__ double2 conj2(double2 a) { return make_double2(a.x, -a.y); }
 
 // Transform of one chain of length P.n held in x[0, n); x and y hold P.len elements each.

@@ -143,6 +143,8 @@ struct DiagArgs {
 	double *partials;        // [blocks][n]
 	double2 *gscratch;       // block teams whose buffers exceed shared memory: [blocks][2][len]
 	int proj_chunk;          // dDNKG: sites per shared-memory chunk of the projection
+	const float2 *tw32;      // FP32 diagnostics (NLC_FLAG_FP32_DIAGNOSTICS): twiddles in FP32; NULL: FP64
+	const float *coef32;     // FP32 diagnostics, real models: [2][n] the coef_a and coef_b in FP32
 };
 
 // FMA-form twiddles of a decimation-in-time pass (nlc_fft.cuh): pass radix p in {2, 3, 4} after Ns

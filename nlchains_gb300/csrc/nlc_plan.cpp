@@ -544,6 +544,24 @@ int setup_diagnostics(nlc_plan &P) {
 				if ((rc = P.dalloc(&g.gscratch, size_t(P.diag_blocks) * 2 * len))) return rc;
 			}
 		}
+		// FP32 diagnostics: for direct transforms held in shared memory (padded lengths and
+		// global-memory passes keep the FP64 transform)
+		if ((P.m.flags & NLC_FLAG_FP32_DIAGNOSTICS) && !g.fft.bluestein && !g.gscratch) {
+			const std::vector<double> tw = fft_twiddles(len);
+			std::vector<float2> tw32(len);
+			for (uint32_t e = 0; e < len; e++) tw32[e] = make_float2(float(tw[2 * e]), float(tw[2 * e + 1]));
+			float2 *d_tw32 = nullptr;
+			if ((rc = P.upload(&d_tw32, tw32.data(), len))) return rc;
+			g.tw32 = d_tw32;
+			if (P.m.model != NLC_DNLS) {
+				std::vector<float> c32(2 * size_t(n));
+				for (uint32_t k = 0; k < n; k++)
+					c32[k] = float((P.omega_host[k] + 1) / 2), c32[n + k] = float((P.omega_host[k] - 1) / 2);
+				float *d_c32 = nullptr;
+				if ((rc = P.upload(&d_c32, c32.data(), c32.size()))) return rc;
+				g.coef32 = d_c32;
+			}
+		}
 	}
 	if (P.diag_smem > size_t(P.prop.sharedMemPerBlockOptin))
 		return set_error(NLC_EUNSUPPORTED, "chain_length too large for the shared-memory diagnostics");
@@ -588,6 +606,7 @@ int set_smem_attr(const void *k, size_t smem, const cudaDeviceProp &prop) {
 // kernels whose dynamic shared memory may exceed 48 KiB
 namespace nlc {
 const void *lin_kernel_ptr(int model, int team_block);
+const void *lin32_kernel_ptr(int team_block);
 const void *dnls_kernel_ptr(int team_block);
 }  // namespace nlc
 
@@ -798,8 +817,9 @@ extern "C" int nlc_plan_create(const nlc_model *model, nlc_plan **out) {
 	}
 	if ((rc = setup_diagnostics(*P))) return rc;
 	{
-		const void *k = lin_kernel_ptr(mdl, P->diag_team_block);
-		if ((rc = set_smem_attr(k, P->diag_smem, P->prop))) return rc;
+		const bool fp32 = P->ga.tw32 != nullptr;
+		const void *k = fp32 ? lin32_kernel_ptr(P->diag_team_block) : lin_kernel_ptr(mdl, P->diag_team_block);
+		if ((rc = set_smem_attr(k, fp32 ? P->diag_smem / 2 : P->diag_smem, P->prop))) return rc;
 	}
 	// every allocation and upload above is ordered on the legacy stream: complete them before the
 	// plan is used from other streams

@@ -100,3 +100,31 @@ def test_blowup_is_reported(gpu):
     with pytest.raises(gpu.NlcError) as e:
         job.linenergies()
     assert e.value.code == gpu.EBLOWUP
+
+
+FP32_CASES = [("DNLS", dict(beta=1.0), 1024), ("DNLS", dict(beta=1.0), 96), ("DNLS", dict(beta=1.0), 100),
+              ("DNKG", dict(m=1.0, beta=1.0), 128), ("FPUT", dict(alpha=0.0, beta=1.0), 64),
+              ("Toda", dict(alpha=0.5), 1536)]
+
+
+@pytest.mark.parametrize("model,params,n", FP32_CASES, ids=[f"{c[0]}-{c[2]}" for c in FP32_CASES])
+def test_fp32_diagnostics_error_stated(gpu, model, params, n):
+    """NLC_FLAG_FP32_DIAGNOSTICS against the FP64 oracle (radix-4, -2, -3 and -5 passes): mode
+    energies within 2e-5 of the largest, the information entropy within 2e-5 relative (an FP32
+    transform, the sum over chains in FP64).  The WT entropy, a sum of logs, is left out: its FP32
+    error grows with the number of weak modes."""
+    copies = 96
+    rng = np.random.default_rng(n + 5)
+    state = rng.standard_normal((copies, n, 2))
+    ctx = gpu.Context(0)
+    job = ctx.job(gpu.Model(model, n, copies, 0.05, flags=gpu.FLAG_FP32_DIAGNOSTICS, **params), 10)
+    job.upload(state)
+    lin, wt, inf = job.linenergies()
+    job.close()
+    ctx.close()
+    mdl = O.Model(model, n, copies, 0.05, **params)
+    elin = O.linenergies(mdl, state)
+    _, einf = O.entropies(elin, O.a0is0(mdl))
+    err = np.abs(lin - elin).max() / np.abs(elin).max()
+    assert 0 < err <= 2e-5, err   # not zero: the FP32 path ran
+    assert abs(inf - einf) <= 2e-5 * abs(einf)
