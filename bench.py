@@ -382,10 +382,12 @@ def cpu_baseline(w, target_s=10.0, threads=None, sample_copies=None, steps_per_c
                       f"({t:.1f} s), oracle port of the reference CPU loop, -Ofast like the reference's CPU build, OpenMP over copies"}
 
 
-def measure_projection(w, local):
-    """One diagnostics sample of the dDNKG workload with the mode projection on the FP64 CUDA cores,
-    on the tensor cores (7 slices, the default) and as BF16x3 (3 slices): times and largest relative
-    difference of the mode energies against the FP64 projection."""
+def measure_projection(w, local, evolve_steps=1000):
+    """One diagnostics sample of the dDNKG workload (its initial state advanced by 1000 steps; at the
+    initial state most modes hold rounding-level energy and the WT entropy, a sum of their logs, is
+    ill-conditioned) with the mode projection on the FP64 CUDA cores, on the tensor cores (7 slices,
+    the default) and as BF16x3 (3 slices): times, and the differences of the mode energies and of
+    both entropies against the FP64 projection."""
     import torch
 
     import nlchains_gb300 as nlc
@@ -396,6 +398,8 @@ def measure_projection(w, local):
     for name, flag in (("fp64", nlc.FLAG_FP64_PROJECTION), ("tensor", nlc.FLAG_TENSOR_PROJECTION),
                        ("bf16x3", nlc.FLAG_BF16X3_PROJECTION)):
         plan = nlc.Plan(nlc.Model(w["model"], n, copies, w["dt"], masses=masses(w), flags=flag, **w["params"]))
+        if name == "fp64":
+            plan.move(dev.data_ptr(), evolve_steps, sp)
         lin = torch.zeros(n, dtype=torch.float64, device="cuda")
         ent = torch.zeros(2, dtype=torch.float64, device="cuda")
         for _ in range(3):
@@ -407,13 +411,20 @@ def measure_projection(w, local):
             plan.linenergies(dev.data_ptr(), lin.data_ptr(), ent.data_ptr(), sp)
         e1.record()
         torch.cuda.synchronize()
-        res[name] = (e0.elapsed_time(e1) / 20, lin.cpu().numpy())
+        res[name] = (e0.elapsed_time(e1) / 20, lin.cpu().numpy(), ent.cpu().numpy())
         plan.close()
-    ref = res["fp64"][1]
+    ref, eref = res["fp64"][1], res["fp64"][2]
     diff = float(np.abs(res["tensor"][1] - ref).max() / np.abs(ref).max())
     diff3 = float(np.abs(res["bf16x3"][1] - ref).max() / np.abs(ref).max())
+
+    def ent_diffs(name):
+        e = res[name][2]
+        return {"wt_abs_diff": float(abs(e[0] - eref[0])), "inf_rel_diff": float(abs(e[1] - eref[1]) / abs(eref[1]))}
+
     return {"fp64_ms": res["fp64"][0], "tensor_ms": res["tensor"][0], "speedup": res["fp64"][0] / res["tensor"][0],
-            "max_rel_diff": diff, "bf16x3_ms": res["bf16x3"][0], "bf16x3_max_rel_diff": diff3,
+            "state": f"the workload's initial state after {evolve_steps} steps",
+            "max_rel_diff": diff, "tensor_entropies": ent_diffs("tensor"), "bf16x3_ms": res["bf16x3"][0],
+            "bf16x3_max_rel_diff": diff3, "bf16x3_entropies": ent_diffs("bf16x3"),
             "flops": 4.0 * copies * n * n,
             "method": "tcgen05 BF16 MMA, 7-slice split of X and of the eigenvectors, FP32 accumulation in TMEM, "
                       "FP64 recombination, energy epilogue fused"}
