@@ -7,7 +7,7 @@ __graft_entry__.smoke() and bench.py's CPU-baseline leg may import this package;
 
 Parity status: unpinned against the reference itself (the reference has no tests, golden vectors or
 fixtures, and it cannot be built in this image: Boost.MPI, MPI, FFTW3 and Armadillo are absent).
-The oracle is pinned by analytic known answers in tests/test_oracle.py.
+The oracle is pinned by analytic known answers in tests/test_oracle.py and tests/test_known_answers.py.
 """
 import ctypes
 import os

@@ -1,11 +1,13 @@
 /*
  * nlc_oracle.c -- TEST INFRASTRUCTURE ONLY (see nlc_oracle.h).  CPU restatement of the nlchains
- * hot path.  Built twice by oracle/build.py: a strict checker (-O2 -ffp-contract=off) and the timed
- * CPU baseline (-O3 -fopenmp -ffp-contract=off, one OpenMP thread per core over copies, the moral
- * equivalent of `mpirun -n <cores> nlchains <model>-cpu`).
+ * hot path.  Built twice by oracle/build.py: a strict checker (-O2 -ffp-contract=off, the one the
+ * tests compare against) and the timed CPU baseline (-Ofast -ffp-contract=fast -fopenmp, as the
+ * reference's CPU build is -Ofast; one OpenMP thread per core over copies, the moral equivalent of
+ * `mpirun -n <cores> nlchains <model>-cpu`).
  *
  * Parity unpinned against the reference (no reference tests or fixtures exist and it cannot be
- * built in this image); pinned by analytic known answers in tests/.
+ * built in this image); pinned by analytic known answers in tests/ (test_oracle.py,
+ * test_known_answers.py).
  */
 #include "nlc_oracle.h"
 
