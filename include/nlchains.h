@@ -112,6 +112,22 @@ int nlc_plan_create(const nlc_model *model, nlc_plan **plan);
 int nlc_plan_destroy(nlc_plan *plan);
 
 /*
+ * A seeded initial ensemble written straight into caller device memory (copies x chain_length in
+ * the state layout above), for ensembles too large to build and upload from the host.  The recipes
+ * and random numbers are those of nlchains_gb300/ic.py: uniform phases from SplitMix64 counters
+ * keyed by (seed, copy first_copy + c, mode), every excited mode with the same energy; to rounding
+ * the same ensemble as ic.py's (a different transform).
+ *   DNKG, FPUT, Toda: `density` = energy per site, spread over the listed wave numbers (DFT
+ *     indices; list +k and n - k for a real standing wave; a zero-frequency mode is skipped);
+ *   DNLS: `density` = norm per site, psi_hat equal in modulus over the listed wave numbers;
+ *   dDNKG: `density` = energy per site over the listed eigenmodes (indices in ascending order of
+ *     frequency).
+ * Synchronous with respect to `stream` (it returns once the state is written).
+ */
+int nlc_initial_state(nlc_plan *plan, uint64_t seed, uint64_t first_copy, double density, const uint32_t *modes,
+                      uint32_t nmodes, void *state_dev, void *stream);
+
+/*
  * Advance every chain of the device state by `steps` Yoshida steps in one fused launch (the merged
  * drift inside the launch and the closing drift dt*c[7] as in DNKG_FPUT_Toda.cu:117-146).
  * Replaces `template<Model> completion move(plane2split*&, cudaStream_t)` (DNKG_FPUT_Toda.hpp:22-23,

@@ -40,7 +40,7 @@ EXPORTS = (
     "nlc_version", "nlc_kernel_launches", "nlc_fp64_peak", "nlc_linenergies_noalloc",
     "nlc_server_create", "nlc_server_destroy", "nlc_server_submit", "nlc_server_poll", "nlc_server_wait",
     "nlc_server_result", "nlc_entropies", "nlc_job_sample_async", "nlc_job_sample_wait", "nlc_energies",
-    "nlc_job_energies", "nlc_job_step_async", "nlc_job_after",
+    "nlc_job_energies", "nlc_job_step_async", "nlc_job_after", "nlc_initial_state",
 )
 
 
@@ -106,6 +106,7 @@ def lib():
         "nlc_job_download": ([vp, u64, vp], i32),
         "nlc_job_wait": ([vp, u64, i32], i32),
         "nlc_job_after": ([vp, u64, u64], i32),
+        "nlc_initial_state": ([vp, u64, u64, ctypes.c_double, P(ctypes.c_uint32), ctypes.c_uint32, vp, vp], i32),
         "nlc_job_state_ptr": ([vp, u64, P(vp)], i32),
         "nlc_program_run": ([ctypes.c_int, P(ctypes.c_char_p)], ctypes.c_int),
         "nlc_last_error": ([], ctypes.c_char_p),
@@ -221,6 +222,13 @@ class Plan:
             self.close()
         except Exception:
             pass
+
+    def initial_state(self, state_ptr, seed, density, modes, first_copy=0, stream=0):
+        """Seeded initial ensemble into device memory (nlc_initial_state; the ic.py recipes)."""
+        m = np.ascontiguousarray(np.asarray(modes, dtype=np.uint32))
+        _check(lib().nlc_initial_state(self._h, int(seed), int(first_copy), float(density),
+                                       m.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)), len(m),
+                                       ctypes.c_void_p(state_ptr), ctypes.c_void_p(stream)))
 
     def move(self, state_ptr, steps, stream=0):
         _check(lib().nlc_move(self._h, ctypes.c_void_p(state_ptr), steps, ctypes.c_void_p(stream)))

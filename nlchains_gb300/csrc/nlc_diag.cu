@@ -162,6 +162,113 @@ __global__ void lin_ddnkg_kernel(const double2 *__restrict__ state, const DiagAr
 	}
 }
 
+// Seeded initial ensembles on the device, the recipes of nlchains_gb300/ic.py: uniform phases from
+// SplitMix64 counters keyed by (seed, stream, copy, mode) (G. Steele, D. Lea, C. Flood, "Fast
+// splittable pseudorandom number generators", OOPSLA 2014), amplitudes from the energy (or norm)
+// density spread equally over the excited modes, then one inverse transform per chain:
+//   real models: z_k = A e^{i theta}, Phi_k = (z_k + conj z_{n-k}) / (2 omega_k), Pi_k =
+//     (z_k - conj z_{n-k}) / (2i); both have Hermitian spectra, so the inverse transform of
+//     Phi + i Pi is phi + i pi, the planar state itself;
+//   DNLS: psi_hat_k = A e^{i theta}, psi = inverse transform;
+//   dDNKG: phi = sum_k A cos(theta) / omega_k e_k, pi = sum_k A sin(theta) e_k over the excited
+//     eigenmodes (eigenvectors read site-major from the diagnostics tables).
+__device__ __forceinline__ unsigned long long splitmix64(unsigned long long x) {
+	unsigned long long z = x + 0x9E3779B97F4A7C15ull;
+	z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+	z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+	return z ^ (z >> 31);
+}
+
+// uniform [0, 1) of counter (key, copy, index) with `count` indices per copy, as ic.uniform
+__device__ __forceinline__ double ic_uniform(unsigned long long key, unsigned long long copy, unsigned int count,
+                                             unsigned int index) {
+	return double(splitmix64(key + copy * count + index) >> 11) * (1.0 / 9007199254740992.0);
+}
+
+template <bool BLOCK>
+__global__ void ic_kernel(double2 *__restrict__ state, const DiagArgs a, const IcArgs c) {
+	extern __shared__ double2 sm[];
+	const int n = int(a.n);
+	const int T = BLOCK ? blockDim.x : 32;
+	const int t = BLOCK ? threadIdx.x : (threadIdx.x & 31);
+	const int team = BLOCK ? 0 : (threadIdx.x >> 5);
+	const int teams = BLOCK ? 1 : (blockDim.x >> 5);
+	const int len = a.fft.len;
+	double2 *x = BLOCK && a.gscratch ? a.gscratch + (size_t) blockIdx.x * 2 * len : sm + (size_t) team * 2 * len;
+	double2 *y = x + len;
+	for (unsigned long long chain = (unsigned long long) blockIdx.x * teams + team; chain < a.copies;
+	     chain += (unsigned long long) gridDim.x * teams) {
+		const unsigned long long copy = c.first_copy + chain;
+		double2 *dst = state + chain * (unsigned long long) n;
+		if (a.model == NLC_DDNKG) {
+			// the excited eigenmodes' amplitudes into the team's nmodes slots, then each site sums them
+			double2 *amp = sm + (size_t) team * c.nmodes;
+			for (int j = t; j < int(c.nmodes); j += T) {
+				const int k = c.modes[j];
+				double s, co;
+				sincospi(2. * ic_uniform(c.key, copy, n, k), &s, &co);
+				amp[j] = make_double2(c.amp * co / a.omega[k], c.amp * s);
+			}
+			team_sync<BLOCK>();
+			for (int site = t; site < n; site += T) {
+				double p = 0., q = 0.;
+				for (int j = 0; j < int(c.nmodes); j++) {
+					const double e = a.eigT[(size_t) site * n + c.modes[j]];
+					p = fma(amp[j].x, e, p), q = fma(amp[j].y, e, q);
+				}
+				dst[site] = make_double2(p, q);
+			}
+			team_sync<BLOCK>();
+			continue;
+		}
+		for (int k = t; k < n; k += T) x[k] = make_double2(0., 0.);
+		team_sync<BLOCK>();
+		for (int j = t; j < int(c.nmodes); j += T) {
+			const int k = c.modes[j];
+			double s, co;
+			sincospi(2. * ic_uniform(c.key, copy, n, k), &s, &co);
+			x[k] = make_double2(c.amp * co, c.amp * s);
+		}
+		team_sync<BLOCK>();
+		double2 *w = x;
+		if (a.model != NLC_DNLS) {
+			// Phi + i Pi from z: Phi_k = (z_k + conj z_{n-k}) / (2 omega_k), Pi_k = (z_k - conj z_{n-k}) / (2i)
+			for (int k = t; k < n; k += T) {
+				const double2 zk = x[k], zc = make_double2(x[k ? n - k : 0].x, -x[k ? n - k : 0].y);
+				const double om = a.omega[k];
+				const double2 ph = om > 0 ? make_double2((zk.x + zc.x) / (2 * om), (zk.y + zc.y) / (2 * om))
+				                          : make_double2(0., 0.);
+				const double2 pk = make_double2((zk.y - zc.y) / 2, -(zk.x - zc.x) / 2);   // (z - zc) / (2i)
+				y[k] = make_double2(ph.x - pk.y, ph.y + pk.x);                           // Phi + i Pi
+			}
+			team_sync<BLOCK>();
+			w = y;
+		}
+		double2 *o = w == x ? y : x;
+		const double2 *r = fft_team<BLOCK, true>(a.fft, w, o, t, T);
+		const double inv_n = 1. / n;
+		for (int k = t; k < n; k += T) dst[k] = make_double2(r[k].x * inv_n, r[k].y * inv_n);
+		team_sync<BLOCK>();
+	}
+}
+
+cudaError_t launch_initial_state(const DiagArgs &a, const IcArgs &c, double2 *state, int blocks, int threads,
+                                 size_t smem, int team_block, cudaStream_t stream) {
+	// dDNKG: warp teams, shared memory for the excited modes' amplitudes; otherwise the transform's
+	// teams and buffers of the diagnostics
+	const bool block = a.model != NLC_DDNKG && team_block;
+	if (a.model == NLC_DDNKG) threads = 128, smem = 4 * size_t(c.nmodes) * sizeof(double2);
+	const void *k = block ? (const void *) ic_kernel<true> : (const void *) ic_kernel<false>;
+	if (smem > 48 * 1024) {
+		const cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+		if (e != cudaSuccess) return e;
+	}
+	count_launch();
+	if (block) ic_kernel<true><<<blocks, threads, smem, stream>>>(state, a, c);
+	else ic_kernel<false><<<blocks, threads, smem, stream>>>(state, a, c);
+	return cudaGetLastError();
+}
+
 cudaError_t launch_linenergies_partials(const DiagArgs &a, const void *state, int blocks, int threads,
                                         size_t smem, int team_block, cudaStream_t stream) {
 	const double2 *st = static_cast<const double2 *>(state);

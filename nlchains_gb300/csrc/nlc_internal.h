@@ -172,6 +172,17 @@ __host__ __device__ inline void fma_twiddle_entry(int p, const double *cu, const
 	}
 }
 
+// Seeded initial ensembles on the device (nlc_initial_state)
+struct IcArgs {
+	unsigned long long key;       // SplitMix64 key of (seed, stream)
+	unsigned long long first_copy;
+	double amp;                   // amplitude of every excited mode
+	const int *modes;             // device: the excited mode indices
+	uint32_t nmodes;
+};
+cudaError_t launch_initial_state(const DiagArgs &a, const IcArgs &c, double2 *state, int blocks, int threads,
+                                 size_t smem, int team_block, cudaStream_t stream);
+
 cudaError_t launch_linenergies_partials(const DiagArgs &a, const void *state, int blocks, int threads,
                                         size_t smem, int team_block, cudaStream_t stream);
 struct FinishArgs {

@@ -516,10 +516,11 @@ int setup_diagnostics(nlc_plan &P) {
 		} else {
 			std::vector<double> ca(n), cb(n);
 			for (uint32_t k = 0; k < n; k++) ca[k] = (P.omega_host[k] + 1) / 2, cb[k] = (P.omega_host[k] - 1) / 2;
-			double *d_a = nullptr, *d_b = nullptr;
+			double *d_a = nullptr, *d_b = nullptr, *d_om = nullptr;
 			if ((rc = P.upload(&d_a, ca.data(), n))) return rc;
 			if ((rc = P.upload(&d_b, cb.data(), n))) return rc;
-			g.coef_a = d_a, g.coef_b = d_b;
+			if ((rc = P.upload(&d_om, P.omega_host.data(), n))) return rc;   // for nlc_initial_state
+			g.coef_a = d_a, g.coef_b = d_b, g.omega = d_om;
 		}
 		// a warp per chain up to a 1024-point pass (2 x 16 KiB ping-pong), else a 256-thread block
 		const uint32_t len = uint32_t(g.fft.len);
@@ -873,6 +874,61 @@ extern "C" int nlc_plan_omegas(const nlc_plan *P, double *omegas) {
 	if (!P || !omegas) return set_error(NLC_EINVAL, "NULL argument");
 	std::memcpy(omegas, P->omega_host.data(), P->omega_host.size() * sizeof(double));
 	return NLC_OK;
+}
+
+extern "C" int nlc_initial_state(nlc_plan *P, uint64_t seed, uint64_t first_copy, double density,
+                                 const uint32_t *modes, uint32_t nmodes, void *state_dev, void *stream) {
+	if (!P || !state_dev || (nmodes && !modes)) return set_error(NLC_EINVAL, "NULL argument");
+	if (!(density > 0)) return set_error(NLC_EINVAL, "nlc_initial_state: density must be > 0");
+	const uint32_t n = P->m.chain_length;
+	const int model = P->m.model;
+	// the excited modes: distinct indices below n; the real models skip a mode of zero frequency
+	std::vector<int> ks;
+	std::vector<char> seen(n, 0);
+	for (uint32_t j = 0; j < nmodes; j++) {
+		if (modes[j] >= n) return set_error(NLC_EINVAL, "nlc_initial_state: mode index >= chain_length");
+		if (seen[modes[j]]) continue;
+		seen[modes[j]] = 1;
+		if ((model == NLC_DNKG || model == NLC_FPUT || model == NLC_TODA) && !(P->omega_host[modes[j]] > 0)) continue;
+		ks.push_back(int(modes[j]));
+	}
+	if (ks.empty()) return set_error(NLC_EINVAL, "nlc_initial_state: no mode to excite");
+	const double M = double(ks.size());
+	IcArgs c{};
+	// the RNG stream and amplitude of each model (nlchains_gb300/ic.py: real 1, DNLS 2, dDNKG 3)
+	uint64_t rng_stream;
+	if (model == NLC_DNLS) rng_stream = 2, c.amp = std::sqrt(double(n) * n * density / M);
+	else if (model == NLC_DDNKG) rng_stream = 3, c.amp = std::sqrt(2 * density * n / M);
+	else rng_stream = 1, c.amp = std::sqrt(2. * n * (density * n / M));
+	auto splitmix = [](uint64_t x) {
+		uint64_t z = x + 0x9E3779B97F4A7C15ull;
+		z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+		z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+		return z ^ (z >> 31);
+	};
+	c.key = splitmix(seed * 0xD1B54A32D192ED03ull + rng_stream);
+	c.first_copy = first_copy;
+	c.nmodes = uint32_t(ks.size());
+	DeviceScope ds(P->device);
+	NvtxRange r("nlc_initial_state");
+	cudaStream_t st = static_cast<cudaStream_t>(stream);
+	int *d_modes = nullptr;
+	int rc = cuda_status(cudaMallocAsync(&d_modes, ks.size() * sizeof(int), st), "cudaMallocAsync");
+	if (rc) return rc;
+	rc = cuda_status(cudaMemcpyAsync(d_modes, ks.data(), ks.size() * sizeof(int), cudaMemcpyHostToDevice, st),
+	                 "mode list upload");
+	if (!rc) {
+		c.modes = d_modes;
+		const unsigned long long blocks = model == NLC_DDNKG
+		                                      ? std::min<unsigned long long>((P->m.copies + 3) / 4, 4ull * P->prop.multiProcessorCount)
+		                                      : (unsigned long long) P->diag_blocks;
+		rc = cuda_status(launch_initial_state(P->ga, c, static_cast<double2 *>(state_dev), int(blocks), P->diag_threads,
+		                                      P->diag_smem, P->diag_team_block, st),
+		                 "initial state launch");
+	}
+	cudaFreeAsync(d_modes, st);
+	if (!rc) rc = cuda_status(cudaStreamSynchronize(st), "initial state");   // the host mode list goes out of scope
+	return rc;
 }
 
 int nlc::plan_device_status(nlc_plan *P) {
