@@ -290,6 +290,11 @@ int nlc_server_destroy(nlc_server *server);
 /* queue a request; host_state (reference layout) is copied before return */
 int nlc_server_submit(nlc_server *server, const nlc_model *model, uint32_t kernel_batching, uint64_t steps,
                       const void *host_state, uint64_t *request);
+/* queue a request whose initial state is generated on the device by nlc_initial_state (seed, density,
+ * modes as there; copies counted from 0): large ensembles need no host copy and no upload */
+int nlc_server_submit_seeded(nlc_server *server, const nlc_model *model, uint32_t kernel_batching, uint64_t steps,
+                             uint64_t seed, double density, const uint32_t *modes, uint32_t nmodes,
+                             uint64_t *request);
 int nlc_server_poll(nlc_server *server, uint64_t request, nlc_request_status *status);   /* non-blocking */
 /* wait until the request is DONE or FAILED, at most timeout_ms (< 0: no limit); NLC_ETIMEDOUT otherwise */
 int nlc_server_wait(nlc_server *server, uint64_t request, int32_t timeout_ms);

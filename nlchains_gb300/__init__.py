@@ -40,7 +40,7 @@ EXPORTS = (
     "nlc_version", "nlc_kernel_launches", "nlc_fp64_peak", "nlc_linenergies_noalloc",
     "nlc_server_create", "nlc_server_destroy", "nlc_server_submit", "nlc_server_poll", "nlc_server_wait",
     "nlc_server_result", "nlc_entropies", "nlc_job_sample_async", "nlc_job_sample_wait", "nlc_energies",
-    "nlc_job_energies", "nlc_job_step_async", "nlc_job_after", "nlc_initial_state",
+    "nlc_job_energies", "nlc_job_step_async", "nlc_job_after", "nlc_initial_state", "nlc_server_submit_seeded",
 )
 
 
@@ -117,6 +117,8 @@ def lib():
         "nlc_server_create": ([P(_CServerConfig), P(vp)], i32),
         "nlc_server_destroy": ([vp], i32),
         "nlc_server_submit": ([vp, P(_CModel), u32, u64, vp, P(u64)], i32),
+        "nlc_server_submit_seeded": ([vp, P(_CModel), u32, u64, u64, ctypes.c_double, P(ctypes.c_uint32),
+                                      ctypes.c_uint32, P(u64)], i32),
         "nlc_server_poll": ([vp, u64, P(_CRequestStatus)], i32),
         "nlc_server_wait": ([vp, u64, i32], i32),
         "nlc_server_result": ([vp, u64, vp, dp, dp, P(u64)], i32),
@@ -395,6 +397,17 @@ class Server:
         rid = ctypes.c_uint64()
         _check(lib().nlc_server_submit(self._h, ctypes.byref(c), int(kernel_batching), int(steps),
                                        state.ctypes.data_as(ctypes.c_void_p), ctypes.byref(rid)))
+        self._models[rid.value] = (model, int(steps), int(kernel_batching))
+        return rid.value
+
+    def submit_seeded(self, model, kernel_batching, steps, seed, density, modes):
+        """A request whose initial state the server generates on the device (nlc_initial_state)."""
+        m = np.ascontiguousarray(np.asarray(modes, dtype=np.uint32))
+        c = model.c_struct()
+        rid = ctypes.c_uint64()
+        _check(lib().nlc_server_submit_seeded(self._h, ctypes.byref(c), int(kernel_batching), int(steps), int(seed),
+                                              float(density), m.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)),
+                                              len(m), ctypes.byref(rid)))
         self._models[rid.value] = (model, int(steps), int(kernel_batching))
         return rid.value
 

@@ -47,6 +47,10 @@ struct Request {
 	uint32_t batching = 1;
 	uint64_t steps = 0;
 	std::vector<double> host_in;    // initial state, then the final state
+	bool seeded = false;            // initial state generated on the device (nlc_initial_state)
+	uint64_t seed = 0;
+	double density = 0;
+	std::vector<uint32_t> modes;
 	size_t state_bytes = 0;
 	size_t need_bytes = 0;          // device memory estimate used for admission
 
@@ -179,6 +183,8 @@ int admit(nlc_server *S, Request &R, cudaStream_t st) {
 	if ((rc = cuda_status(cudaMallocAsync(&R.d_state, R.state_bytes, st), "cudaMallocAsync state"))) return rc;
 	if ((rc = cuda_status(cudaMallocAsync(&R.d_diag, (n + 2) * sizeof(double), st), "cudaMallocAsync"))) return rc;
 	if (!(R.h_diag = pinned_get(S, n + 2))) return set_error(NLC_ENOMEM, "pinned read-back buffer");
+	if (R.seeded)
+		return nlc_initial_state(R.plan, R.seed, 0, R.density, R.modes.data(), uint32_t(R.modes.size()), R.d_state, st);
 	if ((rc = cuda_status(cudaMemcpyAsync(R.d_state, R.host_in.data(), R.state_bytes, cudaMemcpyHostToDevice, st),
 	                      "upload")))
 		return rc;
@@ -586,9 +592,19 @@ extern "C" int nlc_server_destroy(nlc_server *S) {
 	return NLC_OK;
 }
 
-extern "C" int nlc_server_submit(nlc_server *S, const nlc_model *model, uint32_t batching, uint64_t steps,
-                                 const void *host_state, uint64_t *id) {
-	if (!S || !model || !host_state || !id) return set_error(NLC_EINVAL, "NULL argument");
+namespace {
+// a request whose initial state is `host_state` (uploaded) or, with host_state NULL, the seeded
+// ensemble of `seed_spec` (generated on the device by its preparer)
+struct SeedSpec {
+	uint64_t seed;
+	double density;
+	const uint32_t *modes;
+	uint32_t nmodes;
+};
+
+int submit(nlc_server *S, const nlc_model *model, uint32_t batching, uint64_t steps, const void *host_state,
+           const SeedSpec *seed_spec, uint64_t *id) {
+	if (!S || !model || !id || (!host_state && !seed_spec)) return set_error(NLC_EINVAL, "NULL argument");
 	if (!batching) return set_error(NLC_EINVAL, "--kernel_batching must be a positive number");
 	if (steps % batching) return set_error(NLC_EINVAL, "--steps must be a multiple of --kernel_batching");
 	if (model->chain_length < 2 || !model->copies || !(model->dt > 0))
@@ -603,8 +619,19 @@ extern "C" int nlc_server_submit(nlc_server *S, const nlc_model *model, uint32_t
 	R->batching = batching;
 	R->steps = steps;
 	R->state_bytes = n * model->copies * sizeof(double2);
-	const double *src = static_cast<const double *>(host_state);
-	R->host_in.assign(src, src + 2 * n * model->copies);
+	if (host_state) {
+		const double *src = static_cast<const double *>(host_state);
+		R->host_in.assign(src, src + 2 * n * model->copies);
+	} else {
+		if (!seed_spec->nmodes || !seed_spec->modes || !(seed_spec->density > 0))
+			return set_error(NLC_EINVAL, "a seeded request needs modes and a positive density");
+		for (uint32_t j = 0; j < seed_spec->nmodes; j++)
+			if (seed_spec->modes[j] >= n) return set_error(NLC_EINVAL, "mode index >= chain_length");
+		R->seeded = true;
+		R->seed = seed_spec->seed, R->density = seed_spec->density;
+		R->modes.assign(seed_spec->modes, seed_spec->modes + seed_spec->nmodes);
+		R->host_in.resize(2 * n * model->copies);   // receives the final state
+	}
 	// state + diagnostics partial rows (<= one row block per SM) + tables
 	R->need_bytes = R->state_bytes + size_t(4 * 160) * n * sizeof(double) + 16 * n * sizeof(double) +
 	                (model->model == NLC_DDNKG ? n * n * sizeof(double) : 0) + (1 << 16);
@@ -618,6 +645,21 @@ extern "C" int nlc_server_submit(nlc_server *S, const nlc_model *model, uint32_t
 	S->queue.push_back(std::move(R));
 	S->cv_work.notify_all();
 	return NLC_OK;
+}
+
+}  // namespace
+
+extern "C" int nlc_server_submit(nlc_server *S, const nlc_model *model, uint32_t batching, uint64_t steps,
+                                 const void *host_state, uint64_t *id) {
+	if (!host_state) return set_error(NLC_EINVAL, "NULL argument");
+	return submit(S, model, batching, steps, host_state, nullptr, id);
+}
+
+extern "C" int nlc_server_submit_seeded(nlc_server *S, const nlc_model *model, uint32_t batching, uint64_t steps,
+                                        uint64_t seed, double density, const uint32_t *modes, uint32_t nmodes,
+                                        uint64_t *id) {
+	const SeedSpec spec{seed, density, modes, nmodes};
+	return submit(S, model, batching, steps, nullptr, &spec, id);
 }
 
 static Request *lookup(nlc_server *S, uint64_t id) {

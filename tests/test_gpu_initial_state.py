@@ -63,3 +63,35 @@ def test_rejects_bad_modes(gpu):
             plan.initial_state(dev.data_ptr(), 1, 0.1, modes)
         assert e.value.code == gpu.EINVAL
     plan.close()
+
+
+def test_server_seeded_request_equals_job(gpu):
+    """A server request submitted with a seed (its state generated on the device by the preparer)
+    ends bit-identical to a job started from the same generated state, and mixes with a request
+    submitted with a host state."""
+    torch = pytest.importorskip("torch")
+    n, copies, b, steps, seed, density = 96, 200, 10, 40, 123, 0.3
+    modes = ic.low_modes(n, kmax=3, include_zero=False)
+    model = gpu.Model("FPUT", n, copies, 0.05, alpha=0.2, beta=1.0)
+    plan = gpu.Plan(model)
+    dev = torch.zeros((copies, n, 2), dtype=torch.float64, device="cuda")
+    plan.initial_state(dev.data_ptr(), seed, density, modes, stream=torch.cuda.current_stream().cuda_stream)
+    init = dev.cpu().numpy()
+    plan.close()
+    other = 0.2 * np.random.default_rng(1).standard_normal((64, 48, 2))
+    srv = gpu.Server(0)
+    r1 = srv.submit_seeded(model, b, steps, seed, density, modes)
+    r2 = srv.submit(gpu.Model("DNKG", 48, 64, 0.05, m=1.0, beta=1.0), b, steps, other)
+    for rid in (r1, r2):
+        srv.wait(rid, 60000)
+    fstate, _, ents, rc = srv.result(r1)
+    assert rc == gpu.OK and ents.shape == (steps // b + 1, 2)
+    srv.result(r2)
+    srv.close()
+    ctx = gpu.Context(0)
+    job = ctx.job(model, b)
+    job.upload(init)
+    job.advance(steps)
+    assert np.array_equal(fstate.reshape(copies, n, 2), job.download().reshape(copies, n, 2))
+    job.close()
+    ctx.close()
