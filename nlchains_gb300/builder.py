@@ -23,7 +23,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU_SOURCES = ["nlc_real_dnkg.cu", "nlc_real_fput.cu", "nlc_real_toda.cu", "nlc_real_ddnkg.cu",
               "nlc_diag.cu", "nlc_dnls.cu", "nlc_noalloc.cu", "nlc_energy.cu", "nlc_tc.cu"]
-CPP_SOURCES = ["nlc_plan.cpp", "nlc_tables.cpp", "nlc_job.cpp", "nlc_server.cpp"]
+CPP_SOURCES = ["nlc_plan.cpp", "nlc_tables.cpp", "nlc_job.cpp", "nlc_server.cpp", "nlc_eig_device.cpp"]
 HEADERS = ["nlc_device.cuh", "nlc_real.cuh", "nlc_fft.cuh", "nlc_internal.h", "nlc_host.h"]
 
 

@@ -95,6 +95,14 @@ constexpr uint32_t kMaxFftLen = 1u << 18;
 // spectra FFT_m(g_k) / m (interleaved), so that x (*) h_k = IFFT_m(FFT_m(x) G_k) on [0, n).
 std::vector<double> dnls_conv_tables(const std::vector<double> &lin, uint32_t n, uint32_t m);
 
+// The same eigensystem on the GPU (cuSOLVER's divide and conquer, loaded at run time,
+// nlc_eig_device.cpp); false when cuSOLVER is missing, any step fails or NLC_HOST_EIGEN is set, and
+// the caller then uses the host solver.
+bool eigensystem_periodic_device(const std::vector<double> &mp2, std::vector<double> &omegas,
+                                 std::vector<double> &eigvec);
+// the dDNKG plan's eigenvectors (eigvec layout above), the ones its projection uses; NULL otherwise
+const std::vector<double> *plan_eigenvectors(const nlc_plan *plan);
+
 // Host threads of the set-up work (the dDNKG eigensolver): one per core (at most 32, or
 // NLC_HOST_THREADS), or what set_host_setup_threads chose for the calling thread (the request
 // server's preparers share the cores with each other and with its scheduler).

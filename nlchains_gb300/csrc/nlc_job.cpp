@@ -597,11 +597,10 @@ int run_program(int argc, char **argv) {
 		std::vector<double> om(n);
 		nlc_plan_omegas(find_job(ctx, job)->plan, om.data());
 		write_file(prefix + "-omegas", om.data(), n * sizeof(double), "eigensystem");
-		std::vector<double> mp2(masses);
-		for (double &x : mp2) x += 2;
-		std::vector<double> omg, vec;
-		eigensystem_periodic(mp2, omg, vec);
-		write_file(prefix + "-eigenvectors", vec.data(), vec.size() * sizeof(double), "eigensystem");
+		// the eigenvectors the plan's projection uses
+		const std::vector<double> *vec = plan_eigenvectors(find_job(ctx, job)->plan);
+		if (!vec) throw CliError{2, "no eigensystem in the dDNKG plan"};
+		write_file(prefix + "-eigenvectors", vec->data(), vec->size() * sizeof(double), "eigensystem");
 	}
 	if ((rc = nlc_job_upload(ctx, job, host_state))) throw CliError{2, nlc_last_error()};
 

@@ -646,7 +646,10 @@ extern "C" int nlc_plan_create(const nlc_model *model, nlc_plan **out) {
 	if (mdl == NLC_DDNKG) {
 		P->mp2_host.resize(n);
 		for (uint32_t i = 0; i < n; i++) P->mp2_host[i] = model->masses[i] + 2;
-		if (!eigensystem_periodic(P->mp2_host, P->omega_host, P->eig_host))
+		// from 256 sites on the GPU (cuSOLVER syevd, 10-20x the host solver); the host solver below
+		// that, or when the GPU solver is unavailable
+		const bool device = n >= 256 && eigensystem_periodic_device(P->mp2_host, P->omega_host, P->eig_host);
+		if (!device && !eigensystem_periodic(P->mp2_host, P->omega_host, P->eig_host))
 			return set_error(NLC_EINVAL, "Cannot calculate eigensystem!");
 		P->norm = 0.5 / model->copies;   // dDNKG.cpp:141
 	} else if (mdl == NLC_DNLS) {
@@ -929,6 +932,10 @@ extern "C" int nlc_initial_state(nlc_plan *P, uint64_t seed, uint64_t first_copy
 	cudaFreeAsync(d_modes, st);
 	if (!rc) rc = cuda_status(cudaStreamSynchronize(st), "initial state");   // the host mode list goes out of scope
 	return rc;
+}
+
+const std::vector<double> *nlc::plan_eigenvectors(const nlc_plan *P) {
+	return P && P->m.model == NLC_DDNKG ? &P->eig_host : nullptr;
 }
 
 int nlc::plan_device_status(nlc_plan *P) {

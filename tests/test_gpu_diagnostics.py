@@ -128,3 +128,27 @@ def test_fp32_diagnostics_error_stated(gpu, model, params, n):
     err = np.abs(lin - elin).max() / np.abs(elin).max()
     assert 0 < err <= 2e-5, err   # not zero: the FP32 path ran
     assert abs(inf - einf) <= 2e-5 * abs(einf)
+
+
+@pytest.mark.parametrize("n", [256, 300, 1024])
+def test_ddnkg_device_eigensystem_equals_host(gpu, n, monkeypatch):
+    """From 256 sites the dDNKG eigensystem is solved on the GPU (cuSOLVER syevd); against the host
+    solver (NLC_HOST_EIGEN): the same frequencies and, since eigenvectors are defined up to sign, the
+    same mode energies of a state (both through the FP64 projection)."""
+    torch = pytest.importorskip("torch")
+    copies = 16
+    masses = ic.masses_uniform(n, seed=n)
+    state = 0.3 * np.random.default_rng(n).standard_normal((copies, n, 2))
+    dev = torch.from_numpy(state).cuda()
+    out = {}
+    for host in (False, True):
+        if host:
+            monkeypatch.setenv("NLC_HOST_EIGEN", "1")
+        plan = gpu.Plan(gpu.Model("dDNKG", n, copies, 0.05, masses=masses, beta=1.0, flags=gpu.FLAG_FP64_PROJECTION))
+        lin = torch.zeros(n, dtype=torch.float64, device="cuda")
+        plan.linenergies(dev.data_ptr(), lin.data_ptr(), 0, torch.cuda.current_stream().cuda_stream)
+        torch.cuda.synchronize()
+        out[host] = (plan.omegas(), lin.cpu().numpy())
+        plan.close()
+    assert np.abs(out[False][0] - out[True][0]).max() <= 1e-12 * out[True][0].max()
+    assert np.abs(out[False][1] - out[True][1]).max() <= 1e-10 * np.abs(out[True][1]).max()
