@@ -59,12 +59,16 @@ const Cusolver *cusolver() {
 	return g_cs.loaded ? &g_cs : nullptr;
 }
 
+thread_local bool t_eigen_on_host = false;
+
 }  // namespace
+
+void set_eigen_on_host(bool host) { t_eigen_on_host = host; }
 
 bool eigensystem_periodic_device(const std::vector<double> &mp2, std::vector<double> &omegas,
                                  std::vector<double> &eigvec) {
 	const size_t n = mp2.size();
-	if (n < 3) return false;   // the n = 2 corner rule is the host solver's
+	if (n < 3 || t_eigen_on_host) return false;   // the n = 2 corner rule is the host solver's
 	if (const char *e = std::getenv("NLC_HOST_EIGEN"); e && *e && *e != '0') return false;
 	const Cusolver *cs = cusolver();
 	if (!cs) return false;

@@ -100,6 +100,9 @@ std::vector<double> dnls_conv_tables(const std::vector<double> &lin, uint32_t n,
 // the caller then uses the host solver.
 bool eigensystem_periodic_device(const std::vector<double> &mp2, std::vector<double> &omegas,
                                  std::vector<double> &eigvec);
+// for plans made by the calling thread: the eigensystem on the host even where the GPU solver would
+// be used (the request server's preparers: its stream is GPU-bound, and the host solver overlaps)
+void set_eigen_on_host(bool host);
 // the dDNKG plan's eigenvectors (eigvec layout above), the ones its projection uses; NULL otherwise
 const std::vector<double> *plan_eigenvectors(const nlc_plan *plan);
 
