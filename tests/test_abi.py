@@ -1,9 +1,11 @@
 """The C ABI library: it builds, loads, and exports every symbol include/nlchains.h declares; the
-command line rejects invalid arguments before touching a GPU (CPU only)."""
+command line, the plan constructor and the no-alloc entry point reject invalid arguments before
+touching a GPU, and the host entropies keep their error behaviour (CPU only)."""
 import os
 import re
 import subprocess
 
+import numpy as np
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
@@ -55,3 +57,49 @@ def test_cli_usage_without_options(engine):
     assert r.returncode == 0 and "--beta" in r.stdout and "--no_linear_callback" in r.stdout
     r = subprocess.run([engine.EXECUTABLE_PATH], capture_output=True, text=True, timeout=60)
     assert r.returncode == 0 and "subprogram" in r.stdout
+
+
+@pytest.mark.parametrize("kw,needle", [
+    (dict(model=9, chain_length=8, copies=4, dt=0.1), "unknown model id"),
+    (dict(model="DNKG", chain_length=1, copies=4, dt=0.1), "--chain_length must be >= 2"),
+    (dict(model="DNKG", chain_length=65536, copies=4, dt=0.1), "fit 16 bits"),
+    (dict(model="FPUT", chain_length=8, copies=0, dt=0.1), "--copies must be a positive number"),
+    (dict(model="Toda", chain_length=8, copies=4, dt=0.0), "--dt must be a positive number"),
+    (dict(model="DNLS", chain_length=8, copies=4, dt=float("nan")), "--dt must be a positive number"),
+    (dict(model="dDNKG", chain_length=8, copies=4, dt=0.1), "needs the per-site masses"),
+    (dict(model="DNKG", chain_length=65535, copies=1 << 25, dt=0.1), "too large"),
+])
+def test_plan_rejects_invalid_models_before_any_device_call(engine, kw, needle):
+    with pytest.raises(engine.NlcError) as e:
+        engine.Plan(engine.Model(**kw))
+    assert e.value.code == engine.EINVAL and needle in str(e.value)
+    assert needle in engine.last_error()
+
+
+@pytest.mark.parametrize("args,needle", [
+    ((3, 64, 8, 0.0, 16, None, 16, None, None), "model must be DNKG, FPUT, Toda or DNLS"),
+    ((0, 64, 8, 0.0, None, None, 16, None, None), "NULL state or output"),
+    ((0, 1, 8, 0.0, 16, None, 16, None, None), "chain_length >= 2 and copies > 0"),
+    ((0, 64, 0, 0.0, 16, None, 16, None, None), "chain_length >= 2 and copies > 0"),
+    ((4, 4097, 8, 0.0, 16, None, 16, None, None), "does not fit the 4 MiB static scratch"),
+])
+def test_noalloc_rejects_invalid_arguments_before_any_device_call(engine, args, needle):
+    """The pointers given are never dereferenced: every case returns at an argument check that runs
+    before the first CUDA call."""
+    assert engine.lib().nlc_linenergies_noalloc(*args) == engine.EINVAL
+    assert needle in engine.last_error()
+
+
+def test_host_entropies_error_behaviour(engine):
+    lin = np.array([0.0, 1.0, 2.0, 3.0])
+    wt, inf = engine.entropies(lin, a0is0=True)
+    assert np.isfinite(wt) and np.isfinite(inf)
+    with pytest.raises(engine.NlcError) as e:
+        engine.entropies(np.array([1.0, np.inf, 2.0]), a0is0=False)
+    assert e.value.code == engine.EBLOWUP
+    with pytest.raises(engine.NlcError) as e:
+        engine.entropies(lin, a0is0=False, entropy_mask=np.zeros(4, dtype=np.uint8))
+    assert e.value.code == engine.EINVAL and "no mode selected" in str(e.value)
+    # equipartition: both entropies vanish
+    wt, inf = engine.entropies(np.full(8, 0.125), a0is0=False)
+    assert abs(wt) < 1e-14 and abs(inf) < 1e-14
