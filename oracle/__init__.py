@@ -6,8 +6,11 @@ __graft_entry__.smoke() and bench.py's CPU-baseline leg may import this package;
 (nlchains_gb300) never does.
 
 Parity status: unpinned against the reference itself (the reference has no tests, golden vectors or
-fixtures, and it cannot be built in this image: Boost.MPI, MPI, FFTW3 and Armadillo are absent).
-The oracle is pinned by analytic known answers in tests/test_oracle.py and tests/test_known_answers.py.
+fixtures, and its path cannot be built in this image: Boost.MPI, MPI, FFTW3 and Armadillo are
+absent), except for the Yoshida tables: oracle/_ref compiles the reference's own
+common/symplectic.hpp in place where the reference sources are present, and the tests compare the
+oracle's tables with it bit for bit.  The oracle is otherwise pinned by analytic known answers in
+tests/test_oracle.py and tests/test_known_answers.py.
 """
 import ctypes
 import os
@@ -84,6 +87,17 @@ class Model:
 def coefficients():
     c, d = np.zeros(8), np.zeros(8)
     _lib().nlo_coefficients(_dp(c), _dp(d))
+    return c, d
+
+
+def reference_coefficients():
+    """The reference's own (symplectic_c, symplectic_d) from oracle/_ref, or None where it was not
+    built (no reference sources on this machine)."""
+    path = os.path.join(_build.REF_OUT, "libref_symplectic.so")
+    if not os.path.exists(path):
+        return None
+    c, d = np.zeros(8), np.zeros(8)
+    ctypes.CDLL(path).ref_symplectic(_dp(c), _dp(d))
     return c, d
 
 

@@ -7,6 +7,12 @@ Two shared objects are produced under oracle/_build/ from oracle/nlc_oracle.c:
   builds its CPU code (CMakeLists.txt:62), OpenMP over copies.  Timing only: its arithmetic is not
   the checker's.
 
+and, where the reference sources are present, one under oracle/_ref/:
+
+* ``libref_symplectic.so`` -- the reference's own Yoshida tables (common/symplectic.hpp, compiled in
+  place by oracle/ref_symplectic.cpp), which the tests pin the oracle's tables to.  The rest of the
+  reference's path needs Boost, MPI, FFTW3 and Armadillo and is not built.
+
 Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use these libraries.
 """
 import os
@@ -16,6 +22,9 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_build")
 SRC = os.path.join(HERE, "nlc_oracle.c")
+REF_OUT = os.path.join(HERE, "_ref")
+REF_SRC = os.path.join(HERE, "ref_symplectic.cpp")
+REFERENCE_ROOT = os.environ.get("NLC_REFERENCE_ROOT", "/root/reference")
 
 VARIANTS = {
     "libnlc_oracle.so": ["-O2"],
@@ -52,5 +61,23 @@ def build(verbose=False):
     return OUT
 
 
+def build_ref(verbose=False):
+    """Compile oracle/_ref from the reference sources; None where they are absent."""
+    header = os.path.join(REFERENCE_ROOT, "common", "symplectic.hpp")
+    if not os.path.exists(header):
+        return None
+    os.makedirs(REF_OUT, exist_ok=True)
+    target = os.path.join(REF_OUT, "libref_symplectic.so")
+    if _stale(target, [REF_SRC, header, __file__]):
+        cmd = ["g++", "-std=c++17", "-fPIC", "-shared", "-O1", "-I", os.path.dirname(header),
+               "-o", target + ".tmp", REF_SRC]
+        if verbose:
+            print(" ".join(cmd))
+        subprocess.run(cmd, check=True)
+        os.replace(target + ".tmp", target)
+    return REF_OUT
+
+
 if __name__ == "__main__":
     build(verbose="-v" in sys.argv)
+    build_ref(verbose="-v" in sys.argv)

@@ -1,8 +1,10 @@
 """The CPU oracle against analytic known answers (CPU only).
 
-The reference ships no tests, golden vectors or fixtures and cannot be built in this image, so the
-oracle's parity with it is unpinned; these tests pin the oracle instead with exact results the
-reference's algorithm must reproduce:
+The reference ships no tests, golden vectors or fixtures and its path cannot be built in this image,
+so the oracle's parity with it is unpinned apart from the Yoshida tables (compared bit for bit with
+the reference's own common/symplectic.hpp, compiled in place into oracle/_ref where the reference
+sources are present); these tests pin the oracle instead with exact results the reference's
+algorithm must reproduce:
 
 * beta = 0 (linear chains): every Fourier mode evolves by the product of the Yoshida drift/kick
   2x2 matrices (common/symplectic.hpp coefficients), computed independently here in numpy;
@@ -20,6 +22,15 @@ import oracle as O
 from nlchains_gb300 import ic
 
 C, D = O.coefficients()
+
+
+def test_coefficients_match_reference_header():
+    ref = O.reference_coefficients()
+    if ref is None:
+        pytest.skip("oracle/_ref not built: no reference sources on this machine")
+    assert np.array_equal(ref[0], C) and np.array_equal(ref[1], D)
+    # the 6th-order scheme's consistency conditions hold for the reference's rounded digits too
+    assert abs(C.sum() - 1) < 1e-14 and abs(D.sum() - 1) < 1e-14
 
 
 def yoshida_mode_matrix(omega2, dt, steps):
