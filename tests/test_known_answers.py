@@ -6,6 +6,8 @@
   mode 0, then pairs (1, 2), (3, 4), ..., then mode n/2 for even n.
 * FPUT and Toda conserve the total momentum of each chain (the forces are differences of bond
   terms around the ring), up to rounding.
+* The energy error is sixth order in dt, with the dt = 0.1 -> 0.2 ratios the reference records for
+  its own runs in supporting-material/post-processing/examples.nb.
 """
 import numpy as np
 import pytest
@@ -53,3 +55,51 @@ def test_momentum_conserved(name, params):
     out = O.advance(mdl, state, 200, 100, order=O.ORDER_DEVICE).reshape(copies, n, 2)
     p0, p1 = state[:, :, 1].sum(axis=1), out[:, :, 1].sum(axis=1)
     assert np.abs(p1 - p0).max() <= 1e-12 * np.abs(state[:, :, 1]).sum(axis=1).max()
+
+
+# The reference's own record of its integrator's accuracy: mean relative energy error over a
+# 64-site ensemble integrated to t = 10^5 at dt = 0.1 and 0.2, from the outputs of the scalingFPUT,
+# scalingToda, scalingDNKG and scalingdDNKG cells of supporting-material/post-processing/examples.nb
+# (FPUT alpha = beta = 0.1; Toda alpha = 0.1; DNKG m = 1, beta = 1; dDNKG beta = 1).  Their initial
+# states are not shipped, so the error constants cannot be reproduced; the convergence order can.
+REFERENCE_ERROR_AT_DT = {
+    "FPUT": (9.749437104374792e-9, 6.355961257427294e-7),
+    "Toda": (9.21303353288461e-9, 6.44790627595062e-7),
+    "DNKG": (2.0833472702843167e-8, 1.3454726973355405e-6),
+    "dDNKG": (4.08697841377681e-8, 2.7868723797410393e-6),
+}
+
+
+def mean_energy_error(name, params, dt, n=64, copies=16, t_end=200.0, samples=8):
+    """mean over copies and over `samples` evenly spaced times up to t_end of |E(t) - E(0)| / E(0)"""
+    if name == "dDNKG":
+        state = ic.ddnkg_ensemble(params["masses"], copies, 0.5, 8, seed=3)
+    elif name == "DNLS":
+        state = ic.dnls_ensemble(n, copies, 0.5, ic.low_modes(n, kmax=6), seed=3)
+        state = state.view(np.float64).reshape(copies, n, 2)
+    else:
+        state = ic.real_ensemble(n, copies, 0.5, ic.low_modes(n, kmax=6, include_zero=False),
+                                 m=params.get("m", 0.0), seed=3)
+    mdl = O.Model(name, n, copies, dt, **params)
+    e0 = O.energies(mdl, state)
+    per = int(round(t_end / dt)) // samples
+    errs = []
+    for _ in range(samples):
+        state = O.advance(mdl, state, per, per, order=O.ORDER_DEVICE).reshape(copies, n, 2)
+        errs.append(np.mean(np.abs(O.energies(mdl, state) - e0) / np.abs(e0)))
+    return float(np.mean(errs))
+
+
+@pytest.mark.parametrize("name,params", [
+    ("FPUT", dict(alpha=0.1, beta=0.1)), ("Toda", dict(alpha=0.1)), ("DNKG", dict(m=1.0, beta=1.0)),
+    ("dDNKG", dict(masses=ic.masses_uniform(64, seed=5), beta=1.0)), ("DNLS", dict(beta=0.1)),
+])
+def test_energy_error_is_sixth_order_as_recorded_by_the_reference(name, params):
+    """Doubling dt multiplies the energy error by ~2^6.  The reference's recorded ratios are 65.2
+    (FPUT), 70.0 (Toda), 64.6 (DNKG) and 68.2 (dDNKG); its DNLS record sits on a rounding floor at
+    dt <= 0.13 over its 10^6 steps, so DNLS is held to the order alone."""
+    order = np.log2(mean_energy_error(name, params, 0.2) / mean_energy_error(name, params, 0.1))
+    assert abs(order - 6.0) < 0.3, order
+    if name in REFERENCE_ERROR_AT_DT:
+        e1, e2 = REFERENCE_ERROR_AT_DT[name]
+        assert abs(order - np.log2(e2 / e1)) < 0.3, (order, np.log2(e2 / e1))
