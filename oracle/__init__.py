@@ -92,12 +92,16 @@ def coefficients():
 
 def reference_coefficients():
     """The reference's own (symplectic_c, symplectic_d) from oracle/_ref, or None where it was not
-    built (no reference sources on this machine)."""
+    built for this machine (no reference sources here)."""
     path = os.path.join(_build.REF_OUT, "libref_symplectic.so")
     if not os.path.exists(path):
         return None
+    try:
+        lib = ctypes.CDLL(path)
+    except OSError:   # built for another machine
+        return None
     c, d = np.zeros(8), np.zeros(8)
-    ctypes.CDLL(path).ref_symplectic(_dp(c), _dp(d))
+    lib.ref_symplectic(_dp(c), _dp(d))
     return c, d
 
 
