@@ -52,6 +52,33 @@ def test_cli_rejects_invalid_arguments(engine, tmp_path, args, needle):
     assert needle in r.stderr
 
 
+COMMON = ["-n", "8", "-c", "4", "--dt", "0.1", "-b", "10", "-p", "o"]
+
+
+@pytest.mark.parametrize("args,needle", [
+    (["dDNKG", "-i", "init", *COMMON, "-m", "masses5", "--beta", "1"], "could not read m file (masses5)"),
+    (["dDNKG", "-i", "init", *COMMON, "-m", "missing", "--beta", "1"], "could not read m file (missing)"),
+    (["FPUT", "-i", "init", *COMMON, "--alpha", "0", "--beta", "1", "--entropymask", "mask3"],
+     "could not read entropy mask file (mask3)"),
+    (["FPUT", "-i", "init3", *COMMON, "--alpha", "0", "--beta", "1"], "could not read initial state (init3)"),
+    (["FPUT", "-i", "init", "-n", "8", "-c", "4", "--dt", "-1", "-b", "10", "-p", "o", "--alpha", "0", "--beta", "1"],
+     "must be positive numbers"),
+    (["FPUT", "-i", "init", "-n", "8", "-c", "4", "--dt", "0.1", "-b", "0", "-p", "o", "--alpha", "0", "--beta", "1"],
+     "must be positive numbers"),
+    (["DNKG", "-i", "init", *COMMON, "-m", "abc", "--beta", "1"], "the argument ('abc') for option '--m' is invalid"),
+])
+def test_cli_rejects_invalid_files_and_values(engine, tmp_path, args, needle):
+    """Files of the wrong size (masses of 5 sites for 8, a 3-byte mask, 3 of the 4 chains) and
+    non-numeric or non-positive values are refused before the GPU is touched, with exit code 1."""
+    np.zeros((4, 8, 2)).tofile(tmp_path / "init")
+    np.zeros((3, 8, 2)).tofile(tmp_path / "init3")
+    np.ones(5).tofile(tmp_path / "masses5")
+    np.ones(3, dtype=np.uint8).tofile(tmp_path / "mask3")
+    r = subprocess.run([engine.EXECUTABLE_PATH, *args], cwd=tmp_path, capture_output=True, text=True, timeout=60)
+    assert r.returncode == 1
+    assert needle in r.stderr
+
+
 def test_cli_usage_without_options(engine):
     r = subprocess.run([engine.EXECUTABLE_PATH, "DNLS"], capture_output=True, text=True, timeout=60)
     assert r.returncode == 0 and "--beta" in r.stdout and "--no_linear_callback" in r.stdout
