@@ -8,6 +8,8 @@
   terms around the ring), up to rounding.
 * The energy error is sixth order in dt, with the dt = 0.1 -> 0.2 ratios the reference records for
   its own runs in supporting-material/post-processing/examples.nb.
+* Toda is integrable: the spectrum of its periodic Lax matrix is conserved up to the integrator's
+  error.
 """
 import numpy as np
 import pytest
@@ -103,3 +105,43 @@ def test_energy_error_is_sixth_order_as_recorded_by_the_reference(name, params):
     if name in REFERENCE_ERROR_AT_DT:
         e1, e2 = REFERENCE_ERROR_AT_DT[name]
         assert abs(order - np.log2(e2 / e1)) < 0.3, (order, np.log2(e2 / e1))
+
+
+def toda_lax_spectrum(chain, alpha):
+    """Eigenvalues of the periodic Lax matrix of the Toda chain (Flaschka's variables, scaled):
+    diagonal p_i, off-diagonal and corner e^{alpha (q_{i+1} - q_i)} / (2 alpha).  With the
+    reference's potential (e^{2 alpha r} - 2 alpha r - 1) / (4 alpha^2), whose linear part sums to
+    zero around the ring, the flow is isospectral: every trace of every power is conserved (the
+    trace is the momentum, half the trace of the square the energy)."""
+    q, p = chain[:, 0], chain[:, 1]
+    n = len(q)
+    a = np.exp(alpha * (np.roll(q, -1) - q)) / (2 * alpha)
+    lax = np.diag(p)
+    for i in range(n):
+        j = (i + 1) % n
+        lax[i, j] = lax[j, i] = a[i]
+    return np.linalg.eigvalsh(lax)
+
+
+def lax_drift(name, params, state, dt, alpha, t_end=100.0):
+    copies, n = state.shape[:2]
+    mdl = O.Model(name, n, copies, dt, **params)
+    out = O.advance(mdl, state, int(round(t_end / dt)), 100, order=O.ORDER_DEVICE).reshape(copies, n, 2)
+    drift = 0.0
+    for c in range(copies):
+        s0 = toda_lax_spectrum(state[c], alpha)
+        drift = max(drift, np.abs(toda_lax_spectrum(out[c], alpha) - s0).max() / np.abs(s0).max())
+    return drift
+
+
+def test_toda_is_isospectral():
+    """Toda is integrable: its whole Lax spectrum (n conserved quantities) stays put up to the
+    integrator's sixth-order error, while FPUT dynamics from the same state move it by O(1)."""
+    n, copies, alpha = 16, 4, 0.5
+    state = ic.real_ensemble(n, copies, 0.5, ic.low_modes(n, kmax=3, include_zero=False), seed=7)
+    state[:, :, 1] += 0.05   # a non-zero momentum
+    d1 = lax_drift("Toda", dict(alpha=alpha), state, 0.05, alpha)
+    d2 = lax_drift("Toda", dict(alpha=alpha), state, 0.1, alpha)
+    assert d1 < 1e-6
+    assert abs(np.log2(d2 / d1) - 6.0) < 0.3
+    assert lax_drift("FPUT", dict(alpha=0.5, beta=1.0), state, 0.05, alpha) > 1e-2
