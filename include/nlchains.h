@@ -191,6 +191,19 @@ int nlc_plan_shape(const nlc_plan *plan, int32_t *lanes_per_chain, int32_t *site
 /* Linear frequencies omega_k used by the diagnostics, copied to host omegas[chain_length]. */
 int nlc_plan_omegas(const nlc_plan *plan, double *omegas);
 
+/*
+ * The dDNKG eigensystem on its own, into host buffers: the periodic operator
+ * diag(masses[x] + 2) - shift(+-1) (masses = the -m file content), omegas[chain_length] = the
+ * square roots of its eigenvalues in ascending order, eigenvectors[chain_length * chain_length]
+ * column-major with eigenvector k in column k: the `-omegas` and `-eigenvectors` files of
+ * eigensystem.cpp:23-29.  Replaces eigensystem.cpp:13-36 (Armadillo eig_sym) for callers that
+ * keep their own plan.  device >= 0 lets cuSOLVER's divide and conquer run on that CUDA device
+ * from 256 sites; device < 0, shorter chains, or no usable GPU solver: the host Householder +
+ * implicit QR solver.  Synchronous.
+ */
+int nlc_eigensystem(uint32_t chain_length, const double *masses, int32_t device, double *omegas,
+                    double *eigenvectors);
+
 /* ---------------------------------------------------------------------------------------------
  * Level 2: jobs (engine-owned device state; the reference main loop)
  * -------------------------------------------------------------------------------------------*/

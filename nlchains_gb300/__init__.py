@@ -34,7 +34,7 @@ REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_FAILED = 0, 1, 2, 3
 # the exported symbols, as declared in include/nlchains.h
 EXPORTS = (
     "nlc_plan_create", "nlc_plan_destroy", "nlc_move", "nlc_linenergies", "nlc_dnls_evolve_nonlinear",
-    "nlc_dnls_evolve_linear", "nlc_plan_shape", "nlc_plan_omegas", "nlc_create", "nlc_destroy",
+    "nlc_dnls_evolve_linear", "nlc_plan_shape", "nlc_plan_omegas", "nlc_eigensystem", "nlc_create", "nlc_destroy",
     "nlc_job_create", "nlc_job_destroy", "nlc_job_upload", "nlc_job_advance", "nlc_job_linenergies",
     "nlc_job_download", "nlc_job_wait", "nlc_job_state_ptr", "nlc_program_run", "nlc_last_error",
     "nlc_version", "nlc_kernel_launches", "nlc_fp64_peak", "nlc_linenergies_noalloc",
@@ -96,6 +96,7 @@ def lib():
         "nlc_dnls_evolve_linear": ([vp, vp, vp, vp], i32),
         "nlc_plan_shape": ([vp, P(i32), P(i32), P(i32), P(i32)], i32),
         "nlc_plan_omegas": ([vp, dp], i32),
+        "nlc_eigensystem": ([u32, dp, i32, dp, dp], i32),
         "nlc_create": ([P(vp), ctypes.c_int], i32),
         "nlc_destroy": ([vp], i32),
         "nlc_job_create": ([vp, P(_CModel), u32, P(u64)], i32),
@@ -165,6 +166,17 @@ def fp64_peak_tflops(ms=200.0):
     out = ctypes.c_double()
     _check(lib().nlc_fp64_peak(ms, ctypes.byref(out)))
     return out.value
+
+
+def eigensystem(masses, device=-1):
+    """(omegas, eigenvectors) of the dDNKG operator diag(masses + 2) - shift(+-1) (nlc_eigensystem):
+    omegas ascending, eigenvectors[:, k] the k-th; device >= 0 allows the GPU solver from 256 sites."""
+    m = np.ascontiguousarray(masses, dtype=np.float64)
+    n = m.size
+    om, ev = np.zeros(n), np.zeros(n * n)
+    P = ctypes.POINTER(ctypes.c_double)
+    _check(lib().nlc_eigensystem(n, m.ctypes.data_as(P), int(device), om.ctypes.data_as(P), ev.ctypes.data_as(P)))
+    return om, ev.reshape(n, n).T
 
 
 class Model:

@@ -879,6 +879,26 @@ extern "C" int nlc_plan_omegas(const nlc_plan *P, double *omegas) {
 	return NLC_OK;
 }
 
+extern "C" int nlc_eigensystem(uint32_t n, const double *masses, int32_t device, double *omegas,
+                               double *eigenvectors) {
+	if (!masses || !omegas || !eigenvectors) return set_error(NLC_EINVAL, "nlc_eigensystem: NULL argument");
+	if (n < 2 || n > 65535) return set_error(NLC_EINVAL, "nlc_eigensystem: chain_length must be in [2, 65535]");
+	NvtxRange r("nlc_eigensystem");
+	std::vector<double> mp2(n), om, ev;
+	for (uint32_t i = 0; i < n; i++) mp2[i] = masses[i] + 2;
+	bool done = false;
+	int count = 0;
+	if (device >= 0 && n >= 256 && cudaGetDeviceCount(&count) == cudaSuccess && device < count) {
+		DeviceScope scope(device);
+		done = eigensystem_periodic_device(mp2, om, ev);
+	}
+	cudaGetLastError();   // a failed probe leaves no sticky status for the caller
+	if (!done && !eigensystem_periodic(mp2, om, ev)) return set_error(NLC_EINVAL, "Cannot calculate eigensystem!");
+	std::memcpy(omegas, om.data(), size_t(n) * sizeof(double));
+	std::memcpy(eigenvectors, ev.data(), size_t(n) * n * sizeof(double));
+	return NLC_OK;
+}
+
 extern "C" int nlc_initial_state(nlc_plan *P, uint64_t seed, uint64_t first_copy, double density,
                                  const uint32_t *modes, uint32_t nmodes, void *state_dev, void *stream) {
 	if (!P || !state_dev || (nmodes && !modes)) return set_error(NLC_EINVAL, "NULL argument");

@@ -1,0 +1,82 @@
+"""The library's host eigensolver for the dDNKG operator (nlc_eigensystem, device < 0), on the CPU:
+against LAPACK (numpy) and the oracle's own solver.  Eigenvectors are compared through quantities
+that do not depend on their signs or on the basis chosen inside a degenerate eigenspace: the
+residual |A v - omega^2 v|, orthonormality, and the projector onto each eigenspace."""
+import numpy as np
+import pytest
+
+import oracle as O
+from nlchains_gb300 import ic
+
+
+def operator(masses):
+    n = len(masses)
+    a = np.diag(np.asarray(masses, dtype=np.float64) + 2)
+    for i in range(n):
+        j = (i + 1) % n
+        a[i, j] = a[j, i] = -1.0   # n = 2: the one off-diagonal entry is -1 (eigensystem.cpp:16-18)
+    return a
+
+
+def check_eigensystem(masses, omegas, vecs, tol=1e-12):
+    a = operator(masses)
+    n = len(masses)
+    w2 = np.linalg.eigvalsh(a)
+    scale = np.abs(w2).max()
+    assert np.all(np.diff(omegas) >= 0)
+    assert np.abs(omegas ** 2 - w2).max() <= tol * scale
+    assert np.abs(a @ vecs - vecs * omegas ** 2).max() <= 10 * tol * scale
+    assert np.abs(vecs.T @ vecs - np.eye(n)).max() <= 10 * tol * n ** 0.5
+
+
+@pytest.mark.parametrize("n", [2, 3, 5, 16, 64, 255, 300])
+def test_host_solver_random_masses(engine, n):
+    masses = ic.masses_uniform(n, seed=n)
+    om, vecs = engine.eigensystem(masses)
+    check_eigensystem(masses, om, vecs)
+    # non-degenerate spectrum: every eigenvector equals LAPACK's up to its sign
+    _, ref = np.linalg.eigh(operator(masses))
+    assert np.abs(np.abs(np.sum(ref * vecs, axis=0)) - 1).max() < 1e-9
+
+
+@pytest.mark.parametrize("n", [8, 33, 128])
+def test_host_solver_degenerate_spectrum(engine, n):
+    """Constant masses: DNKG's spectrum, omega_k = omega_{n-k}; compare eigenspace projectors."""
+    masses = np.full(n, 0.7)
+    om, vecs = engine.eigensystem(masses)
+    check_eigensystem(masses, om, vecs)
+    k = np.arange(n)
+    assert np.allclose(om, np.sort(np.sqrt(0.7 + 4 * np.sin(np.pi * k / n) ** 2)), rtol=0, atol=1e-13)
+    w2, ref = np.linalg.eigh(operator(masses))
+    groups = np.split(np.arange(n), np.nonzero(np.diff(w2) > 1e-9)[0] + 1)
+    for g in groups:
+        assert np.abs(vecs[:, g] @ vecs[:, g].T - ref[:, g] @ ref[:, g].T).max() < 1e-10
+
+
+def test_host_solver_matches_oracle(engine):
+    n = 96
+    masses = ic.masses_uniform(n, seed=11)
+    om, vecs = engine.eigensystem(masses)
+    oom, oev = O.eigensystem(n, masses + 2)
+    assert np.abs(om - oom).max() <= 1e-13 * om.max()
+    oev = oev.reshape(n, n).T   # column k = eigenvector k
+    assert np.abs(np.abs(np.sum(oev * vecs, axis=0)) - 1).max() < 1e-9
+
+
+def test_host_solver_rejects_bad_arguments(engine):
+    for n in (0, 1):
+        with pytest.raises(engine.NlcError) as e:
+            engine.eigensystem(np.ones(n))
+        assert e.value.code == engine.EINVAL
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("n", [256, 300])
+def test_device_solver_equals_host(gpu, n):
+    """device 0 from 256 sites: cuSOLVER's divide and conquer; the same eigensystem as the host's."""
+    masses = ic.masses_uniform(n, seed=n)
+    om_d, vec_d = gpu.eigensystem(masses, device=0)
+    om_h, vec_h = gpu.eigensystem(masses, device=-1)
+    check_eigensystem(masses, om_d, vec_d)
+    assert np.abs(om_d - om_h).max() <= 1e-12 * om_h.max()
+    assert np.abs(np.abs(np.sum(vec_d * vec_h, axis=0)) - 1).max() < 1e-9
