@@ -23,7 +23,10 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU_SOURCES = ["nlc_real_dnkg.cu", "nlc_real_fput.cu", "nlc_real_toda.cu", "nlc_real_ddnkg.cu",
               "nlc_diag.cu", "nlc_dnls.cu", "nlc_noalloc.cu", "nlc_energy.cu", "nlc_tc.cu"]
-CPP_SOURCES = ["nlc_plan.cpp", "nlc_tables.cpp", "nlc_job.cpp", "nlc_server.cpp", "nlc_eig_device.cpp"]
+CPP_SOURCES = ["nlc_plan.cpp", "nlc_tables.cpp", "nlc_job.cpp", "nlc_server.cpp", "nlc_eig_device.cpp",
+               "nlc_eig_host.cpp"]
+# the host eigensolver's inner loops (products, rotations) want the vectoriser's full cost model
+CPP_OPT = {"nlc_eig_host.cpp": "-O3"}
 HEADERS = ["nlc_device.cuh", "nlc_real.cuh", "nlc_fft.cuh", "nlc_internal.h", "nlc_host.h"]
 
 
@@ -40,7 +43,7 @@ def _cu_cmd(src, obj):
 
 
 def _cpp_cmd(src, obj):
-    return ["g++", "-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-Wall",
+    return ["g++", "-std=c++17", CPP_OPT.get(os.path.basename(src), "-O2"), "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-Wall",
             "-I" + INCLUDE, "-I" + os.path.join(CUDA_HOME, "include"), "-c", src, "-o", obj]
 
 

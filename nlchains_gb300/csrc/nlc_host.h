@@ -115,8 +115,8 @@ void set_host_setup_threads(unsigned threads);
 // Symmetric eigensystem of the periodic dDNKG operator diag(mp2) - shift(+-1) (eigensystem.cpp:
 // 15-18): ascending eigenvalues, omegas = sqrt(eigenvalues), eigenvectors column-major
 // (eigvec[k*n + s] = component s of eigenvector k), as Armadillo's eig_sym would return them.
-// Householder tridiagonalisation followed by the implicit symmetric QR iteration with Wilkinson
-// shifts (Golub and Van Loan, Matrix Computations, algorithms 8.3.1 and 8.3.3).
+// nlc_eig_host.cpp: divide and conquer from 64 sites, else (and as the checked fallback)
+// Householder tridiagonalisation followed by the implicit symmetric QR iteration.
 bool eigensystem_periodic(const std::vector<double> &mp2, std::vector<double> &omegas,
                           std::vector<double> &eigvec);
 

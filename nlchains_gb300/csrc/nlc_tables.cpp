@@ -1,14 +1,11 @@
-// Host-side constant tables of the engine: exp table, dispersion, FFT radices and twiddles, and
-// the dDNKG eigensystem.  Compiled with -ffp-contract=off so that every rounding is the one
-// written here on both x86-64 and aarch64 hosts.
+// Host-side constant tables of the engine: exp table, dispersion, FFT radices and twiddles (the
+// dDNKG eigensystem is in nlc_eig_host.cpp).  Compiled with -ffp-contract=off so that every
+// rounding is the one written here on both x86-64 and aarch64 hosts.
 #include <algorithm>
 #include <cmath>
 #include <complex>
-#include <condition_variable>
 #include <cstdlib>
 #include <cstring>
-#include <functional>
-#include <mutex>
 #include <thread>
 
 #include "nlc_host.h"
@@ -175,75 +172,6 @@ void fft_fma_twiddles(const std::vector<int> &radices, std::vector<double> &gw, 
 	}
 }
 
-namespace {
-
-// Fork-join pool for the O(n^3) loops of the eigensolver: the calling thread plus helpers, each
-// call splits [0, count) into contiguous chunks, one per thread.
-class Pool {
-public:
-	explicit Pool(unsigned threads) {
-		for (unsigned t = 1; t < threads; t++) helpers_.emplace_back([this, t] { run(t); });
-		size_ = threads;
-	}
-	~Pool() {
-		{
-			std::lock_guard<std::mutex> lk(mu_);
-			stop_ = true;
-			gen_++;
-		}
-		cv_.notify_all();
-		for (auto &h : helpers_) h.join();
-	}
-	void parallel_for(size_t count, const std::function<void(size_t, size_t)> &fn) {
-		if (size_ == 1 || count < 64) {
-			fn(0, count);
-			return;
-		}
-		{
-			std::lock_guard<std::mutex> lk(mu_);
-			fn_ = &fn, count_ = count, pending_ = size_ - 1;
-			gen_++;
-		}
-		cv_.notify_all();
-		chunk(0, fn, count);
-		std::unique_lock<std::mutex> lk(mu_);
-		done_.wait(lk, [&] { return pending_ == 0; });
-	}
-
-private:
-	void chunk(unsigned t, const std::function<void(size_t, size_t)> &fn, size_t count) {
-		const size_t b = count * t / size_, e = count * (t + 1) / size_;
-		if (b < e) fn(b, e);
-	}
-	void run(unsigned t) {
-		uint64_t seen = 0;
-		for (;;) {
-			const std::function<void(size_t, size_t)> *fn;
-			size_t count;
-			{
-				std::unique_lock<std::mutex> lk(mu_);
-				cv_.wait(lk, [&] { return gen_ != seen; });
-				seen = gen_;
-				if (stop_) return;
-				fn = fn_, count = count_;
-			}
-			chunk(t, *fn, count);
-			std::lock_guard<std::mutex> lk(mu_);
-			if (--pending_ == 0) done_.notify_one();
-		}
-	}
-	std::vector<std::thread> helpers_;
-	unsigned size_ = 1;
-	std::mutex mu_;
-	std::condition_variable cv_, done_;
-	const std::function<void(size_t, size_t)> *fn_ = nullptr;
-	size_t count_ = 0;
-	unsigned pending_ = 0;
-	uint64_t gen_ = 0;
-	bool stop_ = false;
-};
-
-}  // namespace
 
 namespace {
 
@@ -420,143 +348,6 @@ unsigned host_setup_threads() {
 	unsigned hw = std::max(1u, std::min(32u, std::thread::hardware_concurrency()));
 	if (const char *e = std::getenv("NLC_HOST_THREADS"); e && std::atoi(e) > 0) hw = unsigned(std::atoi(e));
 	return hw;
-}
-
-bool eigensystem_periodic(const std::vector<double> &mp2, std::vector<double> &omegas, std::vector<double> &eigvec) {
-	const size_t n = mp2.size();
-	if (n < 2) return false;
-	Pool pool(n >= 512 ? host_setup_threads() : 1);
-	// dense symmetric matrix, column-major A[j*n + i]
-	std::vector<double> A(n * n, 0.), Q(n * n, 0.);
-	auto a = [&](size_t i, size_t j) -> double & { return A[j * n + i]; };
-	auto q = [&](size_t i, size_t j) -> double & { return Q[j * n + i]; };
-	for (size_t i = 0; i < n; i++) {
-		a(i, i) = mp2[i];
-		const size_t j = (i + 1) % n;
-		a(i, j) = a(j, i) = -1.;   // assignment: for n = 2 the corner entry stays -1 (eigensystem.cpp:16-18)
-		q(i, i) = 1.;
-	}
-
-	// Householder tridiagonalisation: for column k, reflect x = A[k+1:, k] onto alpha e_1.
-	std::vector<double> v(n), p(n), w(n);
-	for (size_t k = 0; k + 2 < n; k++) {
-		double norm2 = 0.;
-		for (size_t i = k + 1; i < n; i++) norm2 += a(i, k) * a(i, k);
-		const double norm = std::sqrt(norm2);
-		if (norm == 0.) continue;
-		const double x0 = a(k + 1, k);
-		const double alpha = x0 > 0 ? -norm : norm;
-		// v = x - alpha e1, normalised
-		std::fill(v.begin(), v.end(), 0.);
-		for (size_t i = k + 1; i < n; i++) v[i] = a(i, k);
-		v[k + 1] -= alpha;
-		double vn2 = 0.;
-		for (size_t i = k + 1; i < n; i++) vn2 += v[i] * v[i];
-		if (vn2 == 0.) continue;
-		const double vinv = 1. / std::sqrt(vn2);
-		for (size_t i = k + 1; i < n; i++) v[i] *= vinv;
-		// p = A v over the trailing block; A is symmetric, so p[i] = sum_j A(j, i) v[j] reads column i
-		pool.parallel_for(n - k, [&](size_t b, size_t e) {
-			for (size_t i = k + b; i < k + e; i++) {
-				const double *col = &A[i * n];
-				double s = 0.;
-				for (size_t j = k + 1; j < n; j++) s += col[j] * v[j];
-				p[i] = s;
-			}
-		});
-		double K = 0.;
-		for (size_t i = k + 1; i < n; i++) K += v[i] * p[i];
-		// A <- A - v w^T - w v^T with w = 2 (p - K v)
-		for (size_t i = k; i < n; i++) w[i] = 2. * (p[i] - K * v[i]);
-		pool.parallel_for(n - k, [&](size_t b, size_t e) {
-			for (size_t j = k + b; j < k + e; j++) {
-				double *col = &A[j * n];
-				const double vj = v[j], wj = w[j];
-				for (size_t i = k; i < n; i++) col[i] -= v[i] * wj + w[i] * vj;
-			}
-		});
-		// exact zeros below the subdiagonal of column k
-		a(k + 1, k) = a(k, k + 1) = alpha;
-		for (size_t i = k + 2; i < n; i++) a(i, k) = a(k, i) = 0.;
-		// Q <- Q H, H = I - 2 v v^T: s = Q v (rows in parallel), then a rank-1 update (columns)
-		pool.parallel_for(n, [&](size_t b, size_t e) {
-			for (size_t i = b; i < e; i++) p[i] = 0.;
-			for (size_t j = k + 1; j < n; j++) {
-				const double *col = &Q[j * n];
-				const double vj = v[j];
-				for (size_t i = b; i < e; i++) p[i] += col[i] * vj;
-			}
-		});
-		pool.parallel_for(n - k - 1, [&](size_t b, size_t e) {
-			for (size_t j = k + 1 + b; j < k + 1 + e; j++) {
-				double *col = &Q[j * n];
-				const double vj2 = 2. * v[j];
-				for (size_t i = 0; i < n; i++) col[i] -= p[i] * vj2;
-			}
-		});
-	}
-	std::vector<double> d(n), e(n, 0.);
-	for (size_t i = 0; i < n; i++) d[i] = a(i, i);
-	for (size_t i = 0; i + 1 < n; i++) e[i] = a(i + 1, i);
-
-	// implicit symmetric QR with Wilkinson shift, deflating from the bottom; the rotations of one
-	// sweep are recorded and then applied to Q by row blocks in parallel
-	const double eps = 2.220446049250313e-16;
-	std::vector<double> rc(n), rs(n);
-	size_t iter = 0, hi = n - 1;
-	while (hi > 0) {
-		if (std::fabs(e[hi - 1]) <= eps * (std::fabs(d[hi - 1]) + std::fabs(d[hi]))) {
-			e[hi - 1] = 0.;
-			hi--;
-			continue;
-		}
-		size_t lo = hi - 1;
-		while (lo > 0 && std::fabs(e[lo - 1]) > eps * (std::fabs(d[lo - 1]) + std::fabs(d[lo]))) lo--;
-		if (++iter > 60 * n) return false;
-		const double delta = (d[hi - 1] - d[hi]) / 2, b2 = e[hi - 1] * e[hi - 1];
-		const double den = delta + (delta >= 0 ? 1. : -1.) * std::hypot(delta, e[hi - 1]);
-		const double mu = den != 0. ? d[hi] - b2 / den : d[hi] - std::fabs(e[hi - 1]);
-		double x = d[lo] - mu, z = e[lo];
-		for (size_t k = lo; k < hi; k++) {
-			const double r = std::hypot(x, z);
-			const double c = r != 0. ? x / r : 1., s = r != 0. ? z / r : 0.;
-			if (k > lo) e[k - 1] = r;
-			// rotate rows/cols k, k+1 of the tridiagonal: T' = P T P^T, P = [c s; -s c]
-			const double ak = d[k], ak1 = d[k + 1], bk = e[k];
-			d[k] = c * c * ak + 2 * c * s * bk + s * s * ak1;
-			d[k + 1] = s * s * ak - 2 * c * s * bk + c * c * ak1;
-			e[k] = c * s * (ak1 - ak) + (c * c - s * s) * bk;
-			if (k + 1 < hi) {
-				z = s * e[k + 1];        // bulge T(k, k+2)
-				e[k + 1] = c * e[k + 1];
-				x = e[k];
-			}
-			rc[k] = c, rs[k] = s;
-		}
-		// Q <- Q P^T on columns (k, k+1), k = lo .. hi-1 in order
-		pool.parallel_for(n, [&](size_t b, size_t e2) {
-			for (size_t k = lo; k < hi; k++) {
-				const double c = rc[k], s = rs[k];
-				double *qk = &Q[k * n], *qk1 = &Q[(k + 1) * n];
-				for (size_t i = b; i < e2; i++) {
-					const double x0 = qk[i], x1 = qk1[i];
-					qk[i] = c * x0 + s * x1;
-					qk1[i] = -s * x0 + c * x1;
-				}
-			}
-		});
-	}
-	// ascending order with vectors
-	std::vector<size_t> idx(n);
-	for (size_t i = 0; i < n; i++) idx[i] = i;
-	std::stable_sort(idx.begin(), idx.end(), [&](size_t x1, size_t x2) { return d[x1] < d[x2]; });
-	omegas.assign(n, 0.);
-	eigvec.assign(n * n, 0.);
-	for (size_t k = 0; k < n; k++) {
-		omegas[k] = std::sqrt(d[idx[k]]);
-		std::memcpy(&eigvec[k * n], &Q[idx[k] * n], n * sizeof(double));
-	}
-	return true;
 }
 
 }  // namespace nlc

@@ -63,6 +63,57 @@ def test_host_solver_matches_oracle(engine):
     assert np.abs(np.abs(np.sum(oev * vecs, axis=0)) - 1).max() < 1e-9
 
 
+def mass_pattern(name, n):
+    rng = np.random.default_rng(n)
+    if name == "uniform":
+        return ic.masses_uniform(n, seed=n)
+    if name == "constant":         # DNKG: degenerate pairs, deflation everywhere
+        return np.full(n, 1.3)
+    if name == "near_constant":    # pairs split by 1e-9: near-degenerate poles
+        return 1.3 + 1e-9 * rng.standard_normal(n)
+    if name == "dimer":            # two alternating masses: two bands
+        return np.where(np.arange(n) % 2 == 0, 1.0, 3.0)
+    if name == "contrast":         # masses over four decades
+        return 10.0 ** rng.uniform(-2, 2, n)
+    if name == "impurity":         # one heavy site in a uniform ring
+        m = np.full(n, 0.5)
+        m[n // 3] = 20.0
+        return m
+    raise ValueError(name)
+
+
+PATTERNS = ["uniform", "constant", "near_constant", "dimer", "contrast", "impurity"]
+
+
+@pytest.mark.parametrize("pattern", PATTERNS)
+@pytest.mark.parametrize("n", [64, 97, 128, 255, 256, 401, 512])
+def test_divide_and_conquer(engine, monkeypatch, pattern, n):
+    """From 64 sites the host solver is divide and conquer; with its fallback switched off it must
+    pass on its own: eigenvalues, residuals, orthogonality, and the projector onto every
+    eigenspace (which is basis independent) against LAPACK."""
+    monkeypatch.setenv("NLC_HOST_EIGEN_DC_ONLY", "1")
+    masses = mass_pattern(pattern, n)
+    om, vecs = engine.eigensystem(masses)
+    check_eigensystem(masses, om, vecs)
+    w2, ref = np.linalg.eigh(operator(masses))
+    scale = np.abs(w2).max()
+    groups = np.split(np.arange(n), np.nonzero(np.diff(w2) > 1e-6 * scale)[0] + 1)
+    for g in groups:
+        assert np.abs(vecs[:, g] @ vecs[:, g].T - ref[:, g] @ ref[:, g].T).max() < 1e-8
+
+
+@pytest.mark.parametrize("pattern", ["uniform", "constant"])
+def test_divide_and_conquer_equals_dense_qr(engine, monkeypatch, pattern):
+    n = 300
+    masses = mass_pattern(pattern, n)
+    om_dc, v_dc = engine.eigensystem(masses)
+    monkeypatch.setenv("NLC_HOST_EIGEN_QR", "1")
+    om_qr, v_qr = engine.eigensystem(masses)
+    assert np.abs(om_dc - om_qr).max() <= 1e-13 * om_qr.max()
+    if pattern == "uniform":
+        assert np.abs(np.abs(np.sum(v_dc * v_qr, axis=0)) - 1).max() < 1e-9
+
+
 def test_host_solver_rejects_bad_arguments(engine):
     for n in (0, 1):
         with pytest.raises(engine.NlcError) as e:
