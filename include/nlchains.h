@@ -103,8 +103,8 @@ typedef struct nlc_plan nlc_plan;
 /*
  * Validate a model and precompute everything its kernels need on the current CUDA device: Yoshida
  * constants scaled by dt, dispersion, the DNLS propagator tables, the dDNKG eigensystem (from 256
- * sites on the GPU with cuSOLVER's divide and conquer, else host Householder + implicit QR; replacing
- * Armadillo eig_sym in eigensystem.cpp:13-36), twiddle tables, the
+ * sites on the GPU with cuSOLVER's divide and conquer, else the host's divide and conquer (dense
+ * QR below 64 sites); replacing Armadillo eig_sym in eigensystem.cpp:13-36), twiddle tables, the
  * integrator launch shape (autotuned once per shape unless NLC_FLAG_NO_TUNE) and the scratch used
  * by the diagnostics.  Replaces the setup half of the reference per-model main
  * (DNKG_FPUT_Toda.cpp:47-95, dDNKG.cpp:50-101, DNLS.cpp:39-126).
@@ -198,8 +198,8 @@ int nlc_plan_omegas(const nlc_plan *plan, double *omegas);
  * column-major with eigenvector k in column k: the `-omegas` and `-eigenvectors` files of
  * eigensystem.cpp:23-29.  Replaces eigensystem.cpp:13-36 (Armadillo eig_sym) for callers that
  * keep their own plan.  device >= 0 lets cuSOLVER's divide and conquer run on that CUDA device
- * from 256 sites; device < 0, shorter chains, or no usable GPU solver: the host Householder +
- * implicit QR solver.  Synchronous.
+ * from 256 sites; device < 0, shorter chains, or no usable GPU solver: the host solver (divide
+ * and conquer from 64 sites, dense Householder + QR below).  Synchronous.
  */
 int nlc_eigensystem(uint32_t chain_length, const double *masses, int32_t device, double *omegas,
                     double *eigenvectors);

@@ -1,9 +1,8 @@
 // dDNKG eigensystem on the GPU: the symmetric eigenproblem of the periodic operator
 // diag(mp2) - shift(+-1) (eigensystem.cpp:13-22) solved by cuSOLVER's divide-and-conquer
 // cusolverDnDsyevd (LAPACK's dsyevd algorithm, the family of Armadillo's eig_sym that the reference
-// calls).  A set-up step, not the hot path: the host Householder + QR solver (nlc_tables.cpp) costs
-// O(n^3) on the CPU, 0.1 s at 256 sites and 0.4 s at 1024 on 16 cores, and served dDNKG requests
-// wait for it; a dDNKG plan of 1024 sites is made in ~70 ms with this solver.
+// calls).  A set-up step, not the hot path: the host solver (nlc_eig_host.cpp) costs O(n^3) on the
+// CPU, and a dDNKG plan of 1024 sites is made in ~70 ms with this one.
 //
 // cuSOLVER is loaded at run time (dlopen), so the library has no link dependency on it: where it is
 // missing, or any step fails, the caller keeps the host solver.
