@@ -20,7 +20,7 @@
 // go to its row of partial sums, which the linenergies finish kernel adds in a fixed order.
 //
 // With 3 slices instead of 7 (NLC_FLAG_BF16X3_PROJECTION: 6 slice products, t = 2..4) the same
-// kernels give P to ~2^-24 of the maxima: the north star's "split BF16x3" precision, faster.
+// kernels give P to ~2^-24 of the maxima: the precision of a three-way BF16 split, faster.
 //
 // One CTA: 128 rows (64 chains) x 64 modes; 8 warps.  Thread 0 drives a two-stage TMA pipeline
 // (64-byte swizzle, 32 sites of K per stage: 7 A tiles of 128 x 32 and 7 B tiles of 64 x 32) and

@@ -1,6 +1,6 @@
 """Per-chain energies (nlc_energies / nlc_job_energies) against the oracle's restatement of the
 reference post-processing's definitions (nlchains.m:40-48), and energy conservation of the
-integrators, the benchmark spec's drift bar."""
+integrators: the energy drift stays at the scheme's own error level."""
 import numpy as np
 import pytest
 
