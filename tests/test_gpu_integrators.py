@@ -87,7 +87,8 @@ def test_bit_exact_against_device_order_oracle(gpu, case):
 
 
 REFERENCE_CASES = [
-    # config 1 (FPUT-beta N=64, dt=0.1, energy density 0.1 over k=+-1..4) and config 2 shapes
+    # the FPUT-beta ensemble (N=64, dt=0.1, energy density 0.1 over k=+-1..4) and the DNKG / Toda
+    # ensembles of 128 sites (dt=0.05, energy density 0.5 over the lowest 8% of the modes)
     ("FPUT", 64, dict(alpha=0.0, beta=1.0), 0.1, 0.1, dict(kmax=4, include_zero=False), 0.0),
     ("DNKG", 128, dict(m=1.0, beta=1.0), 0.05, 0.5, dict(fraction=0.08), 1.0),
     ("Toda", 128, dict(alpha=0.5), 0.05, 0.5, dict(fraction=0.08, include_zero=False), 0.0),
