@@ -102,9 +102,9 @@ typedef struct nlc_plan nlc_plan;
 
 /*
  * Validate a model and precompute everything its kernels need on the current CUDA device: Yoshida
- * constants scaled by dt, dispersion, the DNLS propagator tables, the dDNKG eigensystem (from 256
- * sites on the GPU with cuSOLVER's divide and conquer, else the host's divide and conquer (dense
- * QR below 64 sites); replacing Armadillo eig_sym in eigensystem.cpp:13-36), twiddle tables, the
+ * constants scaled by dt, dispersion, the DNLS propagator tables, the dDNKG eigensystem (the host's
+ * divide and conquer, dense QR below 64 sites; from 4096 sites, or NLC_DEVICE_EIGEN_FROM, on the
+ * GPU with cuSOLVER's; replacing Armadillo eig_sym in eigensystem.cpp:13-36), twiddle tables, the
  * integrator launch shape (autotuned once per shape unless NLC_FLAG_NO_TUNE) and the scratch used
  * by the diagnostics.  Replaces the setup half of the reference per-model main
  * (DNKG_FPUT_Toda.cpp:47-95, dDNKG.cpp:50-101, DNLS.cpp:39-126).

@@ -646,9 +646,13 @@ extern "C" int nlc_plan_create(const nlc_model *model, nlc_plan **out) {
 	if (mdl == NLC_DDNKG) {
 		P->mp2_host.resize(n);
 		for (uint32_t i = 0; i < n; i++) P->mp2_host[i] = model->masses[i] + 2;
-		// from 256 sites on the GPU (cuSOLVER syevd, 10-20x the host solver); the host solver below
-		// that, or when the GPU solver is unavailable
-		const bool device = n >= 256 && eigensystem_periodic_device(P->mp2_host, P->omega_host, P->eig_host);
+		// the host's divide and conquer below 4096 sites: on the 16 Grace cores of a GB300 host it takes
+		// 3.3 ms at 256 sites, 24 ms at 1024 and 60 ms at 2048, against 16-108 ms for cuSOLVER's
+		// syevd (seconds on a process's first call); the GPU solver from 4096 sites, where the host's
+		// n^3 grows past it, or from NLC_DEVICE_EIGEN_FROM sites
+		uint32_t device_from = 4096;
+		if (const char *e = std::getenv("NLC_DEVICE_EIGEN_FROM"); e && std::atoi(e) > 0) device_from = uint32_t(std::atoi(e));
+		const bool device = n >= device_from && eigensystem_periodic_device(P->mp2_host, P->omega_host, P->eig_host);
 		if (!device && !eigensystem_periodic(P->mp2_host, P->omega_host, P->eig_host))
 			return set_error(NLC_EINVAL, "Cannot calculate eigensystem!");
 		P->norm = 0.5 / model->copies;   // dDNKG.cpp:141

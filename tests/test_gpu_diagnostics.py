@@ -132,9 +132,10 @@ def test_fp32_diagnostics_error_stated(gpu, model, params, n):
 
 @pytest.mark.parametrize("n", [256, 300, 1024])
 def test_ddnkg_device_eigensystem_equals_host(gpu, n, monkeypatch):
-    """From 256 sites the dDNKG eigensystem is solved on the GPU (cuSOLVER syevd); against the host
-    solver (NLC_HOST_EIGEN): the same frequencies and, since eigenvectors are defined up to sign, the
-    same mode energies of a state (both through the FP64 projection)."""
+    """A plan's dDNKG eigensystem solved on the GPU (cuSOLVER syevd; plans take it from 4096 sites,
+    here from 256 through NLC_DEVICE_EIGEN_FROM) against the host solver (NLC_HOST_EIGEN): the same
+    frequencies and, since eigenvectors are defined up to sign, the same mode energies of a state
+    (both through the FP64 projection)."""
     torch = pytest.importorskip("torch")
     copies = 16
     masses = ic.masses_uniform(n, seed=n)
@@ -144,6 +145,8 @@ def test_ddnkg_device_eigensystem_equals_host(gpu, n, monkeypatch):
     for host in (False, True):
         if host:
             monkeypatch.setenv("NLC_HOST_EIGEN", "1")
+        else:
+            monkeypatch.setenv("NLC_DEVICE_EIGEN_FROM", "256")
         plan = gpu.Plan(gpu.Model("dDNKG", n, copies, 0.05, masses=masses, beta=1.0, flags=gpu.FLAG_FP64_PROJECTION))
         lin = torch.zeros(n, dtype=torch.float64, device="cuda")
         plan.linenergies(dev.data_ptr(), lin.data_ptr(), 0, torch.cuda.current_stream().cuda_stream)
