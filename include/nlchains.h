@@ -199,7 +199,8 @@ int nlc_plan_omegas(const nlc_plan *plan, double *omegas);
  * eigensystem.cpp:23-29.  Replaces eigensystem.cpp:13-36 (Armadillo eig_sym) for callers that
  * keep their own plan.  device >= 0 lets cuSOLVER's divide and conquer run on that CUDA device
  * from 256 sites; device < 0, shorter chains, or no usable GPU solver: the host solver (divide
- * and conquer from 64 sites, dense Householder + QR below).  Synchronous.
+ * and conquer from 64 sites, dense Householder + QR below), the faster one below about 4096 sites
+ * on a GB300 host.  Synchronous.
  */
 int nlc_eigensystem(uint32_t chain_length, const double *masses, int32_t device, double *omegas,
                     double *eigenvectors);
