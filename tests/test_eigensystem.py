@@ -114,6 +114,19 @@ def test_divide_and_conquer_equals_dense_qr(engine, monkeypatch, pattern):
         assert np.abs(np.abs(np.sum(v_dc * v_qr, axis=0)) - 1).max() < 1e-9
 
 
+def test_device_request_without_a_usable_gpu_uses_the_host(engine):
+    """device >= 0 only allows the GPU solver: with no usable GPU (this CPU run) the host answers."""
+    try:
+        import torch
+        if torch.cuda.is_available():
+            pytest.skip("a GPU is present: the device path is covered by the GPU tests")
+    except ImportError:
+        pass
+    masses = ic.masses_uniform(300, seed=4)
+    om, vecs = engine.eigensystem(masses, device=0)
+    check_eigensystem(masses, om, vecs)
+
+
 def test_host_solver_rejects_bad_arguments(engine):
     for n in (0, 1):
         with pytest.raises(engine.NlcError) as e:
