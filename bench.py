@@ -430,6 +430,28 @@ def measure_projection(w, local, evolve_steps=1000):
                       "FP64 recombination, energy epilogue fused"}
 
 
+def measure_eigensystem(w, sizes=(1024, 2048)):
+    """Set-up cost of the dDNKG eigensystem on this machine's host cores (nlc_eigensystem with no
+    device: the divide-and-conquer solver plans use below 4096 sites), best of three wall-clock
+    times at the workload's chain length and at the given ones.  A failure is reported, not raised."""
+    try:
+        import nlchains_gb300 as nlc
+        from nlchains_gb300 import ic
+        out = {"solver": "host divide and conquer (nlc_eigensystem, device -1)"}
+        for n in sorted({w["n"], *sizes}):
+            m = ic.masses_uniform(n, seed=777)
+            best = float("inf")
+            for _ in range(3):
+                t0 = time.perf_counter()
+                nlc.eigensystem(m, device=-1)
+                best = min(best, time.perf_counter() - t0)
+            out[f"ms_n{n}"] = best * 1e3
+        out["host_threads"] = os.cpu_count()
+        return out
+    except Exception as e:   # the set-up figure is informational
+        return {"error": f"{type(e).__name__}: {e}"}
+
+
 def measure_fp32_diagnostics(w, local, evolve_steps=1000):
     """One diagnostics sample of the DNLS workload (its initial state advanced by 1000 steps, so that
     energy has spread beyond the initial modes) with the FP64 transform and with
@@ -503,6 +525,7 @@ def run_engine(args):
                                ow["batching"] / (o["move_ms"] * 1e-3) / (peak * 1e12 / 2)}
         if ow["model"] == "dDNKG" and rank == 0:
             others["dDNKG"]["projection"] = measure_projection(ow, local)
+            others["dDNKG"]["eigensystem_setup"] = measure_eigensystem(ow)
         if ow["model"] == "DNLS" and rank == 0:
             others["DNLS"]["fp32_diagnostics"] = measure_fp32_diagnostics(ow, local)
     flops = FLOPS_PER_SITE_STEP[w["model"]] * w["n"] * w["copies"] * w["batching"]
