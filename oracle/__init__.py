@@ -5,12 +5,14 @@ diagnostics (each C function cites the reference file:line it follows).  Only te
 __graft_entry__.smoke() and bench.py's CPU-baseline leg may import this package; the product
 (nlchains_gb300) never does.
 
-Parity status: unpinned against the reference itself (the reference has no tests, golden vectors or
-fixtures, and its path cannot be built in this image: Boost.MPI, MPI, FFTW3 and Armadillo are
-absent), except for the Yoshida tables: oracle/_ref compiles the reference's own
-common/symplectic.hpp in place where the reference sources are present, and the tests compare the
-oracle's tables with it bit for bit.  The oracle is otherwise pinned by analytic known answers in
-tests/test_oracle.py and tests/test_known_answers.py.
+Parity status: pinned to the reference itself.  oracle/build.py compiles the reference's CPU
+program (its nlchains-cpu target) in place from its sources, with stand-ins for Boost, MPI, FFTW3 and
+Armadillo (oracle/ref_shim/); the oracle's reference order reproduces that program bit for bit when
+the stand-ins' FFT and eigensolver are the oracle's own, and to rounding with the exact transform
+(tests/golden/reference, tests/test_reference_pin.py).  The reference's GPU kernels, compiled
+unmodified into oracle/_ref/ref_gpu_n<N>.fatbin, run through RefGPU below on the GPU
+(tests/test_gpu_reference.py).  The Yoshida tables are pinned to the reference's header as well, and
+analytic known answers stay in tests/test_oracle.py and tests/test_known_answers.py.
 """
 import ctypes
 import os
@@ -124,13 +126,14 @@ def eigensystem(n, mp2):
     return om, ev
 
 
-def linenergies(model, state):
-    """Normalised per-mode energies of the ensemble (results::calc_linenergies output)."""
+def linenergies(model, state, eig=None):
+    """Normalised per-mode energies of the ensemble (results::calc_linenergies output).  eig: the
+    dDNKG (omegas, eigenvectors) of eigensystem(), computed here when not given."""
     state = np.ascontiguousarray(state, dtype=np.float64)
     out = np.zeros(model.n)
     ev = om = None
     if model.model == DDNKG:
-        om, ev = eigensystem(model.n, model.mp2)
+        om, ev = eig if eig is not None else eigensystem(model.n, model.mp2)
     s = model._struct()
     rc = _lib().nlo_linenergies(ctypes.byref(s), _dp(state), _dp(ev) if ev is not None else None,
                                 _dp(om) if om is not None else None, _dp(out))
@@ -191,3 +194,97 @@ def exp_table(scale):
 
 def exp_scaled(x, table):
     return _lib().nlo_exp_scaled(x, _dp(np.ascontiguousarray(table)))
+
+
+class RefGPU:
+    """The reference's own GPU kernels (oracle/_ref/ref_gpu_n<N>.fatbin, compiled unmodified from its
+    sources) launched by oracle/ref_shim/ref_gpu_host.cpp on device ensembles.  Test infrastructure:
+    the checker and the bench's plain-reference line, never the product.
+
+    ``available(n_opt)`` tells whether the fatbin and the harness exist on this machine.
+    """
+
+    @staticmethod
+    def fatbin(n_opt):
+        return os.path.join(_build.REF_OUT, f"ref_gpu_n{n_opt}.fatbin")
+
+    @staticmethod
+    def available(n_opt):
+        return (os.path.exists(RefGPU.fatbin(n_opt)) and
+                os.path.exists(os.path.join(_build.OUT, "libref_gpu_host.so")))
+
+    _host = None
+
+    @classmethod
+    def _lib(cls):
+        if cls._host is None:
+            _build.build()
+            lib = ctypes.CDLL(os.path.join(_build.OUT, "libref_gpu_host.so"))
+            vp, dp, u32, u64 = ctypes.c_void_p, ctypes.POINTER(ctypes.c_double), ctypes.c_uint32, ctypes.c_uint64
+            lib.refgpu_open.argtypes = [ctypes.c_char_p, ctypes.c_int, dp, dp, ctypes.POINTER(vp)]
+            lib.refgpu_close.argtypes = [vp]
+            lib.refgpu_error.argtypes = [vp]
+            lib.refgpu_error.restype = ctypes.c_char_p
+            lib.refgpu_kernel_count.argtypes = [vp]
+            lib.refgpu_advance.argtypes = [vp, ctypes.c_int, vp, u32, u32, ctypes.c_double, ctypes.c_double,
+                                           ctypes.c_double, ctypes.c_double, dp, u64, u32, ctypes.c_int, vp]
+            lib.refgpu_move_warp_async.argtypes = [vp, ctypes.c_int, vp, u32, u32, u32, u32, vp]
+            lib.refgpu_linenergies.argtypes = [vp, ctypes.c_int, vp, u32, u32, ctypes.c_double, dp, dp, dp, vp]
+            lib.refgpu_dnls_advance.argtypes = [vp, vp, u32, u32, ctypes.c_double, ctypes.c_double, u64, u32, vp]
+            cls._host = lib
+        return cls._host
+
+    def __init__(self, n_opt):
+        self.n_opt = n_opt
+        lib = self._lib()
+        c, d = coefficients()
+        self.h = ctypes.c_void_p()
+        rc = lib.refgpu_open(self.fatbin(n_opt).encode(), n_opt, _dp(c), _dp(d), ctypes.byref(self.h))
+        if rc != 0:
+            msg = lib.refgpu_error(self.h).decode()
+            self.close()
+            raise RuntimeError("reference GPU module: " + msg)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self._lib().refgpu_close(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc):
+        if rc != 0:
+            raise RuntimeError("reference GPU path: " + self._lib().refgpu_error(self.h).decode())
+
+    def kernel_count(self):
+        return self._lib().refgpu_kernel_count(self.h)
+
+    def advance(self, model, state_ptr, steps, batching, force_split=False, stream=0):
+        """move<model> on a device double2[copies][n] (model: an oracle Model), `steps / batching`
+        launches; synchronous."""
+        mp2 = _dp(model.mp2) if model.mp2 is not None else None
+        self._check(self._lib().refgpu_advance(self.h, model.model, state_ptr, model.n, model.copies, model.dt,
+                                               model.m, model.alpha, model.beta, mp2, steps, batching,
+                                               int(force_split), stream))
+
+    def move_warp_async(self, model_id, state_ptr, n, copies, batching, launches=1, stream=0):
+        self._check(self._lib().refgpu_move_warp_async(self.h, model_id, state_ptr, n, copies, batching, launches,
+                                                       stream))
+
+    def linenergies(self, model, state_ptr, stream=0):
+        out = np.zeros(model.n)
+        ev = om = None
+        if model.model == DDNKG:
+            om, ev = eigensystem(model.n, model.mp2)
+        self._check(self._lib().refgpu_linenergies(self.h, model.model, state_ptr, model.n, model.copies, model.m,
+                                                   _dp(ev) if ev is not None else None,
+                                                   _dp(om) if om is not None else None, _dp(out), stream))
+        return out
+
+    def dnls_advance(self, model, state_ptr, steps, batching, stream=0):
+        self._check(self._lib().refgpu_dnls_advance(self.h, state_ptr, model.n, model.copies, model.dt, model.beta,
+                                                    steps, batching, stream))

@@ -5,9 +5,9 @@
  * reference's CPU build is -Ofast; one OpenMP thread per core over copies, the moral equivalent of
  * `mpirun -n <cores> nlchains <model>-cpu`).
  *
- * Parity unpinned against the reference (no reference tests or fixtures exist and it cannot be
- * built in this image); pinned by analytic known answers in tests/ (test_oracle.py,
- * test_known_answers.py).
+ * Parity: pinned to the reference's own CPU program, compiled in place from its sources (see
+ * nlc_oracle.h and tests/test_reference_pin.py), and by analytic known answers in tests/
+ * (test_oracle.py, test_known_answers.py).
  */
 #include "nlc_oracle.h"
 
@@ -321,11 +321,27 @@ void nlo_dispersion(int32_t model, uint32_t n, double m, double *omega) {
  * |sin| = sqrt(1 - cos^2) shortcut of :85-95 (which loses accuracy at small angles)
  * ----------------------------------------------------------------------------------------------*/
 
-static void dnls_nonlinear(uint32_t n, double *psi, double beta_dt_symplectic) {
+static void dnls_nonlinear_sincos(uint32_t n, double *psi, double beta_dt_symplectic) {
 	for (uint32_t s = 0; s < n; s++) {
 		double r1 = psi[2 * s], i1 = psi[2 * s + 1];
 		double norm = r1 * r1 + i1 * i1, angle = -beta_dt_symplectic * norm;
 		double er = cos(angle), ei = sin(angle);
+		psi[2 * s] = r1 * er - i1 * ei;
+		psi[2 * s + 1] = ei * r1 + i1 * er;
+	}
+}
+
+/* The reference CPU rotation itself (DNLS/cpu-implementation/DNLS.cpp:77-98): cos(angle), then
+ * |sin| = sqrt(1 - cos^2) with the sign of sin recovered from the half-turn count of the angle.
+ * Used by NLO_ORDER_REFERENCE to pin the oracle to the reference's CPU program; its sine is off by
+ * up to eps / angle^2 relative at small angles, so the sincos form above is the checker. */
+static void dnls_nonlinear_reference(uint32_t n, double *psi, double beta_dt_symplectic) {
+	for (uint32_t s = 0; s < n; s++) {
+		double r1 = psi[2 * s], i1 = psi[2 * s + 1];
+		double norm = r1 * r1 + i1 * i1, angle = -beta_dt_symplectic * norm;
+		double er = cos(angle), ei = sqrt(1 - er * er);
+		int32_t invert_sign = (int32_t) (angle / M_PI) & 1;
+		ei *= (1. - 2. * invert_sign) * copysign(1., angle);
 		psi[2 * s] = r1 * er - i1 * ei;
 		psi[2 * s + 1] = ei * r1 + i1 * er;
 	}
@@ -347,6 +363,8 @@ static void dnls_tables(uint32_t n, double dt, double *tables /* [7][n][2] */) {
 
 static void move_chain_dnls(const nlo_model *M, const double *tables, double *psi, uint32_t batching) {
 	const uint32_t n = M->n;
+	void (*const dnls_nonlinear)(uint32_t, double *, double) =
+			M->order == NLO_ORDER_REFERENCE ? dnls_nonlinear_reference : dnls_nonlinear_sincos;
 	for (uint32_t i = 0; i < batching; i++)
 		for (int k = 0; k < 7; k++) {
 			dnls_nonlinear(n, psi, M->beta * M->dt * (!k && i ? 2. : 1.) * yoshida_c[k]);
@@ -528,18 +546,11 @@ double nlo_energy(const nlo_model *M, const double *chain) {
 	return h;
 }
 
-/* Cyclic Jacobi with threshold, then ascending sort (LAPACK dsyev order). */
-int nlo_eigensystem(uint32_t n, const double *mp2, double *omegas, double *v) {
-	double *a = calloc((size_t) n * n, sizeof(double));
-	if (!a) return -1;
+/* Cyclic Jacobi with threshold on a symmetric column-major matrix `a` (overwritten), then ascending
+ * sort (LAPACK dsyev order): eigenvalues in w, eigenvectors as the columns of v. */
+int nlo_eig_sym(uint32_t n, double *a, double *w, double *v) {
 #define A(i, j) a[(size_t) (j) * n + (i)]
 #define V(i, j) v[(size_t) (j) * n + (i)]
-	/* eigensystem.cpp:15-18: the corner entries are assigned, not added (n = 2 keeps -1) */
-	for (uint32_t i = 0; i < n; i++) {
-		A(i, i) = mp2[i];
-		uint32_t j = i + 1 < n ? i + 1 : 0;
-		A(i, j) = A(j, i) = -1.;
-	}
 	for (uint32_t i = 0; i < n; i++)
 		for (uint32_t j = 0; j < n; j++) V(i, j) = i == j;
 	for (int sweep = 0; sweep < 100; sweep++) {
@@ -589,9 +600,26 @@ int nlo_eigensystem(uint32_t n, const double *mp2, double *omegas, double *v) {
 			memcpy(&V(0, best), col, sizeof(double) * n);
 		}
 	}
-	for (uint32_t i = 0; i < n; i++) omegas[i] = sqrt(ev[i]);
+	for (uint32_t i = 0; i < n; i++) w[i] = ev[i];
 #undef A
 #undef V
-	free(a), free(ev), free(col);
+	free(ev), free(col);
 	return 0;
+}
+
+/* eigensystem.cpp:13-22: the periodic operator diag(mp2) - shift(+-1), its eigenvectors, and
+ * omegas = sqrt(eigenvalues). */
+int nlo_eigensystem(uint32_t n, const double *mp2, double *omegas, double *v) {
+	double *a = calloc((size_t) n * n, sizeof(double));
+	if (!a) return -1;
+	/* eigensystem.cpp:15-18: the corner entries are assigned, not added (n = 2 keeps -1) */
+	for (uint32_t i = 0; i < n; i++) {
+		a[(size_t) i * n + i] = mp2[i];
+		uint32_t j = i + 1 < n ? i + 1 : 0;
+		a[(size_t) j * n + i] = a[(size_t) i * n + j] = -1.;
+	}
+	int rc = nlo_eig_sym(n, a, omegas, v);
+	for (uint32_t i = 0; !rc && i < n; i++) omegas[i] = sqrt(omegas[i]);
+	free(a);
+	return rc;
 }

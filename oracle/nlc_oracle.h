@@ -5,19 +5,24 @@
  * __graft_entry__.smoke() and by the timed CPU baseline in bench.py as the checker.  The product
  * (libnlchains_gb300.so) never links, loads or calls this code.
  *
- * Parity status: UNPINNED against the reference itself.  The reference ships no tests, golden
- * vectors or fixtures, and it cannot be built here (it needs Boost.MPI/ProgramOptions, MPI, FFTW3
- * and Armadillo, none of which exist in this image).  The oracle is pinned instead by analytic
- * known answers (exact linear-mode transfer of the Yoshida scheme at beta = 0, norm and spectrum
- * conservation of the linear DNLS, the Mathematica entropy/energy definitions) in tests/.
+ * Parity status: PINNED to the reference's own CPU program.  oracle/build.py compiles the
+ * reference's nlchains-cpu sources in place (stand-ins for Boost, MPI, FFTW3 and Armadillo in
+ * oracle/ref_shim/); with the oracle's FFT and eigensolver standing in for FFTW and LAPACK, this
+ * oracle's NLO_ORDER_REFERENCE reproduces that program bit for bit (states, mode energies and
+ * entropies of all five models; tests/golden/reference, tests/test_reference_pin.py).  The
+ * reference's GPU kernels, compiled unmodified from its sources, are compared on the GPU
+ * (tests/test_gpu_reference.py).
  *
  * Two arithmetic orders are provided for the real models:
  *   NLO_ORDER_REFERENCE  the reference CPU code's expressions, one rounding per C operator
  *                        (DNKG_FPUT_Toda/cpu-implementation/DNKG_FPUT_Toda.cpp:23-40,125-142,
- *                        dDNKG/cpu-implementation/dDNKG.cpp:160-162,234-251), libm exp;
+ *                        dDNKG/cpu-implementation/dDNKG.cpp:17-19,91-108), libm exp; for DNLS the
+ *                        reference CPU's |sin| = sqrt(1 - cos^2) rotation
+ *                        (DNLS/cpu-implementation/DNLS.cpp:77-98);
  *   NLO_ORDER_DEVICE     the exact FP64 operation sequence of the sm_103a kernels (explicit fma,
  *                        bond-cached forces, table-driven exp), so GPU results can be compared
- *                        bit for bit.
+ *                        bit for bit; for DNLS the rotation by sincos (the reference GPU's
+ *                        e_pow_I, common/utilities_cuda.cuh:469-473).
  */
 #ifndef NLC_ORACLE_H
 #define NLC_ORACLE_H
@@ -80,6 +85,10 @@ int nlo_entropies(const double *linenergies, uint32_t n, int a0is0, const uint8_
 
 /* Total energy of one chain (supporting-material/post-processing/nlchains.m:40-48). */
 double nlo_energy(const nlo_model *mdl, const double *chain);
+
+/* Symmetric eigenproblem of the column-major n x n matrix a (overwritten) by cyclic Jacobi:
+ * ascending eigenvalues w, eigenvectors as the columns of v (column-major). */
+int nlo_eig_sym(uint32_t n, double *a, double *w, double *v);
 
 /* Symmetric eigensystem of the periodic dDNKG operator diag(mp2) - shift(+-1) (eigensystem.cpp:13-22)
  * by cyclic Jacobi: ascending eigenvalues, omegas = sqrt(eigenvalues), column-major eigenvectors. */
