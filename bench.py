@@ -270,13 +270,19 @@ def measure_e2e(w, steps, warmup, rank, local):
 
 SERVED_PARAMS = {"FPUT": (0.1, dict(alpha=0.0, beta=1.0)), "Toda": (0.05, dict(alpha=0.5)),
                  "DNKG": (0.05, dict(m=1.0, beta=1.0)), "dDNKG": (0.05, dict(beta=1.0)), "DNLS": (0.01, dict(beta=1.0))}
+# the served mixed stream at its stated ranges, with few enough requests for a bench run of minutes
+SERVED_FULL = dict(count=24, seed=2024, n_range=(32, 4096), copies_range=(64, 16384), steps_range=(1000, 100000),
+                   mean_gap_ms=500.0)
+# the smaller stream of earlier measurements (one hundredth of the work per request)
+SERVED_SMALL = dict(count=48, seed=2024, n_range=(32, 1024), copies_range=(64, 4096), steps_range=(100, 2000),
+                    mean_gap_ms=15.0)
 
 
 def served_stream(count=48, seed=2024, n_range=(32, 1024), copies_range=(64, 4096), steps_range=(100, 2000),
                   batching=100, mean_gap_ms=15.0):
     """A seeded mixed request stream: model uniform over the five, chain length, copies and steps
-    log-uniform, energy density U[0.1, 1], Poisson arrivals (the reference's served mix scaled to a
-    bench run: N <= 1024, copies <= 4096, steps <= 2000)."""
+    log-uniform over the given ranges (steps rounded to a multiple of kernel_batching), energy density
+    U[0.1, 1], seeded random-phase low-mode initial states, Poisson arrivals."""
     from nlchains_gb300 import ic
     rng = np.random.default_rng(seed)
     names = ["FPUT", "Toda", "DNKG", "dDNKG", "DNLS"]
@@ -303,10 +309,30 @@ def served_stream(count=48, seed=2024, n_range=(32, 1024), copies_range=(64, 409
     return reqs
 
 
-def measure_served(local):
+def run_alone(nlc, ctx, model, r):
+    """One request alone through the job API with the sampling of the reference's main loop (a sample
+    every kernel_batching steps), pipelined as the command line runs it: each batch and its sample go
+    out as one graph replay into one of two result slots while the host waits for the previous one,
+    so the GPU never idles on a host round trip."""
+    job = ctx.job(model, r["b"])
+    t1 = time.perf_counter()
+    job.upload(r["state"])
+    rounds = r["steps"] // r["b"]
+    job.sample_async(0)
+    for i in range(rounds):
+        job.step_async((i + 1) % 2)
+        job.sample_wait(i % 2)
+    job.sample_wait(rounds % 2)
+    job.download()
+    t = time.perf_counter() - t1
+    job.close()
+    return t
+
+
+def measure_served(local, stream):
     """Continuous batching (nlc_server) against the same requests run alone, one after the other."""
     import nlchains_gb300 as nlc
-    reqs = served_stream()
+    reqs = served_stream(**stream)
     site_steps = sum(float(r["n"]) * r["copies"] * r["steps"] for r in reqs)
 
     def model(r):
@@ -328,35 +354,83 @@ def measure_served(local):
         ids.append(srv.submit(model(r), r["b"], r["steps"], r["state"]))
     lat = []
     for rid in ids:
-        srv.wait(rid, 600000)
+        srv.wait(rid, 1800000)
         st = srv.poll(rid)
         lat.append(st["finish_ms"] - st["submit_ms"])
         srv.result(rid)
     makespan = time.perf_counter() - t0
     srv.close()
 
-    # the same requests alone: one ensemble at a time through the job API (plain per-model path)
+    # the same requests alone, one at a time through the job API (the plain per-model path)
     ctx = nlc.Context(local)
-    alone_s = 0.0
-    for r in reqs:
-        job = ctx.job(model(r), r["b"])
-        t1 = time.perf_counter()
-        job.upload(r["state"])
-        job.linenergies()
-        for _ in range(r["steps"] // r["b"]):
-            job.advance(r["b"])
-            job.linenergies()
-        job.download()
-        alone_s += time.perf_counter() - t1
-        job.close()
+    alone = [run_alone(nlc, ctx, model(r), r) for r in reqs]
     ctx.close()
+    alone_s = sum(alone)
+    slowdown = np.array(lat) / (np.array(alone) * 1e3)
+    per_model = {}
+    for r, lt, al in zip(reqs, lat, alone):
+        m = per_model.setdefault(r["name"], {"requests": 0, "site_steps": 0.0, "alone_s": 0.0, "latency_ms": []})
+        m["requests"] += 1
+        m["site_steps"] += float(r["n"]) * r["copies"] * r["steps"]
+        m["alone_s"] += al
+        m["latency_ms"].append(lt)
+    for m in per_model.values():
+        m["p50_latency_ms"] = float(np.percentile(m.pop("latency_ms"), 50))
     return {"value": site_steps / makespan, "unit": "site-steps/s", "alone_value": site_steps / alone_s,
             "speedup_vs_alone": alone_s / makespan, "p50_ms": float(np.percentile(lat, 50)),
-            "p99_ms": float(np.percentile(lat, 99)), "requests": len(reqs), "makespan_s": makespan,
-            "alone_s": alone_s,
-            "stream": "48 requests, model uniform over FPUT/Toda/DNKG/dDNKG/DNLS, N log-uniform [32, 1024], "
-                      "copies log-uniform [64, 4096], steps log-uniform [100, 2000] (multiples of 100), "
-                      "kernel_batching 100, Poisson arrivals (mean gap 15 ms), seed 2024"}
+            "p99_ms": float(np.percentile(lat, 99)), "slowdown_p50": float(np.percentile(slowdown, 50)),
+            "slowdown_p99": float(np.percentile(slowdown, 99)), "requests": len(reqs), "makespan_s": makespan,
+            "alone_s": alone_s, "largest_request_alone_s": float(max(alone)), "per_model": per_model,
+            "stream": f"{stream['count']} requests, model uniform over FPUT/Toda/DNKG/dDNKG/DNLS, N log-uniform "
+                      f"{list(stream['n_range'])}, copies log-uniform {list(stream['copies_range'])}, steps log-uniform "
+                      f"{list(stream['steps_range'])} (multiples of 100), kernel_batching 100 with a sample every batch, "
+                      f"Poisson arrivals (mean gap {stream['mean_gap_ms']:g} ms), seed {stream['seed']}",
+            "alone": "each request by itself through the job API, batch + sample replayed as one CUDA graph, "
+                     "two result slots (no host round trip between batches)",
+            "slowdown": "latency over the request's own alone time"}
+
+
+def measure_mixed_concurrency(local, full_rates, rounds=20):
+    """Different models sharing the GPU: four small ensembles (DNKG, FPUT, Toda, dDNKG, each about
+    a quarter of the GPU's resident chains) submitted to the request server together, which runs each
+    model's class kernel on its own stream, against (a) the same four run one after the other and
+    (b) the time their work takes at each model's full-GPU rate (`full_rates`, site-steps/s of this
+    bench's full-size workloads).  occupancy = (b) / served makespan: 1.0 means the concurrent
+    per-model launches keep the FP64 pipes as busy as one launch over all four would."""
+    import nlchains_gb300 as nlc
+    from nlchains_gb300 import ic
+    cases = [("DNKG", 128, 4096, 0.05, dict(m=1.0, beta=1.0)), ("FPUT", 64, 8192, 0.1, dict(alpha=0.0, beta=1.0)),
+             ("Toda", 128, 4096, 0.05, dict(alpha=0.5)), ("dDNKG", 256, 2048, 0.05, dict(beta=1.0))]
+    b = 100
+    reqs = []
+    for i, (name, n, copies, dt, params) in enumerate(cases):
+        masses = ic.masses_uniform(n, seed=777) if name == "dDNKG" else None
+        if name == "dDNKG":
+            st = ic.ddnkg_ensemble(masses, copies, 0.5, 20, seed=i)
+        else:
+            st = ic.real_ensemble(n, copies, 0.5, ic.low_modes(n, 0.08, include_zero=params.get("m", 0) > 0),
+                                  m=params.get("m", 0.0), seed=i)
+        reqs.append((nlc.Model(name, n, copies, dt, masses=masses, **params), st, float(n) * copies * b * rounds))
+
+    def serve(subset):
+        srv = nlc.Server(local)
+        t0 = time.perf_counter()
+        ids = [srv.submit(m, b, b * rounds, st) for m, st, _ in subset]
+        for rid in ids:
+            srv.wait(rid, 600000)
+            srv.result(rid)
+        t = time.perf_counter() - t0
+        srv.close()
+        return t
+
+    serve(reqs[:1])   # warm-up
+    together = serve(reqs)
+    alone = sum(serve([r]) for r in reqs)
+    ideal = sum(work / full_rates[m.name] for m, _, work in reqs)
+    return {"ensembles": [f"{m.name} n={m.chain_length} copies={m.copies}" for m, _, _ in reqs],
+            "steps_each": b * rounds, "served_together_s": together, "served_one_by_one_s": alone,
+            "at_full_gpu_rates_s": ideal, "occupancy": ideal / together,
+            "gain_over_one_by_one": alone / together}
 
 
 def cpu_baseline(w, target_s=10.0, threads=None, sample_copies=None, steps_per_call=None):
@@ -488,6 +562,67 @@ def measure_fp32_diagnostics(w, local, evolve_steps=1000):
             "method": "per-chain FFT and mode energies in FP32, sum over chains in FP64"}
 
 
+def measure_reference_gpu(local, engine_kernel_ms, launches=3):
+    """The plain reference GPU path on this GB300: the reference's own integration kernels
+    (move_chain_in_warp<model>, dDNKG::move_chain_in_warp, and DNLS's evolve_* kernels with cuFFT),
+    compiled unmodified for sm_103a from its sources (oracle/_ref/ref_gpu_n<N>.fatbin), on each
+    workload's full ensemble; `launches` launches of kernel_batching steps timed with CUDA events on
+    the launching stream after one warm-up launch.  The reference's per-process copy count is 16-bit
+    (common/configuration.hpp:24), so 65536 copies run as two launches of 32768, as two of its MPI
+    ranks would.  engine_kernel_ms: the engine's integrator time per launch of the same workload."""
+    import torch
+
+    import oracle as O
+    out = {}
+    for w in (WORKLOAD, TODA, OTHERS[0], OTHERS[2], OTHERS[1]):
+        key = w["model"]
+        n_opt = 64 if w["model"] == "DNLS" else w["n"]
+        if not O.RefGPU.available(n_opt):
+            out[key] = {"unavailable": f"oracle/_ref/ref_gpu_n{n_opt}.fatbin was not built from the reference's sources"}
+            continue
+        n, copies, b = w["n"], w["copies"], w["batching"]
+        ref = O.RefGPU(n_opt)
+        state = torch.from_numpy(initial_state(w, copies, 0)).cuda()
+        stream = torch.cuda.current_stream()
+        sp = stream.cuda_stream
+        chunk = 32768
+        parts = [(c0, min(chunk, copies - c0)) for c0 in range(0, copies, chunk)]
+        mp2 = None
+        if w["model"] == "dDNKG":
+            mp2 = torch.from_numpy(masses(w) + 2).cuda()
+        mdl0 = O.Model(w["model"], n, parts[0][1], w["dt"], masses=masses(w), **w["params"])
+
+        def launch_all():
+            for c0, cn in parts:
+                ptr = state.data_ptr() + c0 * n * 16
+                if w["model"] == "DNLS":
+                    ref.dnls_advance(O.Model("DNLS", n, cn, w["dt"], **w["params"]), ptr, b, b, sp, sync=False)
+                else:
+                    ref.move_warp_async(mdl0.model, ptr, n, cn, b, 1, mp2.data_ptr() if mp2 is not None else None, sp)
+
+        if w["model"] != "DNLS":
+            ref.advance(mdl0, state.data_ptr(), 0, b, stream=sp)   # the constants, no steps
+        launch_all()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(launches):
+            launch_all()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / launches
+        ref.close()
+        eng_ms = engine_kernel_ms.get(key)
+        out[key] = {"workload": w["name"], "value": float(n) * copies * b / (ms * 1e-3), "unit": "site-steps/s",
+                    "kernel_ms_per_launch": ms, "steps_per_launch": b,
+                    "launches_per_step": len(parts) * (14 * b + b + 1 if w["model"] == "DNLS" else 1),
+                    "kernel": ("DNLS evolve_nonlinear/evolve_linear + cuFFT Z2Z (no callbacks)" if w["model"] == "DNLS"
+                               else ("dDNKG::" if w["model"] == "dDNKG" else "DNKG_FPUT_Toda::") +
+                               f"move_chain_in_warp, optimized_chain_length={n}"),
+                    "engine_kernel_ms_per_launch": eng_ms, "engine_speedup": (ms / eng_ms) if eng_ms else None}
+    return out
+
+
 def read_traffic(kernel_key):
     """DRAM bytes per launch from the committed ncu summary (profiles/traffic.tsv), or None."""
     path = os.path.join(ROOT, "profiles", "traffic.tsv")
@@ -567,8 +702,16 @@ def run_engine(args):
                  "shape": toda["shape"]},
         "other_workloads": others,
     }
+    if rank == 0:
+        out["plain_reference_gpu"] = measure_reference_gpu(
+            local, {"DNKG": r["move_ms"], "Toda": toda["move_ms"],
+                    **{k: v["kernel_ms"] for k, v in others.items()}})
     if world == 1:
-        out["served"] = measure_served(local)
+        out["served"] = measure_served(local, SERVED_FULL)
+        out["served_small"] = measure_served(local, SERVED_SMALL)
+        out["mixed_models"] = measure_mixed_concurrency(
+            local, {"DNKG": r["value"], "Toda": toda["value"], "FPUT": others["FPUT"]["value"],
+                    "dDNKG": others["dDNKG"]["value"]})
     if rank == 0 and world == 1:
         out["cpu_baseline"] = cpu_baseline(w)
     if rank == 0:

@@ -151,16 +151,17 @@ int nlc_linenergies(nlc_plan *plan, const void *state_dev, double *lin_dev, doub
 
 /*
  * Allocation-free variant of nlc_linenergies, for callers that cannot allocate device memory when
- * they need the diagnostics: a thread recording a CUDA graph (cudaMalloc is refused during stream
- * capture), an application whose device memory is owned by its own pool or framework allocator,
- * or a service that reserves all memory at start-up.  No counterpart in the reference (which
- * allocates its FFT buffers, plans and work areas up front).
+ * they need the diagnostics: an application whose device memory is owned by its own pool or
+ * framework allocator, or a service that reserves all memory at start-up.  No counterpart in the
+ * reference (which allocates its FFT buffers, plans and work areas up front).
  *
  * Inputs and outputs are the caller's: state_dev (reference layout), an optional device mask of
  * chain_length bytes (NULL = all modes; it must select at least two modes), lin_dev[chain_length]
  * and entropies_dev[2] (may be NULL), all device memory, ordered on `stream`.  Models DNKG (m is
  * its -m), FPUT, Toda (m ignored) and DNLS; chain_length <= 4096, larger sizes are rejected with
- * NLC_EINVAL.  Nothing is allocated: every temporary lives in one 4 MiB static device array that
+ * NLC_EINVAL; lengths with a prime factor above 61 are rejected with NLC_EUNSUPPORTED (the
+ * transform of such a length needs padded-length tables that the static array does not hold; the
+ * regular nlc_linenergies handles every length).  Nothing is allocated: every temporary lives in one 4 MiB static device array that
  * each GPU loading the library holds until exit.  The first call on a device looks up that array's
  * device address and sets kernel attributes, so make the first call before any stream capture.
  * All calls share the array: calls that overlap on the GPU race and must be ordered by the caller.
@@ -198,9 +199,9 @@ int nlc_plan_omegas(const nlc_plan *plan, double *omegas);
  * column-major with eigenvector k in column k: the `-omegas` and `-eigenvectors` files of
  * eigensystem.cpp:23-29.  Replaces eigensystem.cpp:13-36 (Armadillo eig_sym) for callers that
  * keep their own plan.  device >= 0 lets cuSOLVER's divide and conquer run on that CUDA device
- * from 256 sites; device < 0, shorter chains, or no usable GPU solver: the host solver (divide
- * and conquer from 64 sites, dense Householder + QR below), the faster one below about 4096 sites
- * on a GB300 host.  Synchronous.
+ * from 4096 sites (or from NLC_DEVICE_EIGEN_FROM sites, the threshold plans use too); device < 0,
+ * shorter chains, or no usable GPU solver: the host solver (divide and conquer from 64 sites, dense
+ * Householder + QR below), the faster one below about 4096 sites on a GB300 host.  Synchronous.
  */
 int nlc_eigensystem(uint32_t chain_length, const double *masses, int32_t device, double *omegas,
                     double *eigenvectors);

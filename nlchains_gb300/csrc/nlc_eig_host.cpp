@@ -416,7 +416,10 @@ bool rank_one_update(std::vector<double> &w, std::vector<double> &V, const std::
 					f += v, fp += v * q, fabs_sum += std::fabs(v);
 				}
 				// f is zero within its own rounding error (its terms can be large and cancel)
-				if (std::fabs(f) <= 16. * kEps * fabs_sum) break;
+				if (std::fabs(f) <= 16. * kEps * fabs_sum) {
+					done = true;
+					break;
+				}
 				if (f > 0.)
 					hi = t;
 				else
@@ -426,8 +429,9 @@ bool rank_one_update(std::vector<double> &w, std::vector<double> &V, const std::
 				done = std::fabs(tn - t) <= 2. * kEps * std::fabs(tn) ||
 				       hi - lo <= 2. * kEps * std::max(std::fabs(lo), std::fabs(hi));
 				t = tn;
-				if (it == 399) found[j] = 0;
 			}
+			// a root that converged on the last iteration counts; only an exhausted search fails
+			if (!done) found[j] = 0;
 			org[j] = o, tau[j] = t;
 		}
 	});

@@ -139,6 +139,10 @@ bool plan_info(const nlc_plan *plan, PlanInfo *info);
 void plan_destroy_ordered(nlc_plan *plan, cudaStream_t stream);
 // nlc_move of one segment of a round (seg: NLC_SEG_* flags)
 int move_segment(nlc_plan *plan, void *state, uint32_t steps, uint32_t seg, cudaStream_t stream);
+// `rounds` consecutive nlc_move launches of round_steps steps each (no sample in between), with up
+// to rounds_per_launch of them fused into one launch: bit-identical to one launch per round
+int move_rounds(nlc_plan *plan, void *state, uint64_t rounds, uint32_t round_steps, cudaStream_t stream);
+uint32_t rounds_per_launch(const nlc_plan *plan, uint32_t round_steps);
 // NLC_ETIMEDOUT (and the flag cleared) when a bounded wait of the plan's tensor-core projection ran
 // out since the last call, else NLC_OK; synchronous.  Asked only when a sample is not finite.
 int plan_device_status(nlc_plan *plan);

@@ -83,6 +83,10 @@ struct RealArgs {
 	int32_t nbatch;
 	unsigned long long batch_units;
 	uint32_t seg;          // NLC_SEG_* of an unbatched launch (batched: per table entry)
+	// rounds fused into one launch (unbatched, unwindowed launches): with round_steps set, the launch
+	// is steps / round_steps rounds of round_steps steps, each closed by its own final drift and the
+	// next opened by an unmerged leading drift -- the operations of one launch per round
+	uint32_t round_steps;
 	// windowed tier (chains longer than one block's registers hold): when win_len is set, each unit
 	// is one window of win_len = G E consecutive sites (mod n) of one chain, integrated as a ring;
 	// the sites that the wrong ring closure can reach, win_halo = 7 x steps at each end, are

@@ -144,11 +144,9 @@ extern "C" int nlc_job_advance(nlc_ctx *ctx, uint64_t id, uint64_t steps) {
 	Job *J = find_job(ctx, id);
 	if (!J) return set_error(NLC_ENOTFOUND, "no such job");
 	if (steps % J->batching) return set_error(NLC_EINVAL, "--steps must be a multiple of --kernel_batching");
-	for (uint64_t t = 0; t < steps; t += J->batching) {
-		const int rc = nlc_move(J->plan, J->d_state, J->batching, J->stream);
-		if (rc) return rc;
-	}
-	return NLC_OK;
+	// one round of kernel_batching steps per reference launch; rounds with no sample in between may
+	// share a launch (move_rounds: the same operations, fewer launches for small ensembles)
+	return move_rounds(J->plan, J->d_state, steps / J->batching, J->batching, J->stream);
 }
 
 extern "C" int nlc_job_linenergies(nlc_ctx *ctx, uint64_t id, double *lin, double *wt, double *inf) {

@@ -1,11 +1,15 @@
 // nlc_linenergies_noalloc: the linear-mode energy diagnostics without any device allocation.
 //
 // Who needs it: code that may not allocate device memory at the moment it wants the diagnostics.
-// Typical cases are a host thread that is recording a CUDA graph (cudaMalloc is not allowed while
-// a stream is being captured), an application whose device memory belongs to its own pool or
-// framework allocator and must not be fragmented by a library, and long-running services that
-// reserve all their memory at start-up and treat any later allocation as a failure.  The regular
+// Typical cases are an application whose device memory belongs to its own pool or framework
+// allocator and must not be fragmented by a library, and long-running services that reserve all
+// their memory at start-up and treat any later allocation as a failure.  The regular
 // nlc_linenergies needs a plan, and creating a plan allocates tables and reduction rows.
+//
+// Limits: chains of at most 4096 sites, and only lengths whose prime factors are all at most 61.
+// The static array has no room for the padded-length (Bluestein) tables that nlc_linenergies uses
+// for a large prime factor, and without them a prime p is one direct p-point DFT per chain done by
+// a single thread (p^2 complex products), which for p near 4096 would take seconds per call.
 //
 // How: every temporary (twiddles, per-mode coefficients, the per-team partial rows of the copy sum)
 // lives in one file-scope device array of kNoAllocScratchBytes (4 MiB), which every GPU that loads
@@ -29,6 +33,7 @@ namespace {
 constexpr size_t kNoAllocScratchBytes = size_t(4) << 20;
 constexpr size_t kNoAllocScratchDoubles = kNoAllocScratchBytes / sizeof(double);
 constexpr uint32_t kNoAllocMaxChain = 4096;
+constexpr int kNoAllocMaxPrime = 61;   // largest prime factor a chain length may have
 constexpr int kMaxDevices = 64;
 
 static __device__ __align__(256) double g_noalloc_scratch[kNoAllocScratchDoubles];
@@ -141,18 +146,23 @@ extern "C" int nlc_linenergies_noalloc(int32_t model, uint32_t chain_length, uin
 	if (chain_length > kNoAllocMaxChain)
 		return set_error(NLC_EINVAL, "nlc_linenergies_noalloc: chain_length above 4096 does not fit the 4 MiB "
 		                             "static scratch; use nlc_plan_create + nlc_linenergies");
-	int dev = 0;
-	int rc = cuda_status(cudaGetDevice(&dev), "cudaGetDevice");
-	if (rc) return rc;
-	DeviceSetup *S = nullptr;
-	if ((rc = setup_device(dev, &S))) return rc;
-
 	const uint32_t n = chain_length;
 	DiagArgs g{};
 	g.n = n, g.copies = copies, g.model = model;
 	g.fft.n = int(n);
 	g.fft.len = int(n);   // direct passes only: the static scratch holds no Bluestein tables
 	if (fill_radices(n, g.fft)) return set_error(NLC_EINVAL, "nlc_linenergies_noalloc: too many prime factors");
+	for (int r = 0; r < g.fft.nradix; r++)
+		if (g.fft.radix[r] > kNoAllocMaxPrime)
+			return set_error(NLC_EUNSUPPORTED, "nlc_linenergies_noalloc: chain_length has a prime factor above 61 "
+			                                   "(a direct transform of that length is too slow without the padded-"
+			                                   "length tables); use nlc_plan_create + nlc_linenergies");
+	int dev = 0;
+	int rc = cuda_status(cudaGetDevice(&dev), "cudaGetDevice");
+	if (rc) return rc;
+	DeviceSetup *S = nullptr;
+	if ((rc = setup_device(dev, &S))) return rc;
+
 	// offsets of the FMA-form twiddle entries: Ns entries for each radix-2/3/4 pass after Ns > 1
 	// points, at most 3 n double2s in all (the Ns of the passes sum to less than n)
 	{

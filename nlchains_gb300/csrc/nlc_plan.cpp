@@ -1,7 +1,9 @@
 // Level-1 operators: plans, the integrator launch shape (with its autotuner), nlc_move,
 // nlc_linenergies and the DNLS elementwise operators.
 #include <algorithm>
+#include <chrono>
 #include <cmath>
+#include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <map>
@@ -10,6 +12,7 @@
 #include <tuple>
 
 #include <cuda.h>
+#include <sys/stat.h>
 
 #include "nlc_host.h"
 
@@ -132,6 +135,7 @@ struct nlc_plan {
 	double2 *d_win = nullptr;              // windowed tier: the second state buffer
 	double block_ops = 0;      // FP64 work of one block's step over the sustained fraction of peak
 	int per_sm = 1, block_warps = 1;   // resident blocks per SM, warps per block of the move kernel
+	double step_us = 0;        // measured time of one step of the whole ensemble (autotuner), 0 = not timed
 
 	// Device memory comes from the stream-ordered allocator, so that creating and destroying plans
 	// (the request server does it per request) never synchronises the whole device.
@@ -157,6 +161,16 @@ struct nlc_plan {
 		return cuda_status(cudaMemcpy(*p, host, count * sizeof(T), cudaMemcpyHostToDevice), "cudaMemcpy");
 	}
 };
+
+// The chain length from which the dDNKG eigensystem goes to cuSOLVER's divide and conquer on the
+// device: the host's divide and conquer is faster below 4096 sites (on the 16 Grace cores of a GB300
+// host 3.3 ms at 256 sites, 24 ms at 1024 and 60 ms at 2048, against 16-108 ms for syevd, seconds
+// on a process's first call); above, the host's n^3 grows past it.  NLC_DEVICE_EIGEN_FROM moves the
+// threshold for plans and nlc_eigensystem alike.
+static uint32_t device_eigen_from() {
+	if (const char *e = std::getenv("NLC_DEVICE_EIGEN_FROM"); e && std::atoi(e) > 0) return uint32_t(std::atoi(e));
+	return 4096;
+}
 
 namespace {
 
@@ -242,27 +256,108 @@ RealShape heuristic_shape(const nlc_plan &P, int model, int variant) {
 	return best;
 }
 
+// Autotuned launch shapes are kept per (device name, model, variant, chain length, copies bucket):
+// in the process, and in a tab-separated file so that later processes skip the timing.  The copies
+// bucket is floor(log2(copies)): ensembles within a factor of two share a shape.  File:
+// $NLC_TUNE_CACHE, else $XDG_CACHE_HOME/nlchains_gb300/shapes.tsv, else
+// $HOME/.cache/nlchains_gb300/shapes.tsv; NLC_TUNE_CACHE=off keeps the cache in memory only.  A
+// line is "device<TAB>model<TAB>variant<TAB>n<TAB>bucket<TAB>lanes<TAB>sites<TAB>threads"; lines
+// that do not parse or name a shape this build cannot launch are ignored.  A ninth field, the
+// measured time of one step of an ensemble of the bucket, feeds the choice of rounds per launch.
 struct TuneKey {
-	int device, model, variant;
-	uint32_t n, copies;
+	std::string device;
+	int model, variant;
+	uint32_t n, bucket;
 	bool operator<(const TuneKey &o) const {
-		return std::tie(device, model, variant, n, copies) < std::tie(o.device, o.model, o.variant, o.n, o.copies);
+		return std::tie(device, model, variant, n, bucket) < std::tie(o.device, o.model, o.variant, o.n, o.bucket);
 	}
 };
+struct TunedShape {
+	int lanes, sites, threads;
+	double step_us;   // one step of the whole ensemble in the timed shape (0: not recorded)
+};
 std::mutex g_tune_mutex;
-std::map<TuneKey, RealShape> g_tune_cache;
+std::map<TuneKey, TunedShape> g_tune_cache;
+bool g_tune_file_read = false;
+
+uint32_t copies_bucket(uint32_t copies) {
+	uint32_t b = 0;
+	while ((copies >> (b + 1)) != 0) b++;
+	return b;
+}
+
+std::string tune_cache_path() {
+	if (const char *e = std::getenv("NLC_TUNE_CACHE")) return std::strcmp(e, "off") ? std::string(e) : std::string();
+	if (const char *x = std::getenv("XDG_CACHE_HOME"); x && *x) return std::string(x) + "/nlchains_gb300/shapes.tsv";
+	if (const char *h = std::getenv("HOME"); h && *h) return std::string(h) + "/.cache/nlchains_gb300/shapes.tsv";
+	return std::string();
+}
+
+// caller holds g_tune_mutex
+void tune_cache_load() {
+	if (g_tune_file_read) return;
+	g_tune_file_read = true;
+	const std::string path = tune_cache_path();
+	if (path.empty()) return;
+	FILE *f = std::fopen(path.c_str(), "r");
+	if (!f) return;
+	char line[512];
+	while (std::fgets(line, sizeof line, f)) {
+		char dev[256];
+		int model, variant, lanes, sites, threads;
+		unsigned n, bucket;
+		double step_us = 0;
+		const int got = std::sscanf(line, "%255[^\t]\t%d\t%d\t%u\t%u\t%d\t%d\t%d\t%lf", dev, &model, &variant, &n,
+		                            &bucket, &lanes, &sites, &threads, &step_us);
+		if (got == 8 || got == 9)
+			g_tune_cache[TuneKey{dev, model, variant, n, bucket}] = TunedShape{lanes, sites, threads, got == 9 ? step_us : 0};
+	}
+	std::fclose(f);
+}
+
+// caller holds g_tune_mutex; a failure to write only loses the entry for later processes
+void tune_cache_append(const TuneKey &k, const TunedShape &t) {
+	const std::string path = tune_cache_path();
+	if (path.empty()) return;
+	for (size_t i = path.find('/', 1); i != std::string::npos; i = path.find('/', i + 1))
+		mkdir(path.substr(0, i).c_str(), 0755);
+	if (FILE *f = std::fopen(path.c_str(), "a")) {
+		std::fprintf(f, "%s\t%d\t%d\t%u\t%u\t%d\t%d\t%d\t%.6g\n", k.device.c_str(), k.model, k.variant, k.n, k.bucket,
+		             t.lanes, t.sites, t.threads, t.step_us);
+		std::fclose(f);
+	}
+}
+
+// Ensembles below this many sites are not timed: every shape then finishes in a few microseconds,
+// so launch overhead decides any ranking, and timing all candidates would cost more GPU time than
+// the work itself (a 64-site, 96-copy ensemble spent ~160 ms in 82 tuning launches).
+constexpr double kTuneMinSites = 65536;
+// Wall-clock budget of one tuning run; candidates after it are skipped, the best so far is kept.
+constexpr double kTuneBudgetMs = 150;
 
 // Time every launchable (G, threads) shape on a zero ensemble for a few steps (best of three
-// launches after a warm-up one); keep the fastest.
-// Results are cached per (device, model, variant, n, copies) for the life of the process.
+// launches after a warm-up one); keep the fastest.  Small ensembles take the heuristic shape.
 RealShape autotune_shape(nlc_plan &P, int model, int variant) {
-	const TuneKey key{P.device, model, variant, P.m.chain_length, P.m.copies};
+	const TuneKey key{P.prop.name, model, variant, P.m.chain_length, copies_bucket(P.m.copies)};
 	{
 		std::lock_guard<std::mutex> lk(g_tune_mutex);
+		tune_cache_load();
 		auto it = g_tune_cache.find(key);
-		if (it != g_tune_cache.end()) return it->second;
+		if (it != g_tune_cache.end()) {
+			RealShape s{};
+			s.lanes = it->second.lanes, s.sites = it->second.sites;
+			if (s.lanes > 0 && (s.lanes & (s.lanes - 1)) == 0 && finish_shape(P, model, variant, s, it->second.threads) &&
+			    s.threads == std::max(std::max(it->second.threads, 32), s.lanes)) {
+				// the bucket's step time, scaled to this ensemble's copies
+				const double bucket_copies = double(1ull << key.bucket);
+				P.step_us = it->second.step_us * std::max(1., double(P.m.copies) / bucket_copies);
+				return s;
+			}
+		}
 	}
 	RealShape fallback = heuristic_shape(P, model, variant);
+	const double sites = double(P.m.chain_length) * double(P.m.copies);
+	if (sites < kTuneMinSites) return fallback;
 	const size_t bytes = size_t(P.m.chain_length) * P.m.copies * sizeof(double2);
 	double *scratch = nullptr;
 	if (!fallback.blocks || cudaMalloc(&scratch, bytes) != cudaSuccess) {
@@ -278,38 +373,52 @@ RealShape autotune_shape(nlc_plan &P, int model, int variant) {
 	RealArgs a = P.ra;
 	// about 2e7 site-steps per timed launch (2 .. 100 steps): small ensembles would otherwise time
 	// launches of a few microseconds, where the launch itself decides the ranking
-	const double sites = double(P.m.chain_length) * double(P.m.copies);
 	a.steps = uint32_t(std::max(2., std::min(100., std::ceil(2e7 / sites))));
 	RealShape best = fallback;
 	float best_ms = 1e30f;
-	for (auto c : shape_candidates(P.m.chain_length)) {
+	const auto t_start = std::chrono::steady_clock::now();
+	// the heuristic's own shape first, so that a budget cut still compares against it
+	std::vector<std::pair<std::pair<int, int>, int>> order;
+	order.push_back({{fallback.lanes, fallback.sites}, fallback.threads});
+	for (auto c : shape_candidates(P.m.chain_length))
 		for (int tpb : {32, 64, 128, 256, 512}) {
 			if (c.first > 32 && tpb != 32) continue;   // block shape fixed by G for multi-warp chains
-			RealShape s{};
-			s.lanes = c.first, s.sites = c.second;
-			if (!finish_shape(P, model, variant, s, tpb)) continue;
-			if (c.first <= 32 && s.threads != std::max(tpb, s.lanes)) continue;
-			float ms = 1e30f;
-			bool ok = true;
-			for (int rep = 0; rep < 4 && ok; rep++) {
-				cudaEventRecord(e0, st);
-				ok = launch_real_move(model, variant, s, scratch, a, st) == cudaSuccess;
-				cudaEventRecord(e1, st);
-				if (cudaEventSynchronize(e1) != cudaSuccess) ok = false;
-				float t = 0;
-				cudaEventElapsedTime(&t, e0, e1);
-				if (rep) ms = std::min(ms, t);
-			}
-			if (ok && ms < best_ms) best_ms = ms, best = s;
+			if (c.first == fallback.lanes && std::max(tpb, c.first) == fallback.threads) continue;
+			order.push_back({c, tpb});
 		}
+	for (auto &cand : order) {
+		if (best_ms < 1e30f &&
+		    std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_start).count() > kTuneBudgetMs)
+			break;
+		RealShape s{};
+		s.lanes = cand.first.first, s.sites = cand.first.second;
+		const int tpb = cand.second;
+		if (!finish_shape(P, model, variant, s, tpb)) continue;
+		if (s.lanes <= 32 && s.threads != std::max(tpb, s.lanes)) continue;
+		float ms = 1e30f;
+		bool ok = true;
+		for (int rep = 0; rep < 4 && ok; rep++) {
+			cudaEventRecord(e0, st);
+			ok = launch_real_move(model, variant, s, scratch, a, st) == cudaSuccess;
+			cudaEventRecord(e1, st);
+			if (cudaEventSynchronize(e1) != cudaSuccess) ok = false;
+			float t = 0;
+			cudaEventElapsedTime(&t, e0, e1);
+			if (rep) ms = std::min(ms, t);
+		}
+		if (ok && ms < best_ms) best_ms = ms, best = s;
 	}
 	cudaGetLastError();
 	cudaEventDestroy(e0);
 	cudaEventDestroy(e1);
 	cudaStreamDestroy(st);
 	cudaFree(scratch);
+	if (best_ms < 1e30f) P.step_us = 1e3 * double(best_ms) / a.steps;
 	std::lock_guard<std::mutex> lk(g_tune_mutex);
-	g_tune_cache[key] = best;
+	const TunedShape t{best.lanes, best.sites, best.threads,
+	                   P.step_us * double(1ull << key.bucket) / std::max(1., double(P.m.copies))};
+	if (!g_tune_cache.count(key)) tune_cache_append(key, t);
+	g_tune_cache[key] = t;
 	return best;
 }
 
@@ -646,13 +755,7 @@ extern "C" int nlc_plan_create(const nlc_model *model, nlc_plan **out) {
 	if (mdl == NLC_DDNKG) {
 		P->mp2_host.resize(n);
 		for (uint32_t i = 0; i < n; i++) P->mp2_host[i] = model->masses[i] + 2;
-		// the host's divide and conquer below 4096 sites: on the 16 Grace cores of a GB300 host it takes
-		// 3.3 ms at 256 sites, 24 ms at 1024 and 60 ms at 2048, against 16-108 ms for cuSOLVER's
-		// syevd (seconds on a process's first call); the GPU solver from 4096 sites, where the host's
-		// n^3 grows past it, or from NLC_DEVICE_EIGEN_FROM sites
-		uint32_t device_from = 4096;
-		if (const char *e = std::getenv("NLC_DEVICE_EIGEN_FROM"); e && std::atoi(e) > 0) device_from = uint32_t(std::atoi(e));
-		const bool device = n >= device_from && eigensystem_periodic_device(P->mp2_host, P->omega_host, P->eig_host);
+		const bool device = n >= device_eigen_from() && eigensystem_periodic_device(P->mp2_host, P->omega_host, P->eig_host);
 		if (!device && !eigensystem_periodic(P->mp2_host, P->omega_host, P->eig_host))
 			return set_error(NLC_EINVAL, "Cannot calculate eigensystem!");
 		P->norm = 0.5 / model->copies;   // dDNKG.cpp:141
@@ -892,7 +995,7 @@ extern "C" int nlc_eigensystem(uint32_t n, const double *masses, int32_t device,
 	for (uint32_t i = 0; i < n; i++) mp2[i] = masses[i] + 2;
 	bool done = false;
 	int count = 0;
-	if (device >= 0 && n >= 256 && cudaGetDeviceCount(&count) == cudaSuccess && device < count) {
+	if (device >= 0 && n >= device_eigen_from() && cudaGetDeviceCount(&count) == cudaSuccess && device < count) {
 		DeviceScope scope(device);
 		done = eigensystem_periodic_device(mp2, om, ev);
 	}
@@ -975,6 +1078,47 @@ extern "C" int nlc_move(nlc_plan *P, void *state, uint32_t steps, void *stream) 
 	DeviceScope ds(P ? P->device : -1);
 	NvtxRange r("nlc_move");
 	return nlc::move_segment(P, state, steps, 0, static_cast<cudaStream_t>(stream));
+}
+
+// Rounds fused into one launch: enough that a launch lasts ~200 us (the launch and its gaps then
+// cost ~2% or less), at most ~20 ms of work and 1024 rounds.  The per-step time is the autotuner's
+// measurement (or the cached one), else the plan's FP64 cost model.
+uint32_t nlc::rounds_per_launch(const nlc_plan *P, uint32_t round_steps) {
+	if (!P || P->m.model == NLC_DNLS || P->win_len || !round_steps) return 1;
+	double step_us = P->step_us;
+	if (!(step_us > 0)) {
+		const unsigned long long gpb = std::max(1, P->rs.threads / std::max(P->rs.lanes, 1));
+		const double blocks = double((P->m.copies + gpb - 1) / gpb);
+		const double waves = std::ceil(blocks / std::max(1.0, double(P->per_sm) * P->prop.multiProcessorCount));
+		step_us = waves * P->block_ops / 3950.;   // ~3950 FP64 lane operations per SM and microsecond
+	}
+	const double round_us = std::max(step_us * round_steps, 1e-3);
+	double r = std::ceil(200. / round_us);
+	r = std::min(r, std::max(1., std::floor(2e4 / round_us)));
+	r = std::min(r, std::min(1024., std::floor(4e9 / round_steps)));
+	return uint32_t(std::max(1., r));
+}
+
+int nlc::move_rounds(nlc_plan *P, void *state, uint64_t rounds, uint32_t round_steps, cudaStream_t st) {
+	if (!P || !state) return set_error(NLC_EINVAL, "NULL argument");
+	const uint32_t per = rounds_per_launch(P, round_steps);
+	for (uint64_t done = 0; done < rounds;) {
+		const uint32_t r = uint32_t(std::min<uint64_t>(per, rounds - done));
+		int rc;
+		if (r == 1) {
+			rc = move_segment(P, state, round_steps, 0, st);
+		} else {
+			RealArgs a = P->ra;
+			a.steps = r * round_steps;
+			a.round_steps = round_steps;
+			a.seg = 0;
+			rc = cuda_status(launch_real_move(P->m.model, P->variant, P->rs, static_cast<double *>(state), a, st),
+			                 "move launch (fused rounds)");
+		}
+		if (rc) return rc;
+		done += r;
+	}
+	return NLC_OK;
 }
 
 int nlc::move_segment(nlc_plan *P, void *state, uint32_t steps, uint32_t seg, cudaStream_t st) {

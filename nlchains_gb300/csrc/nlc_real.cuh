@@ -214,11 +214,21 @@ __global__ void real_move_kernel_t(double2 *__restrict__ state, const RealArgs a
 		const double cd_lead = (seg & NLC_SEG_CONTINUE) ? a.cd0_merged : a.cd[0];
 		auto integrate = [&](auto shfl_tag) {
 		constexpr bool SHFL = decltype(shfl_tag)::value;
+		uint32_t rpos = 0;   // steps of the current round done (fused rounds, a.round_steps)
 		for (uint32_t i = 0; i < steps; i++) {
+			// a round boundary inside the launch: the closing drift of the round just done, then the
+			// next round's leading drift unmerged, as between two launches
+			const bool boundary = a.round_steps && rpos == a.round_steps;
+			if (boundary) {
+				rpos = 0;
+#pragma unroll
+				for (int j = 0; j < E; j++) x[j + 1] = dfma(a.cd_final, p[j], x[j + 1]);
+			}
+			rpos++;
 #pragma unroll
 			for (int k = 0; k < 7; k++) {
 				// the trailing drift of step i-1 (c[7]) merged with the leading drift of step i (c[0])
-				const double cd = k == 0 ? (i != 0 ? a.cd0_merged : cd_lead) : a.cd[k];
+				const double cd = k == 0 ? (i == 0 ? cd_lead : boundary ? a.cd[0] : a.cd0_merged) : a.cd[k];
 #pragma unroll
 				for (int j = 0; j < E; j++) x[j + 1] = dfma(cd, p[j], x[j + 1]);
 

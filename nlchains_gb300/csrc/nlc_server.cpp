@@ -5,7 +5,9 @@
 //     per work unit; for dDNKG the host eigensolve) and allocate and upload its state, each on its own
 //     high-priority stream; the t = 0 samples of newly prepared requests then go out as one group;
 //   * the scheduler thread groups idle prepared requests by kernel class (model, parameters, dt,
-//     launch shape) and launches each group on a free stream slot: one batched launch of the
+//     launch shape) and launches each group, shortest remaining work first, on a free stream slot
+//     of the group's priority band (four bands of stream priority: the GPU dispatches blocks of
+//     nearly finished and short requests ahead of long ones): one batched launch of the
 //     resident integrator advancing every member by its next segment (DNLS and windowed requests run
 //     their own launches), then the diagnostics sample of every member whose round the segment
 //     closes, then an event;
@@ -125,6 +127,7 @@ struct nlc_server {
 	cudaStream_t free_stream = nullptr;   // final read-backs and frees only: never holds queued kernels
 	double quantum_us = 3000;
 	std::vector<cudaStream_t> streams;
+	std::vector<int> slot_band;   // priority band of each stream slot, 0 = the highest stream priority
 	std::vector<cudaEvent_t> events;
 	// per stream slot: the launch group on the GPU, its device job table and pinned staging
 	std::vector<std::vector<Request *>> slot_reqs;
@@ -275,6 +278,24 @@ uint32_t segment_steps(const nlc_server *S, const Request &R, unsigned long long
 	const uint32_t cap = uint32_t(std::max(1., std::floor(S->quantum_us / est)));
 	const uint32_t parts = (left + cap - 1) / cap;
 	return (left + parts - 1) / parts;
+}
+
+// Estimated GPU time of a request's remaining steps with the whole GPU to itself: FP64 work of a
+// block's step times the blocks of one step, at ~3950 FP64 lane operations per SM and microsecond.
+double remaining_us(const Request &R) {
+	if (R.t >= R.steps) return 0.;
+	const double blocks = std::max(R.info.grid, 1);
+	return double(R.steps - R.t) * blocks * R.info.block_ops / (3950. * std::max(R.info.sms, 1));
+}
+
+// Priority band of a launch group from the least remaining work among its members: the GPU's block
+// scheduler dispatches blocks of higher-priority streams first, so requests close to done (or short
+// to begin with) are not held behind long ones -- shortest remaining work first, at block
+// granularity.  Bands: < 20 ms, < 200 ms, < 2 s, longer.
+int priority_band(const std::vector<Request *> &g) {
+	double rem = 1e300;
+	for (const Request *R : g) rem = std::min(rem, remaining_us(*R));
+	return rem < 2e4 ? 0 : rem < 2e5 ? 1 : rem < 2e6 ? 2 : 3;
 }
 
 // Launch the next segment of every request of a group of idle requests of one class (several: one
@@ -478,22 +499,47 @@ void worker_loop(nlc_server *S) {
 		std::vector<std::vector<Request *>> groups;
 		for (auto &kv : classes) groups.push_back(kv.second);
 		for (auto &g : singles) groups.push_back(g);
-		std::stable_sort(groups.begin(), groups.end(),
-		                 [](const std::vector<Request *> &a, const std::vector<Request *> &b) { return a.size() > b.size(); });
+		// shortest remaining work first (ties: larger groups first)
+		std::vector<std::pair<int, double>> urgency(groups.size());
+		for (size_t i = 0; i < groups.size(); i++) {
+			double rem = 1e300;
+			for (const Request *R : groups[i]) rem = std::min(rem, remaining_us(*R));
+			urgency[i] = {priority_band(groups[i]), rem};
+		}
+		std::vector<size_t> order(groups.size());
+		for (size_t i = 0; i < order.size(); i++) order[i] = i;
+		std::stable_sort(order.begin(), order.end(), [&](size_t a, size_t b) {
+			if (urgency[a].second != urgency[b].second) return urgency[a].second < urgency[b].second;
+			return groups[a].size() > groups[b].size();
+		});
+		// a free slot of the wanted band, else of a lower priority, else any free slot
+		auto pick_slot = [&](int band) {
+			long best = -1;
+			for (size_t slot = 0; slot < nslots; slot++) {
+				if (!S->slot_reqs[slot].empty()) continue;
+				const int b = S->slot_band[slot];
+				if (b == band) return long(slot);
+				if (best < 0 || (b > band && (S->slot_band[best] < band || b < S->slot_band[best]))) best = long(slot);
+			}
+			return best;
+		};
 		size_t next = 0;
-		for (size_t slot = 0; slot < nslots && (next < groups.size() || !first_samples.empty()); slot++) {
-			if (!S->slot_reqs[slot].empty()) continue;
+		for (;;) {
+			const bool sample_only = !first_samples.empty();
+			if (!sample_only && next >= groups.size()) break;
+			const long slot_l = pick_slot(sample_only ? 0 : urgency[order[next]].first);
+			if (slot_l < 0) break;
+			const size_t slot = size_t(slot_l);
 			std::vector<Request *> g;
 			int rc = NLC_OK;
 			// the t = 0 samples of newly prepared requests go first, all in one group
-			const bool sample_only = !first_samples.empty();
 			if (sample_only) {
 				g.swap(first_samples);
 				for (Request *R : g)
 					if (!rc) rc = sample(*R, S->streams[slot]);
 				if (!rc) rc = cuda_status(cudaEventRecord(S->events[slot], S->streams[slot]), "cudaEventRecord");
 			} else {
-				g = groups[next++];
+				g = groups[order[next++]];
 				rc = launch_group(S, slot, g);
 			}
 			S->slot_sample_only[slot] = sample_only;
@@ -526,18 +572,23 @@ extern "C" int nlc_server_create(const nlc_server_config *config, nlc_server **o
 		if ((rc = cuda_status(cudaMemGetInfo(&fr, &tot), "cudaMemGetInfo"))) return rc;
 		S->cfg.hbm_budget_bytes = uint64_t(fr * 0.6);
 	}
-	for (int i = 0; i < S->cfg.streams; i++) {
-		cudaStream_t st;
-		cudaEvent_t ev;
-		if ((rc = cuda_status(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking), "cudaStreamCreate"))) return rc;
-		S->streams.push_back(st);
-		if ((rc = cuda_status(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "cudaEventCreate"))) return rc;
-		S->events.push_back(ev);
-	}
 	// request set-up (plan, upload) runs on preparer streams of the highest priority: it gates latency
 	int prio_low = 0, prio_high = 0;
 	cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high);
 	S->prio_high = prio_high;
+	// launch slots in four priority bands (slot i in band i % 4), spread over the device's range
+	for (int i = 0; i < S->cfg.streams; i++) {
+		cudaStream_t st;
+		cudaEvent_t ev;
+		const int band = i % 4;
+		const int prio = prio_high + int(std::lround(band * double(prio_low - prio_high) / 3.));
+		if ((rc = cuda_status(cudaStreamCreateWithPriority(&st, cudaStreamNonBlocking, prio), "cudaStreamCreate")))
+			return rc;
+		S->streams.push_back(st);
+		S->slot_band.push_back(band);
+		if ((rc = cuda_status(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "cudaEventCreate"))) return rc;
+		S->events.push_back(ev);
+	}
 	if ((rc = cuda_status(cudaStreamCreateWithFlags(&S->free_stream, cudaStreamNonBlocking), "cudaStreamCreate")))
 		return rc;
 	// keep the memory returned by cudaFreeAsync cached in the device's pool between requests, and

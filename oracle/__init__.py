@@ -228,9 +228,10 @@ class RefGPU:
             lib.refgpu_kernel_count.argtypes = [vp]
             lib.refgpu_advance.argtypes = [vp, ctypes.c_int, vp, u32, u32, ctypes.c_double, ctypes.c_double,
                                            ctypes.c_double, ctypes.c_double, dp, u64, u32, ctypes.c_int, vp]
-            lib.refgpu_move_warp_async.argtypes = [vp, ctypes.c_int, vp, u32, u32, u32, u32, vp]
+            lib.refgpu_move_warp_async.argtypes = [vp, ctypes.c_int, vp, u32, u32, u32, u32, vp, vp]
             lib.refgpu_linenergies.argtypes = [vp, ctypes.c_int, vp, u32, u32, ctypes.c_double, dp, dp, dp, vp]
-            lib.refgpu_dnls_advance.argtypes = [vp, vp, u32, u32, ctypes.c_double, ctypes.c_double, u64, u32, vp]
+            lib.refgpu_dnls_advance.argtypes = [vp, vp, u32, u32, ctypes.c_double, ctypes.c_double, u64, u32, vp,
+                                                ctypes.c_int]
             cls._host = lib
         return cls._host
 
@@ -271,9 +272,11 @@ class RefGPU:
                                                model.m, model.alpha, model.beta, mp2, steps, batching,
                                                int(force_split), stream))
 
-    def move_warp_async(self, model_id, state_ptr, n, copies, batching, launches=1, stream=0):
+    def move_warp_async(self, model_id, state_ptr, n, copies, batching, launches=1, mp2_ptr=None, stream=0):
+        """Queue `launches` launches of the reference's warp kernel (move_chain_in_warp) on `stream`;
+        constants as the last advance() call set them."""
         self._check(self._lib().refgpu_move_warp_async(self.h, model_id, state_ptr, n, copies, batching, launches,
-                                                       stream))
+                                                       mp2_ptr, stream))
 
     def linenergies(self, model, state_ptr, stream=0):
         out = np.zeros(model.n)
@@ -285,6 +288,6 @@ class RefGPU:
                                                    _dp(om) if om is not None else None, _dp(out), stream))
         return out
 
-    def dnls_advance(self, model, state_ptr, steps, batching, stream=0):
+    def dnls_advance(self, model, state_ptr, steps, batching, stream=0, sync=True):
         self._check(self._lib().refgpu_dnls_advance(self.h, state_ptr, model.n, model.copies, model.dt, model.beta,
-                                                    steps, batching, stream))
+                                                    steps, batching, stream, int(sync)))

@@ -48,6 +48,8 @@ struct refgpu {
 	double c[8], d[8];
 	std::map<std::string, CUfunction> kernels;   /* demangled name without a leading "void " */
 	cublasHandle_t cublas = nullptr;
+	std::map<std::pair<uint32_t, uint32_t>, cufftHandle> dnls_plans;   /* (n, copies): as DNLS.cpp:73-126 keeps them */
+	std::map<std::pair<uint32_t, double>, double2 *> dnls_tables;      /* (n, dt): the 7 linear tables */
 	std::string err;
 };
 
@@ -192,6 +194,8 @@ int refgpu_open(const char *fatbin_path, int n_opt, const double *c, const doubl
 
 void refgpu_close(refgpu *r) {
 	if (!r) return;
+	for (auto &kv: r->dnls_plans) cufftDestroy(kv.second);
+	for (auto &kv: r->dnls_tables) cudaFree(kv.second);
 	if (r->cublas) cublasDestroy(r->cublas);
 	if (r->mod) cuModuleUnload(r->mod);
 	delete r;
@@ -300,20 +304,25 @@ int refgpu_advance(refgpu *r, int model, void *state_dev, uint32_t n, uint32_t c
 
 /* Launch only the integration kernel of a warp-resident real-model ensemble, `launches` times, on
  * `stream` without synchronising (the bench's plain-reference timing; constants as refgpu_advance
- * set them last, sizes as there). */
+ * set them last, sizes as there).  mp2_dev: dDNKG's m_x + 2 in device memory (n values). */
 int refgpu_move_warp_async(refgpu *r, int model, void *state_dev, uint32_t n, uint32_t copies, uint32_t batching,
-                           uint32_t launches, void *stream) {
-	if (model < M_DNKG || model > M_TODA || (int) n != r->n_opt || !check_sizes(r, n, copies))
-		return fail(r, "the warp kernel needs a real model (not dDNKG) at the optimised length");
-	CUfunction k = find_kernel(r, std::string("DNKG_FPUT_Toda::move_chain_in_warp<(DNKG_FPUT_Toda::Model)") +
-	                              std::to_string(model) + ">(");
+                           uint32_t launches, const double *mp2_dev, void *stream) {
+	if (model < M_DNKG || model > M_DDNKG || (int) n != r->n_opt || !check_sizes(r, n, copies) ||
+	    (model == M_DDNKG && !mp2_dev))
+		return fail(r, "the warp kernel needs a real model at the optimised length (dDNKG: with its masses)");
+	CUfunction k = find_kernel(r, model == M_DDNKG ? std::string("dDNKG::move_chain_in_warp(")
+	                                               : std::string("DNKG_FPUT_Toda::move_chain_in_warp<(DNKG_FPUT_Toda::Model)") +
+	                                                 std::to_string(model) + ">(");
 	if (!k) return -1;
 	double2 *planar = (double2 *) state_dev;
 	uint32_t steps_grouping = batching;
 	uint16_t copies16 = (uint16_t) copies;
 	for (uint32_t l = 0; l < launches; l++) {
-		void *args[] = {&planar, &steps_grouping, &copies16};
-		if (!launch(r, k, grid_for(uint64_t(copies) * 32, 256), 256, (cudaStream_t) stream, args)) return -1;
+		void *args_real[] = {&planar, &steps_grouping, &copies16};
+		void *args_dd[] = {&planar, &mp2_dev, &steps_grouping, &copies16};
+		if (!launch(r, k, grid_for(uint64_t(copies) * 32, 256), 256, (cudaStream_t) stream,
+		            model == M_DDNKG ? args_dd : args_real))
+			return -1;
 	}
 	return 0;
 }
@@ -432,31 +441,42 @@ int refgpu_linenergies(refgpu *r, int model, const void *state_dev, uint32_t n, 
 	return 0;
 }
 
-/* Advance a DNLS complex128[copies][n] device ensemble (DNLS.cpp:159-175, no callbacks). */
+/* Advance a DNLS complex128[copies][n] device ensemble (DNLS.cpp:159-175, no callbacks).  The cuFFT
+ * plan and the linear tables are made on first use and kept, as the reference's main keeps them;
+ * sync = 0 returns with the launches queued on `stream`. */
 int refgpu_dnls_advance(refgpu *r, void *state_dev, uint32_t n, uint32_t copies, double dt, double beta, uint64_t steps,
-                        uint32_t batching, void *stream) {
+                        uint32_t batching, void *stream, int sync) {
 	if (!check_sizes(r, n, copies) || !batching || steps % batching) return fail(r, "bad sizes or batching");
 	cudaStream_t s = (cudaStream_t) stream;
-	using namespace std::complex_literals;
-	/* DNLS/dispersion.cpp:10-26 */
-	std::vector<double> omega(n);
-	for (size_t k = 0; k < n; k++) {
-		auto s2 = 2 * sin(k * M_PI / n);
-		omega[k] = s2 * s2;
+	double2 *&table_dev = r->dnls_tables[{n, dt}];
+	if (!table_dev) {
+		using namespace std::complex_literals;
+		/* DNLS/dispersion.cpp:10-26 */
+		std::vector<double> omega(n);
+		for (size_t k = 0; k < n; k++) {
+			auto s2 = 2 * sin(k * M_PI / n);
+			omega[k] = s2 * s2;
+		}
+		std::vector<std::complex<double>> table(size_t(7) * n);
+		auto normalization = 1. / n;
+		std::complex<double> complexdt = -1i * dt;
+		for (size_t i = 0; i < 7; i++)
+			for (size_t j = 0; j < n; j++) table[i * n + j] = exp(complexdt * r->d[i] * omega[j]) * normalization;
+		if (!rt_ok(r, cudaMalloc(&table_dev, sizeof(double2) * table.size()), "cudaMalloc tables") ||
+		    !rt_ok(r, cudaMemcpy(table_dev, table.data(), sizeof(double2) * table.size(), cudaMemcpyHostToDevice),
+		           "tables")) {
+			cudaFree(table_dev);
+			table_dev = nullptr;
+			return -1;
+		}
 	}
-	std::vector<std::complex<double>> table(size_t(7) * n);
-	auto normalization = 1. / n;
-	std::complex<double> complexdt = -1i * dt;
-	for (size_t i = 0; i < 7; i++)
-		for (size_t j = 0; j < n; j++) table[i * n + j] = exp(complexdt * r->d[i] * omega[j]) * normalization;
-	double2 *table_dev = nullptr;
 	int rc = 0;
-	if (!rt_ok(r, cudaMalloc(&table_dev, sizeof(double2) * table.size()), "cudaMalloc tables") ||
-	    !rt_ok(r, cudaMemcpy(table_dev, table.data(), sizeof(double2) * table.size(), cudaMemcpyHostToDevice), "tables"))
-		return -1;
-	cufftHandle plan = 0;
-	if (cufftPlan1d(&plan, (int) n, CUFFT_Z2Z, (int) copies) != CUFFT_SUCCESS || cufftSetStream(plan, s) != CUFFT_SUCCESS)
+	cufftHandle &plan = r->dnls_plans[{n, copies}];
+	if (!plan && cufftPlan1d(&plan, (int) n, CUFFT_Z2Z, (int) copies) != CUFFT_SUCCESS) {
+		plan = 0;
 		rc = fail(r, "cufftPlan1d");
+	}
+	if (!rc && cufftSetStream(plan, s) != CUFFT_SUCCESS) rc = fail(r, "cufftSetStream");
 	CUfunction knl = rc ? nullptr : find_kernel(r, "DNLS::evolve_nonlinear_kernel(");
 	CUfunction kl = rc ? nullptr : find_kernel(r, "DNLS::evolve_linear_kernel(");
 	if (!knl || !kl) rc = -1;
@@ -484,9 +504,8 @@ int refgpu_dnls_advance(refgpu *r, void *state_dev, uint32_t n, uint32_t copies,
 			}
 		if (!rc && !nonlinear(beta * dt * r->c[7])) rc = -1;
 	}
+	if (!sync) return rc;
 	if (!rt_ok(r, cudaStreamSynchronize(s), "reference DNLS")) rc = -1;
-	if (plan) cufftDestroy(plan);
-	cudaFree(table_dev);
 	return rc;
 }
 

@@ -117,6 +117,13 @@ def test_noalloc_rejects_invalid_arguments_before_any_device_call(engine, args, 
     assert needle in engine.last_error()
 
 
+@pytest.mark.parametrize("n", [1021, 4093, 2 * 67, 3 * 1009])
+def test_noalloc_rejects_large_prime_factors_before_any_device_call(engine, n):
+    """A prime factor above 61 would be one thread's direct transform per chain: refused up front."""
+    assert engine.lib().nlc_linenergies_noalloc(0, n, 8, 0.0, 16, None, 16, None, None) == engine.EUNSUPPORTED
+    assert "prime factor above 61" in engine.last_error()
+
+
 def test_host_entropies_error_behaviour(engine):
     lin = np.array([0.0, 1.0, 2.0, 3.0])
     wt, inf = engine.entropies(lin, a0is0=True)

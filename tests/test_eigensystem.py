@@ -136,8 +136,10 @@ def test_host_solver_rejects_bad_arguments(engine):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("n", [256, 300])
-def test_device_solver_equals_host(gpu, n):
-    """device 0 from 256 sites: cuSOLVER's divide and conquer; the same eigensystem as the host's."""
+def test_device_solver_equals_host(gpu, n, monkeypatch):
+    """device 0 with the device threshold moved to 256 sites: cuSOLVER's divide and conquer; the same
+    eigensystem as the host's."""
+    monkeypatch.setenv("NLC_DEVICE_EIGEN_FROM", "256")
     masses = ic.masses_uniform(n, seed=n)
     om_d, vec_d = gpu.eigensystem(masses, device=0)
     om_h, vec_h = gpu.eigensystem(masses, device=-1)

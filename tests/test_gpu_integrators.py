@@ -311,3 +311,35 @@ def test_fput_benchmark_configuration_full_run(gpu):
     assert np.array_equal(job.download().reshape(copies, n, 2), cur.reshape(copies, n, 2))
     job.close()
     ctx.close()
+
+
+@pytest.mark.parametrize("name,n,params,masses_seed", [
+    ("FPUT", 64, dict(alpha=0.0, beta=1.0), None),
+    ("FPUT", 37, dict(alpha=0.3, beta=0.8), None),
+    ("DNKG", 48, dict(m=0.5, beta=1.0), None),
+    ("Toda", 40, dict(alpha=0.5), None),
+    ("dDNKG", 33, dict(beta=1.0), 5),
+])
+def test_fused_rounds_equal_one_launch_per_round(gpu, name, n, params, masses_seed):
+    """Job.advance over several rounds of kernel_batching steps with no sample in between fuses rounds
+    into fewer launches (each round still closed by its own final drift and the next opened unmerged):
+    the result is bit-identical to one launch per round (the oracle's launches of `batching` steps),
+    and for a small ensemble the launch count drops."""
+    copies, b, rounds = 96, 10, 30
+    masses = ic.masses_uniform(n, seed=masses_seed) if masses_seed is not None else None
+    rng = np.random.default_rng(n)
+    state = rng.standard_normal((copies, n, 2)) * 0.3
+    ctx = gpu.Context(0)
+    job = ctx.job(gpu.Model(name, n, copies, 0.05, masses=masses, **params), b)
+    job.upload(state)
+    before = gpu.kernel_launches()
+    job.advance(b * rounds)
+    job.wait()
+    launches = gpu.kernel_launches() - before
+    out = job.download()
+    job.close()
+    ctx.close()
+    mdl = O.Model(name, n, copies, 0.05, masses=masses, **params)
+    exp = O.advance(mdl, state, b * rounds, b, order=O.ORDER_DEVICE).reshape(copies, n, 2)
+    assert np.array_equal(out, exp)
+    assert launches < rounds, f"{launches} launches for {rounds} rounds: no rounds were fused"
