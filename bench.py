@@ -16,8 +16,10 @@ reference's main loop.  Toda (alpha = 0.5) on the same shape is measured as a se
   cpu_baseline  the reference's CPU algorithm (the oracle port of DNKG_FPUT_Toda/cpu-implementation,
           one OpenMP thread per host core over copies) on a bounded sample.
 
-`--impl reference` runs only the reference's CPU implementation (the oracle port; the reference
-itself cannot be built in this image) on the same metric and prints its line.
+`--impl reference` runs only the reference's CPU implementation (the oracle port, bit-identical in its
+strict build to the reference's own CPU program compiled from its sources, which exist only where the
+reference is checked out) on the same metric and prints its line.  `plain_reference_gpu` times the
+reference's own GPU kernels, compiled unmodified for sm_103a, on the same workloads.
 
 Multi-GPU (torchrun): one process per GPU, each integrating its own shard of copies of the same
 size (weak scaling); the only exchange is the reference's all_reduce of the N linear energies per
@@ -367,6 +369,12 @@ def measure_served(local, stream):
     ctx.close()
     alone_s = sum(alone)
     slowdown = np.array(lat) / (np.array(alone) * 1e3)
+    # the plain path as a queue: the same arrivals, each request run alone when the previous is done
+    queue_lat, free_at = [], 0.0
+    for r, al in zip(reqs, alone):
+        start = max(r["arrival_ms"] / 1e3, free_at)
+        free_at = start + al
+        queue_lat.append((free_at - r["arrival_ms"] / 1e3) * 1e3)
     per_model = {}
     for r, lt, al in zip(reqs, lat, alone):
         m = per_model.setdefault(r["name"], {"requests": 0, "site_steps": 0.0, "alone_s": 0.0, "latency_ms": []})
@@ -379,7 +387,9 @@ def measure_served(local, stream):
     return {"value": site_steps / makespan, "unit": "site-steps/s", "alone_value": site_steps / alone_s,
             "speedup_vs_alone": alone_s / makespan, "p50_ms": float(np.percentile(lat, 50)),
             "p99_ms": float(np.percentile(lat, 99)), "slowdown_p50": float(np.percentile(slowdown, 50)),
-            "slowdown_p99": float(np.percentile(slowdown, 99)), "requests": len(reqs), "makespan_s": makespan,
+            "slowdown_p99": float(np.percentile(slowdown, 99)),
+            "alone_queue_p50_ms": float(np.percentile(queue_lat, 50)), "alone_queue_p99_ms": float(np.percentile(queue_lat, 99)),
+            "requests": len(reqs), "makespan_s": makespan,
             "alone_s": alone_s, "largest_request_alone_s": float(max(alone)), "per_model": per_model,
             "stream": f"{stream['count']} requests, model uniform over FPUT/Toda/DNKG/dDNKG/DNLS, N log-uniform "
                       f"{list(stream['n_range'])}, copies log-uniform {list(stream['copies_range'])}, steps log-uniform "
@@ -387,7 +397,9 @@ def measure_served(local, stream):
                       f"Poisson arrivals (mean gap {stream['mean_gap_ms']:g} ms), seed {stream['seed']}",
             "alone": "each request by itself through the job API, batch + sample replayed as one CUDA graph, "
                      "two result slots (no host round trip between batches)",
-            "slowdown": "latency over the request's own alone time"}
+            "slowdown": "latency over the request's own alone time",
+            "alone_queue": "latency percentiles of the plain path run as a first-come-first-served queue on the "
+                           "same arrivals, from the measured alone times"}
 
 
 def measure_mixed_concurrency(local, full_rates, rounds=20):
@@ -660,6 +672,8 @@ def run_engine(args):
                                ow["batching"] / (o["move_ms"] * 1e-3) / (peak * 1e12 / 2)}
         if ow["model"] == "dDNKG" and rank == 0:
             others["dDNKG"]["projection"] = measure_projection(ow, local)
+            others["dDNKG"]["projection_n1024"] = measure_projection(
+                dict(ow, name="dDNKG N=1024 copies=4096", n=1024, nmodes=80), local)
             others["dDNKG"]["eigensystem_setup"] = measure_eigensystem(ow)
         if ow["model"] == "DNLS" and rank == 0:
             others["DNLS"]["fp32_diagnostics"] = measure_fp32_diagnostics(ow, local)
@@ -695,11 +709,14 @@ def run_engine(args):
         "clocks": r["clocks"],
         "energy_drift": r["energy_drift"] if rank == 0 else None,
         "toda": {"value": toda["value"], "unit": "site-steps/s", "workload": TODA["name"],
-                 "roofline_frac": FLOPS_PER_SITE_STEP["Toda"] * TODA["n"] * TODA["copies"] * TODA["batching"] /
-                 (toda["move_ms"] * 1e-3) / 1e12 / peak,
-                 "fp64_issue_frac": FP64_OPS_PER_SITE_STEP["Toda"] * TODA["n"] * TODA["copies"] * TODA["batching"] /
-                 (toda["move_ms"] * 1e-3) / (peak * 1e12 / 2), "kernel_ms": toda["move_ms"],
-                 "shape": toda["shape"]},
+                 # one figure: the FP64 operations the integrator issues per site-step (84: 12 per
+                 # sub-step, 8 of them the table exp) against the measured FMA issue rate
+                 "roofline": {"bound": "fp64", "ops_per_site_step": FP64_OPS_PER_SITE_STEP["Toda"],
+                              "frac": FP64_OPS_PER_SITE_STEP["Toda"] * TODA["n"] * TODA["copies"] * TODA["batching"] /
+                              (toda["move_ms"] * 1e-3) / (peak * 1e12 / 2),
+                              "note": "the reference algorithm's count without its 7 exp (56 flops) would read "
+                                      "as a third of this; every exp costs 8 FP64 operations here"},
+                 "kernel_ms": toda["move_ms"], "shape": toda["shape"]},
         "other_workloads": others,
     }
     if rank == 0:
@@ -749,10 +766,12 @@ def run_reference(args):
                    "dt": w["dt"], **w["params"], "kernel_batching": w["batching"],
                    "sample_copies_per_step": copies},
         "cpu_baseline": {"value": value, "unit": "site-steps/s", "cores": threads, "kind": "port",
-                         "sample": f"{copies} of the {w['copies']} copies x {w['batching']} steps per bench step; "
-                                   "the reference CPU code (DNKG_FPUT_Toda/cpu-implementation) needs Boost, MPI, "
-                                   "FFTW3 and Armadillo, absent here, so its oracle port runs, built -Ofast like "
-                                   "the reference's CPU code, OpenMP over copies"},
+                         "sample": f"{copies} of the {w['copies']} copies x {w['batching']} steps per bench step "
+                                   "(a bounded sample of the workload, not all 65536 copies); the oracle port of the "
+                                   "reference's CPU loop (DNKG_FPUT_Toda/cpu-implementation), whose strict build "
+                                   "reproduces the reference's own CPU program bit for bit (tests/test_reference_pin.py), "
+                                   "here built -Ofast like the reference's CPU code, OpenMP over copies; the reference's "
+                                   "program itself is built from its sources only where they are, not on this host"},
         "e2e": {"value": value, "unit": "site-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "per_step_values": vals,
     }
