@@ -793,6 +793,8 @@ def run_profile_case(args):
         w, steps = dict(OTHERS[1]), 2
     if args.profile == "ddnkg":   # the full dDNKG workload: 4096 chains of 256 sites, tensor-core projection
         w = dict(OTHERS[2])
+    if args.profile == "ddnkg1024":   # 4096 chains of 1024 sites: four read-outs per projection tile
+        w, steps = dict(OTHERS[2], name="dDNKG N=1024 copies=4096", n=1024, nmodes=80), 2
     if args.profile == "long":    # chains beyond one block: the windowed tier (268 MB of state)
         w = dict(name="FPUT-beta N=65535 copies=256 (windowed tier)", model="FPUT", n=65535, copies=256, dt=0.1,
                  params=dict(alpha=0.0, beta=1.0), batching=10, eps=0.1, kmax=4, include_zero=False)
@@ -817,7 +819,7 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["engine", "reference"], default="engine")
-    ap.add_argument("--profile", choices=["dnkg", "toda", "dnls", "ddnkg", "long"], default=None,
+    ap.add_argument("--profile", choices=["dnkg", "toda", "dnls", "ddnkg", "ddnkg1024", "long"], default=None,
                     help="run only a small case of the integrator + diagnostics (for ncu captures)")
     args = ap.parse_args()
     if args.profile:

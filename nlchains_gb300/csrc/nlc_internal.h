@@ -261,7 +261,7 @@ struct TcArgs {
 cudaError_t launch_tc_projection(const TcArgs &a, const void *map_a, const void *map_b, const double2 *state,
                                  cudaStream_t stream);
 size_t tc_projection_smem(int slices);
-const void *tc_projection_kernel_ptr(int slices, bool intacc);
+const void *tc_projection_kernel_ptr(int slices);
 
 // Per-chain energies (nlc_energy.cu)
 struct EnergyArgs {

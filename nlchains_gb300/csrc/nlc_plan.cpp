@@ -579,8 +579,7 @@ int setup_tc_projection(nlc_plan &P, const double *d_omega, int slices) {
 	if (const char *e = std::getenv("NLC_TEST_TC_WAIT"); e && *e && *e != '0') t.wait_test = 1, t.wait_ns = 1000000ull;
 	if ((rc = bf16_map(&P.tc_map_a, d_a, uint64_t(t.kp), uint64_t(slices) * t.mp, 128))) return rc;
 	if ((rc = bf16_map(&P.tc_map_b, d_b, uint64_t(t.kp), uint64_t(slices) * t.np, 64))) return rc;
-	for (bool intacc : {false, true})
-		if ((rc = set_smem_attr(tc_projection_kernel_ptr(slices, intacc), tc_projection_smem(slices), P.prop))) return rc;
+	if ((rc = set_smem_attr(tc_projection_kernel_ptr(slices), tc_projection_smem(slices), P.prop))) return rc;
 	P.diag_rows = t.mp / 128;
 	P.tc = true;
 	return NLC_OK;

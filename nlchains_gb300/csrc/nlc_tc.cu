@@ -28,8 +28,6 @@
 // accumulators: G_t, t = 2..8, with the (2,2) product of G_4 apart (8 x 64 = all 512 TMEM columns).  Every wait is bounded: on a timeout the block records a
 // status, writes NaN into its partial row (the host then sees a non-finite entropy) and returns
 // after freeing its tensor memory.
-#include <type_traits>
-
 #include <cuda.h>
 #include <cuda_bf16.h>
 
@@ -209,10 +207,8 @@ __global__ void tc_split_rows_kernel(const double2 *__restrict__ state, TcArgs a
 // one half of the 64 columns, so the FP64 read-out and epilogue work of a thread is halved and
 // every scheduler has two warps to interleave
 constexpr int kThreads = 256, kCols = kBN / 2;
-// chains up to this many sites (16 read-outs) accumulate the row sums in exact integers
-constexpr int kIntAccSites = 16 * kChunkK;
 
-template <int S, bool INTACC>
+template <int S>
 __global__ void __launch_bounds__(kThreads, 1)
 tc_projection_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b, const TcArgs a) {
 	extern __shared__ __align__(1024) unsigned char smem_raw[];
@@ -266,13 +262,9 @@ tc_projection_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_con
 		}
 	};
 
-	// the row sums of P over all chunks.  INTACC (chains up to kIntAccSites): exact integers in
-	// units of 2^-48, below 2^62 for up to 16 chunks, converted to FP64 once after the last chunk.
-	// Longer chains: FP64 sums, two FMAs per column and chunk.
-	using Acc = typename std::conditional<INTACC, long long, double>::type;
-	Acc acc[kCols];
+	double acc[kCols];
 #pragma unroll
-	for (int c = 0; c < kCols; c++) acc[c] = 0;
+	for (int c = 0; c < kCols; c++) acc[c] = 0.;
 	const uint32_t lane_base = (uint32_t) ((warp & 3) * 32) << 16;
 	int chunks = 0;
 	for (int c0 = 0; c0 < nk; c0 += per_chunk, chunks++) {
@@ -336,53 +328,32 @@ tc_projection_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_con
 		__syncthreads();
 		if (s_fail) break;
 		asm volatile("tcgen05.fence::after_thread_sync;");
-		// the exact integer group sums.  INTACC: added to the integer row sums (no FP64 work per chunk:
-		// GB300's FP64 pipe issues ~2 operations per clock and SM, its integer pipes ~64).  Otherwise
-		// folded into two int64 halves (hi: t = 2..4 in units of 2^-32, below 2^41; lo: t = 5..8 in
-		// units of 2^-64, below 2^49: both exact in FP64), then two FMAs per column into the FP64 sums
+		// the exact integer group sums, folded with shifts into two int64 halves (hi: t = 2..4 in units
+		// of 2^-32, below 2^41; lo: t = 5..8 in units of 2^-64, below 2^49: both exact in FP64), then
+		// two FMAs per column into the FP64 row sums
 #pragma unroll
 		for (int sg = 0; sg < kCols / 8; sg++) {
 			const int seg = half * (kCols / 8) + sg;   // 8-column segment of the tile
-			if constexpr (INTACC) {
-				// group t enters the integer row sum in units of 2^-48, i.e. shifted by 8 (6 - t) for
-				// t <= 6; the groups 7 and 8 (2^-56 and 2^-64 of the tile scale) are added with one
-				// rounding to that unit
-				int g7[8];
+			long long hi[8], lo[8];
 #pragma unroll
-				for (int t = 2; t <= S + 2; t++) {   // t = S + 2: the (2,2) part of G_4 (accumulator S)
-					const int grp = t - 2, tt = t == S + 2 ? 4 : t;
-					float v[8];
-					tmem_ld8(tmem + lane_base + (uint32_t) grp * kBN + seg * 8, v);
+			for (int j = 0; j < 8; j++) hi[j] = 0, lo[j] = 0;
 #pragma unroll
-					for (int j = 0; j < 8; j++) {
-						const int g = __float2int_rn(v[j]);   // an integer below 2^26: a 32-bit conversion
-						if (tt <= 6) acc[sg * 8 + j] += (long long) g << (8 * (6 - tt));
-						else if (tt == 7) g7[j] = g;
-						else acc[sg * 8 + j] += ((long long) g7[j] * 256 + g + (1ll << 15)) >> 16;
-					}
-				}
-			} else {
-				long long hi[8], lo[8];
-#pragma unroll
-				for (int j = 0; j < 8; j++) hi[j] = 0, lo[j] = 0;
-#pragma unroll
-				for (int t = 2; t <= S + 2; t++) {   // t = S + 2: the (2,2) part of G_4 (accumulator S)
-					const int grp = t - 2, tt = t == S + 2 ? 4 : t;
-					float v[8];
-					tmem_ld8(tmem + lane_base + (uint32_t) grp * kBN + seg * 8, v);
-#pragma unroll
-					for (int j = 0; j < 8; j++) {
-						const long long g = __float2int_rn(v[j]);   // an integer below 2^26: a 32-bit conversion
-						if (tt <= 4) hi[j] += g << (8 * (4 - tt));
-						else lo[j] += g << (8 * (8 - tt));
-					}
-				}
+			for (int t = 2; t <= S + 2; t++) {   // t = S + 2: the (2,2) part of G_4 (accumulator S)
+				const int grp = t - 2, tt = t == S + 2 ? 4 : t;
+				float v[8];
+				tmem_ld8(tmem + lane_base + (uint32_t) grp * kBN + seg * 8, v);
 #pragma unroll
 				for (int j = 0; j < 8; j++) {
-					double &x = acc[sg * 8 + j];
-					x = fma(i64_to_double(hi[j]), 0x1p-32, x);
-					if constexpr (S + 1 > 4) x = fma(i64_to_double(lo[j]), 0x1p-64, x);
+					const long long g = __float2int_rn(v[j]);   // an integer below 2^26: a 32-bit conversion
+					if (tt <= 4) hi[j] += g << (8 * (4 - tt));
+					else lo[j] += g << (8 * (8 - tt));
 				}
+			}
+#pragma unroll
+			for (int j = 0; j < 8; j++) {
+				double &x = acc[sg * 8 + j];
+				x = fma(i64_to_double(hi[j]), 0x1p-32, x);
+				if constexpr (S + 1 > 4) x = fma(i64_to_double(lo[j]), 0x1p-64, x);
 			}
 		}
 		asm volatile("tcgen05.fence::before_thread_sync;");
@@ -401,18 +372,12 @@ tc_projection_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_con
 #pragma unroll
 		for (int c = 0; c < kCols; c++) {
 			const int col = half * kCols + c;
-			double e = 0.;
+			double p = 0., w = 1.;
 			if (col0 + col < (int) a.n) {
-				// P = acc 2^(e_r + f_k - 48) (INTACC; FP64 sums: 2^(e_r + f_k)); its weighted square
-				// (omega_k^2 on the phi rows)
-				double p;
-				if constexpr (INTACC) p = __ll2double_rn(acc[c]);
-				else p = acc[c];
-				const double scale = pow2i(2 * (er + s_cexp[col] - (INTACC ? 48 : 0)));
-				e = er == kNonFiniteRow ? __longlong_as_double(0x7ff8000000000000ll)
-				                        : (p * p) * (phi ? s_w[col] * scale : scale);
+				p = er == kNonFiniteRow ? __longlong_as_double(0x7ff8000000000000ll) : acc[c] * pow2i(er + s_cexp[col]);
+				if (phi) w = s_w[col];
 			}
-			red[col * kRedStride + rl] = e;
+			red[col * kRedStride + rl] = w * p * p;
 		}
 	}
 	__syncthreads();
@@ -453,26 +418,18 @@ cudaError_t launch_tc_projection(const TcArgs &a, const void *map_a, const void 
 	const dim3 grid(a.mp / kBM, a.np / kBN);
 	const CUtensorMap &ma = *static_cast<const CUtensorMap *>(map_a), &mb = *static_cast<const CUtensorMap *>(map_b);
 	const unsigned split_blocks = (unsigned) ((a.copies + 7) / 8);
-	const bool intacc = a.kp <= kIntAccSites;
 	if (a.slices == 3) {
 		tc_split_rows_kernel<3><<<split_blocks, 256, 0, stream>>>(state, a);
-		if (intacc) tc_projection_kernel<3, true><<<grid, kThreads, tc_projection_smem(3), stream>>>(ma, mb, a);
-		else tc_projection_kernel<3, false><<<grid, kThreads, tc_projection_smem(3), stream>>>(ma, mb, a);
+		tc_projection_kernel<3><<<grid, kThreads, tc_projection_smem(3), stream>>>(ma, mb, a);
 	} else {
 		tc_split_rows_kernel<kSlicesFull><<<split_blocks, 256, 0, stream>>>(state, a);
-		if (intacc)
-			tc_projection_kernel<kSlicesFull, true><<<grid, kThreads, tc_projection_smem(kSlicesFull), stream>>>(ma, mb, a);
-		else
-			tc_projection_kernel<kSlicesFull, false><<<grid, kThreads, tc_projection_smem(kSlicesFull), stream>>>(ma, mb, a);
+		tc_projection_kernel<kSlicesFull><<<grid, kThreads, tc_projection_smem(kSlicesFull), stream>>>(ma, mb, a);
 	}
 	return cudaGetLastError();
 }
 
-// both accumulation forms of a slice count (the plan sets the shared-memory attribute of each)
-const void *tc_projection_kernel_ptr(int slices, bool intacc) {
-	if (slices == 3) return intacc ? (const void *) tc_projection_kernel<3, true> : (const void *) tc_projection_kernel<3, false>;
-	return intacc ? (const void *) tc_projection_kernel<kSlicesFull, true>
-	              : (const void *) tc_projection_kernel<kSlicesFull, false>;
+const void *tc_projection_kernel_ptr(int slices) {
+	return slices == 3 ? (const void *) tc_projection_kernel<3> : (const void *) tc_projection_kernel<kSlicesFull>;
 }
 
 }  // namespace nlc
