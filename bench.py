@@ -354,11 +354,12 @@ def measure_served(local, stream):
         if delay > 0:
             time.sleep(delay)
         ids.append(srv.submit(model(r), r["b"], r["steps"], r["state"]))
-    lat = []
+    lat, prep = [], []
     for rid in ids:
         srv.wait(rid, 1800000)
         st = srv.poll(rid)
         lat.append(st["finish_ms"] - st["submit_ms"])
+        prep.append(st["ready_ms"] - st["submit_ms"])
         srv.result(rid)
     makespan = time.perf_counter() - t0
     srv.close()
@@ -389,6 +390,7 @@ def measure_served(local, stream):
             "p99_ms": float(np.percentile(lat, 99)), "slowdown_p50": float(np.percentile(slowdown, 50)),
             "slowdown_p99": float(np.percentile(slowdown, 99)),
             "alone_queue_p50_ms": float(np.percentile(queue_lat, 50)), "alone_queue_p99_ms": float(np.percentile(queue_lat, 99)),
+            "ready_p50_ms": float(np.percentile(prep, 50)), "ready_p99_ms": float(np.percentile(prep, 99)),
             "requests": len(reqs), "makespan_s": makespan,
             "alone_s": alone_s, "largest_request_alone_s": float(max(alone)), "per_model": per_model,
             "stream": f"{stream['count']} requests, model uniform over FPUT/Toda/DNKG/dDNKG/DNLS, N log-uniform "
@@ -398,6 +400,7 @@ def measure_served(local, stream):
             "alone": "each request by itself through the job API, batch + sample replayed as one CUDA graph, "
                      "two result slots (no host round trip between batches)",
             "slowdown": "latency over the request's own alone time",
+            "ready": "submit to prepared (plan, tables, eigensystem, upload)",
             "alone_queue": "latency percentiles of the plain path run as a first-come-first-served queue on the "
                            "same arrivals, from the measured alone times"}
 
@@ -778,6 +781,29 @@ def run_reference(args):
     print(json.dumps(out), flush=True)
 
 
+def run_reference_profile_case():
+    """The reference's own DNKG warp kernel (move_chain_in_warp<DNKG>, compiled unmodified for sm_103a)
+    on the small DNKG profile case: 16384 of the 65536 copies, 4 launches of 10 steps."""
+    import torch
+
+    import oracle as O
+    w = dict(WORKLOAD, copies=16384)
+    if not O.RefGPU.available(w["n"]):
+        print(json.dumps({"profile_case": "reference", "unavailable": "no reference fatbin"}))
+        return
+    ref = O.RefGPU(w["n"])
+    state = torch.from_numpy(initial_state(w, w["copies"], 0)).cuda()
+    mdl = O.Model(w["model"], w["n"], w["copies"], w["dt"], **w["params"])
+    ref.advance(mdl, state.data_ptr(), 0, 10)   # the constants
+    sp = torch.cuda.current_stream().cuda_stream
+    for _ in range(4):
+        ref.move_warp_async(mdl.model, state.data_ptr(), w["n"], w["copies"], 10, 1, None, sp)
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_case": "reference move_chain_in_warp<DNKG> N=128 copies=16384",
+                      "state_norm": float(state.norm().item())}))
+    ref.close()
+
+
 def run_profile_case(args):
     """Small cases of the headline kernels for ncu captures: 4 launches (10 steps; DNLS 2 steps),
     each followed by one diagnostics sample.  DNKG / Toda: 16384 of the 65536 copies (33.5 MB);
@@ -819,9 +845,11 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["engine", "reference"], default="engine")
-    ap.add_argument("--profile", choices=["dnkg", "toda", "dnls", "ddnkg", "ddnkg1024", "long"], default=None,
+    ap.add_argument("--profile", choices=["dnkg", "toda", "dnls", "ddnkg", "ddnkg1024", "long", "refdnkg"], default=None,
                     help="run only a small case of the integrator + diagnostics (for ncu captures)")
     args = ap.parse_args()
+    if args.profile == "refdnkg":
+        return run_reference_profile_case()
     if args.profile:
         return run_profile_case(args)
     if args.warmup < 3:

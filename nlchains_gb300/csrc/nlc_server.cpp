@@ -1,7 +1,8 @@
 // Request server: continuous batching of ensemble-integration requests on one GPU.
 //
 // Requests move queue -> admitted (by HBM budget) -> prepared -> running -> finished:
-//   * four preparer threads build each admitted request's plan (canonical launch shape, one block
+//   * four preparer threads build each admitted request's plan (smallest request first; canonical
+//     launch shape, one block
 //     per work unit; for dDNKG the host eigensolve) and allocate and upload its state, each on its own
 //     high-priority stream; the t = 0 samples of newly prepared requests then go out as one group;
 //   * the scheduler thread groups idle prepared requests by kernel class (model, parameters, dt,
@@ -55,6 +56,7 @@ struct Request {
 	std::vector<uint32_t> modes;
 	size_t state_bytes = 0;
 	size_t need_bytes = 0;          // device memory estimate used for admission
+	double work = 0;                // site-steps of the request (weighted by model), orders set-up
 
 	nlc_plan *plan = nullptr;
 	PlanInfo info;
@@ -247,8 +249,12 @@ void preparer_loop(nlc_server *S) {
 				if (st) cudaStreamSynchronize(st), cudaStreamDestroy(st);
 				return;
 			}
-			R = S->to_prepare.front();
-			S->to_prepare.pop_front();
+			// the smallest admitted request first: a short request is not held behind the set-up of a
+			// large one (a long host eigensolve, large tables)
+			auto it = std::min_element(S->to_prepare.begin(), S->to_prepare.end(),
+			                           [](const Request *a, const Request *b) { return a->work < b->work; });
+			R = *it;
+			S->to_prepare.erase(it);
 		}
 		int rc = st ? admit(S, *R, st) : set_error(NLC_ECUDA, "preparer stream");
 		if (!rc) rc = cuda_status(cudaStreamSynchronize(st), "request set-up");
@@ -673,6 +679,9 @@ int submit(nlc_server *S, const nlc_model *model, uint32_t batching, uint64_t st
 	R->batching = batching;
 	R->steps = steps;
 	R->state_bytes = n * model->copies * sizeof(double2);
+	// rough FP64 cost per site-step: Toda's exp doubles it, DNLS's transforms make it ~15x
+	R->work = double(n) * model->copies * double(steps) *
+	          (model->model == NLC_DNLS ? 15. : model->model == NLC_TODA ? 2.4 : 1.);
 	if (host_state) {
 		const double *src = static_cast<const double *>(host_state);
 		R->host_in.assign(src, src + 2 * n * model->copies);
