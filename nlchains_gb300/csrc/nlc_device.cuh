@@ -68,11 +68,20 @@ __device__ __forceinline__ double exp_scaled(double x, const double *__restrict_
 // in two FMAs against pi/512 split into two doubles, |r| <= pi/1024; sin r and cos r - 1 by their
 // Taylor series to r^5 / r^4 (next terms below 2^-59 relative), then
 //   cos th = C_j + C_j (cos r - 1) - S_j sin r,  sin th = S_j + S_j (cos r - 1) + C_j sin r.
-// 14 FP64 operations; the 16 KB table is read through the read-only cache.  |th| >= 2^20, inf and
-// NaN go to the library sincos.
+// 14 FP64 operations; the 16 KB table is read through the read-only cache.  Angles below 2^-4 (the
+// DNLS phase rotation's usual range, beta dt c_k |psi|^2) skip the reduction and the table: their
+// Taylor series to th^9 / th^8, 10 operations.  |th| >= 2^20, inf and NaN go to the library sincos.
 __device__ __forceinline__ void sincos_table(double th, const double2 *__restrict__ tab, const SinCosConsts &C,
                                              const FpOnes &k, double *s, double *c) {
-	if ((__double2hiint(th) & 0x7fffffff) >= 0x41300000) {
+	const int hi = __double2hiint(th) & 0x7fffffff;
+	if (hi < 0x3fb00000) {   // |th| < 2^-4
+		const double t2 = fmul(th, th, k);
+		const double ps = dfma(t2, dfma(t2, dfma(t2, C.q9, C.q7), C.q5), C.q3);
+		*s = dfma(fmul(th, t2, k), ps, th);
+		*c = dfma(t2, dfma(t2, dfma(t2, dfma(t2, C.w8, C.w6), C.w4), C.w2), k.one);
+		return;
+	}
+	if (hi >= 0x41300000) {
 		sincos(th, s, c);
 		return;
 	}

@@ -36,6 +36,11 @@ struct SinCosConsts {
 	double p2 = 1.2246467991473532072e-16 / 512;    // pi / 512, trailing part
 	double s3 = -1. / 6, s5 = 1. / 120;             // sin r = r + r^3 (s3 + r^2 s5)   (r^7/5040 < 2^-60 r)
 	double c2 = -1. / 2, c4 = 1. / 24;              // cos r - 1 = r^2 (c2 + r^2 c4)  (r^6/720 < 2^-59)
+	// |th| < 2^-4, no reduction: sin th = th + th^3 (q3 + th^2 (q5 + th^2 (q7 + th^2 q9))),
+	// cos th = 1 + th^2 (w2 + th^2 (w4 + th^2 (w6 + th^2 w8))): the next terms, th^11/11! and
+	// th^10/10!, are below 2^-60 of the result
+	double q3 = -1. / 6, q5 = 1. / 120, q7 = -1. / 5040, q9 = 1. / 362880;
+	double w2 = -1. / 2, w4 = 1. / 24, w6 = -1. / 720, w8 = 1. / 40320;
 };
 
 constexpr int kMaxSitesPerLane = 16;   // E: sites of a chain held in registers by one thread

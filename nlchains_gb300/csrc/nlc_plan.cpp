@@ -518,14 +518,15 @@ EncodeTiledFn encode_tiled() {
 	return fn;
 }
 
-// 2-D BF16 tensor map of `rows` rows of kp elements, boxes of 32 x box_rows, 64-byte swizzle
+// 2-D BF16 tensor map of `rows` rows of kp elements, boxes of 16 x box_rows (16 sites: 32 bytes a
+// row), 32-byte swizzle
 int bf16_map(CUtensorMap *map, void *base, uint64_t kp, uint64_t rows, uint32_t box_rows) {
 	EncodeTiledFn enc = encode_tiled();
 	if (!enc) return set_error(NLC_ECUDA, "cuTensorMapEncodeTiled is not available");
 	const cuuint64_t dims[2] = {kp, rows}, strides[1] = {kp * 2};
-	const cuuint32_t box[2] = {32, box_rows}, es[2] = {1, 1};
+	const cuuint32_t box[2] = {16, box_rows}, es[2] = {1, 1};
 	const CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, base, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
-	                       CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+	                       CU_TENSOR_MAP_SWIZZLE_32B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
 	return r == CUDA_SUCCESS ? NLC_OK : set_error(NLC_ECUDA, "cuTensorMapEncodeTiled failed");
 }
 

@@ -22,12 +22,17 @@
 // With 3 slices instead of 7 (NLC_FLAG_BF16X3_PROJECTION: 6 slice products, t = 2..4) the same
 // kernels give P to ~2^-24 of the maxima: the precision of a three-way BF16 split, faster.
 //
-// One CTA: 128 rows (64 chains) x 64 modes; 8 warps.  Thread 0 drives a two-stage TMA pipeline
-// (64-byte swizzle, 32 sites of K per stage: 7 A tiles of 128 x 32 and 7 B tiles of 64 x 32) and
-// issues 56 tcgen05.mma (M = 128, N = 64, K = 16, BF16 in, FP32 in TMEM) per stage into eight
-// accumulators: G_t, t = 2..8, with the (2,2) product of G_4 apart (8 x 64 = all 512 TMEM columns).  Every wait is bounded: on a timeout the block records a
-// status, writes NaN into its partial row (the host then sees a non-finite entropy) and returns
-// after freeing its tensor memory.
+// One CTA: 128 rows (64 chains) x 64 modes; 8 warps.  Thread 0 drives a TMA pipeline of 5 stages
+// (S = 3: 8), each 16 sites of K (32-byte swizzle: S A tiles of 128 x 16 and S B tiles of 64 x 16),
+// and issues S (S + 1) / 2 tcgen05.mma (M = 128, N = 64, K = 16, BF16 in, FP32 in TMEM) per stage into
+// eight accumulators: G_t, t = 2..8, with the (2,2) product of G_4 apart (8 x 64 = all 512 TMEM
+// columns).  A stage is refilled one stage late (once the MMAs of the stage before the current one
+// are done), so the tensor pipe always holds the current stage's MMAs queued while thread 0 waits,
+// and the loads run four stages ahead.  Tiles are numbered with the 64-mode columns fastest: the
+// CTAs resident at one time share row tiles, so the slices of X come from DRAM once and the
+// eigenvector slices stay in L2.  Every wait is bounded: on a timeout the block records a status,
+// writes NaN into its partial row (the host then sees a non-finite entropy) and returns after
+// freeing its tensor memory.
 #include <cuda.h>
 #include <cuda_bf16.h>
 
@@ -38,7 +43,7 @@ namespace nlc {
 namespace {
 
 constexpr int kSlicesFull = 7;   // FP64-accurate; 3: the BF16x3 option (~2^-24 of the maxima)
-constexpr int kBM = 128, kBN = 64, kBK = 32;
+constexpr int kBM = 128, kBN = 64, kBK = 16;
 // sites of K between two read-outs of the accumulators.  With 256, G_2 <= 256 x 256^2, G_3 <= 256 x
 // 2 x 256 x 128 and, the (2,2) product kept in an accumulator of its own, both parts of G_4 stay
 // within 2^24, so the FP32 accumulation in tensor memory is exact for every group the result
@@ -49,6 +54,9 @@ template <int S>
 __host__ __device__ constexpr uint32_t stage_a() { return S * kBM * kBK * 2; }
 template <int S>
 __host__ __device__ constexpr uint32_t stage_bytes() { return S * (kBM + kBN) * kBK * 2; }
+// pipeline depth: 5 x 42 KB (S = 7) or 8 x 18 KB (S = 3) of dynamic shared memory
+template <int S>
+__host__ __device__ constexpr int stages() { return S == 3 ? 8 : 5; }
 constexpr int kNonFiniteRow = 0x7fff;   // row exponent of a row holding inf or NaN
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t) __cvta_generic_to_shared(p); }
@@ -90,11 +98,13 @@ __device__ __forceinline__ bool mbar_wait_sleep(uint32_t bar, uint32_t parity, u
 	return false;
 }
 
-// Shared-memory matrix descriptor of a K-major tile written by TMA with the 64-byte swizzle:
-// 8-row atoms of 512 bytes (stride byte offset), descriptor version 1, layout type 4.
+// Shared-memory matrix descriptor of a K-major tile written by TMA with the 32-byte swizzle (one
+// 16-site row of BF16 per 32 bytes): 8-row atoms of 256 bytes (stride byte offset), descriptor
+// version 1, layout type 6.  The tiles start on 1024-byte boundaries, so the base offset is 0 and a
+// tile's descriptor is the stage's plus its byte offset / 16 (addresses stay below 2^18).
 __device__ __forceinline__ uint64_t smem_desc(uint32_t saddr) {
-	return (uint64_t) ((saddr & 0x3FFFF) >> 4) | ((uint64_t) 1 << 16) | ((uint64_t) (512 >> 4) << 32) |
-	       ((uint64_t) 1 << 46) | ((uint64_t) 4 << 61);
+	return (uint64_t) ((saddr & 0x3FFFF) >> 4) | ((uint64_t) 1 << 16) | ((uint64_t) (256 >> 4) << 32) |
+	       ((uint64_t) 1 << 46) | ((uint64_t) 6 << 61);
 }
 
 // Instruction descriptor of kind::f16: FP32 accumulator, BF16 A and B, both K-major, N = 64, M = 128.
@@ -106,14 +116,36 @@ __device__ __forceinline__ void tma_load(uint32_t dst, const CUtensorMap *map, i
 	             ::"r"(dst), "l"((uint64_t) map), "r"(x), "r"(y), "r"(bar) : "memory");
 }
 
-__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float (&v)[8]) {
-	uint32_t r[8];
+// 8 columns of this warp's 32 TMEM lanes; tmem_wait_ld() completes every load issued before it
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, uint32_t (&r)[8]) {
 	asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
 	             : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
 	             : "r"(taddr));
-	asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+// One stage's slice products: for t = 2..S + 1 the products A_i B_j^T with i + j = t into
+// accumulator t - 2, the (2,2) product into accumulator S.  `first`: the chunk's first stage, whose
+// first product into each accumulator overwrites it.  Unrolled: every descriptor is the stage's
+// plus a constant.
+template <int S>
+__device__ __forceinline__ void issue_stage_mmas(uint32_t tmem, uint64_t da, uint64_t db, bool first, uint32_t idesc) {
 #pragma unroll
-	for (int j = 0; j < 8; j++) v[j] = __uint_as_float(r[j]);
+	for (int t = 2; t <= S + 1; t++) {
+		const int ilo = t - S > 1 ? t - S : 1, ihi = t - 1 < S ? t - 1 : S;
+#pragma unroll
+		for (int i = ilo; i <= ihi; i++) {
+			const int j = t - i;
+			const bool own = t == 4 && i == 2;
+			const uint32_t d = tmem + (uint32_t) (own ? S : t - 2) * kBN;
+			const uint64_t ad = da + (uint64_t) (((i - 1) * kBM * kBK * 2) >> 4);
+			const uint64_t bd = db + (uint64_t) (((j - 1) * kBN * kBK * 2) >> 4);
+			const uint32_t accum = (first && (own || i == ilo)) ? 0u : 1u;
+			asm volatile("{ .reg .pred p; setp.ne.b32 p, %4, 0; tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p; }"
+			             ::"r"(d), "l"(ad), "l"(bd), "r"(idesc), "r"(accum));
+		}
+	}
 }
 
 // an int64 of magnitude below 2^51 as a double, exactly: added to the bit pattern of 1.5 * 2^52 it
@@ -213,7 +245,8 @@ __global__ void __launch_bounds__(kThreads, 1)
 tc_projection_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b, const TcArgs a) {
 	extern __shared__ __align__(1024) unsigned char smem_raw[];
 	unsigned char *smem = (unsigned char *) (((uintptr_t) smem_raw + 1023) & ~(uintptr_t) 1023);
-	__shared__ __align__(8) unsigned long long bars[6];   // full[2], empty[2], acc, test
+	constexpr int kS = stages<S>();
+	__shared__ __align__(8) unsigned long long bars[2 * kS + 2];   // full[kS], empty[kS], acc, test
 	__shared__ uint32_t tmem_slot;
 	__shared__ int s_fail;
 	__shared__ double s_w[kBN];   // per column of the tile: omega_k^2 (weight of the phi rows)
@@ -221,10 +254,13 @@ tc_projection_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_con
 	const int tid = threadIdx.x, warp = tid >> 5;
 	const int rl = (warp & 3) * 32 + (tid & 31);   // this thread's row of the tile (its TMEM lane)
 	const int half = warp >> 2;                    // its columns: [kCols half, kCols (half + 1))
-	const int row0 = blockIdx.x * kBM, col0 = blockIdx.y * kBN;
-	const uint32_t full0 = smem_u32(&bars[0]), empty0 = smem_u32(&bars[2]), accb = smem_u32(&bars[4]);
+	// tiles numbered with the column tiles fastest (see the header)
+	const int col_tiles = a.np / kBN;
+	const int row_tile = (int) (blockIdx.x / col_tiles), col_tile = (int) (blockIdx.x % col_tiles);
+	const int row0 = row_tile * kBM, col0 = col_tile * kBN;
+	const uint32_t full0 = smem_u32(&bars[0]), empty0 = smem_u32(&bars[kS]), accb = smem_u32(&bars[2 * kS]);
 	if (tid == 0) {
-		for (int i = 0; i < 6; i++) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&bars[i])));
+		for (int i = 0; i < 2 * kS + 2; i++) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&bars[i])));
 		asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 		s_fail = 0;
 	}
@@ -239,7 +275,7 @@ tc_projection_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_con
 		s_cexp[tid] = k < (int) a.n ? a.col_exp[k] : 0;
 	}
 	// tests only: a wait that runs out (nothing arrives at the test barrier) takes the failure path
-	if (a.wait_test && tid == 0 && !mbar_wait(smem_u32(&bars[5]), 0, a.wait_ns)) s_fail = 1;
+	if (a.wait_test && tid == 0 && !mbar_wait(smem_u32(&bars[2 * kS + 1]), 0, a.wait_ns)) s_fail = 1;
 	asm volatile("tcgen05.fence::before_thread_sync;");
 	__syncthreads();
 	asm volatile("tcgen05.fence::after_thread_sync;");
@@ -272,47 +308,29 @@ tc_projection_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_con
 		if (tid == 0 && !s_fail) {
 			bool ok = true;
 			committed = false;
-			if (c0 == 0) {
-				load_stage(0, 0);
-				if (nk > 1) load_stage(1, 1);
-			}
+			if (c0 == 0)
+				for (int it = 0; it < kS && it < nk; it++) load_stage(it, it);
 			for (int it = c0; it < c1 && ok; it++) {
-				const int s = it & 1;
-				const uint32_t ph = (it >> 1) & 1;
-				if (!mbar_wait(full0 + 8 * s, ph, a.wait_ns)) {
+				const int s = it % kS;
+				if (!mbar_wait(full0 + 8 * s, (it / kS) & 1, a.wait_ns)) {
 					ok = false;
 					break;
 				}
 				consumed = it + 1;
 				asm volatile("tcgen05.fence::after_thread_sync;");
-				const uint32_t sa = smem_u32(stage_ptr(s)), sb = sa + kStageA;
-#pragma unroll 1
-				for (int t = 2; t <= S + 1; t++) {
-					const int ilo = t - S > 1 ? t - S : 1, ihi = t - 1 < S ? t - 1 : S;
-					for (int i = ilo; i <= ihi; i++) {
-						const int j = t - i;
-						// accumulator t - 2; the (2,2) product of G_4 in accumulator S
-						const bool own = t == 4 && i == 2;
-						const uint32_t d = tmem + (uint32_t) (own ? S : t - 2) * kBN;
-						for (int kk = 0; kk < kBK / 16; kk++) {
-							const uint64_t ad = smem_desc(sa + (uint32_t) (i - 1) * kBM * kBK * 2 + kk * 32);
-							const uint64_t bd = smem_desc(sb + (uint32_t) (j - 1) * kBN * kBK * 2 + kk * 32);
-							const uint32_t accum = (it == c0 && (own || i == ilo) && kk == 0) ? 0u : 1u;
-							asm volatile(
-							    "{ .reg .pred p; setp.ne.b32 p, %4, 0; tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p; }"
-							    ::"r"(d), "l"(ad), "l"(bd), "r"(kIdesc), "r"(accum));
-						}
-					}
-				}
+				const uint32_t sa = smem_u32(stage_ptr(s));
+				issue_stage_mmas<S>(tmem, smem_desc(sa), smem_desc(sa + kStageA), it == c0, kIdesc);
 				asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(empty0 + 8 * s)
 				             : "memory");
-				if (it + 2 < nk) {
-					// the stage is free once its MMAs are done; then prefetch two stages ahead
-					if (!mbar_wait(empty0 + 8 * s, ph, a.wait_ns)) {
+				// refill the previous stage once its MMAs are done (this stage's are queued behind them)
+				const int prev = it - 1;
+				if (prev >= 0 && prev + kS < nk) {
+					const int ps = prev % kS;
+					if (!mbar_wait(empty0 + 8 * ps, (prev / kS) & 1, a.wait_ns)) {
 						ok = false;
 						break;
 					}
-					load_stage(it + 2, s);
+					load_stage(prev + kS, ps);
 				}
 			}
 			if (ok) {
@@ -330,7 +348,9 @@ tc_projection_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_con
 		asm volatile("tcgen05.fence::after_thread_sync;");
 		// the exact integer group sums, folded with shifts into two int64 halves (hi: t = 2..4 in units
 		// of 2^-32, below 2^41; lo: t = 5..8 in units of 2^-64, below 2^49: both exact in FP64), then
-		// two FMAs per column into the FP64 row sums
+		// two FMAs per column into the FP64 row sums.  Accumulators are read four at a time, one wait
+		// for the four loads.
+		constexpr int kGroups = S + 1;   // accumulators: G_2..G_{S+1} and the (2,2) part of G_4
 #pragma unroll
 		for (int sg = 0; sg < kCols / 8; sg++) {
 			const int seg = half * (kCols / 8) + sg;   // 8-column segment of the tile
@@ -338,15 +358,23 @@ tc_projection_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_con
 #pragma unroll
 			for (int j = 0; j < 8; j++) hi[j] = 0, lo[j] = 0;
 #pragma unroll
-			for (int t = 2; t <= S + 2; t++) {   // t = S + 2: the (2,2) part of G_4 (accumulator S)
-				const int grp = t - 2, tt = t == S + 2 ? 4 : t;
-				float v[8];
-				tmem_ld8(tmem + lane_base + (uint32_t) grp * kBN + seg * 8, v);
+			for (int g0 = 0; g0 < kGroups; g0 += 4) {
+				uint32_t v[4][8];
 #pragma unroll
-				for (int j = 0; j < 8; j++) {
-					const long long g = __float2int_rn(v[j]);   // an integer below 2^26: a 32-bit conversion
-					if (tt <= 4) hi[j] += g << (8 * (4 - tt));
-					else lo[j] += g << (8 * (8 - tt));
+				for (int q = 0; q < 4; q++)
+					if (g0 + q < kGroups) tmem_ld8(tmem + lane_base + (uint32_t) (g0 + q) * kBN + seg * 8, v[q]);
+				tmem_wait_ld();
+#pragma unroll
+				for (int q = 0; q < 4; q++) {
+					const int grp = g0 + q;
+					if (grp >= kGroups) break;
+					const int tt = grp == S ? 4 : grp + 2;   // accumulator S: the (2,2) part of G_4
+#pragma unroll
+					for (int j = 0; j < 8; j++) {
+						const long long g = __float2int_rn(__uint_as_float(v[q][j]));   // below 2^26: a 32-bit conversion
+						if (tt <= 4) hi[j] += g << (8 * (4 - tt));
+						else lo[j] += g << (8 * (8 - tt));
+					}
 				}
 			}
 #pragma unroll
@@ -364,6 +392,8 @@ tc_projection_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_con
 	// buffer (over the finished stages) is column-major with a padded stride: the rows' stores and
 	// the column sums' loads are both free of bank conflicts.
 	constexpr int kRedStride = kBM + 1;
+	static_assert(kBN * kRedStride * sizeof(double) <= (size_t) kS * kStageBytes, "reduction buffer exceeds the stages");
+	static_assert((size_t) kS * kStageBytes + 1024 + 1024 <= 227 * 1024, "shared memory above 227 KB");
 	double *red = reinterpret_cast<double *>(smem);   // [64][129]
 	const int r = row0 + rl;
 	const bool phi = (r & 1) == 0;
@@ -389,14 +419,14 @@ tc_projection_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_con
 			double s0 = 0., s1 = 0., s2 = 0., s3 = 0.;
 			for (int rr = 0; rr < kBM; rr += 4) s0 += col[rr], s1 += col[rr + 1], s2 += col[rr + 2], s3 += col[rr + 3];
 			const double s = (s0 + s1) + (s2 + s3);
-			a.partials[(size_t) blockIdx.x * a.n + k] = s_fail ? __longlong_as_double(0x7ff8000000000000ll) : s;
+			a.partials[(size_t) row_tile * a.n + k] = s_fail ? __longlong_as_double(0x7ff8000000000000ll) : s;
 		}
 	}
 	if (tid == 0 && s_fail) {
 		// after a timeout: wait (each wait bounded again) for the loads this block issued and has not
 		// consumed, then for every MMA it issued, so that nothing lands in shared memory or TMEM after
 		// the block has released them
-		for (int it = consumed; it < issued; it++) mbar_wait(full0 + 8 * (it & 1), (it >> 1) & 1, a.wait_ns);
+		for (int it = consumed; it < issued; it++) mbar_wait(full0 + 8 * (it % kS), (it / kS) & 1, a.wait_ns);
 		if (!committed)
 			asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(accb)
 			             : "memory");
@@ -409,13 +439,14 @@ tc_projection_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_con
 }
 
 size_t tc_projection_smem(int slices) {
-	return 2 * (size_t) (slices == 3 ? stage_bytes<3>() : stage_bytes<kSlicesFull>()) + 1024;
+	return slices == 3 ? (size_t) stages<3>() * stage_bytes<3>() + 1024
+	                   : (size_t) stages<kSlicesFull>() * stage_bytes<kSlicesFull>() + 1024;
 }
 
 cudaError_t launch_tc_projection(const TcArgs &a, const void *map_a, const void *map_b, const double2 *state,
                                  cudaStream_t stream) {
 	count_launch(2);
-	const dim3 grid(a.mp / kBM, a.np / kBN);
+	const dim3 grid((unsigned) ((size_t) (a.mp / kBM) * (a.np / kBN)));
 	const CUtensorMap &ma = *static_cast<const CUtensorMap *>(map_a), &mb = *static_cast<const CUtensorMap *>(map_b);
 	const unsigned split_blocks = (unsigned) ((a.copies + 7) / 8);
 	if (a.slices == 3) {

@@ -78,15 +78,16 @@ def test_elementwise_operators(gpu):
 
 
 def test_phase_rotation_accuracy(gpu):
-    """The table-driven sincos of the phase rotation against numpy for |theta| from 1e-8 to 1e7 (the
-    library sincos takes |theta| >= 2^20): psi = (x, 0) with x a 13-bit dyadic number in [0.5, 2],
-    so |psi|^2 is exact, theta = -coef x^2 is rounded once on both sides, and the result must be
+    """The sincos of the phase rotation against numpy for |theta| from 1e-8 to 1e7 (a Taylor series
+    below 2^-4, the table method above, the library sincos from 2^20; coef 0.0156 and 0.03 put warps
+    on both sides of 2^-4): psi = (x, 0) with x a 13-bit dyadic number in [0.5, 2], so |psi|^2 is
+    exact, theta = -coef x^2 is rounded once on both sides, and the result must be
     x (cos theta, sin theta) to a few ulp."""
     torch = pytest.importorskip("torch")
     n, copies = 64, 64
     x = np.round(np.random.default_rng(4).uniform(0.5, 2.0, n * copies) * 2 ** 12) / 2 ** 12
     plan = gpu.Plan(gpu.Model("DNLS", n, copies, 0.01, beta=1.0))
-    for coef in (1e-8, 1e-3, 0.37, 3.0, 123.0, 4.1e4, 3e6):
+    for coef in (1e-8, 1e-3, 0.0156, 0.03, 0.37, 3.0, 123.0, 4.1e4, 3e6):
         dev = torch.from_numpy(np.stack([x, np.zeros_like(x)], axis=1).copy()).cuda()
         plan.dnls_evolve_nonlinear(dev.data_ptr(), coef, torch.cuda.current_stream().cuda_stream)
         torch.cuda.synchronize()

@@ -204,14 +204,18 @@ def test_dnls_as_accurate_as_reference_kernels(gpu, path):
         if cp == 100:
             assert rel(eng, rgpu) <= STATE_TOL
         if cp == int(d["checkpoints"][-1]):
-            drift_e = np.abs(O.energies(mdl, eng) - e0).max()
-            drift_r = np.abs(O.energies(mdl, rgpu) - e0).max()
-            drift_x = np.abs(O.energies(mdl, ext) - e0).max()
-            print(f"   energy drift: engine {drift_e:.3e}, reference kernels {drift_r:.3e}, extended {drift_x:.3e}")
-            # the drift here is mostly the splitting error itself (the extended-precision run has it
-            # too); rounding moves it, and the engine's rounding may move it no more than the
-            # reference kernels' does
-            assert abs(drift_e - drift_x) <= max(2 * abs(drift_r - drift_x), 1e-3 * drift_x)
+            en_e, en_r, en_x = O.energies(mdl, eng), O.energies(mdl, rgpu), O.energies(mdl, ext)
+            drift_x = np.abs(en_x - e0).max()
+            err_e, err_r = np.abs(en_e - en_x).max(), np.abs(en_r - en_x).max()
+            print(f"   energy drift: engine {np.abs(en_e - e0).max():.3e}, reference kernels "
+                  f"{np.abs(en_r - e0).max():.3e}, extended {drift_x:.3e}; energy error per chain against the "
+                  f"extended run: engine {err_e:.3e}, reference kernels {err_r:.3e}")
+            # the drift is mostly the splitting error itself (the extended-precision run has it too);
+            # each chain's energy in double precision departs from its extended-precision energy by the
+            # rounding of the whole run, and the engine's departure may be no larger than the
+            # reference kernels' (the largest drift over the chains is not compared: a run can drift
+            # less than the extended one)
+            assert err_e <= max(2 * err_r, 1e-3 * drift_x)
     job.close()
     ctx.close()
     ref.close()

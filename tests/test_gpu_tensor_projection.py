@@ -21,8 +21,9 @@ def lin_of(nlc, n, copies, state, masses, flags):
     return lin, wt, inf
 
 
-# 300 and 700 sites: K in two and three read-out chunks; 4096 copies: 64 row tiles
-@pytest.mark.parametrize("n,copies", [(16, 19), (100, 64), (256, 4096), (300, 33), (700, 11)])
+# 16 sites: one 16-site stage, fewer stages than the pipeline holds; 300 and 700 sites: K in two
+# and three read-out chunks; 1100: five chunks, the last one 6 stages; 4096 copies: 64 row tiles
+@pytest.mark.parametrize("n,copies", [(16, 19), (100, 64), (256, 4096), (300, 33), (700, 11), (1100, 70)])
 def test_tensor_projection_matches_fp64(gpu, n, copies):
     masses = ic.masses_uniform(n, seed=n)
     state = np.random.default_rng(n + copies).standard_normal((copies, n, 2))
