@@ -27,7 +27,7 @@ CPP_SOURCES = ["nlc_plan.cpp", "nlc_tables.cpp", "nlc_job.cpp", "nlc_server.cpp"
                "nlc_eig_host.cpp"]
 # the host eigensolver's inner loops (products, rotations) want the vectoriser's full cost model
 CPP_OPT = {"nlc_eig_host.cpp": "-O3"}
-HEADERS = ["nlc_device.cuh", "nlc_real.cuh", "nlc_fft.cuh", "nlc_internal.h", "nlc_host.h"]
+HEADERS = ["nlc_device.cuh", "nlc_real.cuh", "nlc_fft.cuh", "nlc_internal.h", "nlc_host.h", "nlc_fixed.h"]
 
 
 def _newer(target, deps):

@@ -250,21 +250,40 @@ uint64_t launch_count();
 // dDNKG projection on the tensor cores (nlc_tc.cu): 7 (or 3) BF16 slices of X (rows 2c, 2c + 1 = phi_c,
 // pi_c of chain c) and of the eigenvector matrix E, each padded with zeros to mp / np rows (multiples
 // of 128 / 64) and kp sites (a multiple of 32), slice i at rows [i mp, (i + 1) mp)
+#ifdef __CUDACC__
+#define NLC_HD_INLINE __host__ __device__ inline
+#else
+#define NLC_HD_INLINE inline
+#endif
+// BF16 slices of the tensor-core projection, laid out as the kernel's shared memory wants them:
+// [16-site block][128-row tile][slice][row in tile][16 sites].  The slices of one tile and block
+// are one contiguous run (4 KB a slice), so a pipeline stage is two bulk copies (A's slices, B's
+// slices), and a sweep that reads slices 1..3 reads a prefix of the run.  Within a row (32 bytes)
+// the two 16-byte halves trade places on rows 4..7 of every 8: the 32-byte swizzle of the MMA's
+// shared-memory descriptor.
+NLC_HD_INLINE size_t tc_slice_index(int slice, int kb, size_t rows, size_t row, int site_in_block, int slices) {
+	const int e = site_in_block;
+	const size_t tiles = rows / 128, tile = row / 128, r = row % 128;
+	return ((((size_t) kb * tiles + tile) * slices + slice) * 128 + r) * 16 +
+	       (size_t) (((((e >> 3) ^ (int) (r >> 2)) & 1) << 3) | (e & 7));
+}
+
 struct TcArgs {
 	uint32_t n, copies;
-	int mp, np, kp;
+	int mp, np, kp, nkb;       // padded rows of X, of E; padded sites; 16-site blocks (kp / 16)
 	int slices;                // 7 (FP64-accurate) or 3 (BF16x3)
-	uint16_t *a_slices;        // [7][mp][kp] BF16 bit patterns, written per sample by the split kernel
+	uint16_t *a_slices;        // slices of X (tc_slice_index, mp rows), written per sample by the split kernel
+	const uint16_t *b_slices;  // slices of E (tc_slice_index, np rows), written once at set-up
 	int *row_exp;              // [2 copies] power-of-two exponent of each row of X
 	const int *col_exp;        // [n] exponent of each eigenvector (row of E)
 	const double *omega;       // [n]
 	double *partials;          // [mp / 128][n] weighted squared sums per row tile
+	long long *park;           // [mp][np] the hi sums of the first sweep (7 slices only)
 	int *status;               // set on a bounded-wait timeout
 	unsigned long long wait_ns;  // limit of every mbarrier wait (wall clock)
 	int wait_test;             // tests only: thread 0 first waits on a barrier nothing arrives at
 };
-cudaError_t launch_tc_projection(const TcArgs &a, const void *map_a, const void *map_b, const double2 *state,
-                                 cudaStream_t stream);
+cudaError_t launch_tc_projection(const TcArgs &a, const double2 *state, cudaStream_t stream);
 size_t tc_projection_smem(int slices);
 const void *tc_projection_kernel_ptr(int slices);
 

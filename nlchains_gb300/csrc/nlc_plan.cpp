@@ -130,7 +130,6 @@ struct nlc_plan {
 	// dDNKG projection on the tensor cores
 	bool tc = false;
 	TcArgs tca{};
-	CUtensorMap tc_map_a{}, tc_map_b{};
 	uint32_t win_len = 0, win_steps = 0;   // windowed tier: sites per window, steps per launch
 	double2 *d_win = nullptr;              // windowed tier: the second state buffer
 	double block_ops = 0;      // FP64 work of one block's step over the sustained fraction of peak
@@ -501,37 +500,9 @@ int setup_fft(nlc_plan &P, FftPlanDev &f, bool convolution) {
 
 int set_smem_attr(const void *k, size_t smem, const cudaDeviceProp &prop);
 
-// cuTensorMapEncodeTiled from the driver, without linking libcuda
-using EncodeTiledFn = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
-                                   const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
-                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
-
-EncodeTiledFn encode_tiled() {
-	static EncodeTiledFn fn = [] {
-		void *p = nullptr;
-		cudaDriverEntryPointQueryResult q{};
-		if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
-		    q != cudaDriverEntryPointSuccess)
-			p = nullptr;
-		return reinterpret_cast<EncodeTiledFn>(p);
-	}();
-	return fn;
-}
-
-// 2-D BF16 tensor map of `rows` rows of kp elements, boxes of 16 x box_rows (16 sites: 32 bytes a
-// row), 32-byte swizzle
-int bf16_map(CUtensorMap *map, void *base, uint64_t kp, uint64_t rows, uint32_t box_rows) {
-	EncodeTiledFn enc = encode_tiled();
-	if (!enc) return set_error(NLC_ECUDA, "cuTensorMapEncodeTiled is not available");
-	const cuuint64_t dims[2] = {kp, rows}, strides[1] = {kp * 2};
-	const cuuint32_t box[2] = {16, box_rows}, es[2] = {1, 1};
-	const CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, base, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
-	                       CU_TENSOR_MAP_SWIZZLE_32B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-	return r == CUDA_SUCCESS ? NLC_OK : set_error(NLC_ECUDA, "cuTensorMapEncodeTiled failed");
-}
-
-// Tensor-core projection set-up: the 7 (or 3) BF16 slices of every eigenvector (rows of E, host, once),
-// the per-sample slice buffer of X (zero padding included), and the tensor maps.  Slicing as in
+// Tensor-core projection set-up: the 7 (or 3) BF16 slices of every eigenvector (rows of E, host, once,
+// in the tiled, swizzled layout of tc_slice_index), the per-sample slice buffer of X (zero padding
+// included) and the parking space of the first sweep's sums.  Slicing as in
 // nlc_tc.cu: a row scaled by 2^-f (max |e| = m 2^f, 0.5 <= m < 1), v = 256 e 2^-f, then
 // sigma_i = round(v), v <- 256 (v - sigma_i).
 int setup_tc_projection(nlc_plan &P, const double *d_omega, int slices) {
@@ -540,8 +511,9 @@ int setup_tc_projection(nlc_plan &P, const double *d_omega, int slices) {
 	t.n = n, t.copies = P.m.copies;
 	t.slices = slices;
 	t.mp = int((2ull * P.m.copies + 127) / 128 * 128);
-	t.np = int((n + 63) / 64 * 64);
-	t.kp = int((n + 31) / 32 * 32);
+	t.np = int((n + 127) / 128 * 128);
+	t.kp = int((n + 15) / 16 * 16);
+	t.nkb = t.kp / 16;
 	std::vector<uint16_t> b(size_t(slices) * t.np * t.kp, 0);
 	std::vector<int> fexp(n, 0);
 	for (uint32_t k = 0; k < n; k++) {
@@ -558,7 +530,7 @@ int setup_tc_projection(nlc_plan &P, const double *d_omega, int slices) {
 				const float fs = float(sg);   // an integer of at most 9 bits: exact in BF16
 				uint32_t bits;
 				std::memcpy(&bits, &fs, 4);
-				b[(size_t(i) * t.np + k) * t.kp + s] = uint16_t(bits >> 16);
+				b[tc_slice_index(i, int(s >> 4), size_t(t.np), k, int(s & 15), slices)] = uint16_t(bits >> 16);
 				v = (v - sg) * 256.;
 			}
 		}
@@ -571,15 +543,16 @@ int setup_tc_projection(nlc_plan &P, const double *d_omega, int slices) {
 	const std::vector<uint16_t> zeros(size_t(slices) * t.mp * t.kp, 0);   // padding rows and sites stay 0
 	if ((rc = P.upload(&d_a, zeros.data(), zeros.size()))) return rc;
 	if ((rc = P.dalloc(&d_rexp, 2ull * P.m.copies))) return rc;
+	long long *d_park = nullptr;
+	if (slices == 7 && (rc = P.dalloc(&d_park, size_t(t.mp) * t.np))) return rc;
 	const int zero = 0;
 	if ((rc = P.upload(&d_status, &zero, 1))) return rc;
-	t.a_slices = d_a, t.row_exp = d_rexp, t.col_exp = d_fexp, t.omega = d_omega, t.status = d_status;
+	t.a_slices = d_a, t.b_slices = d_b, t.row_exp = d_rexp, t.col_exp = d_fexp, t.omega = d_omega, t.status = d_status,
+	t.park = d_park;
 	// every mbarrier wait of the projection gives up after 2 s; NLC_TEST_TC_WAIT (tests only) makes
 	// each block first wait 1 ms on a barrier nothing arrives at, to exercise the failure path
 	t.wait_ns = 2000000000ull;
 	if (const char *e = std::getenv("NLC_TEST_TC_WAIT"); e && *e && *e != '0') t.wait_test = 1, t.wait_ns = 1000000ull;
-	if ((rc = bf16_map(&P.tc_map_a, d_a, uint64_t(t.kp), uint64_t(slices) * t.mp, 128))) return rc;
-	if ((rc = bf16_map(&P.tc_map_b, d_b, uint64_t(t.kp), uint64_t(slices) * t.np, 64))) return rc;
 	if ((rc = set_smem_attr(tc_projection_kernel_ptr(slices), tc_projection_smem(slices), P.prop))) return rc;
 	P.diag_rows = t.mp / 128;
 	P.tc = true;
@@ -1193,7 +1166,7 @@ extern "C" int nlc_linenergies(nlc_plan *P, const void *state, double *lin, doub
 	if (P->tc) {
 		TcArgs t = P->tca;
 		t.partials = P->d_partials;
-		rc = cuda_status(launch_tc_projection(t, &P->tc_map_a, &P->tc_map_b, static_cast<const double2 *>(state), st),
+		rc = cuda_status(launch_tc_projection(t, static_cast<const double2 *>(state), st),
 		                 "tensor projection launch");
 	} else {
 		rc = cuda_status(launch_linenergies_partials(P->ga, state, P->diag_blocks, P->diag_threads, P->diag_smem,

@@ -14,49 +14,62 @@
 //
 // Every G_t is a sum of integer products below 2^16, accumulated in FP32 in tensor memory; it is
 // read out every 256 sites of K, while the partial sums that matter are still exact (below 2^24),
-// and the groups are combined exactly in integers and added in FP64.  The slices beyond t = 8 and the residual of the 7-slice truncation are
-// below 2^-56 of the row and column maxima, so P carries FP64-level error.  The squares, the omega
-// weights and the sum over the tile's 128 rows are fused into the epilogue; a block's column sums
-// go to its row of partial sums, which the linenergies finish kernel adds in a fixed order.
+// and added with shifts into two exact int64 sums per element of P: hi (t = 2..4, units of 2^-32)
+// and lo (t = 5..8, units of 2^-64).  The slices beyond t = 8 and the residual of the 7-slice
+// truncation are below 2^-56 of the row and column maxima, so P carries FP64-level error.  At the
+// end each element's square becomes one double by an integer-only conversion (nlc_fixed.h,
+// truncated to 53 bits); the omega weights and the sum over the tile's 128 rows are fused into the
+// epilogue, and a block's column sums go to its row of partial sums, which the linenergies
+// finish kernel adds in a fixed order.
 //
 // With 3 slices instead of 7 (NLC_FLAG_BF16X3_PROJECTION: 6 slice products, t = 2..4) the same
 // kernels give P to ~2^-24 of the maxima: the precision of a three-way BF16 split, faster.
 //
-// One CTA: 128 rows (64 chains) x 64 modes; 8 warps.  Thread 0 drives a TMA pipeline of 5 stages
-// (S = 3: 8), each 16 sites of K (32-byte swizzle: S A tiles of 128 x 16 and S B tiles of 64 x 16),
-// and issues S (S + 1) / 2 tcgen05.mma (M = 128, N = 64, K = 16, BF16 in, FP32 in TMEM) per stage into
-// eight accumulators: G_t, t = 2..8, with the (2,2) product of G_4 apart (8 x 64 = all 512 TMEM
-// columns).  A stage is refilled one stage late (once the MMAs of the stage before the current one
-// are done), so the tensor pipe always holds the current stage's MMAs queued while thread 0 waits,
-// and the loads run four stages ahead.  Tiles are numbered with the 64-mode columns fastest: the
-// CTAs resident at one time share row tiles, so the slices of X come from DRAM once and the
-// eigenvector slices stay in L2.  Every wait is bounded: on a timeout the block records a status,
-// writes NaN into its partial row (the host then sees a non-finite entropy) and returns after
-// freeing its tensor memory.
+// Tile and sweeps.  A tcgen05.mma costs about 80 cycles to issue whatever its width (measured on
+// GB300: N = 32 and 64 take as long as N = 128; N = 256 runs at the full tensor rate), so the MMAs
+// must be wide.  Eight accumulators of N = 128 columns would need 1024 TMEM columns, twice the 512
+// an SM has, so one CTA (128 rows x 128 modes, 16 warps) sweeps K twice with four accumulators:
+//   sweep 0: G_2, G_3, G_4 without (2,2), and (2,2): 6 MMAs per 16-site stage, slices 1..3;
+//   sweep 1: G_5, G_6, G_7, G_8: 22 MMAs per stage, slices 1..7.
+// Between the sweeps every thread parks its hi sums in a global scratch array and takes them back
+// for the conversion.  The slices are stored tiled and pre-swizzled (tc_slice_index), so a
+// pipeline stage (16 sites: 7 stages of 24 KB in sweep 0, 3 of 56 KB in sweep 1) is two bulk copies,
+// one for A's slices and one for B's.  Thread 32 issues the copies, refilling a stage's buffer as
+// soon as the MMAs that read it are done; thread 0 issues the MMAs (M = 128, N = 128, K = 16, BF16
+// in, FP32 in TMEM) as soon as a stage has landed.  Each tcgen05 or bulk-copy instruction costs
+// the issuing thread tens of cycles, so the two streams run on two threads.  Tiles are numbered with the 128-mode columns fastest: the CTAs resident at one
+// time share row tiles, so the slices of X come from DRAM once per sweep and the eigenvector
+// slices stay in L2.  Every wait is bounded: on a timeout the block records a status, writes NaN
+// into its partial row (the host then sees a non-finite entropy) and returns after freeing its
+// tensor memory.
 #include <cuda.h>
 #include <cuda_bf16.h>
 
+#include <type_traits>
+
 #include "nlc_device.cuh"
+#include "nlc_fixed.h"
 
 namespace nlc {
 
 namespace {
 
 constexpr int kSlicesFull = 7;   // FP64-accurate; 3: the BF16x3 option (~2^-24 of the maxima)
-constexpr int kBM = 128, kBN = 64, kBK = 16;
+constexpr int kBM = 128, kBN = 128, kBK = 16;
 // sites of K between two read-outs of the accumulators.  With 256, G_2 <= 256 x 256^2, G_3 <= 256 x
 // 2 x 256 x 128 and, the (2,2) product kept in an accumulator of its own, both parts of G_4 stay
 // within 2^24, so the FP32 accumulation in tensor memory is exact for every group the result
 // depends on above 2^-40; the groups t >= 5 may round in their last bit, 2^-40 below the maxima.
 constexpr int kChunkK = 256;
 constexpr uint32_t kTmemCols = 512;
-template <int S>
-__host__ __device__ constexpr uint32_t stage_a() { return S * kBM * kBK * 2; }
-template <int S>
-__host__ __device__ constexpr uint32_t stage_bytes() { return S * (kBM + kBN) * kBK * 2; }
-// pipeline depth: 5 x 42 KB (S = 7) or 8 x 18 KB (S = 3) of dynamic shared memory
-template <int S>
-__host__ __device__ constexpr int stages() { return S == 3 ? 8 : 5; }
+constexpr uint32_t kTile = kBM * kBK * 2;   // one slice tile of A or B: 128 rows x 16 sites, 4 KB
+static_assert(kBN == kBM, "A and B tiles share one size");
+// slices a sweep reads, its stage size, and the stages that fit in the stage memory
+__host__ __device__ constexpr int sweep_slices(int S, int sweep) { return sweep == 0 ? (S < 3 ? S : 3) : S; }
+__host__ __device__ constexpr uint32_t sweep_stage_bytes(int ns) { return 2u * (uint32_t) ns * kTile; }
+constexpr uint32_t kStageMem = 168 * 1024;
+__host__ __device__ constexpr int sweep_stages(int ns) { return (int) (kStageMem / sweep_stage_bytes(ns)); }
+static_assert(sweep_stages(3) == 7 && sweep_stages(7) == 3, "stage geometry");
 constexpr int kNonFiniteRow = 0x7fff;   // row exponent of a row holding inf or NaN
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t) __cvta_generic_to_shared(p); }
@@ -71,7 +84,15 @@ __device__ __forceinline__ unsigned long long global_ns() {
 	return t;
 }
 
+__device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
+	uint32_t ok;
+	asm volatile("{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
+	             : "=r"(ok) : "r"(bar), "r"(parity) : "memory");
+	return ok != 0;
+}
+
 __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, unsigned long long limit_ns) {
+	if (mbar_try(bar, parity)) return true;   // the usual case: no clock read
 	const unsigned long long t0 = global_ns();
 	for (long long i = 0; i < kWaitTriesMax; i++) {
 		uint32_t ok;
@@ -107,13 +128,15 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t saddr) {
 	       ((uint64_t) 1 << 46) | ((uint64_t) 6 << 61);
 }
 
-// Instruction descriptor of kind::f16: FP32 accumulator, BF16 A and B, both K-major, N = 64, M = 128.
+// Instruction descriptor of kind::f16: FP32 accumulator, BF16 A and B, both K-major, N = 128, M = 128.
 constexpr uint32_t kIdesc =
     (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t) (kBN >> 3) << 17) | ((uint32_t) (kBM >> 4) << 24);
 
-__device__ __forceinline__ void tma_load(uint32_t dst, const CUtensorMap *map, int x, int y, uint32_t bar) {
-	asm volatile("cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
-	             ::"r"(dst), "l"((uint64_t) map), "r"(x), "r"(y), "r"(bar) : "memory");
+// one contiguous run of global memory into shared memory (the bulk-copy engine), completing on
+// the mbarrier `bar`: both addresses 16-byte aligned, bytes a multiple of 16
+__device__ __forceinline__ void bulk_load(uint32_t dst, const void *src, uint32_t bytes, uint32_t bar) {
+	asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+	             ::"r"(dst), "l"((uint64_t) src), "r"(bytes), "r"(bar) : "memory");
 }
 
 // 8 columns of this warp's 32 TMEM lanes; tmem_wait_ld() completes every load issued before it
@@ -125,38 +148,32 @@ __device__ __forceinline__ void tmem_ld8(uint32_t taddr, uint32_t (&r)[8]) {
 
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
-// One stage's slice products: for t = 2..S + 1 the products A_i B_j^T with i + j = t into
-// accumulator t - 2, the (2,2) product into accumulator S.  `first`: the chunk's first stage, whose
-// first product into each accumulator overwrites it.  Unrolled: every descriptor is the stage's
-// plus a constant.
-template <int S>
-__device__ __forceinline__ void issue_stage_mmas(uint32_t tmem, uint64_t da, uint64_t db, bool first, uint32_t idesc) {
+// One stage's slice products of a sweep into its four accumulators (128 TMEM columns each):
+//   sweep 0: (1,1) -> 0 (G_2), (1,2) (2,1) -> 1 (G_3), (1,3) (3,1) -> 2 (G_4 without (2,2)),
+//            (2,2) -> 3;
+//   sweep 1: the products of G_t, t = 5..8, into t - 5.
+// `first`: the chunk's first stage, whose first product into each accumulator overwrites it.  The
+// stage holds NS A tiles, then NS B tiles.  Unrolled: every descriptor is the stage's plus a
+// constant.
+template <int S, int SWEEP>
+__device__ __forceinline__ void issue_sweep_mmas(uint32_t tmem, uint64_t da, uint64_t db, bool first, uint32_t idesc) {
+	constexpr int t0 = SWEEP == 0 ? 2 : 5, t1 = SWEEP == 0 ? 4 : S + 1;
 #pragma unroll
-	for (int t = 2; t <= S + 1; t++) {
+	for (int t = t0; t <= t1; t++) {
 		const int ilo = t - S > 1 ? t - S : 1, ihi = t - 1 < S ? t - 1 : S;
 #pragma unroll
 		for (int i = ilo; i <= ihi; i++) {
 			const int j = t - i;
-			const bool own = t == 4 && i == 2;
-			const uint32_t d = tmem + (uint32_t) (own ? S : t - 2) * kBN;
-			const uint64_t ad = da + (uint64_t) (((i - 1) * kBM * kBK * 2) >> 4);
-			const uint64_t bd = db + (uint64_t) (((j - 1) * kBN * kBK * 2) >> 4);
+			const bool own = SWEEP == 0 && t == 4 && i == 2;
+			const int acc = SWEEP == 0 ? (own ? 3 : t - 2) : t - 5;
+			const uint32_t d = tmem + (uint32_t) acc * kBN;
+			const uint64_t ad = da + (uint64_t) (((i - 1) * kTile) >> 4);
+			const uint64_t bd = db + (uint64_t) (((j - 1) * kTile) >> 4);
 			const uint32_t accum = (first && (own || i == ilo)) ? 0u : 1u;
 			asm volatile("{ .reg .pred p; setp.ne.b32 p, %4, 0; tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p; }"
 			             ::"r"(d), "l"(ad), "l"(bd), "r"(idesc), "r"(accum));
 		}
 	}
-}
-
-// an int64 of magnitude below 2^51 as a double, exactly: added to the bit pattern of 1.5 * 2^52 it
-// lands in the low mantissa bits, and one FP64 subtraction removes the offset
-__device__ __forceinline__ double i64_to_double(long long x) {
-	return __longlong_as_double(x + 0x4338000000000000ll) - 0x1.8p52;
-}
-
-// 2^k for a normal-range k, built from its bit pattern (an exact scaling, no library call)
-__device__ __forceinline__ double pow2i(int k) {
-	return k >= -1022 && k <= 1023 ? __longlong_as_double((long long) (k + 1023) << 52) : ldexp(1., k);
 }
 
 }  // namespace
@@ -229,40 +246,44 @@ __global__ void tc_split_rows_kernel(const double2 *__restrict__ state, TcArgs a
 		split7(v.y, epi, sq);
 #pragma unroll
 		for (int i = 0; i < S; i++) {
-			a.a_slices[((size_t) i * a.mp + r) * a.kp + s] = sp[i];
-			a.a_slices[((size_t) i * a.mp + r + 1) * a.kp + s] = sq[i];
+			a.a_slices[tc_slice_index(i, (int) (s >> 4), a.mp, r, (int) (s & 15), S)] = sp[i];
+			a.a_slices[tc_slice_index(i, (int) (s >> 4), a.mp, r + 1, (int) (s & 15), S)] = sq[i];
 		}
 	}
 }
 
-// 8 warps: warps w and w + 4 read the same 32 rows of the tile (TMEM lane quarter w mod 4), each
-// one half of the 64 columns, so the FP64 read-out and epilogue work of a thread is halved and
-// every scheduler has two warps to interleave
-constexpr int kThreads = 256, kCols = kBN / 2;
+// 16 warps: warps w, w + 4, w + 8 and w + 12 read the same 32 rows of the tile (TMEM lane quarter
+// w mod 4), each a quarter of the 128 columns: a thread's exact row sums (one int64 per column)
+// fit in its 128 registers
+constexpr int kWarps = 16, kThreads = 32 * kWarps, kCols = kBN / (kWarps / 4);
+constexpr int kProducer = 32;   // lane 0 of warp 1 issues the copies; thread 0 issues the MMAs
 
 template <int S>
 __global__ void __launch_bounds__(kThreads, 1)
-tc_projection_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b, const TcArgs a) {
+tc_projection_kernel(const TcArgs a) {
 	extern __shared__ __align__(1024) unsigned char smem_raw[];
 	unsigned char *smem = (unsigned char *) (((uintptr_t) smem_raw + 1023) & ~(uintptr_t) 1023);
-	constexpr int kS = stages<S>();
-	__shared__ __align__(8) unsigned long long bars[2 * kS + 2];   // full[kS], empty[kS], acc, test
+	constexpr int kS0 = sweep_stages(sweep_slices(S, 0)), kS1 = sweep_stages(sweep_slices(S, 1));
+	// full and empty barriers of sweep 0, then of sweep 1, then acc, test
+	constexpr int kBarFull0 = 0, kBarEmpty0 = kS0, kBarFull1 = 2 * kS0, kBarEmpty1 = 2 * kS0 + kS1;
+	constexpr int kBarAcc = 2 * (kS0 + kS1), kBars = kBarAcc + 2;
+	__shared__ __align__(8) unsigned long long bars[kBars];
 	__shared__ uint32_t tmem_slot;
-	__shared__ int s_fail;
+	__shared__ int s_fail, s_issued;
 	__shared__ double s_w[kBN];   // per column of the tile: omega_k^2 (weight of the phi rows)
 	__shared__ int s_cexp[kBN];   // per column: the eigenvector's power-of-two exponent
 	const int tid = threadIdx.x, warp = tid >> 5;
 	const int rl = (warp & 3) * 32 + (tid & 31);   // this thread's row of the tile (its TMEM lane)
-	const int half = warp >> 2;                    // its columns: [kCols half, kCols (half + 1))
+	const int part = warp >> 2;                    // its columns: [kCols part, kCols (part + 1))
 	// tiles numbered with the column tiles fastest (see the header)
 	const int col_tiles = a.np / kBN;
 	const int row_tile = (int) (blockIdx.x / col_tiles), col_tile = (int) (blockIdx.x % col_tiles);
 	const int row0 = row_tile * kBM, col0 = col_tile * kBN;
-	const uint32_t full0 = smem_u32(&bars[0]), empty0 = smem_u32(&bars[kS]), accb = smem_u32(&bars[2 * kS]);
+	const uint32_t accb = smem_u32(&bars[kBarAcc]);
 	if (tid == 0) {
-		for (int i = 0; i < 2 * kS + 2; i++) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&bars[i])));
+		for (int i = 0; i < kBars; i++) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&bars[i])));
 		asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-		s_fail = 0;
+		s_fail = 0, s_issued = 0;
 	}
 	if (warp == 0) {
 		asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_slot)),
@@ -275,7 +296,7 @@ tc_projection_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_con
 		s_cexp[tid] = k < (int) a.n ? a.col_exp[k] : 0;
 	}
 	// tests only: a wait that runs out (nothing arrives at the test barrier) takes the failure path
-	if (a.wait_test && tid == 0 && !mbar_wait(smem_u32(&bars[2 * kS + 1]), 0, a.wait_ns)) s_fail = 1;
+	if (a.wait_test && tid == 0 && !mbar_wait(smem_u32(&bars[kBarAcc + 1]), 0, a.wait_ns)) s_fail = 1;
 	asm volatile("tcgen05.fence::before_thread_sync;");
 	__syncthreads();
 	asm volatile("tcgen05.fence::after_thread_sync;");
@@ -283,154 +304,180 @@ tc_projection_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_con
 
 	const int nk = a.kp / kBK;   // stages of K
 	const int per_chunk = kChunkK / kBK;
-	constexpr uint32_t kStageA = stage_a<S>(), kStageBytes = stage_bytes<S>();
-	auto stage_ptr = [&](int s) { return smem + (size_t) s * kStageBytes; };
-	int issued = 0, consumed = 0;    // thread 0: stages loaded / stages whose load has landed
-	bool committed = false;          // thread 0: the current chunk's MMAs are committed to accb
-	auto load_stage = [&](int it, int s) {
-		issued = it + 1;
-		const uint32_t full = full0 + 8 * s;
-		asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(full), "r"(kStageBytes) : "memory");
-		unsigned char *base = stage_ptr(s);
-		for (int i = 0; i < S; i++) {
-			tma_load(smem_u32(base + (size_t) i * kBM * kBK * 2), &map_a, it * kBK, i * a.mp + row0, full);
-			tma_load(smem_u32(base + kStageA + (size_t) i * kBN * kBK * 2), &map_b, it * kBK, i * a.np + col0, full);
-		}
-	};
+	// thread 0's bookkeeping for the failure path: the sweep's barriers and stage count, stages
+	// landed (the producer's loads: s_issued), and whether the current chunk's MMAs are committed
+	uint32_t cur_full = smem_u32(&bars[kBarFull0]);
+	int cur_stages = kS0, consumed = 0;
+	bool committed = false;
+	int rounds = 0;   // chunks read out so far (both sweeps): the parity of accb's next phase
 
-	double acc[kCols];
+	// this thread's row of P over its columns: the current sweep's exact group sums (hi: units of
+	// 2^-32, below 2^49 over 256 chunks; lo: units of 2^-64, below 2^57)
+	long long acc[kCols];
 #pragma unroll
-	for (int c = 0; c < kCols; c++) acc[c] = 0.;
+	for (int c = 0; c < kCols; c++) acc[c] = 0;
 	const uint32_t lane_base = (uint32_t) ((warp & 3) * 32) << 16;
-	int chunks = 0;
-	for (int c0 = 0; c0 < nk; c0 += per_chunk, chunks++) {
-		const int c1 = min(nk, c0 + per_chunk);
-		if (tid == 0 && !s_fail) {
-			bool ok = true;
-			committed = false;
-			if (c0 == 0)
-				for (int it = 0; it < kS && it < nk; it++) load_stage(it, it);
-			for (int it = c0; it < c1 && ok; it++) {
-				const int s = it % kS;
-				if (!mbar_wait(full0 + 8 * s, (it / kS) & 1, a.wait_ns)) {
-					ok = false;
-					break;
-				}
-				consumed = it + 1;
-				asm volatile("tcgen05.fence::after_thread_sync;");
-				const uint32_t sa = smem_u32(stage_ptr(s));
-				issue_stage_mmas<S>(tmem, smem_desc(sa), smem_desc(sa + kStageA), it == c0, kIdesc);
-				asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(empty0 + 8 * s)
-				             : "memory");
-				// refill the previous stage once its MMAs are done (this stage's are queued behind them)
-				const int prev = it - 1;
-				if (prev >= 0 && prev + kS < nk) {
-					const int ps = prev % kS;
-					if (!mbar_wait(empty0 + 8 * ps, (prev / kS) & 1, a.wait_ns)) {
+
+	auto sweep = [&](auto sweep_tag) {
+		constexpr int W = decltype(sweep_tag)::value;
+		constexpr int NS = sweep_slices(S, W), KS = W == 0 ? kS0 : kS1;
+		constexpr uint32_t kStageBytes = sweep_stage_bytes(NS);
+		const uint32_t full0 = smem_u32(&bars[W == 0 ? kBarFull0 : kBarFull1]);
+		const uint32_t empty0 = smem_u32(&bars[W == 0 ? kBarEmpty0 : kBarEmpty1]);
+		auto stage_ptr = [&](int s) { return smem + (size_t) s * kStageBytes; };
+		auto load_stage = [&](int it, int s) {   // the producer thread
+			s_issued = it + 1;
+			const uint32_t full = full0 + 8 * s;
+			asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(full), "r"(kStageBytes) : "memory");
+			unsigned char *base = stage_ptr(s);
+			bulk_load(smem_u32(base), a.a_slices + tc_slice_index(0, it, a.mp, row0, 0, S), NS * kTile, full);
+			bulk_load(smem_u32(base + (size_t) NS * kTile), a.b_slices + tc_slice_index(0, it, a.np, col0, 0, S), NS * kTile,
+			          full);
+		};
+		if (tid == 0) cur_full = full0, cur_stages = KS, consumed = 0;
+		if (tid == kProducer) s_issued = 0;
+		for (int c0 = 0; c0 < nk; c0 += per_chunk) {
+			const int c1 = min(nk, c0 + per_chunk);
+			if (tid == kProducer && !s_fail) {
+				// the loads: the first KS stages, then stage it + KS into stage it's buffer once the
+				// MMAs that read stage it are done
+				bool ok = true;
+				if (c0 == 0)
+					for (int it = 0; it < KS && it < nk; it++) load_stage(it, it);
+				for (int it = c0; it < c1 && it + KS < nk; it++) {
+					const int s = it % KS;
+					if (!mbar_wait(empty0 + 8 * s, (it / KS) & 1, a.wait_ns)) {
 						ok = false;
 						break;
 					}
-					load_stage(prev + kS, ps);
+					load_stage(it + KS, s);
+				}
+				if (!ok) s_fail = 1;
+			}
+			if (tid == 0 && !s_fail) {
+				// the MMAs: each stage as soon as it has landed, then its buffer released to the loads
+				bool ok = true;
+				committed = false;
+				for (int it = c0; it < c1; it++) {
+					const int s = it % KS;
+					if (!mbar_wait(full0 + 8 * s, (it / KS) & 1, a.wait_ns)) {
+						ok = false;
+						break;
+					}
+					consumed = it + 1;
+					asm volatile("tcgen05.fence::after_thread_sync;");
+					const uint32_t sa = smem_u32(stage_ptr(s));
+					issue_sweep_mmas<S, W>(tmem, smem_desc(sa), smem_desc(sa + NS * kTile), it == c0, kIdesc);
+					asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(empty0 + 8 * s)
+					             : "memory");
+				}
+				if (ok) {
+					asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(accb)
+					             : "memory");
+					committed = true;
+				} else {
+					s_fail = 1;
 				}
 			}
-			if (ok) {
-				asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(accb)
-				             : "memory");
-				committed = true;
-			} else {
-				s_fail = 1;
-			}
-		}
-		// every thread: wait for the chunk's MMAs, then add its groups into the FP64 row sums
-		if (!s_fail && !mbar_wait_sleep(accb, chunks & 1, a.wait_ns)) s_fail = 1;
-		__syncthreads();
-		if (s_fail) break;
-		asm volatile("tcgen05.fence::after_thread_sync;");
-		// the exact integer group sums, folded with shifts into two int64 halves (hi: t = 2..4 in units
-		// of 2^-32, below 2^41; lo: t = 5..8 in units of 2^-64, below 2^49: both exact in FP64), then
-		// two FMAs per column into the FP64 row sums.  Accumulators are read four at a time, one wait
-		// for the four loads.
-		constexpr int kGroups = S + 1;   // accumulators: G_2..G_{S+1} and the (2,2) part of G_4
+			// every thread: wait for the chunk's MMAs, then add its four groups into the row sums,
+			// shifted to the sweep's unit (no FP64 operation); accumulators read two per wait
+			if (!s_fail && !mbar_wait_sleep(accb, rounds & 1, a.wait_ns)) s_fail = 1;
+			__syncthreads();
+			if (s_fail) return;
+			asm volatile("tcgen05.fence::after_thread_sync;");
 #pragma unroll
-		for (int sg = 0; sg < kCols / 8; sg++) {
-			const int seg = half * (kCols / 8) + sg;   // 8-column segment of the tile
-			long long hi[8], lo[8];
+			for (int sg = 0; sg < kCols / 8; sg++) {
+				const int seg = part * (kCols / 8) + sg;   // 8-column segment of the tile
 #pragma unroll
-			for (int j = 0; j < 8; j++) hi[j] = 0, lo[j] = 0;
+				for (int g0 = 0; g0 < 4; g0 += 2) {
+					uint32_t v[2][8];
+					tmem_ld8(tmem + lane_base + (uint32_t) g0 * kBN + seg * 8, v[0]);
+					tmem_ld8(tmem + lane_base + (uint32_t) (g0 + 1) * kBN + seg * 8, v[1]);
+					tmem_wait_ld();
 #pragma unroll
-			for (int g0 = 0; g0 < kGroups; g0 += 4) {
-				uint32_t v[4][8];
+					for (int q = 0; q < 2; q++) {
+						const int g = g0 + q;
+						// sweep 0: G_2 << 16, G_3 << 8, G_4 parts << 0; sweep 1: G_t << 8 (8 - t)
+						const int shift = W == 0 ? (g == 0 ? 16 : g == 1 ? 8 : 0) : 8 * (3 - g);
 #pragma unroll
-				for (int q = 0; q < 4; q++)
-					if (g0 + q < kGroups) tmem_ld8(tmem + lane_base + (uint32_t) (g0 + q) * kBN + seg * 8, v[q]);
-				tmem_wait_ld();
-#pragma unroll
-				for (int q = 0; q < 4; q++) {
-					const int grp = g0 + q;
-					if (grp >= kGroups) break;
-					const int tt = grp == S ? 4 : grp + 2;   // accumulator S: the (2,2) part of G_4
-#pragma unroll
-					for (int j = 0; j < 8; j++) {
-						const long long g = __float2int_rn(__uint_as_float(v[q][j]));   // below 2^26: a 32-bit conversion
-						if (tt <= 4) hi[j] += g << (8 * (4 - tt));
-						else lo[j] += g << (8 * (8 - tt));
+						for (int j = 0; j < 8; j++) {
+							const long long gv = __float2int_rn(__uint_as_float(v[q][j]));   // below 2^26: a 32-bit conversion
+							acc[sg * 8 + j] += gv << shift;
+						}
 					}
 				}
 			}
-#pragma unroll
-			for (int j = 0; j < 8; j++) {
-				double &x = acc[sg * 8 + j];
-				x = fma(i64_to_double(hi[j]), 0x1p-32, x);
-				if constexpr (S + 1 > 4) x = fma(i64_to_double(lo[j]), 0x1p-64, x);
-			}
+			rounds++;
+			asm volatile("tcgen05.fence::before_thread_sync;");
+			__syncthreads();
 		}
-		asm volatile("tcgen05.fence::before_thread_sync;");
-		__syncthreads();
+	};
+
+	// parked hi sums of this thread, column-major within the tile ([col][row]): the 32 threads of a
+	// warp, 32 consecutive rows, store and load 256 contiguous bytes per column
+	long long *park = a.park + ((size_t) blockIdx.x * kBN + part * kCols) * kBM + rl;
+	sweep(std::integral_constant<int, 0>{});
+	if constexpr (S == kSlicesFull) {
+		if (!s_fail) {
+#pragma unroll
+			for (int c = 0; c < kCols; c++) park[c * kBM] = acc[c], acc[c] = 0;
+			sweep(std::integral_constant<int, 1>{});
+		}
 	}
 
-	// epilogue: this thread's row r of P, squared and weighted, summed over the tile's rows.  The
-	// buffer (over the finished stages) is column-major with a padded stride: the rows' stores and
-	// the column sums' loads are both free of bank conflicts.
+	// epilogue: this thread's row r of P, squared, into a column-major buffer with a padded stride
+	// (over the finished stages; stores and column loads free of bank conflicts); then every thread
+	// sums a quarter of a column's rows, phi rows and pi rows apart, and one thread per column adds
+	// the four quarters in a fixed order: e_k = omega_k^2 sum_phi + sum_pi
 	constexpr int kRedStride = kBM + 1;
-	static_assert(kBN * kRedStride * sizeof(double) <= (size_t) kS * kStageBytes, "reduction buffer exceeds the stages");
-	static_assert((size_t) kS * kStageBytes + 1024 + 1024 <= 227 * 1024, "shared memory above 227 KB");
-	double *red = reinterpret_cast<double *>(smem);   // [64][129]
+	double *red = reinterpret_cast<double *>(smem);                            // [128][129]
+	double2 *quarter = reinterpret_cast<double2 *>(smem + kBN * kRedStride * 8);   // [4][128] {phi, pi}
+	static_assert(kBN * kRedStride * 8 + 4 * kBN * 16 <= kStageMem, "reduction buffers exceed the stages");
+	static_assert(kStageMem + 1024 + 2048 <= 227 * 1024, "shared memory above 227 KB");
+	static_assert(kThreads == 4 * kBN, "four threads per column");
 	const int r = row0 + rl;
-	const bool phi = (r & 1) == 0;
 	const int er = r < 2 * (int) a.copies ? a.row_exp[r] : 0;
 	if (!s_fail) {
 #pragma unroll
 		for (int c = 0; c < kCols; c++) {
-			const int col = half * kCols + c;
-			double p = 0., w = 1.;
+			const int col = part * kCols + c;
+			double p2 = 0.;
 			if (col0 + col < (int) a.n) {
-				p = er == kNonFiniteRow ? __longlong_as_double(0x7ff8000000000000ll) : acc[c] * pow2i(er + s_cexp[col]);
-				if (phi) w = s_w[col];
+				const long long hi = S == kSlicesFull ? park[c * kBM] : acc[c], lo = S == kSlicesFull ? acc[c] : 0;
+				p2 = er == kNonFiniteRow ? __longlong_as_double(0x7ff8000000000000ll)
+				                         : fixed128_square_to_double(hi, lo, er + s_cexp[col]);
 			}
-			red[col * kRedStride + rl] = w * p * p;
+			red[col * kRedStride + rl] = p2;
 		}
+	}
+	__syncthreads();
+	{
+		// rows 32 q .. 32 q + 31 of column tid mod 128; rows 0 and 2 mod 4 are phi rows
+		const int cc = tid & (kBN - 1), q = tid >> 7;
+		const double *col = red + cc * kRedStride + 32 * q;
+		double s0 = 0., s1 = 0., s2 = 0., s3 = 0.;
+#pragma unroll
+		for (int rr = 0; rr < 32; rr += 4) s0 += col[rr], s1 += col[rr + 1], s2 += col[rr + 2], s3 += col[rr + 3];
+		quarter[q * kBN + cc] = make_double2(s0 + s2, s1 + s3);
 	}
 	__syncthreads();
 	if (tid < kBN) {
 		const int k = col0 + tid;
 		if (k < (int) a.n) {
-			// four interleaved partial sums in a fixed order, then added pairwise
-			const double *col = red + tid * kRedStride;
-			double s0 = 0., s1 = 0., s2 = 0., s3 = 0.;
-			for (int rr = 0; rr < kBM; rr += 4) s0 += col[rr], s1 += col[rr + 1], s2 += col[rr + 2], s3 += col[rr + 3];
-			const double s = (s0 + s1) + (s2 + s3);
-			a.partials[(size_t) row_tile * a.n + k] = s_fail ? __longlong_as_double(0x7ff8000000000000ll) : s;
+			const double2 q0 = quarter[tid], q1 = quarter[kBN + tid], q2 = quarter[2 * kBN + tid], q3 = quarter[3 * kBN + tid];
+			const double e = s_w[tid] * ((q0.x + q1.x) + (q2.x + q3.x)) + ((q0.y + q1.y) + (q2.y + q3.y));
+			a.partials[(size_t) row_tile * a.n + k] = s_fail ? __longlong_as_double(0x7ff8000000000000ll) : e;
 		}
 	}
 	if (tid == 0 && s_fail) {
-		// after a timeout: wait (each wait bounded again) for the loads this block issued and has not
-		// consumed, then for every MMA it issued, so that nothing lands in shared memory or TMEM after
-		// the block has released them
-		for (int it = consumed; it < issued; it++) mbar_wait(full0 + 8 * (it % kS), (it / kS) & 1, a.wait_ns);
+		// after a timeout: wait (each wait bounded again) for the loads this block issued in the
+		// current sweep and has not consumed, then for every MMA it issued, so that nothing lands in
+		// shared memory or TMEM after the block has released them
+		for (int it = consumed; it < s_issued; it++) mbar_wait(cur_full + 8 * (it % cur_stages), (it / cur_stages) & 1, a.wait_ns);
 		if (!committed)
 			asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(accb)
 			             : "memory");
-		mbar_wait(accb, chunks & 1, a.wait_ns);
+		mbar_wait(accb, rounds & 1, a.wait_ns);
 		atomicOr(a.status, 1);
 	}
 	asm volatile("tcgen05.fence::before_thread_sync;");
@@ -438,23 +485,18 @@ tc_projection_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_con
 	if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols));
 }
 
-size_t tc_projection_smem(int slices) {
-	return slices == 3 ? (size_t) stages<3>() * stage_bytes<3>() + 1024
-	                   : (size_t) stages<kSlicesFull>() * stage_bytes<kSlicesFull>() + 1024;
-}
+size_t tc_projection_smem(int) { return kStageMem + 1024; }
 
-cudaError_t launch_tc_projection(const TcArgs &a, const void *map_a, const void *map_b, const double2 *state,
-                                 cudaStream_t stream) {
+cudaError_t launch_tc_projection(const TcArgs &a, const double2 *state, cudaStream_t stream) {
 	count_launch(2);
 	const dim3 grid((unsigned) ((size_t) (a.mp / kBM) * (a.np / kBN)));
-	const CUtensorMap &ma = *static_cast<const CUtensorMap *>(map_a), &mb = *static_cast<const CUtensorMap *>(map_b);
 	const unsigned split_blocks = (unsigned) ((a.copies + 7) / 8);
 	if (a.slices == 3) {
 		tc_split_rows_kernel<3><<<split_blocks, 256, 0, stream>>>(state, a);
-		tc_projection_kernel<3><<<grid, kThreads, tc_projection_smem(3), stream>>>(ma, mb, a);
+		tc_projection_kernel<3><<<grid, kThreads, tc_projection_smem(3), stream>>>(a);
 	} else {
 		tc_split_rows_kernel<kSlicesFull><<<split_blocks, 256, 0, stream>>>(state, a);
-		tc_projection_kernel<kSlicesFull><<<grid, kThreads, tc_projection_smem(kSlicesFull), stream>>>(ma, mb, a);
+		tc_projection_kernel<kSlicesFull><<<grid, kThreads, tc_projection_smem(kSlicesFull), stream>>>(a);
 	}
 	return cudaGetLastError();
 }
