@@ -29,15 +29,16 @@
 // GB300: N = 32 and 64 take as long as N = 128; N = 256 runs at the full tensor rate), so the MMAs
 // must be wide.  Eight accumulators of N = 128 columns would need 1024 TMEM columns, twice the 512
 // an SM has, so one CTA (128 rows x 128 modes, 16 warps) sweeps K twice with four accumulators:
-//   sweep 0: G_2, G_3, G_4 without (2,2), and (2,2): 6 MMAs per 16-site stage, slices 1..3;
-//   sweep 1: G_5, G_6, G_7, G_8: 22 MMAs per stage, slices 1..7.
+//   sweep 0: G_2, G_3, G_4 without (2,2), and (2,2): 6 MMAs per 16-site block, slices 1..3;
+//   sweep 1: G_5, G_6, G_7, G_8: 22 MMAs per block, slices 1..7.
 // Between the sweeps every thread parks its hi sums in a global scratch array and takes them back
-// for the conversion.  The slices are stored tiled and pre-swizzled (tc_slice_index), so a
-// pipeline stage (16 sites: 7 stages of 24 KB in sweep 0, 3 of 56 KB in sweep 1) is two bulk copies,
-// one for A's slices and one for B's.  Thread 32 issues the copies, refilling a stage's buffer as
-// soon as the MMAs that read it are done; thread 0 issues the MMAs (M = 128, N = 128, K = 16, BF16
-// in, FP32 in TMEM) as soon as a stage has landed.  Each tcgen05 or bulk-copy instruction costs
-// the issuing thread tens of cycles, so the two streams run on two threads.  Tiles are numbered with the 128-mode columns fastest: the CTAs resident at one
+// for the conversion.  The slices are stored tiled and pre-swizzled (tc_slice_index), so each
+// 16-site block of a pipeline stage is two bulk copies, one for A's slices and one for B's (sweep
+// 0: 4 stages of two blocks, 48 KB; sweep 1: 3 stages of one block, 56 KB).  Thread 32 issues the
+// copies, refilling a stage's buffer as soon as the MMAs that read it are done; thread 0 issues
+// the MMAs (M = 128, N = 128, K = 16, BF16 in, FP32 in TMEM) as soon as a stage has landed.  Each
+// tcgen05 or bulk-copy instruction costs the issuing thread tens of cycles, so the two streams run
+// on two threads.  Tiles are numbered with the 128-mode columns fastest: the CTAs resident at one
 // time share row tiles, so the slices of X come from DRAM once per sweep and the eigenvector
 // slices stay in L2.  Every wait is bounded: on a timeout the block records a status, writes NaN
 // into its partial row (the host then sees a non-finite entropy) and returns after freeing its
@@ -66,10 +67,13 @@ constexpr uint32_t kTile = kBM * kBK * 2;   // one slice tile of A or B: 128 row
 static_assert(kBN == kBM, "A and B tiles share one size");
 // slices a sweep reads, its stage size, and the stages that fit in the stage memory
 __host__ __device__ constexpr int sweep_slices(int S, int sweep) { return sweep == 0 ? (S < 3 ? S : 3) : S; }
-__host__ __device__ constexpr uint32_t sweep_stage_bytes(int ns) { return 2u * (uint32_t) ns * kTile; }
-constexpr uint32_t kStageMem = 168 * 1024;
-__host__ __device__ constexpr int sweep_stages(int ns) { return (int) (kStageMem / sweep_stage_bytes(ns)); }
-static_assert(sweep_stages(3) == 7 && sweep_stages(7) == 3, "stage geometry");
+// 16-site blocks per stage: sweep 0's products are few (6 per block), so its stages hold two blocks
+// and the per-stage costs (the wait, the commit) are paid once per 12 MMAs
+__host__ __device__ constexpr int sweep_blocks(int sweep) { return sweep == 0 ? 2 : 1; }
+__host__ __device__ constexpr uint32_t sweep_stage_bytes(int ns, int kb) { return 2u * (uint32_t) (ns * kb) * kTile; }
+constexpr uint32_t kStageMem = 200 * 1024;
+__host__ __device__ constexpr int sweep_stages(int ns, int kb) { return (int) (kStageMem / sweep_stage_bytes(ns, kb)); }
+static_assert(sweep_stages(3, 2) == 4 && sweep_stages(7, 1) == 3, "stage geometry");
 constexpr int kNonFiniteRow = 0x7fff;   // row exponent of a row holding inf or NaN
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t) __cvta_generic_to_shared(p); }
@@ -263,7 +267,7 @@ __global__ void __launch_bounds__(kThreads, 1)
 tc_projection_kernel(const TcArgs a) {
 	extern __shared__ __align__(1024) unsigned char smem_raw[];
 	unsigned char *smem = (unsigned char *) (((uintptr_t) smem_raw + 1023) & ~(uintptr_t) 1023);
-	constexpr int kS0 = sweep_stages(sweep_slices(S, 0)), kS1 = sweep_stages(sweep_slices(S, 1));
+	constexpr int kS0 = sweep_stages(sweep_slices(S, 0), sweep_blocks(0)), kS1 = sweep_stages(sweep_slices(S, 1), sweep_blocks(1));
 	// full and empty barriers of sweep 0, then of sweep 1, then acc, test
 	constexpr int kBarFull0 = 0, kBarEmpty0 = kS0, kBarFull1 = 2 * kS0, kBarEmpty1 = 2 * kS0 + kS1;
 	constexpr int kBarAcc = 2 * (kS0 + kS1), kBars = kBarAcc + 2;
@@ -302,8 +306,7 @@ tc_projection_kernel(const TcArgs a) {
 	asm volatile("tcgen05.fence::after_thread_sync;");
 	const uint32_t tmem = tmem_slot;
 
-	const int nk = a.kp / kBK;   // stages of K
-	const int per_chunk = kChunkK / kBK;
+	const int nkb = a.kp / kBK;   // 16-site blocks of K
 	// thread 0's bookkeeping for the failure path: the sweep's barriers and stage count, stages
 	// landed (the producer's loads: s_issued), and whether the current chunk's MMAs are committed
 	uint32_t cur_full = smem_u32(&bars[kBarFull0]);
@@ -320,19 +323,27 @@ tc_projection_kernel(const TcArgs a) {
 
 	auto sweep = [&](auto sweep_tag) {
 		constexpr int W = decltype(sweep_tag)::value;
-		constexpr int NS = sweep_slices(S, W), KS = W == 0 ? kS0 : kS1;
-		constexpr uint32_t kStageBytes = sweep_stage_bytes(NS);
+		constexpr int NS = sweep_slices(S, W), KS = W == 0 ? kS0 : kS1, KB = sweep_blocks(W);
+		constexpr uint32_t kStageBytes = sweep_stage_bytes(NS, KB), kBlockBytes = 2u * NS * kTile;
+		const int nk = (nkb + KB - 1) / KB;      // stages of the sweep (the last one may hold one block)
+		constexpr int per_chunk = kChunkK / (kBK * KB);
 		const uint32_t full0 = smem_u32(&bars[W == 0 ? kBarFull0 : kBarFull1]);
 		const uint32_t empty0 = smem_u32(&bars[W == 0 ? kBarEmpty0 : kBarEmpty1]);
 		auto stage_ptr = [&](int s) { return smem + (size_t) s * kStageBytes; };
+		// a stage: per block, NS A tiles then NS B tiles
 		auto load_stage = [&](int it, int s) {   // the producer thread
 			s_issued = it + 1;
 			const uint32_t full = full0 + 8 * s;
-			asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(full), "r"(kStageBytes) : "memory");
+			const int blocks = min(KB, nkb - it * KB);
+			asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(full), "r"(blocks * kBlockBytes) : "memory");
 			unsigned char *base = stage_ptr(s);
-			bulk_load(smem_u32(base), a.a_slices + tc_slice_index(0, it, a.mp, row0, 0, S), NS * kTile, full);
-			bulk_load(smem_u32(base + (size_t) NS * kTile), a.b_slices + tc_slice_index(0, it, a.np, col0, 0, S), NS * kTile,
-			          full);
+			for (int b = 0; b < blocks; b++) {
+				const int kb = it * KB + b;
+				unsigned char *blk = base + (size_t) b * kBlockBytes;
+				bulk_load(smem_u32(blk), a.a_slices + tc_slice_index(0, kb, a.mp, row0, 0, S), NS * kTile, full);
+				bulk_load(smem_u32(blk + (size_t) NS * kTile), a.b_slices + tc_slice_index(0, kb, a.np, col0, 0, S), NS * kTile,
+				          full);
+			}
 		};
 		if (tid == 0) cur_full = full0, cur_stages = KS, consumed = 0;
 		if (tid == kProducer) s_issued = 0;
@@ -367,7 +378,12 @@ tc_projection_kernel(const TcArgs a) {
 					consumed = it + 1;
 					asm volatile("tcgen05.fence::after_thread_sync;");
 					const uint32_t sa = smem_u32(stage_ptr(s));
-					issue_sweep_mmas<S, W>(tmem, smem_desc(sa), smem_desc(sa + NS * kTile), it == c0, kIdesc);
+					const int blocks = min(KB, nkb - it * KB);
+#pragma unroll
+					for (int b = 0; b < KB; b++)
+						if (b < blocks)
+							issue_sweep_mmas<S, W>(tmem, smem_desc(sa + b * kBlockBytes), smem_desc(sa + b * kBlockBytes + NS * kTile),
+							                       it == c0 && b == 0, kIdesc);
 					asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(empty0 + 8 * s)
 					             : "memory");
 				}
