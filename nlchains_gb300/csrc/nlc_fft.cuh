@@ -100,16 +100,28 @@ __device__ __forceinline__ void stockham_pass(const FftPlanDev &P, int r, int Ns
 		for (int j = t; j < n; j += T) x[j] = pre(j, x[j]);
 		team_sync<BLOCK>();
 	}
+	// the four outputs of a radix-4 butterfly, stored in an order rotated by b / max(Ns, 2): with
+	// Ns < 8 the natural order puts the 8 threads of a 128-byte store phase on the same banks (Ns = 1:
+	// a 64-byte stride, 4-way; Ns = 4: runs of four 256 bytes apart, 2-way), the rotated one on 8
+	// different 16-byte bank groups.  The addresses written are the same.
+	auto store4 = [&](int o, int b, double2 X0, double2 X1, double2 X2, double2 X3) {
+		if (Ns >= 8) {
+			out(o, 0, X0), out(o, 1, X1), out(o, 2, X2), out(o, 3, X3);
+			return;
+		}
+		const int r = b / (Ns < 2 ? 2 : Ns);
+#pragma unroll
+		for (int i = 0; i < 4; i++) {
+			const int v = (i + r) & 3;
+			out(o, v, v == 0 ? X0 : v == 1 ? X1 : v == 2 ? X2 : X3);
+		}
+	};
 	if (p == 4) {
 		if (Ns == 1) {
 			for (int b = t; b < m; b += T) {
 				const double2 a0 = in(b, 0), a1 = in(b, 1), a2 = in(b, 2), a3 = in(b, 3);
 				const double2 b0 = cadd(a0, a2, k), b1 = csub(a0, a2, k), b2 = cadd(a1, a3, k), b3 = rot_mi<INV>(csub(a1, a3, k));
-				const int o = 4 * b;
-				out(o, 0, cadd(b0, b2, k));
-				out(o, 1, cadd(b1, b3, k));
-				out(o, 2, csub(b0, b2, k));
-				out(o, 3, csub(b1, b3, k));
+				store4(4 * b, b, cadd(b0, b2, k), cadd(b1, b3, k), csub(b0, b2, k), csub(b1, b3, k));
 			}
 		} else {
 			for (int b = t; b < m; b += T) {
@@ -124,11 +136,7 @@ __device__ __forceinline__ void stockham_pass(const FftPlanDev &P, int r, int Ns
 				// X1 = (A0 - A2) -+ i (A1 - A3), X3 = (A0 - A2) +- i (A1 - A3) (forward / inverse)
 				const double2 bm = make_double2(dfma(c1, p3.y, b1.x), dfma(-c1, p3.x, b1.y));   // b1 - i c1 p3
 				const double2 bp = make_double2(dfma(-c1, p3.y, b1.x), dfma(c1, p3.x, b1.y));   // b1 + i c1 p3
-				const int o = q * 4 * Ns + kk;
-				out(o, 0, fma2(c1, p2, b0));
-				out(o, 1, INV ? bp : bm);
-				out(o, 2, fma2(-c1, p2, b0));
-				out(o, 3, INV ? bm : bp);
+				store4(q * 4 * Ns + kk, b, fma2(c1, p2, b0), INV ? bp : bm, fma2(-c1, p2, b0), INV ? bm : bp);
 			}
 		}
 	} else if (p == 2) {
