@@ -515,8 +515,21 @@ def measure_projection(w, local, evolve_steps=1000):
             "max_rel_diff": diff, "tensor_entropies": ent_diffs("tensor"), "bf16x3_ms": res["bf16x3"][0],
             "bf16x3_max_rel_diff": diff3, "bf16x3_entropies": ent_diffs("bf16x3"),
             "flops": 4.0 * copies * n * n,
-            "method": "tcgen05 BF16 MMA, 7-slice split of X and of the eigenvectors, FP32 accumulation in TMEM, "
-                      "FP64 recombination, energy epilogue fused"}
+            # the 28 BF16 slice products of the 7-slice form, over the whole sample (split, projection
+            # and finish kernels), against the measured cuBLAS BF16 rate
+            "bf16_tflops": 28 * 4.0 * copies * n * n / (res["tensor"][0] * 1e-3) / 1e12,
+            "bf16_frac_of_measured_peak": 28 * 4.0 * copies * n * n / (res["tensor"][0] * 1e-3) / 1e12 / bf16_peak(),
+            "method": "tcgen05 BF16 MMA (M = N = 128), 7-slice split of X and of the eigenvectors, FP32 accumulation "
+                      "in TMEM read out every 256 sites, exact integer recombination, energy epilogue fused"}
+
+
+def bf16_peak():
+    """The measured burst BF16 rate of this GPU type (TFLOP/s), or the stated fallback."""
+    try:
+        with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["bf16_tflops"])
+    except (OSError, KeyError, ValueError):
+        return 1900.0
 
 
 def measure_eigensystem(w, sizes=(1024, 2048)):
