@@ -11,7 +11,6 @@
 #include <mutex>
 #include <tuple>
 
-#include <cuda.h>
 #include <sys/stat.h>
 
 #include "nlc_host.h"

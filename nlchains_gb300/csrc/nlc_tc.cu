@@ -43,7 +43,6 @@
 // slices stay in L2.  Every wait is bounded: on a timeout the block records a status, writes NaN
 // into its partial row (the host then sees a non-finite entropy) and returns after freeing its
 // tensor memory.
-#include <cuda.h>
 #include <cuda_bf16.h>
 
 #include <type_traits>
