@@ -151,13 +151,13 @@ __device__ __forceinline__ void tmem_ld8(uint32_t taddr, uint32_t (&r)[8]) {
 
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
-// One stage's slice products of a sweep into its four accumulators (128 TMEM columns each):
+// One 16-site block's slice products of a sweep into its four accumulators (128 TMEM columns each):
 //   sweep 0: (1,1) -> 0 (G_2), (1,2) (2,1) -> 1 (G_3), (1,3) (3,1) -> 2 (G_4 without (2,2)),
 //            (2,2) -> 3;
 //   sweep 1: the products of G_t, t = 5..8, into t - 5.
-// `first`: the chunk's first stage, whose first product into each accumulator overwrites it.  The
-// stage holds NS A tiles, then NS B tiles.  Unrolled: every descriptor is the stage's plus a
-// constant.
+// `first`: the chunk's first block, whose first product into each accumulator overwrites it.  In
+// shared memory the block is NS A tiles, then NS B tiles (da, db: their descriptors).  Unrolled:
+// every descriptor is the block's plus a constant.
 template <int S, int SWEEP>
 __device__ __forceinline__ void issue_sweep_mmas(uint32_t tmem, uint64_t da, uint64_t db, bool first, uint32_t idesc) {
 	constexpr int t0 = SWEEP == 0 ? 2 : 5, t1 = SWEEP == 0 ? 4 : S + 1;
