@@ -199,13 +199,23 @@ __device__ __forceinline__ void split7(double x, int e, uint16_t (&out)[7]) {
 	else if (shift > -63) F = (m + (1ll << (-shift - 1))) >> (-shift);
 	else F = 0;
 	if (bits < 0) F = -F;
+	// |sg| <= 256: exact in BF16; converted from 32 bits (a 64-bit conversion uses the FP64 pipe)
+	auto bf16 = [](int sg) { return uint16_t(__float_as_uint(__int2float_rn(sg)) >> 16); };
 #pragma unroll
-	for (int i = 0; i < 7; i++) {
+	for (int i = 0; i < 4; i++) {
 		const int pos = 8 * (6 - i);
-		const long long sg = pos ? (F + (1ll << (pos - 1))) >> pos : F;
+		const long long sg = (F + (1ll << (pos - 1))) >> pos;
 		F -= sg << pos;
-		// |sg| <= 256: exact in BF16; converted from 32 bits (a 64-bit conversion uses the FP64 pipe)
-		out[i] = uint16_t(__float_as_uint(__int2float_rn(int(sg))) >> 16);
+		out[i] = bf16(int(sg));
+	}
+	// after four digits the remainder lies in [-2^23, 2^23): the rest in 32-bit arithmetic
+	int f = int(F);
+#pragma unroll
+	for (int i = 4; i < 7; i++) {
+		const int pos = 8 * (6 - i);
+		const int sg = pos ? (f + (1 << (pos - 1))) >> pos : f;
+		f -= sg << pos;
+		out[i] = bf16(sg);
 	}
 }
 
@@ -247,11 +257,11 @@ __global__ void tc_split_rows_kernel(const double2 *__restrict__ state, TcArgs a
 		uint16_t sp[7], sq[7];
 		split7(v.x, ephi, sp);
 		split7(v.y, epi, sq);
+		// slice i lies 128 x 16 elements after slice i - 1; rows 2c and 2c + 1 share a tile and a
+		// swizzle phase, so the pi row is the phi row's position plus one row
+		uint16_t *dst = a.a_slices + tc_slice_index(0, (int) (s >> 4), a.mp, r, (int) (s & 15), S);
 #pragma unroll
-		for (int i = 0; i < S; i++) {
-			a.a_slices[tc_slice_index(i, (int) (s >> 4), a.mp, r, (int) (s & 15), S)] = sp[i];
-			a.a_slices[tc_slice_index(i, (int) (s >> 4), a.mp, r + 1, (int) (s & 15), S)] = sq[i];
-		}
+		for (int i = 0; i < S; i++) dst[i * 128 * 16] = sp[i], dst[i * 128 * 16 + 16] = sq[i];
 	}
 }
 
