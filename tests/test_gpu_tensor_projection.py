@@ -93,11 +93,12 @@ def test_bf16x3_projection_error_stated(gpu, n, copies):
     assert abs(w3 - w64) <= 1e-6 * max(1.0, abs(w64)) and abs(i3 - i64) <= 1e-6 * max(1.0, abs(i64))
 
 
-def test_projection_wait_timeout_reported(gpu, monkeypatch):
+# 256 and 700 sites: one and three read-out chunks per sweep
+@pytest.mark.parametrize("n,copies", [(256, 64), (700, 16)])
+def test_projection_wait_timeout_reported(gpu, monkeypatch, n, copies):
     """A projection whose bounded wait runs out (tests only: each block first waits 1 ms on a barrier
     nothing arrives at) reports NLC_ETIMEDOUT, not a blow-up, and leaves the context usable: a plan
     made afterwards without the test wait gives the normal result."""
-    n, copies = 256, 64
     masses = ic.masses_uniform(n, seed=9)
     state = ic.ddnkg_ensemble(masses, copies, 0.5, 8, seed=9)
     model = gpu.Model("dDNKG", n, copies, 0.05, masses=masses, beta=1.0)
