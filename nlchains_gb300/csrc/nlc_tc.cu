@@ -35,12 +35,13 @@
 // for the conversion.  The slices are stored tiled and pre-swizzled (tc_slice_index), so each
 // 16-site block of a pipeline stage is two bulk copies, one for A's slices and one for B's (sweep
 // 0: 4 stages of two blocks, 48 KB; sweep 1: 3 stages of one block, 56 KB).  Thread 32 issues the
-// copies, refilling a stage's buffer as soon as the MMAs that read it are done; thread 0 issues
-// the MMAs (M = 128, N = 128, K = 16, BF16 in, FP32 in TMEM) as soon as a stage has landed.  Each
-// tcgen05 or bulk-copy instruction costs the issuing thread tens of cycles, so the two streams run
-// on two threads.  Tiles are numbered with the 128-mode columns fastest: the CTAs resident at one
-// time share row tiles, so the slices of X come from DRAM once per sweep and the eigenvector
-// slices stay in L2.  Every wait is bounded: on a timeout the block records a status, writes NaN
+// copies, refilling a stage's buffer as soon as the MMAs that read it are done; threads 0 and 64
+// issue the MMAs (M = 128, N = 128, K = 16, BF16 in, FP32 in TMEM), each for two of the four
+// accumulators, as soon as a stage has landed.  Each tcgen05 or bulk-copy instruction costs the
+// issuing thread tens of cycles (one thread issues N = 128 MMAs at 0.83 of the tensor rate, two
+// at the full rate), so the three streams run on three threads.  Tiles are numbered with the
+// 128-mode columns fastest: the CTAs resident at one time share row tiles, so the slices of X come
+// from DRAM once per sweep and the eigenvector slices stay in L2.  Every wait is bounded: on a timeout the block records a status, writes NaN
 // into its partial row (the host then sees a non-finite entropy) and returns after freeing its
 // tensor memory.
 #include <cuda_bf16.h>
@@ -155,10 +156,15 @@ __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.
 //   sweep 0: (1,1) -> 0 (G_2), (1,2) (2,1) -> 1 (G_3), (1,3) (3,1) -> 2 (G_4 without (2,2)),
 //            (2,2) -> 3;
 //   sweep 1: the products of G_t, t = 5..8, into t - 5.
+// Two threads issue them, each the products of two accumulators (ISSUER 0: accumulators 0 and 1 in
+// sweep 0, 0 and 3 in sweep 1; ISSUER 1 the others: 3 + 3 and 11 + 11 MMAs per block).
 // `first`: the chunk's first block, whose first product into each accumulator overwrites it.  In
 // shared memory the block is NS A tiles, then NS B tiles (da, db: their descriptors).  Unrolled:
 // every descriptor is the block's plus a constant.
-template <int S, int SWEEP>
+template <int SWEEP>
+__host__ __device__ constexpr int mma_issuer(int acc) { return SWEEP == 0 ? (acc < 2 ? 0 : 1) : (acc == 0 || acc == 3 ? 0 : 1); }
+
+template <int S, int SWEEP, int ISSUER>
 __device__ __forceinline__ void issue_sweep_mmas(uint32_t tmem, uint64_t da, uint64_t db, bool first, uint32_t idesc) {
 	constexpr int t0 = SWEEP == 0 ? 2 : 5, t1 = SWEEP == 0 ? 4 : S + 1;
 #pragma unroll
@@ -169,6 +175,7 @@ __device__ __forceinline__ void issue_sweep_mmas(uint32_t tmem, uint64_t da, uin
 			const int j = t - i;
 			const bool own = SWEEP == 0 && t == 4 && i == 2;
 			const int acc = SWEEP == 0 ? (own ? 3 : t - 2) : t - 5;
+			if (mma_issuer<SWEEP>(acc) != ISSUER) continue;
 			const uint32_t d = tmem + (uint32_t) acc * kBN;
 			const uint64_t ad = da + (uint64_t) (((i - 1) * kTile) >> 4);
 			const uint64_t bd = db + (uint64_t) (((j - 1) * kTile) >> 4);
@@ -269,7 +276,9 @@ __global__ void tc_split_rows_kernel(const double2 *__restrict__ state, TcArgs a
 // w mod 4), each a quarter of the 128 columns: a thread's exact row sums (one int64 per column)
 // fit in its 128 registers
 constexpr int kWarps = 16, kThreads = 32 * kWarps, kCols = kBN / (kWarps / 4);
-constexpr int kProducer = 32;   // lane 0 of warp 1 issues the copies; thread 0 issues the MMAs
+// lane 0 of warp 1 issues the copies; lane 0 of warps 0 and 2 issue the MMAs (one tcgen05.mma costs
+// its issuing thread about 80 cycles; two issuing threads reach the full tensor rate with N = 128)
+constexpr int kProducer = 32, kMma1 = 64;
 
 template <int S>
 __global__ void __launch_bounds__(kThreads, 1)
@@ -294,7 +303,12 @@ tc_projection_kernel(const TcArgs a) {
 	const int row0 = row_tile * kBM, col0 = col_tile * kBN;
 	const uint32_t accb = smem_u32(&bars[kBarAcc]);
 	if (tid == 0) {
-		for (int i = 0; i < kBars; i++) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&bars[i])));
+		// a full barrier completes on the producer's arrival (with the bytes); empty and acc barriers on
+		// one commit from each MMA thread
+		for (int i = 0; i < kBars; i++) {
+			const bool two = (i >= kBarEmpty0 && i < kBarFull1) || (i >= kBarEmpty1 && i < kBarAcc) || i == kBarAcc;
+			asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&bars[i])), "r"(two ? 2 : 1));
+		}
 		asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 		s_fail = 0, s_issued = 0;
 	}
@@ -316,7 +330,7 @@ tc_projection_kernel(const TcArgs a) {
 	const uint32_t tmem = tmem_slot;
 
 	const int nkb = a.kp / kBK;   // 16-site blocks of K
-	// thread 0's bookkeeping for the failure path: the sweep's barriers and stage count, stages
+	// the MMA threads' bookkeeping for the failure path: the sweep's barriers and stage count, stages
 	// landed (the producer's loads: s_issued), and whether the current chunk's MMAs are committed
 	uint32_t cur_full = smem_u32(&bars[kBarFull0]);
 	int cur_stages = kS0, consumed = 0;
@@ -374,7 +388,7 @@ tc_projection_kernel(const TcArgs a) {
 				}
 				if (!ok) s_fail = 1;
 			}
-			if (tid == 0 && !s_fail) {
+			if ((tid == 0 || tid == kMma1) && !s_fail) {
 				// the MMAs: each stage as soon as it has landed, then its buffer released to the loads
 				bool ok = true;
 				committed = false;
@@ -389,10 +403,12 @@ tc_projection_kernel(const TcArgs a) {
 					const uint32_t sa = smem_u32(stage_ptr(s));
 					const int blocks = min(KB, nkb - it * KB);
 #pragma unroll
-					for (int b = 0; b < KB; b++)
-						if (b < blocks)
-							issue_sweep_mmas<S, W>(tmem, smem_desc(sa + b * kBlockBytes), smem_desc(sa + b * kBlockBytes + NS * kTile),
-							                       it == c0 && b == 0, kIdesc);
+					for (int b = 0; b < KB; b++) {
+						if (b >= blocks) break;
+						const uint64_t da = smem_desc(sa + b * kBlockBytes), db = smem_desc(sa + b * kBlockBytes + NS * kTile);
+						if (tid == 0) issue_sweep_mmas<S, W, 0>(tmem, da, db, it == c0 && b == 0, kIdesc);
+						else issue_sweep_mmas<S, W, 1>(tmem, da, db, it == c0 && b == 0, kIdesc);
+					}
 					asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(empty0 + 8 * s)
 					             : "memory");
 				}
@@ -494,16 +510,20 @@ tc_projection_kernel(const TcArgs a) {
 			a.partials[(size_t) row_tile * a.n + k] = s_fail ? __longlong_as_double(0x7ff8000000000000ll) : e;
 		}
 	}
-	if (tid == 0 && s_fail) {
-		// after a timeout: wait (each wait bounded again) for the loads this block issued in the
-		// current sweep and has not consumed, then for every MMA it issued, so that nothing lands in
-		// shared memory or TMEM after the block has released them
-		for (int it = consumed; it < s_issued; it++) mbar_wait(cur_full + 8 * (it % cur_stages), (it / cur_stages) & 1, a.wait_ns);
-		if (!committed)
+	if (s_fail) {
+		// after a timeout: each MMA thread commits what it issued in the current chunk (if it has not),
+		// then thread 0 waits (each wait bounded again) for the loads this block issued in the current
+		// sweep and has not consumed, and for every MMA, so that nothing lands in shared memory or TMEM
+		// after the block has released them
+		if ((tid == 0 || tid == kMma1) && !committed)
 			asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(accb)
 			             : "memory");
-		mbar_wait(accb, rounds & 1, a.wait_ns);
-		atomicOr(a.status, 1);
+		if (tid == 0) {
+			for (int it = consumed; it < s_issued; it++)
+				mbar_wait(cur_full + 8 * (it % cur_stages), (it / cur_stages) & 1, a.wait_ns);
+			mbar_wait(accb, rounds & 1, a.wait_ns);
+			atomicOr(a.status, 1);
+		}
 	}
 	asm volatile("tcgen05.fence::before_thread_sync;");
 	__syncthreads();
