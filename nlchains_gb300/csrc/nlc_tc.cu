@@ -479,16 +479,24 @@ tc_projection_kernel(const TcArgs a) {
 	const int r = row0 + rl;
 	const int er = r < 2 * (int) a.copies ? a.row_exp[r] : 0;
 	if (!s_fail) {
+		// eight columns at a time: their parked sums loaded together, so a warp waits for L2 once per
+		// eight columns rather than once per column
 #pragma unroll
-		for (int c = 0; c < kCols; c++) {
-			const int col = part * kCols + c;
-			double p2 = 0.;
-			if (col0 + col < (int) a.n) {
-				const long long hi = S == kSlicesFull ? park[c * kBM] : acc[c], lo = S == kSlicesFull ? acc[c] : 0;
-				p2 = er == kNonFiniteRow ? __longlong_as_double(0x7ff8000000000000ll)
-				                         : fixed128_square_to_double(hi, lo, er + s_cexp[col]);
+		for (int c0 = 0; c0 < kCols; c0 += 8) {
+			long long hv[8];
+#pragma unroll
+			for (int j = 0; j < 8; j++) hv[j] = S == kSlicesFull ? __ldcg(park + (c0 + j) * kBM) : acc[c0 + j];
+#pragma unroll
+			for (int j = 0; j < 8; j++) {
+				const int c = c0 + j, col = part * kCols + c;
+				double p2 = 0.;
+				if (col0 + col < (int) a.n) {
+					const long long lo = S == kSlicesFull ? acc[c] : 0;
+					p2 = er == kNonFiniteRow ? __longlong_as_double(0x7ff8000000000000ll)
+					                         : fixed128_square_to_double(hv[j], lo, er + s_cexp[col]);
+				}
+				red[col * kRedStride + rl] = p2;
 			}
-			red[col * kRedStride + rl] = p2;
 		}
 	}
 	__syncthreads();
