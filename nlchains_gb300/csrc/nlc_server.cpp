@@ -699,6 +699,16 @@ int submit(nlc_server *S, const nlc_model *model, uint32_t batching, uint64_t st
 	R->need_bytes = R->state_bytes + size_t(4 * 160) * n * sizeof(double) + 16 * n * sizeof(double) +
 	                (model->model == NLC_DDNKG ? n * n * sizeof(double) : 0) + (1 << 16);
 	if (n > 4096) R->need_bytes += R->state_bytes + size_t(2 * 1024) * 4 * n * sizeof(double2);   // windows / FFT scratch
+	if (model->model == NLC_DDNKG) {
+		// the tensor-core projection (the plan's rule): BF16 slices of the state and of the
+		// eigenvectors, and with 7 slices the first sweep's integer sums
+		const bool bf16x3 = model->flags & NLC_FLAG_BF16X3_PROJECTION;
+		if (bf16x3 || (model->flags & NLC_FLAG_TENSOR_PROJECTION) || (n >= 128 && !(model->flags & NLC_FLAG_FP64_PROJECTION))) {
+			const size_t mp = (2ull * model->copies + 127) / 128 * 128, np = (size_t(n) + 127) / 128 * 128,
+			             kp = (size_t(n) + 15) / 16 * 16, slices = bf16x3 ? 3 : 7;
+			R->need_bytes += slices * (mp + np) * kp * 2 + (bf16x3 ? 0 : mp * np * 8);
+		}
+	}
 	std::lock_guard<std::mutex> lk(S->mu);
 	if (!S->fatal.empty()) return set_error(NLC_ECUDA, "server stopped after a CUDA error: " + S->fatal);
 	R->id = S->next_id++;
