@@ -109,7 +109,7 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, unsigne
 }
 
 // The same wait with a suspend-time hint (1 us): the thread sleeps in the barrier until it completes
-// or the hint elapses, leaving the issue slots to the thread that issues the loads and MMAs.
+// or the hint elapses, leaving the issue slots to the threads that issue the copies and MMAs.
 constexpr uint32_t kSleepHintNs = 1000;
 __device__ __forceinline__ bool mbar_wait_sleep(uint32_t bar, uint32_t parity, unsigned long long limit_ns) {
 	const unsigned long long t0 = global_ns();
@@ -123,9 +123,9 @@ __device__ __forceinline__ bool mbar_wait_sleep(uint32_t bar, uint32_t parity, u
 	return false;
 }
 
-// Shared-memory matrix descriptor of a K-major tile written by TMA with the 32-byte swizzle (one
-// 16-site row of BF16 per 32 bytes): 8-row atoms of 256 bytes (stride byte offset), descriptor
-// version 1, layout type 6.  The tiles start on 1024-byte boundaries, so the base offset is 0 and a
+// Shared-memory matrix descriptor of a K-major tile in the 32-byte-swizzled layout that the bulk
+// copies bring in (tc_slice_index; one 16-site row of BF16 per 32 bytes): 8-row atoms of 256 bytes
+// (stride byte offset), descriptor version 1, layout type 6.  The tiles start on 1024-byte boundaries, so the base offset is 0 and a
 // tile's descriptor is the stage's plus its byte offset / 16 (addresses stay below 2^18).
 __device__ __forceinline__ uint64_t smem_desc(uint32_t saddr) {
 	return (uint64_t) ((saddr & 0x3FFFF) >> 4) | ((uint64_t) 1 << 16) | ((uint64_t) (256 >> 4) << 32) |
