@@ -132,7 +132,7 @@ def test_real_diagnostics_global_memory(gpu, n):
 
 @pytest.mark.parametrize("n", [700, 1800])
 def test_ddnkg_projection_chunked(gpu, n):
-    # beyond 512 sites the projection streams the chains through shared memory in chunks; the
+    # the tensor-core projection over three and eight 256-site read-out chunks per sweep; the
     # expected energies come from LAPACK's eigensystem of the same operator (eigensystem.cpp:15-18)
     copies = 11
     masses = ic.masses_uniform(n, seed=n)
