@@ -69,10 +69,16 @@ enum {
 	NLC_FLAG_FP64_PROJECTION = 64,   /* dDNKG: the mode projection on the FP64 CUDA cores at any length */
 	NLC_FLAG_BF16X3_PROJECTION = 128, /* dDNKG: the tensor-core projection with 3 BF16 slices: faster, with
 	                                    mode energies to ~1e-7 relative instead of FP64 level */
-	NLC_FLAG_FP32_DIAGNOSTICS = 256  /* DNKG, FPUT, Toda, DNLS: the per-chain transform and mode energies
+	NLC_FLAG_FP32_DIAGNOSTICS = 256, /* DNKG, FPUT, Toda, DNLS: the per-chain transform and mode energies
 	                                    in FP32 (the sum over chains in FP64): mode energies to ~1e-7 of
 	                                    the largest; lengths that need the padded transform or
 	                                    global-memory passes keep the FP64 diagnostics */
+	NLC_FLAG_DNLS_FOURIER = 512      /* DNLS: the linear sub-steps through transforms of the chain, as
+	                                    the reference does, at every length.  By default, where dt is
+	                                    small enough (propagator taps beyond 11 sites below 2^-64, dt up
+	                                    to ~0.05) and 2R + 2 <= chain_length <= 4096, each linear
+	                                    sub-step is the same operator applied as its real-space stencil
+	                                    (nlc_dnls_stencil_coefficients) */
 };
 
 /*
@@ -181,11 +187,22 @@ int nlc_energies(nlc_plan *plan, const void *state_dev, double *energies_dev, vo
 int nlc_dnls_evolve_nonlinear(nlc_plan *plan, void *psi_dev, double beta_dt_symplectic, void *stream);
 int nlc_dnls_evolve_linear(nlc_plan *plan, void *psi_k_dev, const void *table_dev, void *stream);
 
+/* The DNLS linear propagator of sub-step k, psi <- IFFT(FFT(psi) exp(-i dt d_k omega_j) / n) with
+ * omega_j = 4 sin^2(pi j / n) (DNLS.cu:19-25, dispersion.cpp:19-26), in real space (Jacobi-Anger):
+ * psi'_s = exp(-2 i tau_k) sum_{|x| <= R} i^|x| J_|x|(2 tau_k) psi_{s+x}, tau_k = dt d_k, exact up to
+ * terms below 2^-64 for chain_length >= 2R + 2.  Host only (no device is touched): c0m1[7] =
+ * J_0(2 tau_k) - 1, taps[7 * max_radius] (row k, x = 1..max_radius) = J_x(2 tau_k) times the sign of
+ * i^x (negative for x = 2, 3 mod 4), phase[7] = -2 tau_k; *radius = the R beyond which every tap is
+ * below 2^-64 (max_radius + 1 if that is larger than max_radius).  max_radius in 1..32. */
+int nlc_dnls_stencil_coefficients(double dt, int32_t max_radius, int32_t *radius, double *c0m1, double *taps,
+                                  double *phase);
+
 /* Launch shape chosen for the integrator: lanes per chain, sites per lane, threads per block, and
  * the tier: 1 = register-resident, a chain on G <= 32 lanes of a warp; 2 = register-resident, a
  * chain on one block of G > 32 lanes; 3 = DNLS, chains resident in shared memory (or, beyond it, in
  * per-block global scratch); 4 = windowed, chains longer than one block holds, integrated in
- * overlapping windows of G x E sites (lanes x sites per lane) between two state buffers. */
+ * overlapping windows of G x E sites (lanes x sites per lane) between two state buffers; 5 = DNLS
+ * in registers, G lanes of E or E - 1 sites, the linear sub-steps as real-space stencils. */
 int nlc_plan_shape(const nlc_plan *plan, int32_t *lanes_per_chain, int32_t *sites_per_lane,
                    int32_t *threads_per_block, int32_t *tier);
 

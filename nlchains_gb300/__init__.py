@@ -28,7 +28,7 @@ MODEL_NAMES = {v: k for k, v in MODELS.items()}
 OK, EINVAL, ECUDA, ENOMEM, EIO, ETIMEDOUT, ENOTFOUND, EBLOWUP, EUNSUPPORTED = 0, -1, -2, -3, -4, -5, -6, -7, -8
 FLAG_SPLIT_KERNEL, FLAG_NO_TUNE, FLAG_CANONICAL_SHAPE, FLAG_COMPACT_DIAG = 1, 2, 4, 8
 FLAG_SHARED_GPU, FLAG_TENSOR_PROJECTION, FLAG_FP64_PROJECTION, FLAG_BF16X3_PROJECTION = 16, 32, 64, 128
-FLAG_FP32_DIAGNOSTICS = 256
+FLAG_FP32_DIAGNOSTICS, FLAG_DNLS_FOURIER = 256, 512
 REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_FAILED = 0, 1, 2, 3
 
 # the exported symbols, as declared in include/nlchains.h
@@ -41,6 +41,7 @@ EXPORTS = (
     "nlc_server_create", "nlc_server_destroy", "nlc_server_submit", "nlc_server_poll", "nlc_server_wait",
     "nlc_server_result", "nlc_entropies", "nlc_job_sample_async", "nlc_job_sample_wait", "nlc_energies",
     "nlc_job_energies", "nlc_job_step_async", "nlc_job_after", "nlc_initial_state", "nlc_server_submit_seeded",
+    "nlc_dnls_stencil_coefficients",
 )
 
 
@@ -129,6 +130,7 @@ def lib():
         "nlc_energies": ([vp, vp, vp, vp], i32),
         "nlc_job_energies": ([vp, u64, dp], i32),
         "nlc_job_step_async": ([vp, u64, i32, i32], i32),
+        "nlc_dnls_stencil_coefficients": ([ctypes.c_double, i32, P(i32), dp, dp, dp], i32),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -177,6 +179,18 @@ def eigensystem(masses, device=-1):
     P = ctypes.POINTER(ctypes.c_double)
     _check(lib().nlc_eigensystem(n, m.ctypes.data_as(P), int(device), om.ctypes.data_as(P), ev.ctypes.data_as(P)))
     return om, ev.reshape(n, n).T
+
+
+def dnls_stencil_coefficients(dt, max_radius=11):
+    """The DNLS linear propagators as real-space stencils (nlc_dnls_stencil_coefficients, host only):
+    (radius, c0m1[7], taps[7, max_radius], phase[7]) with c0m1 = J_0(2 dt d_k) - 1, taps[k, x - 1] =
+    J_x(2 dt d_k) times the sign of i^x, phase = -2 dt d_k."""
+    r = ctypes.c_int32()
+    c0, taps, ph = np.zeros(7), np.zeros(7 * max_radius), np.zeros(7)
+    P = ctypes.POINTER(ctypes.c_double)
+    _check(lib().nlc_dnls_stencil_coefficients(float(dt), int(max_radius), ctypes.byref(r), c0.ctypes.data_as(P),
+                                               taps.ctypes.data_as(P), ph.ctypes.data_as(P)))
+    return r.value, c0, taps.reshape(7, max_radius), ph
 
 
 class Model:

@@ -95,6 +95,14 @@ constexpr uint32_t kMaxFftLen = 1u << 18;
 // spectra FFT_m(g_k) / m (interleaved), so that x (*) h_k = IFFT_m(FFT_m(x) G_k) on [0, n).
 std::vector<double> dnls_conv_tables(const std::vector<double> &lin, uint32_t n, uint32_t m);
 
+// The same propagators in real space (Jacobi-Anger): for n >= 2R + 2, IFFT_n diag(exp(-i tau
+// omega_q)) FFT_n = exp(-2 i tau) sum_{|x| <= R} i^|x| J_|x|(2 tau) S^x (S the cyclic shift) up to
+// terms below 2^-64, tau = dt d_k.  Fills, for the 7 sub-steps, c0m1[k] = J_0(2 tau_k) - 1,
+// taps[k max_radius + x - 1] = J_x(2 tau_k) times the sign of i^x (x = 1..max_radius) and phase[k]
+// = -2 tau_k, all from the series in double-double (the same bits on every IEEE host), and returns
+// the radius R beyond which every |J_x(2 tau_k)| <= 2^-64 (max_radius + 1 when it is larger).
+int dnls_stencil_coefficients(double dt, int max_radius, double c0m1[7], double *taps, double phase[7]);
+
 // The same eigensystem on the GPU (cuSOLVER's divide and conquer, loaded at run time,
 // nlc_eig_device.cpp); false when cuSOLVER is missing, any step fails or NLC_HOST_EIGEN is set, and
 // the caller then uses the host solver.

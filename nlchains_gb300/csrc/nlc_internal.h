@@ -234,6 +234,26 @@ struct DnlsArgs {
 };
 cudaError_t launch_dnls_move(const DnlsArgs &a, double2 *psi, int blocks, int threads, size_t smem,
                              int team_block, cudaStream_t stream);
+// DNLS with the linear sub-steps as a real-space stencil (nlc_dnls_stencil.cu): chains of n sites on
+// `lanes` lanes of E or E - 1 sites in registers, stencil radius R (instantiated: E in {8, 12, 16}
+// with R = 7, E in {12, 16} with R = 11)
+constexpr int kMaxStencilRadius = 11;
+struct DnlsStencilArgs {
+	uint32_t n, copies, steps, seg;
+	int lanes;
+	double nl[8], nl_final;    // as DnlsArgs
+	double phase[7];           // -2 dt d_k: the propagator's common phase, added to the rotation angle before it
+	double c0m1[7];            // J_0(2 dt d_k) - 1
+	double taps[7][kMaxStencilRadius];   // x = 1..R: J_x(2 dt d_k) times the sign of i^x (x = 2, 3 mod 4 negative)
+	unsigned long long *work_counter;
+	const double2 *sctab;
+	SinCosConsts sc;
+	FpOnes k1;
+};
+cudaError_t launch_dnls_stencil(const DnlsStencilArgs &a, double2 *psi, int sites, int radius, int blocks,
+                                cudaStream_t stream);
+const void *dnls_stencil_kernel_ptr(int sites, int radius, bool team);
+size_t dnls_stencil_smem(int lanes, int radius);
 cudaError_t launch_dnls_nonlinear(double2 *psi, uint64_t elements, double coef, const double2 *sctab,
                                   cudaStream_t stream);
 cudaError_t launch_dnls_linear(double2 *psi, uint64_t elements, uint32_t n, const double2 *table,

@@ -122,10 +122,14 @@ struct nlc_plan {
 	DnlsArgs da{};
 	int dnls_blocks = 0, dnls_threads = 0, dnls_team_block = 0;
 	size_t dnls_smem = 0;
+	DnlsStencilArgs sa{};      // DNLS in the real-space stencil form (tier 5)
+	bool dnls_stencil = false;
+	int dnls_sites = 0, dnls_radius = 0;
 	DiagArgs ga{};
 	int diag_blocks = 0, diag_threads = 0, diag_team_block = 0, diag_rows = 0;
 	size_t diag_smem = 0;
-	int tier = 0;   // 1 = resident lanes (G <= 32), 2 = resident block (G > 32), 3 = DNLS, 4 = windowed
+	int tier = 0;   // 1 = resident lanes (G <= 32), 2 = resident block (G > 32), 3 = DNLS, 4 = windowed,
+	                // 5 = DNLS stencil
 	// dDNKG projection on the tensor cores
 	bool tc = false;
 	TcArgs tca{};
@@ -693,6 +697,119 @@ const void *lin32_kernel_ptr(int team_block);
 const void *dnls_kernel_ptr(int team_block);
 }  // namespace nlc
 
+// DNLS in the real-space stencil form (nlc_dnls_stencil.cu), where it applies: the propagator's
+// taps beyond radius 11 below 2^-64 (dt d_k up to ~0.05), n >= 2R + 2, and a launch shape of G lanes
+// (up to 256) of E or E - 1 sites, E in {16, 12, 8} with E - 1 >= R.  Among the shapes, the one
+// with the fewest lane-sites computed per chain site (idle lanes of a warp, the short lanes' inert
+// slot); otherwise P.dnls_stencil stays false and the plan takes the Fourier form.
+static int setup_dnls_stencil(nlc_plan &P) {
+	const uint32_t n = P.m.chain_length;
+	DnlsStencilArgs &a = P.sa;
+	const int need = dnls_stencil_coefficients(P.m.dt, kMaxStencilRadius, a.c0m1, &a.taps[0][0], a.phase);
+	const int R = need <= 7 ? 7 : need <= kMaxStencilRadius ? kMaxStencilRadius : 0;
+	if (!R || n < uint32_t(2 * R + 2)) return NLC_OK;
+	int lanes = 0, sites = 0;
+	double best = 0;
+	for (int E : {16, 12, 8}) {
+		if (E - 1 < R) continue;
+		// G (E - 1) < n <= G E: every lane holds E or E - 1 sites
+		for (uint32_t G = (n + E - 1) / E; G <= 256 && uint64_t(G) * (E - 1) < n; G++) {
+			const double occupied = G <= 32 ? 32. / double(32 / G) : double((G + 31) / 32 * 32);
+			const double eff = double(n) / (occupied * E);
+			if (eff > best * 1.0001) best = eff, lanes = int(G), sites = E;
+		}
+	}
+	if (!lanes) return NLC_OK;
+	const void *k = dnls_stencil_kernel_ptr(sites, R, lanes <= 32);
+	if (!k) return NLC_OK;
+	const DnlsArgs &d = P.da;
+	a.n = n, a.copies = P.m.copies, a.lanes = lanes;
+	std::memcpy(a.nl, d.nl, sizeof a.nl);
+	a.nl_final = d.nl_final;
+	a.work_counter = P.d_counter;
+	a.sctab = d.sctab;
+	P.dnls_threads = lanes <= 32 ? 128 : (lanes + 31) / 32 * 32;
+	P.dnls_smem = dnls_stencil_smem(lanes, R);
+	int per_sm = 0, rc;
+	if ((rc = cuda_status(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, P.dnls_threads, P.dnls_smem),
+	                      "occupancy")))
+		return rc;
+	if (per_sm < 1) return NLC_OK;
+	const int chains = lanes <= 32 ? (32 / lanes) * (P.dnls_threads / 32) : 1;   // per block
+	const unsigned long long units = (P.m.copies + chains - 1) / chains;
+	P.dnls_blocks = int(std::min<unsigned long long>(
+	    units, (P.m.flags & NLC_FLAG_SHARED_GPU) ? 0x7fffffffull
+	                                            : (unsigned long long) per_sm * P.prop.multiProcessorCount));
+	P.dnls_sites = sites, P.dnls_radius = R;
+	P.dnls_stencil = true;
+	// a block's step: 7 sub-steps of 19 + 4R FP64 operations on the lane-sites it computes, at ~85%
+	P.block_ops = 7. * (19 + 4 * R) * double(sites) * (lanes <= 32 ? 32 * (P.dnls_threads / 32) : P.dnls_threads) / 0.85;
+	P.per_sm = per_sm;
+	P.block_warps = P.dnls_threads / 32;
+	P.tier = 5;
+	return NLC_OK;
+}
+
+// DNLS in the Fourier form: the shared-memory split step of nlc_dnls.cu (transforms of n, or for a
+// length with a large prime factor the padded convolution form); lin: the 7 propagator tables
+static int setup_dnls_fourier(nlc_plan *P, const std::vector<double> &tab) {
+	int rc;
+	DnlsArgs &d = P->da;
+	const nlc_model *model = &P->m;
+	const uint32_t n = model->chain_length;
+	if ((rc = setup_fft(*P, d.fft, true))) return rc;
+	if (d.fft.bluestein) {
+		// lengths whose padded form is cheaper (large prime factors): each linear sub-step as one
+		// zero-padded cyclic convolution of the smooth length len (two passes) instead of two
+		// Bluestein transforms (four passes and three chirp products)
+		const uint32_t m = uint32_t(d.fft.len);
+		const std::vector<double> conv = dnls_conv_tables(tab, n, m);
+		double2 *d_conv = nullptr;
+		if ((rc = P->upload(&d_conv, reinterpret_cast<const double2 *>(conv.data()), 7 * size_t(m)))) return rc;
+		d.conv_tables = d_conv;
+	}
+	// team: up to a 256-point pass, len/4 lanes (4 .. 32, a power of two) per chain and several
+	// chains per warp; beyond, a block of up to 256 threads per chain
+	const int sms = P->prop.multiProcessorCount;
+	const uint32_t len = uint32_t(d.fft.len);
+	if (len <= 256) {
+		int T = 4;
+		while (T < 32 && uint32_t(T) * 4 < len) T <<= 1;
+		d.team = T;
+		P->dnls_team_block = 0;
+		P->dnls_threads = 128;
+		P->dnls_smem = size_t(128 / T) * 2 * len * sizeof(double2);
+	} else {
+		P->dnls_team_block = 1;
+		P->dnls_threads = int(std::min<uint32_t>(256, std::max<uint32_t>(64, (len / 4 + 31) / 32 * 32)));
+		P->dnls_smem = 2 * size_t(len) * sizeof(double2);
+	}
+	const bool global = len > smem_fft_len(*P);   // the chain's two buffers in global memory
+	if (global) P->dnls_threads = 512, P->dnls_smem = 0;
+	const void *k = dnls_kernel_ptr(P->dnls_team_block);
+	if ((rc = set_smem_attr(k, P->dnls_smem, P->prop))) return rc;
+	int per_sm = 0;
+	if ((rc = cuda_status(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, P->dnls_threads, P->dnls_smem),
+	                      "occupancy")))
+		return rc;
+	if (per_sm < 1) return set_error(NLC_EUNSUPPORTED, "DNLS kernel does not fit an SM");
+	const int teams = P->dnls_team_block ? 1 : P->dnls_threads / d.team;
+	P->block_ops = block_step_ops(NLC_DNLS, n, len, d.fft.bluestein, teams) * (global ? 2 : 1);
+	P->per_sm = per_sm;
+	P->block_warps = P->dnls_threads / 32;
+	P->dnls_blocks = int(std::min<unsigned long long>((model->copies + teams - 1) / teams, (unsigned long long) per_sm * sms));
+	if ((model->flags & NLC_FLAG_SHARED_GPU) && !global)   // one block per unit of work: a warp's chains per unit
+		P->dnls_blocks = int(std::min<unsigned long long>(
+		    P->dnls_team_block ? model->copies : (model->copies + (32 / d.team) - 1) / (32 / d.team) / 4 + 1,
+		    0x7fffffffull));
+	if (global) {
+		// scratch for the resident blocks of the persistent grid
+		if ((rc = P->dalloc(&d.gscratch, size_t(P->dnls_blocks) * 2 * len))) return rc;
+	}
+	P->tier = 3;
+	return NLC_OK;
+}
+
 extern "C" int nlc_plan_create(const nlc_model *model, nlc_plan **out) {
 	if (!out) return set_error(NLC_EINVAL, "plan pointer is NULL");
 	*out = nullptr;
@@ -749,7 +866,6 @@ extern "C" int nlc_plan_create(const nlc_model *model, nlc_plan **out) {
 	if (mdl == NLC_DNLS) {
 		DnlsArgs &d = P->da;
 		d.n = n, d.copies = model->copies;
-		if ((rc = setup_fft(*P, d.fft, true))) return rc;
 		const double bdt = model->beta * model->dt;
 		for (int k = 0; k < 7; k++) d.nl[k] = bdt * 1. * kYoshidaC[k];
 		d.nl[7] = bdt * 2. * kYoshidaC[0];   // merged c7 + c0 (DNLS.cpp:162)
@@ -772,56 +888,11 @@ extern "C" int nlc_plan_create(const nlc_model *model, nlc_plan **out) {
 			if ((rc = P->upload(&d_sct, reinterpret_cast<const double2 *>(sct.data()), kSinCosTable))) return rc;
 			d.sctab = d_sct;
 		}
-		if (d.fft.bluestein) {
-			// lengths whose padded form is cheaper (large prime factors): each linear sub-step as one
-			// zero-padded cyclic convolution of the smooth length len (two passes) instead of two
-			// Bluestein transforms (four passes and three chirp products)
-			const uint32_t m = uint32_t(d.fft.len);
-			const std::vector<double> conv = dnls_conv_tables(tab, n, m);
-			double2 *d_conv = nullptr;
-			if ((rc = P->upload(&d_conv, reinterpret_cast<const double2 *>(conv.data()), 7 * size_t(m)))) return rc;
-			d.conv_tables = d_conv;
-		}
 		d.work_counter = P->d_counter;
-		// team: up to a 256-point pass, len/4 lanes (4 .. 32, a power of two) per chain and several
-		// chains per warp; beyond, a block of up to 256 threads per chain
-		const int sms = P->prop.multiProcessorCount;
-		const uint32_t len = uint32_t(d.fft.len);
-		if (len <= 256) {
-			int T = 4;
-			while (T < 32 && uint32_t(T) * 4 < len) T <<= 1;
-			d.team = T;
-			P->dnls_team_block = 0;
-			P->dnls_threads = 128;
-			P->dnls_smem = size_t(128 / T) * 2 * len * sizeof(double2);
-		} else {
-			P->dnls_team_block = 1;
-			P->dnls_threads = int(std::min<uint32_t>(256, std::max<uint32_t>(64, (len / 4 + 31) / 32 * 32)));
-			P->dnls_smem = 2 * size_t(len) * sizeof(double2);
+		if (!(model->flags & NLC_FLAG_DNLS_FOURIER)) {
+			if ((rc = setup_dnls_stencil(*P))) return rc;
 		}
-		const bool global = len > smem_fft_len(*P);   // the chain's two buffers in global memory
-		if (global) P->dnls_threads = 512, P->dnls_smem = 0;
-		const void *k = dnls_kernel_ptr(P->dnls_team_block);
-		if ((rc = set_smem_attr(k, P->dnls_smem, P->prop))) return rc;
-		int per_sm = 0;
-		if ((rc = cuda_status(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, P->dnls_threads, P->dnls_smem),
-		                      "occupancy")))
-			return rc;
-		if (per_sm < 1) return set_error(NLC_EUNSUPPORTED, "DNLS kernel does not fit an SM");
-		const int teams = P->dnls_team_block ? 1 : P->dnls_threads / d.team;
-		P->block_ops = block_step_ops(NLC_DNLS, n, len, d.fft.bluestein, teams) * (global ? 2 : 1);
-		P->per_sm = per_sm;
-		P->block_warps = P->dnls_threads / 32;
-		P->dnls_blocks = int(std::min<unsigned long long>((model->copies + teams - 1) / teams, (unsigned long long) per_sm * sms));
-		if ((model->flags & NLC_FLAG_SHARED_GPU) && !global)   // one block per unit of work: a warp's chains per unit
-			P->dnls_blocks = int(std::min<unsigned long long>(
-			    P->dnls_team_block ? model->copies : (model->copies + (32 / d.team) - 1) / (32 / d.team) / 4 + 1,
-			    0x7fffffffull));
-		if (global) {
-			// scratch for the resident blocks of the persistent grid
-			if ((rc = P->dalloc(&d.gscratch, size_t(P->dnls_blocks) * 2 * len))) return rc;
-		}
-		P->tier = 3;
+		if (!P->dnls_stencil && (rc = setup_dnls_fourier(P.get(), tab))) return rc;
 	} else {
 		RealArgs &a = P->ra;
 		for (int k = 0; k < 7; k++) {
@@ -946,6 +1017,13 @@ void nlc::plan_destroy_ordered(nlc_plan *plan, cudaStream_t stream) {
 
 extern "C" int nlc_plan_shape(const nlc_plan *P, int32_t *lanes, int32_t *sites, int32_t *threads, int32_t *tier) {
 	if (!P) return set_error(NLC_EINVAL, "plan is NULL");
+	if (P->m.model == NLC_DNLS && P->dnls_stencil) {
+		if (lanes) *lanes = P->sa.lanes;
+		if (sites) *sites = P->dnls_sites;
+		if (threads) *threads = P->dnls_threads;
+		if (tier) *tier = P->tier;
+		return NLC_OK;
+	}
 	if (lanes) *lanes = P->m.model == NLC_DNLS ? (P->dnls_team_block ? P->dnls_threads : P->da.team) : P->rs.lanes;
 	if (sites) *sites = P->m.model == NLC_DNLS ? 0 : P->rs.sites;
 	if (threads) *threads = P->m.model == NLC_DNLS ? P->dnls_threads : P->rs.threads;
@@ -1097,6 +1175,14 @@ int nlc::move_rounds(nlc_plan *P, void *state, uint64_t rounds, uint32_t round_s
 int nlc::move_segment(nlc_plan *P, void *state, uint32_t steps, uint32_t seg, cudaStream_t st) {
 	if (!P || !state) return set_error(NLC_EINVAL, "NULL argument");
 	if (!steps) return NLC_OK;
+	if (P->m.model == NLC_DNLS && P->dnls_stencil) {
+		DnlsStencilArgs a = P->sa;
+		a.steps = steps;
+		a.seg = seg;
+		return cuda_status(launch_dnls_stencil(a, static_cast<double2 *>(state), P->dnls_sites, P->dnls_radius,
+		                                       P->dnls_blocks, st),
+		                   "DNLS stencil move launch");
+	}
 	if (P->m.model == NLC_DNLS) {
 		DnlsArgs a = P->da;
 		a.steps = steps;
@@ -1207,6 +1293,14 @@ extern "C" int nlc_dnls_evolve_linear(nlc_plan *P, void *psi, const void *table,
 	return cuda_status(launch_dnls_linear(static_cast<double2 *>(psi), uint64_t(P->m.copies) * P->m.chain_length,
 	                                      P->m.chain_length, tab, static_cast<cudaStream_t>(stream)),
 	                   "evolve_linear launch");
+}
+
+extern "C" int nlc_dnls_stencil_coefficients(double dt, int32_t max_radius, int32_t *radius, double *c0m1,
+                                             double *taps, double *phase) {
+	if (!radius || !c0m1 || !taps || !phase) return set_error(NLC_EINVAL, "NULL argument");
+	if (max_radius < 1 || max_radius > 32 || !(dt > 0)) return set_error(NLC_EINVAL, "max_radius in 1..32, dt > 0");
+	*radius = dnls_stencil_coefficients(dt, max_radius, c0m1, taps, phase);
+	return NLC_OK;
 }
 
 extern "C" const char *nlc_last_error(void) { return nlc::g_last_error.c_str(); }

@@ -679,9 +679,11 @@ int submit(nlc_server *S, const nlc_model *model, uint32_t batching, uint64_t st
 	R->batching = batching;
 	R->steps = steps;
 	R->state_bytes = n * model->copies * sizeof(double2);
-	// rough FP64 cost per site-step: Toda's exp doubles it, DNLS's transforms make it ~15x
+	// rough FP64 cost per site-step against DNKG's: Toda's exp 2.4x, DNLS's stencils ~10x (its
+	// transforms ~15x)
+	const double dnls = (model->flags & NLC_FLAG_DNLS_FOURIER) ? 15. : 10.;
 	R->work = double(n) * model->copies * double(steps) *
-	          (model->model == NLC_DNLS ? 15. : model->model == NLC_TODA ? 2.4 : 1.);
+	          (model->model == NLC_DNLS ? dnls : model->model == NLC_TODA ? 2.4 : 1.);
 	if (host_state) {
 		const double *src = static_cast<const double *>(host_state);
 		R->host_in.assign(src, src + 2 * n * model->copies);

@@ -99,6 +99,52 @@ void sincos_table(double table[2 * kSinCosTable]) {
 	}
 }
 
+namespace {
+
+// J_x(2t) = sum_m (-1)^m t^(2m + x) / (m! (m + x)!) in double-double (|t| well below 1 here); with
+// minus_one and x = 0 the series without its leading 1, i.e. J_0(2t) - 1 to full relative precision
+DD bessel_j_2t(unsigned x, DD t, bool minus_one) {
+	const DD t2 = dd_mul(t, t);
+	DD term{1., 0.};
+	for (unsigned i = 1; i <= x; i++) term = dd_div_u(dd_mul(term, t), i);   // t^x / x!
+	unsigned m = 0;
+	if (minus_one) {   // start at m = 1: -t^2
+		term = dd_mul(t2, DD{-1., 0.});
+		m = 1;
+	}
+	DD sum{0., 0.};
+	for (; m < 60; m++) {
+		sum = dd_add(sum, term);
+		term = dd_div_u(dd_mul(term, t2), (m + 1) * (m + 1 + x));
+		term = {-term.hi, -term.lo};
+		if (std::fabs(term.hi) < 1e-40 * std::fabs(sum.hi) || term.hi == 0.) break;
+	}
+	return sum;
+}
+
+}  // namespace
+
+int dnls_stencil_coefficients(double dt, int max_radius, double c0m1[7], double *taps, double phase[7]) {
+	const double limit = 0x1p-64;
+	int radius = 0;
+	for (int k = 0; k < 7; k++) {
+		const DD tau = dd_mul(DD{dt, 0.}, DD{kYoshidaD[k], 0.});
+		const DD c = bessel_j_2t(0, tau, true);
+		c0m1[k] = c.hi + c.lo;
+		const DD ph = dd_mul(tau, DD{-2., 0.});
+		phase[k] = ph.hi + ph.lo;
+		int r = 0;
+		for (int x = 1; x <= max_radius + 1; x++) {
+			const DD j = bessel_j_2t(unsigned(x), tau, false);
+			const double v = j.hi + j.lo;
+			if (x <= max_radius) taps[k * max_radius + x - 1] = (x & 2) ? -v : v;   // the sign of i^x
+			if (std::fabs(v) > limit) r = x;
+		}
+		radius = std::max(radius, r);
+	}
+	return radius;
+}
+
 void exp_table(double scale, double table[kExpTable]) {
 	const DD ln2{0x1.62e42fefa39efp-1, 0x1.abc9e3b39803fp-56};
 	for (unsigned j = 0; j < unsigned(kExpTable); j++) {

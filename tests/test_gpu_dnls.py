@@ -8,9 +8,13 @@ from nlchains_gb300 import ic
 pytestmark = pytest.mark.gpu
 
 
-def run(nlc, n, copies, dt, beta, psi, steps, batching):
+# the linear sub-steps as real-space stencils (the default where dt and n allow) and through transforms
+FORMS = {"stencil": 0, "fourier": 512}
+
+
+def run(nlc, n, copies, dt, beta, psi, steps, batching, flags=0):
     ctx = nlc.Context(0)
-    job = ctx.job(nlc.Model("DNLS", n, copies, dt, beta=beta), batching)
+    job = ctx.job(nlc.Model("DNLS", n, copies, dt, beta=beta, flags=flags), batching)
     job.upload(psi.view(np.float64).reshape(copies, n, 2))
     job.advance(steps)
     out = job.download().view(np.complex128).reshape(copies, n)
@@ -22,36 +26,47 @@ def run(nlc, n, copies, dt, beta, psi, steps, batching):
 # 70 = 2 x 5 x 7 (direct radix-5 and radix-7 passes), 39 / 86 (factors 13, 43) and 97 / 211 / 997 /
 # 3001 prime (Bluestein), 1000 smooth: every FFT path and every team width of the shared-memory step
 # 664 pads to 1536 points: exactly 48 KiB of dynamic shared memory per block, plus the static part
-@pytest.mark.parametrize("n", [2, 8, 12, 39, 64, 70, 86, 97, 100, 211, 256, 512, 664, 997, 1000, 1024, 2048, 3001])
-def test_against_oracle(gpu, n):
+# the stencil form: 16 (one lane of 16 sites), 39 / 53 .. 211 / 256 / 512 (5 .. 32 lanes of a warp, 8,
+# 12 or 16 sites), 664 .. 3001 (a block of 56 .. 188 lanes); 2, 8, 12 are too short for its radius
+# and take the Fourier form either way
+@pytest.mark.parametrize("form", FORMS)
+@pytest.mark.parametrize("n", [2, 8, 12, 16, 39, 64, 70, 86, 97, 100, 211, 256, 512, 664, 997, 1000, 1024, 2048,
+                               3001])
+def test_against_oracle(gpu, n, form):
     copies, dt = 11, 0.01
     steps, b = (20, 10) if n <= 2048 else (4, 2)   # the oracle's prime-length DFT is O(n^2)
     if n > 2048:
         copies = 3
     psi = ic.dnls_ensemble(n, copies, 1.0, ic.low_modes(n, 0.1), seed=n)
-    out = run(gpu, n, copies, dt, 1.0, psi, steps, b)
+    tier = gpu.Plan(gpu.Model("DNLS", n, copies, dt, beta=1.0, flags=FORMS[form])).shape()["tier"]
+    assert tier == (5 if form == "stencil" and n >= 16 else 3)
+    out = run(gpu, n, copies, dt, 1.0, psi, steps, b, FORMS[form])
     mdl = O.Model("DNLS", n, copies, dt, beta=1.0)
     exp = O.advance(mdl, psi.view(np.float64), steps, b).view(np.complex128).reshape(copies, n)
     # different FFT algorithms and sincos implementations: agreement to rounding
     assert np.abs(out - exp).max() <= 1e-12 * np.abs(exp).max()
 
 
-# 128: direct passes; 97, 211, 1021 (prime): the linear sub-steps as padded cyclic convolutions
+# Fourier form: 128 direct passes; 97, 211, 1021 (prime) padded cyclic convolutions.  Stencil form
+# (radius 11 at dt = 0.05): 128, 211 and 1021 on lanes of 16 sites; 97 has no shape at that radius
+# and keeps the Fourier form
+@pytest.mark.parametrize("form", FORMS)
 @pytest.mark.parametrize("n", [128, 97, 211, 1021])
-def test_linear_exact_phase_advance(gpu, n):
+def test_linear_exact_phase_advance(gpu, n, form):
     copies, dt, steps = 5, 0.05, 40
     rng = np.random.default_rng(1)
     psi = rng.standard_normal((copies, n)) + 1j * rng.standard_normal((copies, n))
-    out = run(gpu, n, copies, dt, 0.0, psi, steps, 20)
+    out = run(gpu, n, copies, dt, 0.0, psi, steps, 20, FORMS[form])
     omega = 4 * np.sin(np.pi * np.arange(n) / n) ** 2
     exp = np.fft.ifft(np.fft.fft(psi, axis=1) * np.exp(-1j * omega * dt * steps), axis=1)
     assert np.abs(out - exp).max() <= 1e-12 * np.abs(exp).max()
 
 
-def test_norm_and_energy_conservation(gpu):
+@pytest.mark.parametrize("form", FORMS)
+def test_norm_and_energy_conservation(gpu, form):
     n, copies = 1024, 8
     psi = ic.dnls_ensemble(n, copies, 1.0, ic.low_modes(n, 0.1), seed=7)
-    out = run(gpu, n, copies, 0.01, 1.0, psi, 200, 100)
+    out = run(gpu, n, copies, 0.01, 1.0, psi, 200, 100, FORMS[form])
     assert np.allclose((np.abs(out) ** 2).sum(1), (np.abs(psi) ** 2).sum(1), rtol=1e-12)
     mdl = O.Model("DNLS", n, copies, 0.01, beta=1.0)
     e0 = O.energies(mdl, psi.view(np.float64))
@@ -111,3 +126,31 @@ def test_long_run_conservation(gpu):
     e0 = O.energies(mdl, psi.view(np.float64))
     e1 = O.energies(mdl, out.view(np.float64))
     assert np.abs(e1 / e0 - 1).max() < 1e-7
+
+
+@pytest.mark.parametrize("n", [53, 1024, 2953])
+def test_stencil_and_fourier_forms_agree(gpu, n):
+    """The same split step with the linear sub-steps as stencils and through transforms (for the
+    prime lengths, padded convolutions): agreement to rounding after 50 steps of the DNLS
+    benchmark's dynamics, in one launch and in launches of 10 steps (merged rotations between them)."""
+    copies, dt = 6, 0.01
+    psi = ic.dnls_ensemble(n, copies, 1.0, ic.low_modes(n, 0.1), seed=n + 1)
+    a = run(gpu, n, copies, dt, 1.0, psi, 50, 50)
+    b = run(gpu, n, copies, dt, 1.0, psi, 50, 10)
+    f = run(gpu, n, copies, dt, 1.0, psi, 50, 10, FORMS["fourier"])
+    assert np.abs(a - f).max() <= 1e-12 * np.abs(f).max()
+    assert np.abs(a - b).max() <= 1e-13 * np.abs(f).max()
+
+
+def test_form_selection(gpu):
+    """The stencil form where its radius (dt) and the chain length allow, the Fourier form otherwise
+    or on request."""
+    def tier(n, dt, flags=0):
+        return gpu.Plan(gpu.Model("DNLS", n, 4, dt, beta=1.0, flags=flags)).shape()["tier"]
+    assert tier(1024, 0.01) == 5 and tier(2953, 0.01) == 5 and tier(53, 0.01) == 5
+    assert tier(1024, 0.01, FORMS["fourier"]) == 3
+    assert tier(1024, 0.2) == 3                 # taps beyond radius 11 above 2^-64
+    assert tier(12, 0.01) == 3                  # shorter than 2R + 2
+    assert tier(8192, 0.01) == 3                # beyond 256 lanes of 16 sites
+    shape = gpu.Plan(gpu.Model("DNLS", 2953, 4, 0.01, beta=1.0)).shape()
+    assert shape["sites_per_lane"] == 16 and shape["lanes_per_chain"] == 185 and shape["threads"] == 192

@@ -177,8 +177,13 @@ def test_engine_matches_reference_cpu_program(gpu, path):
 EXTENDED = sorted(glob.glob(os.path.join(HERE, "golden", "extended", "*.npz")))
 
 
+# the linear sub-steps as real-space stencils (the default) and through transforms
+DNLS_FORMS = {"stencil": 0, "fourier": 512}
+
+
+@pytest.mark.parametrize("form", DNLS_FORMS)
 @pytest.mark.parametrize("path", EXTENDED, ids=lambda p: os.path.basename(p)[:-4])
-def test_dnls_as_accurate_as_reference_kernels(gpu, path):
+def test_dnls_as_accurate_as_reference_kernels(gpu, path, form):
     torch = pytest.importorskip("torch")
     d = dict(np.load(path))
     n, copies, dt, beta, b = int(d["n"]), int(d["copies"]), float(d["dt"]), float(d["beta"]), int(d["batching"])
@@ -186,7 +191,7 @@ def test_dnls_as_accurate_as_reference_kernels(gpu, path):
     mdl = O.Model("DNLS", n, copies, dt, beta=beta)
     state = d["state_in"]
     ctx = gpu.Context(0)
-    job = ctx.job(gpu.Model("DNLS", n, copies, dt, beta=beta), b)
+    job = ctx.job(gpu.Model("DNLS", n, copies, dt, beta=beta, flags=DNLS_FORMS[form]), b)
     job.upload(state)
     dev = torch.from_numpy(state.copy()).cuda()
     e0 = O.energies(mdl, state)
@@ -198,7 +203,7 @@ def test_dnls_as_accurate_as_reference_kernels(gpu, path):
         t = cp
         eng, rgpu, ext = job.download().reshape(state.shape), dev.cpu().numpy().reshape(state.shape), d[f"state_{cp}"]
         e_err, r_err = rel(eng, ext), rel(rgpu, ext)
-        print(f"DNLS n={n} t={cp}: engine {e_err:.2e}, reference kernels {r_err:.2e} from the extended-precision "
+        print(f"DNLS n={n} t={cp} ({form}): engine {e_err:.2e}, reference kernels {r_err:.2e} from the extended-precision "
               f"run; engine vs reference kernels {rel(eng, rgpu):.2e}")
         assert e_err <= 2 * r_err + 1e-14, f"t={cp}: the engine is less accurate than the reference kernels"
         if cp == 100:
@@ -262,7 +267,8 @@ def test_ddnkg_configuration_full_run(gpu):
     assert drift_e <= 1.1 * drift_r
 
 
-def test_dnls_long_run_drift(gpu):
+@pytest.mark.parametrize("form", DNLS_FORMS)
+def test_dnls_long_run_drift(gpu, form):
     """DNLS over 10^4 steps from a state with every mode excited (norm density 1): the engine's
     energy drift stays at or below the reference kernels'."""
     torch = pytest.importorskip("torch")
@@ -271,7 +277,7 @@ def test_dnls_long_run_drift(gpu):
     psi = ic.dnls_ensemble(n, copies, 1.0, list(range(n)), seed=12345)
     state = np.ascontiguousarray(psi).view(np.float64).reshape(copies, n, 2)
     mdl = O.Model("DNLS", n, copies, dt, beta=1.0)
-    eng, _, _ = engine_run(gpu, "DNLS", n, copies, dt, dict(beta=1.0), None, state, steps, b)
+    eng, _, _ = engine_run(gpu, "DNLS", n, copies, dt, dict(beta=1.0, flags=DNLS_FORMS[form]), None, state, steps, b)
     dev = torch.from_numpy(state.copy()).cuda()
     ref.dnls_advance(mdl, dev.data_ptr(), steps, b)
     rg = dev.cpu().numpy().reshape(state.shape)
@@ -279,5 +285,5 @@ def test_dnls_long_run_drift(gpu):
     e0 = O.energies(mdl, state)
     drift_e = np.abs(O.energies(mdl, eng) - e0).max()
     drift_r = np.abs(O.energies(mdl, rg) - e0).max()
-    print(f"DNLS n={n} 10^4 steps: energy drift engine {drift_e:.3e}, reference kernels {drift_r:.3e}")
+    print(f"DNLS n={n} 10^4 steps ({form}): energy drift engine {drift_e:.3e}, reference kernels {drift_r:.3e}")
     assert drift_e <= 1.1 * drift_r
