@@ -710,8 +710,12 @@ static int setup_dnls_stencil(nlc_plan &P) {
 	if (!R || n < uint32_t(2 * R + 2)) return NLC_OK;
 	int lanes = 0, sites = 0;
 	double best = 0;
+	// NLC_DNLS_SITES=<E> restricts the shapes to E sites per lane (used by the tests to cover every
+	// instantiation)
+	int only = 0;
+	if (const char *e = std::getenv("NLC_DNLS_SITES")) only = std::atoi(e);
 	for (int E : {16, 12, 8}) {
-		if (E - 1 < R) continue;
+		if (E - 1 < R || (only && E != only)) continue;
 		// G (E - 1) < n <= G E: every lane holds E or E - 1 sites
 		for (uint32_t G = (n + E - 1) / E; G <= 256 && uint64_t(G) * (E - 1) < n; G++) {
 			const double occupied = G <= 32 ? 32. / double(32 / G) : double((G + 31) / 32 * 32);

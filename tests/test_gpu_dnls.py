@@ -154,3 +154,24 @@ def test_form_selection(gpu):
     assert tier(8192, 0.01) == 3                # beyond 256 lanes of 16 sites
     shape = gpu.Plan(gpu.Model("DNLS", 2953, 4, 0.01, beta=1.0)).shape()
     assert shape["sites_per_lane"] == 16 and shape["lanes_per_chain"] == 185 and shape["threads"] == 192
+
+
+# (n, dt, sites per lane) -> every instantiation: radius 7 (dt = 0.01) with 8, 12, 16 sites and
+# radius 11 (dt = 0.05) with 12, 16, each on lanes of one warp (team) and on a block
+INSTANTIATIONS = [(62, 0.01, 8, "team"), (512, 0.01, 8, "block"), (128, 0.01, 12, "team"),
+                  (1024, 0.01, 12, "block"), (256, 0.01, 16, "team"), (1024, 0.01, 16, "block"),
+                  (128, 0.05, 12, "team"), (1000, 0.05, 12, "block"), (128, 0.05, 16, "team"),
+                  (1021, 0.05, 16, "block")]
+
+
+@pytest.mark.parametrize("n,dt,sites,kind", INSTANTIATIONS)
+def test_every_stencil_instantiation(gpu, monkeypatch, n, dt, sites, kind):
+    monkeypatch.setenv("NLC_DNLS_SITES", str(sites))
+    copies = 9
+    shape = gpu.Plan(gpu.Model("DNLS", n, copies, dt, beta=1.0)).shape()
+    assert shape["tier"] == 5 and shape["sites_per_lane"] == sites
+    assert (shape["lanes_per_chain"] <= 32) == (kind == "team")
+    psi = ic.dnls_ensemble(n, copies, 1.0, ic.low_modes(n, 0.1), seed=sites + n)
+    a = run(gpu, n, copies, dt, 1.0, psi, 20, 10)
+    f = run(gpu, n, copies, dt, 1.0, psi, 20, 10, FORMS["fourier"])
+    assert np.abs(a - f).max() <= 1e-12 * np.abs(f).max()
