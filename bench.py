@@ -391,6 +391,7 @@ def measure_served(local, stream):
             "p99_ms": float(np.percentile(lat, 99)), "slowdown_p50": float(np.percentile(slowdown, 50)),
             "slowdown_p99": float(np.percentile(slowdown, 99)),
             "alone_queue_p50_ms": float(np.percentile(queue_lat, 50)), "alone_queue_p99_ms": float(np.percentile(queue_lat, 99)),
+            "alone_queue_makespan_s": free_at, "speedup_vs_alone_queue": free_at / makespan,
             "ready_p50_ms": float(np.percentile(prep, 50)), "ready_p99_ms": float(np.percentile(prep, 99)),
             "requests": len(reqs), "makespan_s": makespan,
             "alone_s": alone_s, "largest_request_alone_s": float(max(alone)), "per_model": per_model,
@@ -402,8 +403,9 @@ def measure_served(local, stream):
                      "two result slots (no host round trip between batches)",
             "slowdown": "latency over the request's own alone time",
             "ready": "submit to prepared (plan, tables, eigensystem, upload)",
-            "alone_queue": "latency percentiles of the plain path run as a first-come-first-served queue on the "
-                           "same arrivals, from the measured alone times"}
+            "alone_queue": "latency percentiles and makespan of the plain path run as a first-come-first-served "
+                           "queue on the same arrivals, from the measured alone times (both makespans run from the "
+                           "stream's start, so both include the GPU's idle time before arrivals)"}
 
 
 def measure_mixed_concurrency(local, full_rates, rounds=20):
