@@ -22,7 +22,7 @@ import numpy as np
 from . import build as _build
 
 DNKG, FPUT, TODA, DDNKG, DNLS = range(5)
-ORDER_REFERENCE, ORDER_DEVICE = 0, 1
+ORDER_REFERENCE, ORDER_DEVICE, ORDER_STENCIL = 0, 1, 2
 MODEL_NAMES = {"DNKG": DNKG, "FPUT": FPUT, "Toda": TODA, "dDNKG": DDNKG, "DNLS": DNLS}
 
 
@@ -54,6 +54,7 @@ def _lib(mt=False):
         lib.nlo_exp_scaled.argtypes = [ctypes.c_double, dp]
         lib.nlo_exp_scaled.restype = ctypes.c_double
         lib.nlo_coefficients.argtypes = [dp, dp]
+        lib.nlo_dnls_stencil_coefficients.argtypes = [ctypes.c_double, ctypes.c_int, dp, dp, dp]
         _libs[name] = lib
     return _libs[name]
 
@@ -90,6 +91,14 @@ def coefficients():
     c, d = np.zeros(8), np.zeros(8)
     _lib().nlo_coefficients(_dp(c), _dp(d))
     return c, d
+
+
+def dnls_stencil_coefficients(dt, max_radius=11):
+    """(radius, c0m1[7], taps[7, max_radius], phase[7]) of the DNLS stencil form, computed by the
+    oracle's own double-double series (nlo_dnls_stencil_coefficients)."""
+    c0, taps, ph = np.zeros(7), np.zeros(7 * max_radius), np.zeros(7)
+    r = _lib().nlo_dnls_stencil_coefficients(float(dt), int(max_radius), _dp(c0), _dp(taps), _dp(ph))
+    return r, c0, taps.reshape(7, max_radius), ph
 
 
 def reference_coefficients():

@@ -381,6 +381,187 @@ static void move_chain_dnls(const nlo_model *M, const double *tables, double *ps
 }
 
 /* ------------------------------------------------------------------------------------------------
+ * DNLS, the engine's stencil form (NLO_ORDER_STENCIL): each linear sub-step as the propagator's
+ * real-space kernel exp(-2 i tau) i^|x| J_|x|(2 tau) (Jacobi-Anger), replayed operation for
+ * operation from nlchains_gb300/csrc/nlc_dnls_stencil.cu, with the device's table sincos
+ * (nlc_device.cuh sincos_table) and its table (nlc_tables.cpp sincos_table).
+ * ----------------------------------------------------------------------------------------------*/
+
+#define NLO_SINCOS_TABLE 1024
+
+/* sin and cos of x in [0, pi/4] by their Taylor series in double-double */
+static void dd_sincos_small(dd x, dd *s, dd *c) {
+	const dd x2 = dd_mul(x, x);
+	dd term = x;
+	*s = x;
+	for (unsigned k = 1; k < 40; k++) {
+		term = dd_div_u(dd_mul(term, x2), (2 * k) * (2 * k + 1));
+		term.hi = -term.hi, term.lo = -term.lo;
+		*s = dd_add(*s, term);
+		if (fabs(term.hi) < 1e-40) break;
+	}
+	term.hi = 1., term.lo = 0.;
+	*c = term;
+	for (unsigned k = 1; k < 40; k++) {
+		term = dd_div_u(dd_mul(term, x2), (2 * k - 1) * (2 * k));
+		term.hi = -term.hi, term.lo = -term.lo;
+		*c = dd_add(*c, term);
+		if (fabs(term.hi) < 1e-40) break;
+	}
+}
+
+/* (cos, sin)(2 pi j / 1024): octant values m pi / 512, m = 0..128, then the quarter-turn symmetries */
+static void sincos_table_1024(double *table /* [1024][2] */) {
+	const unsigned Q = NLO_SINCOS_TABLE / 4, O = NLO_SINCOS_TABLE / 8;
+	const dd pi = {3.141592653589793116, 1.2246467991473532072e-16};
+	double cs[NLO_SINCOS_TABLE / 8 + 1], sn[NLO_SINCOS_TABLE / 8 + 1];
+	for (unsigned m = 0; m <= O; m++) {
+		dd s, c, mm = {(double) m, 0.};
+		dd_sincos_small(dd_div_u(dd_mul(pi, mm), NLO_SINCOS_TABLE / 2), &s, &c);
+		sn[m] = s.hi + s.lo, cs[m] = c.hi + c.lo;
+	}
+	for (unsigned j = 0; j < NLO_SINCOS_TABLE; j++) {
+		const unsigned q = j / Q, jj = j % Q;
+		const double c0 = jj <= O ? cs[jj] : sn[Q - jj], s0 = jj <= O ? sn[jj] : cs[Q - jj];
+		table[2 * j] = q == 0 ? c0 : q == 1 ? -s0 : q == 2 ? -c0 : s0;
+		table[2 * j + 1] = q == 0 ? s0 : q == 1 ? c0 : q == 2 ? -s0 : -c0;
+	}
+}
+
+/* the device's sincos: Taylor series below 2^-4, the table method below 2^20, libm beyond */
+static void sincos_device(double th, const double *tab, double *s, double *c) {
+	int64_t b;
+	memcpy(&b, &th, 8);
+	const int32_t hi = (int32_t) (b >> 32) & 0x7fffffff;
+	if (hi < 0x3fb00000) {
+		const double t2 = th * th;
+		const double ps = fma(t2, fma(t2, fma(t2, 1. / 362880, -1. / 5040), 1. / 120), -1. / 6);
+		*s = fma(th * t2, ps, th);
+		*c = fma(t2, fma(t2, fma(t2, fma(t2, 1. / 40320, -1. / 720), 1. / 24), -1. / 2), 1.);
+		return;
+	}
+	if (hi >= 0x41300000) {
+		*s = sin(th), *c = cos(th);
+		return;
+	}
+	const double shifter = 0x1.8p52, inv = 512. / 3.141592653589793116;
+	const double p1 = 3.141592653589793116 / 512, p2 = 1.2246467991473532072e-16 / 512;
+	const double t = fma(th, inv, shifter);
+	const double kd = t - shifter;
+	const double r = fma(-kd, p2, fma(-kd, p1, th));
+	int64_t tb;
+	memcpy(&tb, &t, 8);
+	const double *e = tab + 2 * ((uint32_t) tb & (NLO_SINCOS_TABLE - 1));
+	const double r2 = r * r;
+	const double sr = fma(r * r2, fma(r2, 1. / 120, -1. / 6), r);
+	const double cm1 = r2 * fma(r2, 1. / 24, -1. / 2);
+	*c = fma(e[0], cm1, fma(-e[1], sr, e[0]));
+	*s = fma(e[1], cm1, fma(e[0], sr, e[1]));
+}
+
+/* psi exp(i (neg_coef |psi|^2 + neg_phase)) in the device's order */
+static void rotate_device(double *v, double neg_coef, double neg_phase, const double *tab) {
+	const double norm = fma(v[0], v[0], v[1] * v[1]);
+	double s, c;
+	sincos_device(fma(neg_coef, norm, neg_phase), tab, &s, &c);
+	const double re = fma(v[0], c, -(v[1] * s)), im = fma(v[0], s, v[1] * c);
+	v[0] = re, v[1] = im;
+}
+
+/* J_x(2t) = sum_m (-1)^m t^(2m + x) / (m! (m + x)!) in double-double; minus_one (x = 0): without
+ * the leading 1 */
+static dd bessel_j_2t(unsigned x, dd t, int minus_one) {
+	const dd t2 = dd_mul(t, t);
+	dd term = {1., 0.};
+	for (unsigned i = 1; i <= x; i++) term = dd_div_u(dd_mul(term, t), i);
+	unsigned m = 0;
+	if (minus_one) {
+		const dd mone = {-1., 0.};
+		term = dd_mul(t2, mone);
+		m = 1;
+	}
+	dd sum = {0., 0.};
+	for (; m < 60; m++) {
+		sum = dd_add(sum, term);
+		term = dd_div_u(dd_mul(term, t2), (m + 1) * (m + 1 + x));
+		term.hi = -term.hi, term.lo = -term.lo;
+		if (fabs(term.hi) < 1e-40 * fabs(sum.hi) || term.hi == 0.) break;
+	}
+	return sum;
+}
+
+int nlo_dnls_stencil_coefficients(double dt, int max_radius, double *c0m1, double *taps, double *phase) {
+	const double limit = 0x1p-64;
+	int radius = 0;
+	for (int k = 0; k < 7; k++) {
+		const dd a = {dt, 0.}, d = {yoshida_d[k], 0.}, m2 = {-2., 0.};
+		const dd tau = dd_mul(a, d);
+		const dd c = bessel_j_2t(0, tau, 1);
+		c0m1[k] = c.hi + c.lo;
+		const dd ph = dd_mul(tau, m2);
+		phase[k] = ph.hi + ph.lo;
+		int r = 0;
+		for (int x = 1; x <= max_radius + 1; x++) {
+			const dd j = bessel_j_2t((unsigned) x, tau, 0);
+			const double v = j.hi + j.lo;
+			if (x <= max_radius) taps[k * max_radius + x - 1] = (x & 2) ? -v : v;
+			if (fabs(v) > limit) r = x;
+		}
+		if (r > radius) radius = r;
+	}
+	return radius;
+}
+
+#define NLO_STENCIL_MAX 11
+
+typedef struct {
+	int radius;   /* the instantiated radius the engine runs: 7, or 11 */
+	double c0m1[7], taps[7 * NLO_STENCIL_MAX], phase[7];
+	double tab[2 * NLO_SINCOS_TABLE];
+} stencil_consts;
+
+/* 0 when the engine's stencil form does not apply to this dt (taps beyond radius 11) */
+static int make_stencil(double dt, stencil_consts *S) {
+	const int need = nlo_dnls_stencil_coefficients(dt, NLO_STENCIL_MAX, S->c0m1, S->taps, S->phase);
+	S->radius = need <= 7 ? 7 : need <= NLO_STENCIL_MAX ? NLO_STENCIL_MAX : 0;
+	sincos_table_1024(S->tab);
+	return S->radius;
+}
+
+/* One launch of `batching` steps on one chain (psi: n interleaved complex), w: 2 n scratch */
+static void move_chain_dnls_stencil(const nlo_model *M, const stencil_consts *S, double *psi, double *w,
+                                    uint32_t batching) {
+	const int64_t n = M->n;
+	const int R = S->radius;
+	const double bdt = M->beta * M->dt;
+	for (uint32_t i = 0; i < batching; i++)
+		for (int k = 0; k < 7; k++) {
+			const double nc = -(k == 0 && i ? bdt * 2. * yoshida_c[0] : bdt * 1. * yoshida_c[k]);
+			for (int64_t s = 0; s < n; s++) rotate_device(psi + 2 * s, nc, S->phase[k], S->tab);
+			memcpy(w, psi, sizeof(double) * 2 * n);
+			const double c0 = S->c0m1[k];
+			const double *tp = S->taps + k * NLO_STENCIL_MAX;
+			for (int64_t s = 0; s < n; s++) {
+				const double *c = w + 2 * s;
+				double yr = fma(c0, c[0], c[0]), yi = fma(c0, c[1], c[1]);
+				for (int x = 1; x <= R; x++) {
+					const double *a = w + 2 * ((s + x) % n), *b = w + 2 * ((s - x + n) % n);
+					const double sr = a[0] + b[0], si = a[1] + b[1];
+					if (x & 1) {
+						yr = fma(-tp[x - 1], si, yr);
+						yi = fma(tp[x - 1], sr, yi);
+					} else {
+						yr = fma(tp[x - 1], sr, yr);
+						yi = fma(tp[x - 1], si, yi);
+					}
+				}
+				psi[2 * s] = yr, psi[2 * s + 1] = yi;
+			}
+		}
+	for (int64_t s = 0; s < n; s++) rotate_device(psi + 2 * s, -(bdt * yoshida_c[7]), 0., S->tab);
+}
+
+/* ------------------------------------------------------------------------------------------------
  * Driver
  * ----------------------------------------------------------------------------------------------*/
 
@@ -391,7 +572,14 @@ int nlo_advance(const nlo_model *M, double *state, uint64_t steps, uint32_t batc
 	consts *K = malloc(sizeof(consts));
 	make_consts(M, K);
 	double *tables = 0;
-	if (M->model == NLO_DNLS) {
+	stencil_consts *S = 0;
+	if (M->model == NLO_DNLS && M->order == NLO_ORDER_STENCIL) {
+		S = malloc(sizeof(stencil_consts));
+		if (!make_stencil(M->dt, S) || n < (uint32_t) (2 * S->radius + 2)) {
+			free(S), free(K);
+			return -1;
+		}
+	} else if (M->model == NLO_DNLS) {
 		tables = malloc(sizeof(double) * 2 * 7 * n);
 		dnls_tables(n, M->dt, tables);
 	}
@@ -402,7 +590,8 @@ int nlo_advance(const nlo_model *M, double *state, uint64_t steps, uint32_t batc
 #endif
 	{
 		double *a = malloc(sizeof(double) * (n + 2)), *b = malloc(sizeof(double) * n),
-		       *g = malloc(sizeof(double) * n), *z = malloc(sizeof(double) * 2 * n);
+		       *g = malloc(sizeof(double) * n), *z = malloc(sizeof(double) * 2 * n),
+		       *zw = malloc(sizeof(double) * 2 * n);
 #ifdef _OPENMP
 #pragma omp for schedule(static)
 #endif
@@ -410,7 +599,9 @@ int nlo_advance(const nlo_model *M, double *state, uint64_t steps, uint32_t batc
 			double *chain = state + 2 * (size_t) c * n;
 			if (M->model == NLO_DNLS) {
 				memcpy(z, chain, sizeof(double) * 2 * n);
-				for (uint64_t t = 0; t < steps; t += batching) move_chain_dnls(M, tables, z, batching);
+				for (uint64_t t = 0; t < steps; t += batching)
+					if (S) move_chain_dnls_stencil(M, S, z, zw, batching);
+					else move_chain_dnls(M, tables, z, batching);
 				memcpy(chain, z, sizeof(double) * 2 * n);
 				continue;
 			}
@@ -424,10 +615,11 @@ int nlo_advance(const nlo_model *M, double *state, uint64_t steps, uint32_t batc
 				for (uint32_t s = 0; s < n; s++) chain[2 * s] = a[s], chain[2 * s + 1] = b[s];
 			}
 		}
-		free(a), free(b), free(g), free(z);
+		free(a), free(b), free(g), free(z), free(zw);
 	}
 	free(K);
 	free(tables);
+	free(S);
 	return 0;
 }
 

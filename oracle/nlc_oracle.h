@@ -23,6 +23,11 @@
  *                        bond-cached forces, table-driven exp), so GPU results can be compared
  *                        bit for bit; for DNLS the rotation by sincos (the reference GPU's
  *                        e_pow_I, common/utilities_cuda.cuh:469-473).
+ * and for DNLS a third:
+ *   NLO_ORDER_STENCIL    the engine's stencil form operation for operation (its table sincos, the
+ *                        propagator's real-space taps J_x(2 dt d_k) from the same double-double
+ *                        series, the same FMA order), so that form can be compared bit for bit;
+ *                        it is tied to the transform form (the reference's) by the tests.
  */
 #ifndef NLC_ORACLE_H
 #define NLC_ORACLE_H
@@ -34,7 +39,7 @@ extern "C" {
 #endif
 
 enum { NLO_DNKG = 0, NLO_FPUT = 1, NLO_TODA = 2, NLO_DDNKG = 3, NLO_DNLS = 4 };
-enum { NLO_ORDER_REFERENCE = 0, NLO_ORDER_DEVICE = 1 };
+enum { NLO_ORDER_REFERENCE = 0, NLO_ORDER_DEVICE = 1, NLO_ORDER_STENCIL = 2 };
 
 typedef struct {
 	int32_t model;
@@ -59,6 +64,12 @@ void nlo_coefficients(double c[8], double d[8]);
  * dt*c[7] closes the launch (DNKG_FPUT_Toda.cu:138-146).  steps must be a multiple of batching.
  */
 int nlo_advance(const nlo_model *mdl, double *state, uint64_t steps, uint32_t batching);
+
+/* The stencil form's coefficients (NLO_ORDER_STENCIL): for the 7 sub-steps, c0m1[k] = J_0(2 tau_k) - 1,
+ * taps[k * max_radius + x - 1] = J_x(2 tau_k) times the sign of i^x (x = 1..max_radius), phase[k] =
+ * -2 tau_k, tau_k = dt d_k; returns the radius beyond which every tap is below 2^-64 (max_radius + 1
+ * if larger). */
+int nlo_dnls_stencil_coefficients(double dt, int max_radius, double *c0m1, double *taps, double *phase);
 
 /* Linear dispersion: real models sqrt(m + 4 sin^2(pi k/n)) (DNKG_FPUT_Toda/dispersion.cpp:9-16),
  * DNLS 4 sin^2(pi k/n) (DNLS/dispersion.cpp:10-17). */

@@ -63,3 +63,29 @@ def test_invalid_arguments(engine):
         engine.dnls_stencil_coefficients(0.01, 0)
     with pytest.raises(engine.NlcError):
         engine.dnls_stencil_coefficients(-1.0, 11)
+
+
+@pytest.mark.parametrize("dt", [0.001, 0.01, 0.05, 0.2])
+def test_oracle_builds_the_same_coefficients(engine, dt):
+    """The oracle's stencil replay uses its own double-double series: the same bits as the engine's."""
+    a = engine.dnls_stencil_coefficients(dt, 11)
+    b = O.dnls_stencil_coefficients(dt, 11)
+    assert a[0] == b[0]
+    for x, y in zip(a[1:], b[1:]):
+        assert np.array_equal(x, y)
+
+
+@pytest.mark.parametrize("n", [16, 53, 256])
+def test_oracle_stencil_order_agrees_with_the_transform_form(n):
+    """The oracle's replay of the stencil form against its transform form (the reference's split step
+    with sincos): the same dynamics to rounding after 20 steps."""
+    from nlchains_gb300 import ic
+    copies, dt = 3, 0.01
+    psi = ic.dnls_ensemble(n, copies, 1.0, ic.low_modes(n, 0.1), seed=n)
+    mdl = O.Model("DNLS", n, copies, dt, beta=1.0)
+    st = np.ascontiguousarray(psi).view(np.float64)
+    a = O.advance(mdl, st, 20, 10, order=O.ORDER_STENCIL)
+    b = O.advance(mdl, st, 20, 10, order=O.ORDER_DEVICE)
+    assert np.abs(a - b).max() <= 1e-12 * np.abs(b).max()
+    with pytest.raises(ValueError):
+        O.advance(O.Model("DNLS", 12, 1, dt, beta=1.0), np.zeros(24), 1, 1, order=O.ORDER_STENCIL)

@@ -175,3 +175,19 @@ def test_every_stencil_instantiation(gpu, monkeypatch, n, dt, sites, kind):
     a = run(gpu, n, copies, dt, 1.0, psi, 20, 10)
     f = run(gpu, n, copies, dt, 1.0, psi, 20, 10, FORMS["fourier"])
     assert np.abs(a - f).max() <= 1e-12 * np.abs(f).max()
+
+
+@pytest.mark.parametrize("n,sites", [(16, 0), (53, 0), (62, 8), (62, 16), (128, 12), (1024, 8), (1024, 12),
+                                     (1024, 16), (2953, 0)])
+def test_stencil_form_bit_exact_against_the_oracle(gpu, monkeypatch, n, sites):
+    """The stencil form against the oracle's replay of it (NLO_ORDER_STENCIL): bit for bit, whatever
+    the launch shape (lanes of a warp or a block, 8, 12 or 16 sites per lane), across launches."""
+    if sites:
+        monkeypatch.setenv("NLC_DNLS_SITES", str(sites))
+    copies, dt, steps, b = (5, 0.01, 20, 10) if n < 2000 else (2, 0.01, 4, 2)
+    assert gpu.Plan(gpu.Model("DNLS", n, copies, dt, beta=1.0)).shape()["tier"] == 5
+    psi = ic.dnls_ensemble(n, copies, 1.0, ic.low_modes(n, 0.1), seed=3 * n + sites)
+    out = run(gpu, n, copies, dt, 1.0, psi, steps, b)
+    exp = O.advance(O.Model("DNLS", n, copies, dt, beta=1.0), np.ascontiguousarray(psi).view(np.float64), steps, b,
+                    order=O.ORDER_STENCIL).view(np.complex128).reshape(copies, n)
+    assert np.array_equal(out, exp), np.abs(out - exp).max()
