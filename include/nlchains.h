@@ -76,9 +76,9 @@ enum {
 	NLC_FLAG_DNLS_FOURIER = 512      /* DNLS: the linear sub-steps through transforms of the chain, as
 	                                    the reference does, at every length.  By default, where dt is
 	                                    small enough (propagator taps beyond 11 sites below 2^-64, dt up
-	                                    to ~0.05) and 2R + 2 <= chain_length <= 4096, each linear
-	                                    sub-step is the same operator applied as its real-space stencil
-	                                    (nlc_dnls_stencil_coefficients) */
+	                                    to ~0.05) and chain_length >= 2R + 2 (16 at dt = 0.01), each
+	                                    linear sub-step is the same operator applied as its real-space
+	                                    stencil (nlc_dnls_stencil_coefficients) */
 };
 
 /*
@@ -202,7 +202,8 @@ int nlc_dnls_stencil_coefficients(double dt, int32_t max_radius, int32_t *radius
  * chain on one block of G > 32 lanes; 3 = DNLS, chains resident in shared memory (or, beyond it, in
  * per-block global scratch); 4 = windowed, chains longer than one block holds, integrated in
  * overlapping windows of G x E sites (lanes x sites per lane) between two state buffers; 5 = DNLS
- * in registers, G lanes of E or E - 1 sites, the linear sub-steps as real-space stencils. */
+ * in registers, G lanes of E or E - 1 sites, the linear sub-steps as real-space stencils; 6 = the
+ * same for DNLS chains longer than one block holds, in overlapping windows of G x E sites. */
 int nlc_plan_shape(const nlc_plan *plan, int32_t *lanes_per_chain, int32_t *sites_per_lane,
                    int32_t *threads_per_block, int32_t *tier);
 

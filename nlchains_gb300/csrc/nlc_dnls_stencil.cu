@@ -25,6 +25,12 @@
 // G > 32: one chain per block, halos by shuffles inside warps and through shared memory across
 // them, one barrier per sub-step.  The grid is persistent (self-resetting work counter) as for the
 // real models.
+//
+// Chains longer than one block holds (WIN): windows of G E sites of the periodic chain (every lane
+// full), advanced a few steps per launch as if the window were a ring.  A sub-step moves
+// information R sites, so after s steps only the 7 R s sites at each end of the window have seen
+// the false wrap-around; the interior between them is exact and is written to the second buffer,
+// and the windows' interiors tile the chain.
 #include "nlc_device.cuh"
 #include "nlc_internal.h"
 
@@ -48,10 +54,12 @@ __device__ __forceinline__ double2 rotate_phase(double2 v, double neg_coef, doub
 
 }  // namespace
 
-// TEAM: G <= 32, 128-thread blocks; otherwise one chain per block of ceil(G / 32) warps
-template <int E, int R, bool TEAM>
+// TEAM: G <= 32, 128-thread blocks; otherwise one chain (WIN: one window) per block of ceil(G / 32)
+// warps
+template <int E, int R, bool TEAM, bool WIN>
 __global__ void __launch_bounds__(TEAM ? 128 : 256) dnls_stencil_kernel(double2 *__restrict__ psi, const DnlsStencilArgs a) {
 	static_assert(E - 1 >= R, "a lane's halo comes from one neighbour: E - 1 >= R sites");
+	static_assert(!(WIN && TEAM), "windows are block-wide");
 	// G > 32: the halos crossing warps, [2 parities][2 directions][warps][R]
 	extern __shared__ double2 xb[];
 	__shared__ unsigned long long s_unit;
@@ -74,30 +82,42 @@ __global__ void __launch_bounds__(TEAM ? 128 : 256) dnls_stencil_kernel(double2 
 	const int left_warp = lane == 0 ? ((G - 1) >> 5) : warp - 1;   // warp of lane - 1 (mod G)
 	const int right_warp = lane == G - 1 ? 0 : warp + 1;            // warp of lane + 1 (mod G)
 
-	const int full = n - G * (E - 1);
+	const int full = WIN ? G : n - G * (E - 1);
 	const bool fl = lane < full;
 	const int ne = fl ? E : E - 1;
 	const int first = fl ? lane * E : full * E + (lane - full) * (E - 1);
 	const FpOnes &k1 = a.k1;
 	int parity = 0;
 
-	const unsigned long long units = (a.copies + gpb - 1) / gpb;
+	const unsigned long long units =
+	    WIN ? (unsigned long long) a.copies * a.win_count : (a.copies + gpb - 1) / gpb;
 	for (;;) {
 		__syncthreads();
 		if (tid == 0) s_unit = atomicAdd(&a.work_counter[0], 1ull);
 		__syncthreads();
 		const unsigned long long u = s_unit;
 		if (u >= units) break;
-		unsigned long long chain = u * gpb + gib;
+		unsigned long long chain = WIN ? u / a.win_count : u * gpb + gib;
+		const uint32_t win = WIN ? uint32_t(u - chain * a.win_count) : 0;
+		// WIN: the chain site of this lane's first site (the window starts win_halo sites before its
+		// interior)
+		const uint32_t wsite = WIN ? uint32_t((win * (unsigned long long) a.win_inner + n - a.win_halo + first) % n) : 0;
 		const bool active = chain < a.copies && !idle;
 		if (chain >= a.copies) chain = a.copies - 1;   // redundant work keeps shuffles and barriers convergent
-		double2 *g = psi + chain * (unsigned long long) n + (idle ? 0 : first);
+		double2 *g = psi + chain * (unsigned long long) n + (idle || WIN ? 0 : first);
 
 		// w: [0, R) left halo, [R, R + E) this lane's sites, [R + E, R + E + R) right halo; a short
 		// lane's slot R + E - 1 is inert (zero) between sub-steps
 		double2 w[E + 2 * R];
 #pragma unroll
-		for (int j = 0; j < E; j++) w[R + j] = (!idle && j < ne) ? g[j] : make_double2(0., 0.);
+		for (int j = 0; j < E; j++) {
+			uint32_t sj = j;
+			if (WIN) {
+				sj = wsite + j;
+				if (sj >= uint32_t(n)) sj -= n;
+			}
+			w[R + j] = (!idle && j < ne) ? g[sj] : make_double2(0., 0.);
+		}
 
 		for (uint32_t i = 0; i < a.steps; i++) {
 #pragma unroll 1
@@ -177,9 +197,23 @@ __global__ void __launch_bounds__(TEAM ? 128 : 256) dnls_stencil_kernel(double2 
 		}
 		if (active) {
 			const bool open = a.seg & NLC_SEG_OPEN;
+			double2 *dst = g;
+			// WIN: the interior's window positions [lo, hi) relative to this lane's first site, and the
+			// chain site of this lane's first site, written to win_out
+			int lo = 0, hi = E;
+			long long site0 = 0;
+			if (WIN) {
+				const uint32_t base = win * a.win_inner;   // chain site of the interior's first site
+				const uint32_t inner = min(a.win_inner, uint32_t(n) - base);
+				dst = a.win_out + chain * (unsigned long long) n;
+				lo = int(a.win_halo) - first;
+				hi = int(a.win_halo + inner) - first;
+				site0 = (long long) base - a.win_halo + first;
+			}
 #pragma unroll
 			for (int j = 0; j < E; j++)
-				if (j < ne) g[j] = open ? w[R + j] : rotate_phase(w[R + j], -a.nl_final, 0., a.sctab, a.sc, k1);
+				if (j < ne && j >= lo && j < hi)
+					dst[site0 + j] = open ? w[R + j] : rotate_phase(w[R + j], -a.nl_final, 0., a.sctab, a.sc, k1);
 		}
 	}
 
@@ -199,17 +233,22 @@ namespace {
 
 using StencilKernel = void (*)(double2 *, const DnlsStencilArgs);
 
-StencilKernel stencil_kernel(int sites, int radius, bool team) {
+StencilKernel stencil_kernel(int sites, int radius, bool team, bool win) {
+	if (win) {   // windows: 16 sites per lane
+		if (sites != 16 || team) return nullptr;
+		return radius == 7 ? dnls_stencil_kernel<16, 7, false, true>
+		                   : radius == 11 ? dnls_stencil_kernel<16, 11, false, true> : nullptr;
+	}
 	if (radius == 7) {
 		switch (sites) {
-			case 8: return team ? dnls_stencil_kernel<8, 7, true> : dnls_stencil_kernel<8, 7, false>;
-			case 12: return team ? dnls_stencil_kernel<12, 7, true> : dnls_stencil_kernel<12, 7, false>;
-			case 16: return team ? dnls_stencil_kernel<16, 7, true> : dnls_stencil_kernel<16, 7, false>;
+			case 8: return team ? dnls_stencil_kernel<8, 7, true, false> : dnls_stencil_kernel<8, 7, false, false>;
+			case 12: return team ? dnls_stencil_kernel<12, 7, true, false> : dnls_stencil_kernel<12, 7, false, false>;
+			case 16: return team ? dnls_stencil_kernel<16, 7, true, false> : dnls_stencil_kernel<16, 7, false, false>;
 		}
 	} else if (radius == 11) {
 		switch (sites) {
-			case 12: return team ? dnls_stencil_kernel<12, 11, true> : dnls_stencil_kernel<12, 11, false>;
-			case 16: return team ? dnls_stencil_kernel<16, 11, true> : dnls_stencil_kernel<16, 11, false>;
+			case 12: return team ? dnls_stencil_kernel<12, 11, true, false> : dnls_stencil_kernel<12, 11, false, false>;
+			case 16: return team ? dnls_stencil_kernel<16, 11, true, false> : dnls_stencil_kernel<16, 11, false, false>;
 		}
 	}
 	return nullptr;
@@ -217,8 +256,8 @@ StencilKernel stencil_kernel(int sites, int radius, bool team) {
 
 }  // namespace
 
-const void *dnls_stencil_kernel_ptr(int sites, int radius, bool team) {
-	return (const void *) stencil_kernel(sites, radius, team);
+const void *dnls_stencil_kernel_ptr(int sites, int radius, bool team, bool windowed) {
+	return (const void *) stencil_kernel(sites, radius, team, windowed);
 }
 
 size_t dnls_stencil_smem(int lanes, int radius) {
@@ -228,8 +267,17 @@ size_t dnls_stencil_smem(int lanes, int radius) {
 cudaError_t launch_dnls_stencil(const DnlsStencilArgs &a, double2 *psi, int sites, int radius, int blocks,
                                 cudaStream_t stream) {
 	const bool team = a.lanes <= 32;
-	const StencilKernel k = stencil_kernel(sites, radius, team);
-	if (!k) return cudaErrorInvalidValue;
+	const StencilKernel k = stencil_kernel(sites, radius, team, a.win_len != 0);
+	if (!k || a.lanes < 1 || a.lanes > 256 || !a.copies || blocks < 1) return cudaErrorInvalidConfiguration;
+	if (a.win_len) {
+		// a window fills every lane, lies inside the chain, and keeps a non-empty interior
+		if (a.win_len != uint32_t(a.lanes) * uint32_t(sites) || a.n <= a.win_len || !a.win_inner ||
+		    2ull * a.win_halo + a.win_inner > a.win_len || !a.win_out ||
+		    a.win_count != (a.n + a.win_inner - 1) / a.win_inner)
+			return cudaErrorInvalidConfiguration;
+	} else if (uint64_t(a.lanes) * (sites - 1) >= a.n || uint64_t(a.lanes) * sites < a.n || a.n < uint32_t(2 * radius + 2)) {
+		return cudaErrorInvalidConfiguration;   // every lane holds sites or sites - 1 >= radius sites
+	}
 	count_launch();
 	const int threads = team ? 128 : (a.lanes + 31) / 32 * 32;
 	k<<<blocks, threads, dnls_stencil_smem(a.lanes, radius), stream>>>(psi, a);

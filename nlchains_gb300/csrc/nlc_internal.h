@@ -249,10 +249,15 @@ struct DnlsStencilArgs {
 	const double2 *sctab;
 	SinCosConsts sc;
 	FpOnes k1;
+	// windowed launches (chains beyond one block, win_len != 0): windows of win_len = lanes x E
+	// sites, every lane full, win_halo sites at each end recomputed and discarded, the interiors
+	// written to win_out
+	uint32_t win_len, win_halo, win_inner, win_count;
+	double2 *win_out;
 };
 cudaError_t launch_dnls_stencil(const DnlsStencilArgs &a, double2 *psi, int sites, int radius, int blocks,
                                 cudaStream_t stream);
-const void *dnls_stencil_kernel_ptr(int sites, int radius, bool team);
+const void *dnls_stencil_kernel_ptr(int sites, int radius, bool team, bool windowed = false);
 size_t dnls_stencil_smem(int lanes, int radius);
 cudaError_t launch_dnls_nonlinear(double2 *psi, uint64_t elements, double coef, const double2 *sctab,
                                   cudaStream_t stream);

@@ -697,6 +697,12 @@ const void *lin32_kernel_ptr(int team_block);
 const void *dnls_kernel_ptr(int team_block);
 }  // namespace nlc
 
+// Steps per launch of a windowed DNLS stencil launch: the discarded ends (7 R sites per step each)
+// about 5% of a window each.
+static uint32_t dnls_window_steps(uint32_t win_len, int radius) {
+	return std::max<uint32_t>(1, win_len / (140 * uint32_t(radius)));
+}
+
 // DNLS in the real-space stencil form (nlc_dnls_stencil.cu), where it applies: the propagator's
 // taps beyond radius 11 below 2^-64 (dt d_k up to ~0.05), n >= 2R + 2, and a launch shape of G lanes
 // (up to 256) of E or E - 1 sites, E in {16, 12, 8} with E - 1 >= R.  Among the shapes, the one
@@ -711,11 +717,13 @@ static int setup_dnls_stencil(nlc_plan &P) {
 	int lanes = 0, sites = 0;
 	double best = 0;
 	// NLC_DNLS_SITES=<E> restricts the shapes to E sites per lane (used by the tests to cover every
-	// instantiation)
+	// instantiation); NLC_FORCE_WINDOW=<G> integrates in windows of G lanes where a block would hold
+	// the chain (used by the tests to cover the windowed form on short chains)
 	int only = 0;
 	if (const char *e = std::getenv("NLC_DNLS_SITES")) only = std::atoi(e);
+	const char *force_win = std::getenv("NLC_FORCE_WINDOW");
 	for (int E : {16, 12, 8}) {
-		if (E - 1 < R || (only && E != only)) continue;
+		if (force_win || E - 1 < R || (only && E != only)) continue;
 		// G (E - 1) < n <= G E: every lane holds E or E - 1 sites
 		for (uint32_t G = (n + E - 1) / E; G <= 256 && uint64_t(G) * (E - 1) < n; G++) {
 			const double occupied = G <= 32 ? 32. / double(32 / G) : double((G + 31) / 32 * 32);
@@ -723,8 +731,26 @@ static int setup_dnls_stencil(nlc_plan &P) {
 			if (eff > best * 1.0001) best = eff, lanes = int(G), sites = E;
 		}
 	}
-	if (!lanes) return NLC_OK;
-	const void *k = dnls_stencil_kernel_ptr(sites, R, lanes <= 32);
+	bool windowed = false;
+	if (!lanes) {
+		// longer than one block holds: windows of G lanes x 16 sites of the periodic chain, ping-ponging
+		// between the caller's buffer and a second one of the same size.  G (a multiple of 32 up to
+		// 256) with the least work per chain: windows x window length, the windows' interiors
+		// (window minus 7 R s sites at each end, s = dnls_window_steps) tiling the chain
+		int G = force_win ? std::atoi(force_win) : 0;
+		if (!G) {
+			uint64_t least = ~0ull;
+			for (int g = 256; g >= 64; g -= 32) {
+				const uint32_t len = uint32_t(g) * 16, halo = 7 * uint32_t(R) * dnls_window_steps(len, R);
+				if (len >= n || 2 * halo >= len) continue;
+				const uint64_t work = uint64_t((n + len - 2 * halo - 1) / (len - 2 * halo)) * len;
+				if (work < least) least = work, G = g;
+			}
+		}
+		if (G <= 32 || G > 256 || G % 32 || uint64_t(G) * 16 >= n) return NLC_OK;
+		lanes = G, sites = 16, windowed = true;
+	}
+	const void *k = dnls_stencil_kernel_ptr(sites, R, lanes <= 32, windowed);
 	if (!k) return NLC_OK;
 	const DnlsArgs &d = P.da;
 	a.n = n, a.copies = P.m.copies, a.lanes = lanes;
@@ -744,13 +770,20 @@ static int setup_dnls_stencil(nlc_plan &P) {
 	P.dnls_blocks = int(std::min<unsigned long long>(
 	    units, (P.m.flags & NLC_FLAG_SHARED_GPU) ? 0x7fffffffull
 	                                            : (unsigned long long) per_sm * P.prop.multiProcessorCount));
+	if (windowed) {
+		P.win_len = uint32_t(lanes) * sites;
+		P.win_steps = dnls_window_steps(P.win_len, R);
+		int rc2;
+		if ((rc2 = P.dalloc(&P.d_win, size_t(P.m.copies) * n))) return rc2;
+		P.dnls_blocks = per_sm * P.prop.multiProcessorCount;   // per launch: at most one block per window
+	}
 	P.dnls_sites = sites, P.dnls_radius = R;
 	P.dnls_stencil = true;
 	// a block's step: 7 sub-steps of 19 + 4R FP64 operations on the lane-sites it computes, at ~85%
 	P.block_ops = 7. * (19 + 4 * R) * double(sites) * (lanes <= 32 ? 32 * (P.dnls_threads / 32) : P.dnls_threads) / 0.85;
 	P.per_sm = per_sm;
 	P.block_warps = P.dnls_threads / 32;
-	P.tier = 5;
+	P.tier = windowed ? 6 : 5;
 	return NLC_OK;
 }
 
@@ -1179,6 +1212,37 @@ int nlc::move_rounds(nlc_plan *P, void *state, uint64_t rounds, uint32_t round_s
 int nlc::move_segment(nlc_plan *P, void *state, uint32_t steps, uint32_t seg, cudaStream_t st) {
 	if (!P || !state) return set_error(NLC_EINVAL, "NULL argument");
 	if (!steps) return NLC_OK;
+	if (P->m.model == NLC_DNLS && P->dnls_stencil && P->win_len) {
+		// windows: launches of at most win_steps steps (open segments in between), each reading one
+		// buffer and writing the interiors of its windows to the other
+		const uint32_t n = P->m.chain_length;
+		double2 *in = static_cast<double2 *>(state), *out = P->d_win;
+		DnlsStencilArgs a = P->sa;
+		for (uint32_t done = 0; done < steps;) {
+			const uint32_t s = std::min(steps - done, P->win_steps);
+			a.steps = s;
+			a.seg = ((done || (seg & NLC_SEG_CONTINUE)) ? NLC_SEG_CONTINUE : 0u) |
+			        ((done + s < steps || (seg & NLC_SEG_OPEN)) ? NLC_SEG_OPEN : 0u);
+			a.win_len = P->win_len;
+			a.win_halo = 7 * uint32_t(P->dnls_radius) * s;
+			a.win_inner = P->win_len - 2 * a.win_halo;
+			a.win_count = (n + a.win_inner - 1) / a.win_inner;
+			a.win_out = out;
+			const unsigned long long units = (unsigned long long) P->m.copies * a.win_count;
+			const int blocks = int(std::min<unsigned long long>(
+			    units, (P->m.flags & NLC_FLAG_SHARED_GPU) ? 0x7fffffffull : (unsigned long long) P->dnls_blocks));
+			int rc = cuda_status(launch_dnls_stencil(a, in, P->dnls_sites, P->dnls_radius, blocks, st),
+			                     "DNLS windowed stencil launch");
+			if (rc) return rc;
+			std::swap(in, out);
+			done += s;
+		}
+		if (in != state)
+			return cuda_status(cudaMemcpyAsync(state, in, size_t(P->m.copies) * n * sizeof(double2),
+			                                   cudaMemcpyDeviceToDevice, st),
+			                   "windowed state copy");
+		return NLC_OK;
+	}
 	if (P->m.model == NLC_DNLS && P->dnls_stencil) {
 		DnlsStencilArgs a = P->sa;
 		a.steps = steps;

@@ -699,7 +699,8 @@ int submit(nlc_server *S, const nlc_model *model, uint32_t batching, uint64_t st
 	}
 	// state + diagnostics partial rows (<= one row block per SM) + tables
 	R->need_bytes = R->state_bytes + size_t(4 * 160) * n * sizeof(double) + 16 * n * sizeof(double) +
-	                (model->model == NLC_DDNKG ? n * n * sizeof(double) : 0) + (1 << 16);
+	                (model->model == NLC_DDNKG ? n * n * sizeof(double) : 0) + (1 << 16) +
+	                (n > 4096 ? R->state_bytes : 0);   // windowed integrators: a second state buffer
 	if (n > 4096) R->need_bytes += R->state_bytes + size_t(2 * 1024) * 4 * n * sizeof(double2);   // windows / FFT scratch
 	if (model->model == NLC_DDNKG) {
 		// the tensor-core projection (the plan's rule): BF16 slices of the state and of the

@@ -151,7 +151,8 @@ def test_form_selection(gpu):
     assert tier(1024, 0.01, FORMS["fourier"]) == 3
     assert tier(1024, 0.2) == 3                 # taps beyond radius 11 above 2^-64
     assert tier(12, 0.01) == 3                  # shorter than 2R + 2
-    assert tier(8192, 0.01) == 3                # beyond 256 lanes of 16 sites
+    assert tier(8192, 0.01) == 6                # beyond 256 lanes of 16 sites: windows
+    assert tier(8192, 0.2) == 3
     shape = gpu.Plan(gpu.Model("DNLS", 2953, 4, 0.01, beta=1.0)).shape()
     assert shape["sites_per_lane"] == 16 and shape["lanes_per_chain"] == 185 and shape["threads"] == 192
 
@@ -187,6 +188,25 @@ def test_stencil_form_bit_exact_against_the_oracle(gpu, monkeypatch, n, sites):
     copies, dt, steps, b = (5, 0.01, 20, 10) if n < 2000 else (2, 0.01, 4, 2)
     assert gpu.Plan(gpu.Model("DNLS", n, copies, dt, beta=1.0)).shape()["tier"] == 5
     psi = ic.dnls_ensemble(n, copies, 1.0, ic.low_modes(n, 0.1), seed=3 * n + sites)
+    out = run(gpu, n, copies, dt, 1.0, psi, steps, b)
+    exp = O.advance(O.Model("DNLS", n, copies, dt, beta=1.0), np.ascontiguousarray(psi).view(np.float64), steps, b,
+                    order=O.ORDER_STENCIL).view(np.complex128).reshape(copies, n)
+    assert np.array_equal(out, exp), np.abs(out - exp).max()
+
+
+@pytest.mark.parametrize("n,dt,force,copies,steps,b", [
+    (5000, 0.01, None, 3, 20, 10),     # windows of 192 lanes x 16 sites, 3 steps per launch (3 + 3 + 3 + 1)
+    (5000, 0.05, None, 2, 6, 3),       # radius 11: 1 step per launch
+    (1500, 0.01, "64", 4, 9, 3),       # forced windows of 64 lanes on a shorter chain, 1 step per launch
+    (65535, 0.01, None, 1, 4, 4),      # the longest 16-bit chain
+])
+def test_windowed_stencil_bit_exact(gpu, monkeypatch, n, dt, force, copies, steps, b):
+    """Chains beyond one block in overlapping windows (tier 6): bit for bit the oracle's replay of the
+    stencil form, over launches that leave the batch open and continue it."""
+    if force:
+        monkeypatch.setenv("NLC_FORCE_WINDOW", force)
+    assert gpu.Plan(gpu.Model("DNLS", n, copies, dt, beta=1.0)).shape()["tier"] == 6
+    psi = ic.dnls_ensemble(n, copies, 1.0, ic.low_modes(n, 0.1), seed=n + 7)
     out = run(gpu, n, copies, dt, 1.0, psi, steps, b)
     exp = O.advance(O.Model("DNLS", n, copies, dt, beta=1.0), np.ascontiguousarray(psi).view(np.float64), steps, b,
                     order=O.ORDER_STENCIL).view(np.complex128).reshape(copies, n)
