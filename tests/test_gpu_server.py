@@ -30,6 +30,8 @@ MIX = [
     ("dDNKG", 48, 40, 10, 20, dict(beta=1.0)),
     ("dDNKG", 48, 41, 10, 30, dict(beta=1.0)),
     ("DNLS", 128, 30, 5, 10, dict(beta=1.0)),
+    ("DNLS", 62, 40, 5, 10, dict(beta=1.0)),      # the stencil form on 4 lanes of a warp
+    ("DNLS", 5000, 3, 5, 10, dict(beta=1.0)),     # the stencil form in windows (tier 6)
 ]
 
 
