@@ -827,7 +827,8 @@ def run_reference_profile_case():
 def run_profile_case(args):
     """Small cases of the headline kernels for ncu captures: 4 launches (10 steps; DNLS 2 steps),
     each followed by one diagnostics sample.  DNKG / Toda: 16384 of the 65536 copies (33.5 MB);
-    DNLS: the full 8192 copies of N = 1024 (134 MB, above the L2); dDNKG: the full 4096 x 256;
+    DNLS: the full 8192 copies of N = 1024 (134 MB, above the L2); dnlslong: 512 DNLS chains of 16384
+    sites in windows (6 steps: two launches of 3); dDNKG: the full 4096 x 256;
     long: 256 FPUT chains of 65535 sites (windowed tier, 268 MB)."""
     import torch
 
@@ -837,6 +838,8 @@ def run_profile_case(args):
         w = dict(TODA, copies=16384)
     if args.profile == "dnls":
         w, steps = dict(OTHERS[1]), 2
+    if args.profile == "dnlslong":   # DNLS beyond one block: the stencil form in windows (134 MB of state)
+        w, steps = dict(OTHERS[1], name="DNLS N=16384 copies=512 (windowed)", n=16384, copies=512), 6
     if args.profile == "ddnkg":   # the full dDNKG workload: 4096 chains of 256 sites, tensor-core projection
         w = dict(OTHERS[2])
     if args.profile == "ddnkg1024":   # 4096 chains of 1024 sites: four read-outs per projection tile
@@ -865,7 +868,8 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["engine", "reference"], default="engine")
-    ap.add_argument("--profile", choices=["dnkg", "toda", "dnls", "ddnkg", "ddnkg1024", "long", "refdnkg"], default=None,
+    ap.add_argument("--profile", choices=["dnkg", "toda", "dnls", "dnlslong", "ddnkg", "ddnkg1024", "long", "refdnkg"],
+                    default=None,
                     help="run only a small case of the integrator + diagnostics (for ncu captures)")
     args = ap.parse_args()
     if args.profile == "refdnkg":
