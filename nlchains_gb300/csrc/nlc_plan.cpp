@@ -264,7 +264,7 @@ RealShape heuristic_shape(const nlc_plan &P, int model, int variant) {
 // $NLC_TUNE_CACHE, else $XDG_CACHE_HOME/nlchains_gb300/shapes.tsv, else
 // $HOME/.cache/nlchains_gb300/shapes.tsv; NLC_TUNE_CACHE=off keeps the cache in memory only.  A
 // line is "device<TAB>model<TAB>variant<TAB>n<TAB>bucket<TAB>lanes<TAB>sites<TAB>threads"; lines
-// that do not parse or name a shape this build cannot launch are ignored.  A ninth field, the
+// that do not parse or name a shape this library cannot launch are ignored.  A ninth field, the
 // measured time of one step of an ensemble of the bucket, feeds the choice of rounds per launch.
 struct TuneKey {
 	std::string device;
