@@ -21,7 +21,7 @@ CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-CU_SOURCES = ["nlc_real_dnkg.cu", "nlc_real_fput.cu", "nlc_real_toda.cu", "nlc_real_ddnkg.cu",
+CU_SOURCES = ["nlc_real_toda.cu", "nlc_real_toda_short.cu", "nlc_real_dnkg.cu", "nlc_real_fput.cu", "nlc_real_ddnkg.cu",
               "nlc_diag.cu", "nlc_dnls.cu", "nlc_dnls_stencil.cu", "nlc_noalloc.cu", "nlc_energy.cu", "nlc_tc.cu"]
 CPP_SOURCES = ["nlc_plan.cpp", "nlc_tables.cpp", "nlc_job.cpp", "nlc_server.cpp", "nlc_eig_device.cpp",
                "nlc_eig_host.cpp"]

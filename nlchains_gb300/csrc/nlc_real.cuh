@@ -311,17 +311,12 @@ struct RealKernels {
 	static constexpr K get(int variant) {
 		return variant ? real_move_kernel_t<MODEL, E, 1, WIN> : real_move_kernel_t<MODEL, E, 0, WIN>;
 	}
-	static K lookup(int variant, int e, bool win) {
-		if (win) {
-			switch (e) {
-				case 4: return get<4, true>(variant);
-				case 8: return get<8, true>(variant);
-				case 12: return get<12, true>(variant);
-				case 14: return get<14, true>(variant);
-				case 16: return get<16, true>(variant);
-				default: return nullptr;
-			}
-		}
+	// Two halves of about equal compile time, so that a model whose kernels take long to compile can
+	// build them in two translation units: lanes of 2..13 sites and 4-site windows; lanes of 14..16
+	// sites and the wider windows
+	static bool is_short(int e, bool win) { return win ? e == 4 : e <= 13; }
+	static K lookup_short(int variant, int e, bool win) {
+		if (win) return e == 4 ? get<4, true>(variant) : nullptr;
 		switch (e) {
 			case 2: return get<2>(variant);
 			case 3: return get<3>(variant);
@@ -335,11 +330,28 @@ struct RealKernels {
 			case 11: return get<11>(variant);
 			case 12: return get<12>(variant);
 			case 13: return get<13>(variant);
+			default: return nullptr;
+		}
+	}
+	static K lookup_long(int variant, int e, bool win) {
+		if (win) {
+			switch (e) {
+				case 8: return get<8, true>(variant);
+				case 12: return get<12, true>(variant);
+				case 14: return get<14, true>(variant);
+				case 16: return get<16, true>(variant);
+				default: return nullptr;
+			}
+		}
+		switch (e) {
 			case 14: return get<14>(variant);
 			case 15: return get<15>(variant);
 			case 16: return get<16>(variant);
 			default: return nullptr;
 		}
+	}
+	static K lookup(int variant, int e, bool win) {
+		return is_short(e, win) ? lookup_short(variant, e, win) : lookup_long(variant, e, win);
 	}
 };
 
