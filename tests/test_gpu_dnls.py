@@ -155,6 +155,10 @@ def test_form_selection(gpu):
     assert tier(8192, 0.2) == 3
     shape = gpu.Plan(gpu.Model("DNLS", 2953, 4, 0.01, beta=1.0)).shape()
     assert shape["sites_per_lane"] == 16 and shape["lanes_per_chain"] == 185 and shape["threads"] == 192
+    # windows: the width with the least work per chain (windows x window length)
+    for n, lanes in ((8192, 192), (16384, 224), (65535, 96)):
+        shape = gpu.Plan(gpu.Model("DNLS", n, 4, 0.01, beta=1.0)).shape()
+        assert shape["tier"] == 6 and shape["lanes_per_chain"] == lanes and shape["sites_per_lane"] == 16, (n, shape)
 
 
 # (n, dt, sites per lane) -> every instantiation: radius 7 (dt = 0.01) with 8, 12, 16 sites and
